@@ -1,0 +1,197 @@
+/*
+ * mfx -- GB300-native engine for monofonIC's initial-condition hot path.
+ *
+ * Thin C ABI over the CUDA engine (libmfx.so).  No C++ or torch types cross
+ * it: plain pointers, sizes and integer status codes.  Every entry point
+ * returns MFX_OK (0) or a negative status; mfx_last_error() returns the
+ * message of the calling thread's last failure.  C++ exceptions never cross
+ * this boundary.
+ *
+ * Each declaration names the reference interface it replaces
+ * (file:line inside the monofonIC source tree).
+ */
+#ifndef MFX_H
+#define MFX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MFX_OK 0
+#define MFX_EINVAL (-1)    /* invalid argument                          */
+#define MFX_ENOMEM (-2)    /* device or host allocation failed           */
+#define MFX_ECUDA (-3)     /* CUDA / cuFFT error                         */
+#define MFX_ETIMEOUT (-4)  /* wait timed out                             */
+#define MFX_ECANCEL (-5)   /* job cancelled                              */
+#define MFX_ESTATE (-6)    /* call not valid in the object's state       */
+#define MFX_EADMIT (-7)    /* serving: job does not fit the HBM budget   */
+
+/* ---- enums --------------------------------------------------------------- */
+/* particle::lattice, particle_generator.hh:31-39 (Bravais lattices only) */
+#define MFX_LATTICE_SC 0
+#define MFX_LATTICE_BCC 1
+#define MFX_LATTICE_FCC 2
+
+/* arithmetic form of a job */
+#define MFX_FP64 0  /* plain form: the reference's FP64 algorithm            */
+#define MFX_FP32C 1 /* FP32 FFTs/products, compensated 3LPT source sums,
+                       FP64 tables and FP64 q+Psi position sum              */
+
+/* fields fetchable with mfx_job_fetch_field (k-space, N x N x (N/2+1) complex) */
+#define MFX_FIELD_NOISE 0 /* white noise as RNG_plugin::Fill_Grid leaves it   */
+#define MFX_FIELD_PHI1 1  /* phi(1), unscaled, ic_generator.cc:509-516         */
+#define MFX_FIELD_PHI2 2  /* phi(2), unscaled, ic_generator.cc:523-548         */
+#define MFX_FIELD_PHI3 3  /* phi(3), unscaled, ic_generator.cc:571-611         */
+#define MFX_FIELD_A3X 4   /* A(3) components, unscaled, ic_generator.cc:613-628 */
+#define MFX_FIELD_A3Y 5
+#define MFX_FIELD_A3Z 6
+
+/* ---- objects -------------------------------------------------------------- */
+typedef struct mfx_engine mfx_engine;
+typedef struct mfx_job mfx_job;
+
+typedef struct {
+  int device;              /* CUDA device ordinal                               */
+  size_t hbm_budget_bytes; /* 0 = 90% of free memory at creation                */
+} mfx_engine_opts;
+
+/*
+ * One initial-conditions job.  Replaces the parameter set that
+ * ic_generator::run reads (ic_generator.cc:100-273) plus the inputs the hot
+ * path takes from the RNG / transfer-function plugins.
+ */
+typedef struct {
+  uint32_t ngrid;    /* [setup] GridRes, even, >= 8                          */
+  double boxlen;     /* [setup] BoxLength (Mpc/h)                            */
+  int lpt_order;     /* 1, 2 or 3                                            */
+  int lattice;       /* MFX_LATTICE_*                                        */
+  int plt;           /* 1: PLT gradient + vfac_corr (needs plt_table)        */
+  int precision;     /* MFX_FP64 or MFX_FP32C                                */
+  int fixing;        /* [setup] DoFixing                                     */
+  int inversion;     /* [setup] DoInversion                                  */
+  /* NGenIC per-column seed table, N*N uint32 (random_ngenic.cc:47-74) */
+  const uint32_t *seed_table;
+  /* amplitude table indexed by n = i^2+j^2+k^2 over signed mode indices:
+     amp_table[n] = get_amplitude(kf*sqrt(n)) / (kf^2 n), amp_table[0] = 0,
+     kf = 2 pi / boxlen; length >= 3*(N/2)^2 + 1 (cosmology_calculator.hh:429-432) */
+  const double *amp_table;
+  size_t amp_table_len;
+  /* PLT tables from mfx_plt_table_build (NULL when plt == 0) */
+  const double *plt_table;
+  /* LPT time coefficients, ic_generator.cc:252-269 */
+  double g1, g2, g3, g3c;
+  double vfac1, vfac2, vfac3;
+  /* output_plugin::position_unit / velocity_unit (output_plugin.hh:86-90) */
+  double lunit, vunit;
+  int pos64;  /* positions as double (else float)                           */
+  int vel64;  /* velocities as double (else float)                          */
+  int id64;   /* IDs as uint64 (else uint32), output_plugin::has_64bit_ids    */
+  uint64_t id_offset; /* lattice_generator IDoffset (particle_generator.hh:232) */
+  int want_particles; /* 0: stop after the LPT potentials (fields only)     */
+} mfx_job_desc;
+
+/* ---- errors -------------------------------------------------------------- */
+/* Copies the calling thread's last error message; returns its full length. */
+size_t mfx_last_error(char *buf, size_t len);
+const char *mfx_version(void);
+
+/* ---- engine -------------------------------------------------------------- */
+/* Replaces the process-wide FFTW/OpenMP set-up of main.cc:156-182. */
+int mfx_engine_create(const mfx_engine_opts *opts, mfx_engine **out);
+int mfx_engine_destroy(mfx_engine *eng);
+/* Device bytes a job with this descriptor needs (arena + FFT work area). */
+int mfx_job_footprint(mfx_engine *eng, const mfx_job_desc *desc, size_t *bytes);
+
+/* ---- jobs ----------------------------------------------------------------- */
+/* Allocates the job's device arena, creates (or reuses) its FFT plans and
+   uploads the descriptor's tables.  Replaces the Grid_FFT / OrszagConvolver /
+   lattice_generator allocations of ic_generator.cc:288-310, 475, 743-745. */
+int mfx_job_create(mfx_engine *eng, const mfx_job_desc *desc, mfx_job **out);
+/* Re-uploads the tables of `desc` (same sizes as at creation) from host
+   memory, asynchronously on the job's stream. */
+int mfx_job_upload(mfx_job *job, const mfx_job_desc *desc);
+/* Enqueues the whole hot path on the job's stream: RNG_plugin::Fill_Grid
+   (random_ngenic.cc:84-154) through the particle read-out of
+   lattice_generator::set_positions / set_velocities
+   (particle_generator.hh:499-687), i.e. ic_generator.cc:288-1060. */
+int mfx_job_run(mfx_job *job);
+/* Waits for the job's stream; timeout_ms < 0 waits forever.  MFX_ETIMEOUT
+   leaves the job running and usable. */
+int mfx_job_wait(mfx_job *job, int timeout_ms);
+/* Copies the particle container (particle_container.hh:29-188 layout:
+   interleaved xyz) into caller buffers; each pointer may be host or device
+   memory or NULL to skip. */
+int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids);
+/* Device pointers of the particle arrays (valid until the next run/destroy). */
+int mfx_job_particles_device(mfx_job *job, const void **pos, const void **vel, const void **ids,
+                             size_t *num_particles);
+/* Copies one k-space field as complex128, N*N*(N/2+1) entries.  Test hook
+   standing in for output_plugin::write_grid_data (output_plugin.hh:71). */
+int mfx_job_fetch_field(mfx_job *job, int field_id, double *out);
+/* Runs only the white-noise fill (raw = 1: as Fill_Grid leaves it;
+   raw = 0: normalised, fixed / inverted, ic_generator.cc:378-383). */
+int mfx_job_run_noise(mfx_job *job, int raw);
+/* Per-stage device times (ms) of the last run: noise+phi1, phi2, phi3+A3,
+   assembly+particles.  Returns the number of stages written. */
+int mfx_job_stage_times(mfx_job *job, double *ms, int max_stages);
+/* Device-side algorithmic byte count of one run (ideal-fused stage model). */
+int mfx_job_algorithmic_bytes(mfx_job *job, double *bytes);
+/* Number of kernels (own + cuFFT) the last run launched. */
+int mfx_job_launch_count(mfx_job *job, int *own_kernels, int *fft_execs);
+/* Per-launch profiling: when on, every kernel and FFT of a run is bracketed
+   by CUDA events on the job's stream and tagged with its algorithmic bytes
+   (the reference's equivalent is its per-stage "took" log lines,
+   ic_generator.cc:506-628).  mfx_job_kernel_profile aggregates the last run
+   by kernel name (32-byte name slots) and returns the number of names. */
+int mfx_job_set_profiling(mfx_job *job, int on);
+int mfx_job_kernel_profile(mfx_job *job, int max_entries, char *names, double *ms, double *bytes, int *launches);
+int mfx_job_destroy(mfx_job *job);
+
+/* Debug hook: first `count` 48-bit words of the ranlxd1 stream of `seed`,
+   computed on the device (bit-exactness check of the device generator). */
+int mfx_debug_ranlxd1_words(mfx_engine *eng, unsigned long seed, size_t count, uint64_t *out);
+
+/* ---- host-side plugin logic (C++ host library, same .so) ------------------ */
+/* RNG_ngenic constructor: the N*N per-column seed table
+   (random_ngenic.cc:39-75). */
+int mfx_ngenic_seed_table(long seed, size_t ngrid, uint32_t *table);
+
+/* PLT eigenmode tables for a lattice on the 64^3 mesh
+   (particle::lattice_gradient::init_D, particle_plt.hh:68-515).
+   `out` receives 4 * 64*64*33 doubles: D_r, D_theta, D_phi, alpha^{-1}
+   in kelem order.  The Ewald sums run on the device of `eng`. */
+#define MFX_PLT_NGRID 64
+#define MFX_PLT_TABLE_DOUBLES (4 * 64 * 64 * 33)
+int mfx_plt_table_build(mfx_engine *eng, int lattice, double *out);
+
+/* cosmology::calculator (cosmology_calculator.hh:44-523) with the
+   Eisenstein & Hu transfer plugin (transfer_eisenstein.cc:25-258), built
+   from INI text in the reference's config_file format (config_file.hh:96-164). */
+typedef struct mfx_cosmology mfx_cosmology;
+int mfx_cosmology_create(const char *ini_text, mfx_cosmology **out);
+int mfx_cosmology_destroy(mfx_cosmology *c);
+/* named scalars: "dplus_start", "vfact_start", "pnorm", "sqrtpnorm",
+   "Omega_m", "Omega_b", "Omega_DE", "Omega_r", "h", "n_s", "sigma_8", ... */
+int mfx_cosmology_get(mfx_cosmology *c, const char *name, double *value);
+/* get_amplitude(k, delta_matter) (cosmology_calculator.hh:429-432) for k in h/Mpc */
+int mfx_cosmology_amplitude(mfx_cosmology *c, const double *k, size_t count, double *out);
+/* transfer_function_->compute(k, delta_matter) */
+int mfx_cosmology_transfer(mfx_cosmology *c, const double *k, size_t count, double *out);
+/* D+(a) normalised to D+(1) = 1 */
+int mfx_cosmology_growth(mfx_cosmology *c, double a, double *dplus);
+/* Fills amp_table (length 3*(N/2)^2+1) for grid size N and box L. */
+int mfx_cosmology_amp_table(mfx_cosmology *c, uint32_t ngrid, double boxlen, double *table, size_t len);
+
+/* Whole-run driver: the equivalent of `monofonIC <config>` for the in-scope
+   path (ic_generator::run, ic_generator.cc:92-1181), writing through the
+   selected output plugin.  Returns MFX_OK on success. */
+int mfx_run_config(mfx_engine *eng, const char *ini_text);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFX_H */

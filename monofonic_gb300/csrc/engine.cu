@@ -1,0 +1,990 @@
+// GB300 engine for monofonIC's IC hot path: job arena, cuFFT plans, the stage
+// pipeline and the C ABI declared in include/mfx.h.
+//
+// Pipeline of one job (reference: ic_generator.cc:288-1060):
+//   noise -> phi1                               k_noise_phi1
+//   phi1 Hessians (6, padded M^3)              k_pad_hessian + 6 c2r
+//   phi2 source -> r2c -> unpad/invLap         k_src2, r2c, k_unpad_invlap
+//   phi3a: 5 pairwise products, each           k_mul, r2c, k_trunc_repad, c2r, k_acc3a
+//   phi2 Hessians (6)                          k_pad_hessian + 6 c2r
+//   phi3b + A3 sources                          k_src3
+//   4 x (r2c -> unpad/invLap)                   phi3, A3x, A3y, A3z
+//   assembly of all sub-lattices in k-space    k_assemble
+//   per sub-lattice: 6 c2r + particle read-out k_particles
+// Sums of convolve2 results that the reference unpads one by one are summed
+// in real space before a single forward transform (linearity of unpad); this
+// changes only rounding.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <time.h>
+#include <string>
+#include <vector>
+
+#include "../../include/mfx.h"
+#include "common.h"
+#include "kernels.cuh"
+
+namespace mfx {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+const char *cufft_name(cufftResult r) {
+  switch (r) {
+    case CUFFT_SUCCESS: return "CUFFT_SUCCESS";
+    case CUFFT_INVALID_PLAN: return "CUFFT_INVALID_PLAN";
+    case CUFFT_ALLOC_FAILED: return "CUFFT_ALLOC_FAILED";
+    case CUFFT_INVALID_VALUE: return "CUFFT_INVALID_VALUE";
+    case CUFFT_INTERNAL_ERROR: return "CUFFT_INTERNAL_ERROR";
+    case CUFFT_EXEC_FAILED: return "CUFFT_EXEC_FAILED";
+    case CUFFT_SETUP_FAILED: return "CUFFT_SETUP_FAILED";
+    case CUFFT_INVALID_SIZE: return "CUFFT_INVALID_SIZE";
+    default: return "CUFFT_ERROR";
+  }
+}
+
+#define CU(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return set_error(e_ == cudaErrorMemoryAllocation ? MFX_ENOMEM : MFX_ECUDA, "%s: %s (%s:%d)", \
+                       #call, cudaGetErrorString(e_), __FILE__, __LINE__);                        \
+  } while (0)
+#define CF(call)                                                                                        \
+  do {                                                                                                  \
+    cufftResult r_ = (call);                                                                            \
+    if (r_ != CUFFT_SUCCESS)                                                                            \
+      return set_error(r_ == CUFFT_ALLOC_FAILED ? MFX_ENOMEM : MFX_ECUDA, "%s: %s (%s:%d)", #call,        \
+                       cufft_name(r_), __FILE__, __LINE__);                                             \
+  } while (0)
+#define TRY(x)                 \
+  do {                         \
+    int rc_ = (x);             \
+    if (rc_ != MFX_OK) return rc_; \
+  } while (0)
+
+static size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
+
+int lattice_nshift(int lattice) { return 1 << lattice; }
+
+// particle_generator.hh:47-54
+static const double kShifts[3][4][3] = {
+    {{0, 0, 0}},
+    {{0, 0, 0}, {0.5, 0.5, 0.5}},
+    {{0, 0, 0}, {0.0, 0.5, 0.5}, {0.5, 0.0, 0.5}, {0.5, 0.5, 0.0}},
+};
+
+}  // namespace mfx
+
+using namespace mfx;
+
+struct mfx_engine {
+  int device = 0;
+  size_t budget = 0;
+  std::mutex mu;
+  size_t in_use = 0;
+};
+
+struct Plan {
+  cufftHandle h = 0;
+  size_t work = 0;
+  bool valid = false;
+};
+
+struct mfx_job {
+  mfx_engine *eng = nullptr;
+  mfx_job_desc d{};
+  int N = 0, M = 0, nh = 0, nk = 0, mk = 0, ns = 0, group = 0;
+  bool fp64 = true;
+  size_t rsize = 8;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[6] = {};
+  bool timed = false;
+  // arena
+  char *arena = nullptr;
+  size_t arena_bytes = 0;
+  size_t n_field_bytes = 0, m_field_bytes = 0;
+  // device pointers
+  uint32_t *seeds = nullptr;
+  double *amp = nullptr;
+  double *plt = nullptr;
+  double2 *phase = nullptr;
+  void *nf[6] = {};       // phi1, phi2, phi3, A3x, A3y, A3z
+  char *region = nullptr; // M-region / assembly union
+  size_t region_bytes = 0;
+  void *mslot[18] = {};
+  void *asmbuf[24] = {};
+  void *pos = nullptr, *vel = nullptr, *ids = nullptr;
+  void *work = nullptr;
+  size_t work_bytes = 0;
+  Plan m_r2c, m_c2r, n_c2r;
+  // accounting
+  int own_launches = 0, fft_execs = 0;
+  bool has_run = false, noise_only = false;
+  size_t npart = 0;
+  double scale1 = 1, scale2 = 1, scale3 = 1;  // per-field scales of the FP32 form
+  // per-launch profiling (events on the job stream + algorithmic bytes)
+  struct ProfRec {
+    const char *name;
+    double bytes;
+    cudaEvent_t a, b;
+  };
+  bool prof = false;
+  std::vector<ProfRec> prof_recs;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_next = 0;
+  cudaEvent_t pend = nullptr;
+  cudaEvent_t next_event() {
+    if (ev_next == ev_pool.size()) {
+      cudaEvent_t e = nullptr;
+      cudaEventCreate(&e);
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_next++];
+  }
+};
+
+int mfx::engine_device(const mfx_engine *eng) { return eng ? eng->device : 0; }
+
+// ---------------------------------------------------------------------------
+// sizes
+// ---------------------------------------------------------------------------
+struct Layout {
+  size_t seeds, amp, plt, phase, nfields, region, work_est, total;
+  size_t n_field, m_field, asm_bytes, part_bytes, mregion;
+  int nslots, group;
+};
+
+static size_t n_field_bytes(int N, size_t rs) { return size_t(N) * N * (N / 2 + 1) * 2 * rs; }
+
+static int check_desc(const mfx_job_desc *d) {
+  if (!d) return set_error(MFX_EINVAL, "null job descriptor");
+  if (d->ngrid < 8 || (d->ngrid % 4) != 0)
+    return set_error(MFX_EINVAL, "ngrid must be a multiple of 4 and >= 8 (got %u)", d->ngrid);
+  if (d->ngrid > 2048) return set_error(MFX_EINVAL, "ngrid %u above the supported maximum 2048", d->ngrid);
+  if (!(d->boxlen > 0)) return set_error(MFX_EINVAL, "boxlen must be positive");
+  if (d->lpt_order < 1 || d->lpt_order > 3) return set_error(MFX_EINVAL, "lpt_order must be 1, 2 or 3");
+  if (d->lattice < 0 || d->lattice > 2) return set_error(MFX_EINVAL, "lattice must be SC, BCC or FCC");
+  if (d->precision != MFX_FP64 && d->precision != MFX_FP32C) return set_error(MFX_EINVAL, "bad precision");
+  if (!d->seed_table) return set_error(MFX_EINVAL, "seed_table is required");
+  size_t need = 3 * size_t(d->ngrid / 2) * (d->ngrid / 2) + 1;
+  if (!d->amp_table || d->amp_table_len < need)
+    return set_error(MFX_EINVAL, "amp_table needs at least %zu entries", need);
+  if (d->plt && !d->plt_table) return set_error(MFX_EINVAL, "plt requested without plt_table");
+  return MFX_OK;
+}
+
+static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
+  Layout L{};
+  const int N = d->ngrid, M = 3 * N / 2;
+  const size_t rs = d->precision == MFX_FP64 ? 8 : 4;
+  const int ns = lattice_nshift(d->lattice);
+  L.n_field = n_field_bytes(N, rs);
+  L.m_field = size_t(M) * M * (M / 2 + 1) * 2 * rs;
+  L.seeds = align_up(size_t(N) * N * 4);
+  L.amp = align_up(d->amp_table_len * 8);
+  L.plt = d->plt ? align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 8) : 0;
+  L.phase = align_up(size_t(ns) * 3 * N * sizeof(double2));
+  const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
+  L.nfields = nfield * align_up(L.n_field);
+  L.nslots = d->lpt_order == 1 ? 0 : (d->lpt_order == 2 ? 7 : (rs == 4 ? 18 : 17));
+  L.mregion = size_t(L.nslots) * align_up(L.m_field);
+  const size_t np = size_t(ns) * N * N * N;
+  L.part_bytes = 0;
+  if (d->want_particles) {
+    L.part_bytes = align_up(np * 3 * (d->pos64 ? 8 : 4)) + align_up(np * 3 * (d->vel64 ? 8 : 4)) +
+                   align_up(np * (d->id64 ? 8 : 4));
+  }
+  // all sub-lattices assembled in one pass when it fits beside the particles
+  // in the region the padded fields leave behind, else one at a time
+  int group = ns;
+  if (d->want_particles) {
+    size_t full = L.part_bytes + size_t(6 * ns) * align_up(L.n_field);
+    if (L.mregion > 0 && full > L.mregion) group = 1;
+  }
+  L.group = group;
+  L.asm_bytes = d->want_particles ? L.part_bytes + size_t(6 * group) * align_up(L.n_field) : 0;
+  L.region = std::max(L.mregion, L.asm_bytes);
+  L.work_est = align_up(work_bytes);
+  L.total = L.seeds + L.amp + L.plt + L.phase + L.nfields + L.region + L.work_est;
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// cuFFT plans (in-place, padded rows as in the reference's Grid_FFT)
+// ---------------------------------------------------------------------------
+static int make_plan(Plan &p, int n, bool fp64, bool r2c) {
+  CF(cufftCreate(&p.h));
+  CF(cufftSetAutoAllocation(p.h, 0));
+  long long dims[3] = {n, n, n};
+  long long rembed[3] = {n, n, n + 2};
+  long long cembed[3] = {n, n, n / 2 + 1};
+  long long rdist = (long long)n * n * (n + 2), cdist = (long long)n * n * (n / 2 + 1);
+  cufftType t = fp64 ? (r2c ? CUFFT_D2Z : CUFFT_Z2D) : (r2c ? CUFFT_R2C : CUFFT_C2R);
+  size_t ws = 0;
+  if (r2c)
+    CF(cufftMakePlanMany64(p.h, 3, dims, rembed, 1, rdist, cembed, 1, cdist, t, 1, &ws));
+  else
+    CF(cufftMakePlanMany64(p.h, 3, dims, cembed, 1, cdist, rembed, 1, rdist, t, 1, &ws));
+  p.work = ws;
+  p.valid = true;
+  return MFX_OK;
+}
+
+static void destroy_plan(Plan &p) {
+  if (p.valid) cufftDestroy(p.h);
+  p.valid = false;
+}
+
+static void kbegin(mfx_job *j);
+static void kend_prof(mfx_job *j, const char *name, double bytes);
+
+static int exec_fft(mfx_job *j, Plan &p, void *buf, bool r2c) {
+  kbegin(j);
+  if (j->fp64) {
+    if (r2c) CF(cufftExecD2Z(p.h, (cufftDoubleReal *)buf, (cufftDoubleComplex *)buf));
+    else CF(cufftExecZ2D(p.h, (cufftDoubleComplex *)buf, (cufftDoubleReal *)buf));
+  } else {
+    if (r2c) CF(cufftExecR2C(p.h, (cufftReal *)buf, (cufftComplex *)buf));
+    else CF(cufftExecC2R(p.h, (cufftComplex *)buf, (cufftReal *)buf));
+  }
+  j->fft_execs++;
+  const bool m = (&p != &j->n_c2r);
+  kend_prof(j, m ? (r2c ? "cufft_r2c_M" : "cufft_c2r_M") : "cufft_c2r_N",
+            2.0 * double(m ? j->m_field_bytes : j->n_field_bytes));
+  return MFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+static unsigned grid_for(size_t n, int block, int num_sm) {
+  size_t b = (n + block - 1) / block;
+  size_t cap = size_t(num_sm) * 16;  // grid-stride beyond 16 resident blocks / SM
+  return unsigned(std::max<size_t>(1, std::min(b, cap)));
+}
+
+static int g_num_sm = 0;
+static int num_sm() {
+  if (!g_num_sm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sm, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sm <= 0) g_num_sm = 148;
+  }
+  return g_num_sm;
+}
+
+// KBEGIN / KEND bracket every launch: launch-error check, launch count and,
+// when profiling is on, events on the job stream plus the launch's
+// algorithmic byte count (each distinct input read once, each output written once).
+static void kbegin(mfx_job *j) {
+  j->pend = nullptr;
+  if (j->prof) {
+    j->pend = j->next_event();
+    cudaEventRecord(j->pend, j->stream);
+  }
+}
+static void kend_prof(mfx_job *j, const char *name, double bytes) {
+  if (j->prof && j->pend) {
+    cudaEvent_t b = j->next_event();
+    cudaEventRecord(b, j->stream);
+    j->prof_recs.push_back({name, bytes, j->pend, b});
+  }
+  j->pend = nullptr;
+}
+#define KBEGIN(j) kbegin(j)
+#define KEND(j, name, bytes)                                                                       \
+  do {                                                                                             \
+    cudaError_t e_ = cudaGetLastError();                                                           \
+    if (e_ != cudaSuccess)                                                                         \
+      return set_error(MFX_ECUDA, "kernel launch: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, __LINE__); \
+    (j)->own_launches++;                                                                           \
+    kend_prof((j), (name), double(bytes));                                                         \
+  } while (0)
+
+template <typename R> static int launch_noise(mfx_job *j, int mode, void *out) {
+  NoiseArgs a;
+  a.seeds = j->seeds;
+  a.amp = j->amp;
+  a.amp_len = j->d.amp_table_len;
+  a.N = j->N;
+  a.mode = mode;
+  a.fixing = j->d.fixing;
+  const double volfac = std::pow(j->d.boxlen / j->N / 2.0 / M_PI, 1.5);
+  a.norm = (j->d.inversion ? -1.0 : 1.0) / volfac;
+  a.out_scale = j->scale1;
+  const int cols = j->N * j->N;
+  KBEGIN(j);
+  k_noise_phi1<R><<<(cols + 127) / 128, 128, 0, j->stream>>>(a, (typename Cplx<R>::T *)out);
+  KEND(j, "noise_phi1", j->n_field_bytes + 4.0 * cols + 8.0 * j->d.amp_table_len);
+  return MFX_OK;
+}
+
+static const int8_t kHa[6] = {0, 1, 2, 0, 0, 1};
+static const int8_t kHb[6] = {0, 1, 2, 1, 2, 2};
+
+template <typename R> static int hessians(mfx_job *j, const void *phi, void **out) {
+  PadArgs a;
+  a.phi = phi;
+  for (int c = 0; c < 6; ++c) {
+    a.out[c] = out[c];
+    a.ca[c] = kHa[c];
+    a.cb[c] = kHb[c];
+  }
+  a.ncomp = 6;
+  a.N = j->N;
+  a.M = j->M;
+  a.kfac = 2.0 * M_PI / j->d.boxlen;
+  const double M3 = double(j->M) * j->M * j->M;
+  a.fac = std::pow(1.5, 1.5) / std::sqrt(M3);
+  const size_t total = size_t(j->M) * j->M * j->mk;
+  KBEGIN(j);
+  k_pad_hessian<R><<<grid_for(total, 256, num_sm()), 256, 0, j->stream>>>(a);
+  KEND(j, "pad_hessian", j->n_field_bytes + 6.0 * j->m_field_bytes);
+  for (int c = 0; c < 6; ++c) TRY(exec_fft(j, j->m_c2r, out[c], false));
+  return MFX_OK;
+}
+
+template <typename R> static int unpad_invlap(mfx_job *j, void *F, void *out) {
+  TRY(exec_fft(j, j->m_r2c, F, true));
+  UnpadArgs a;
+  a.F = F;
+  a.out = out;
+  a.N = j->N;
+  a.M = j->M;
+  a.kfac = 2.0 * M_PI / j->d.boxlen;
+  const double M3 = double(j->M) * j->M * j->M, N3 = double(j->N) * j->N * j->N;
+  const double rfac_u = std::sqrt(M3) / std::sqrt(N3);
+  a.fac = 1.0 / std::sqrt(M3) / rfac_u;
+  const size_t total = size_t(j->N) * j->N * j->nk;
+  KBEGIN(j);
+  k_unpad_invlap<R><<<grid_for(total, 256, num_sm()), 256, 0, j->stream>>>(a);
+  KEND(j, "unpad_invlap", 2.0 * j->n_field_bytes);
+  return MFX_OK;
+}
+
+template <typename R> static int run_pipeline(mfx_job *j) {
+  const int order = j->d.lpt_order;
+  const size_t mreal = size_t(j->M) * j->M * (j->M + 2);
+  const int nsm = num_sm();
+  j->own_launches = 0;
+  j->fft_execs = 0;
+  j->prof_recs.clear();
+  j->ev_next = 0;
+  if (j->timed) CU(cudaEventRecord(j->ev[0], j->stream));
+  TRY(launch_noise<R>(j, 2, j->nf[0]));
+  if (j->timed) CU(cudaEventRecord(j->ev[1], j->stream));
+  void **H1 = &j->mslot[0];
+  if (order >= 2) {
+    TRY(hessians<R>(j, j->nf[0], H1));
+    SrcArgs s{};
+    for (int c = 0; c < 6; ++c) s.h1[c] = H1[c];
+    s.out[0] = j->mslot[6];
+    s.count = mreal;
+    KBEGIN(j);
+    k_src2<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(s);
+    KEND(j, "src2", 7.0 * j->m_field_bytes);
+    TRY(unpad_invlap<R>(j, j->mslot[6], j->nf[1]));
+  }
+  if (j->timed) CU(cudaEventRecord(j->ev[2], j->stream));
+  if (order >= 3) {
+    // phi3a: pairwise dealiased triple products (ic_generator.cc:577-586)
+    struct Tri { int a, b, c; double coef; };
+    const Tri tri[5] = {{0, 1, 2, 1.0}, {3, 4, 5, 2.0}, {5, 5, 0, -1.0}, {4, 4, 1, -1.0}, {3, 3, 2, -1.0}};
+    void *T = j->mslot[6], *hi = j->mslot[7];
+    void *lo = j->fp64 ? nullptr : j->mslot[17];
+    const double M3 = double(j->M) * j->M * j->M, N3 = double(j->N) * j->N * j->N;
+    const double rfac_u = std::sqrt(M3) / std::sqrt(N3), rfac_p = std::pow(1.5, 1.5);
+    for (int t = 0; t < 5; ++t) {
+      SrcArgs s{};
+      s.h1[0] = H1[tri[t].a];
+      s.h1[1] = H1[tri[t].b];
+      s.out[0] = T;
+      s.count = mreal;
+      KBEGIN(j);
+      k_mul<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(s);
+      KEND(j, "mul_pair", 3.0 * j->m_field_bytes);
+      TRY(exec_fft(j, j->m_r2c, T, true));
+      TruncArgs ta;
+      ta.F = T;
+      ta.N = j->N;
+      ta.M = j->M;
+      ta.fac = (1.0 / std::sqrt(M3) / rfac_u) * rfac_p / std::sqrt(M3);
+      KBEGIN(j);
+      k_trunc_repad<R><<<grid_for(size_t(j->M) * j->M * j->mk, 256, nsm), 256, 0, j->stream>>>(ta);
+      KEND(j, "trunc_repad", 2.0 * j->m_field_bytes);
+      TRY(exec_fft(j, j->m_c2r, T, false));
+      SrcArgs u{};
+      u.t = T;
+      u.third = H1[tri[t].c];
+      u.hi = hi;
+      u.lo = lo;
+      u.coef = tri[t].coef;
+      u.init = (t == 0);
+      u.count = mreal;
+      KBEGIN(j);
+      k_acc3a<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(u);
+      KEND(j, "acc3a", (u.init ? 3.0 : 4.0) * j->m_field_bytes + (lo ? (u.init ? 1.0 : 2.0) : 0.0) * j->m_field_bytes);
+    }
+    // phi2 Hessians, then phi3b and A3 sources in one pass
+    void **H2 = &j->mslot[11];
+    TRY(hessians<R>(j, j->nf[1], H2));
+    SrcArgs s{};
+    for (int c = 0; c < 6; ++c) {
+      s.h1[c] = H1[c];
+      s.h2[c] = H2[c];
+    }
+    s.hi = hi;
+    s.lo = lo;
+    s.out[0] = hi;
+    s.out[1] = j->mslot[8];
+    s.out[2] = j->mslot[9];
+    s.out[3] = j->mslot[10];
+    s.count = mreal;
+    KBEGIN(j);
+    k_src3<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(s);
+    KEND(j, "src3", (lo ? 18.0 : 17.0) * j->m_field_bytes);
+    TRY(unpad_invlap<R>(j, hi, j->nf[2]));
+    for (int d = 0; d < 3; ++d) TRY(unpad_invlap<R>(j, j->mslot[8 + d], j->nf[3 + d]));
+  }
+  if (j->timed) CU(cudaEventRecord(j->ev[3], j->stream));
+  if (j->d.want_particles) {
+    const int N = j->N;
+    const double N3 = double(N) * N * N;
+    AsmArgs a{};
+    for (int q = 0; q < 3; ++q) {
+      a.phi[q] = j->nf[q];
+      a.A3[q] = j->nf[3 + q];
+    }
+    a.plt = j->d.plt ? j->plt : nullptr;
+    a.phase = j->phase;
+    a.N = N;
+    a.order = order;
+    a.kfac = 2.0 * M_PI / j->d.boxlen;
+    a.mapratio = double(MFX_PLT_NGRID) / double(N);
+    a.boxlen = j->d.boxlen;
+    a.g1 = j->d.g1;
+    a.g2 = j->d.g2;
+    a.g3 = j->d.g3;
+    a.g3c = j->d.g3c;
+    a.vfac1 = j->d.vfac1;
+    a.vfac2 = j->d.vfac2;
+    a.vfac3 = j->d.vfac3;
+    a.pfac = j->d.lunit / j->d.boxlen / std::sqrt(N3);
+    a.vfac = j->d.vunit / j->d.boxlen / std::sqrt(N3);
+    a.in_scale1 = 1.0 / j->scale1;
+    a.in_scale2 = 1.0 / j->scale2;
+    a.in_scale3 = 1.0 / j->scale3;
+    const size_t total = size_t(N) * N * j->nk;
+    for (int s0 = 0; s0 < j->ns; s0 += j->group) {
+      const int g = std::min(j->group, j->ns - s0);
+      a.shift0 = s0;
+      a.nshift = g;
+      for (int q = 0; q < 6 * g; ++q) a.out[q] = j->asmbuf[q];
+      KBEGIN(j);
+      if (a.plt) k_assemble<R, true><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(a);
+      else k_assemble<R, false><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(a);
+      KEND(j, "assemble", ((order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) + 6.0 * g) * j->n_field_bytes);
+      for (int s = 0; s < g; ++s) {
+        for (int q = 0; q < 6; ++q) TRY(exec_fft(j, j->n_c2r, j->asmbuf[s * 6 + q], false));
+        PartArgs p{};
+        for (int q = 0; q < 6; ++q) p.f[q] = j->asmbuf[s * 6 + q];
+        p.pos = j->pos;
+        p.vel = j->vel;
+        p.ids = j->ids;
+        p.N = N;
+        p.nshift_total = j->ns;
+        p.ishift = s0 + s;
+        p.pos64 = j->d.pos64;
+        p.vel64 = j->d.vel64;
+        p.id64 = j->d.id64;
+        p.sx = kShifts[j->d.lattice][s0 + s][0];
+        p.sy = kShifts[j->d.lattice][s0 + s][1];
+        p.sz = kShifts[j->d.lattice][s0 + s][2];
+        p.lunit = j->d.lunit;
+        p.id_offset = j->d.id_offset * uint64_t(j->ns) * uint64_t(N3);
+        KBEGIN(j);
+        k_particles<R><<<grid_for(size_t(N) * N * N, 256, nsm), 256, 0, j->stream>>>(p);
+        KEND(j, "particles", N3 * (6.0 * j->rsize + 3.0 * (p.pos64 ? 8 : 4) + 3.0 * (p.vel64 ? 8 : 4) + (p.id64 ? 8 : 4)));
+      }
+    }
+  }
+  if (j->timed) CU(cudaEventRecord(j->ev[4], j->stream));
+  j->has_run = true;
+  j->noise_only = false;
+  return MFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// job set-up
+// ---------------------------------------------------------------------------
+static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
+  const int N = j->N;
+  CU(cudaMemcpyAsync(j->seeds, d->seed_table, size_t(N) * N * 4, cudaMemcpyHostToDevice, j->stream));
+  CU(cudaMemcpyAsync(j->amp, d->amp_table, d->amp_table_len * 8, cudaMemcpyHostToDevice, j->stream));
+  if (d->plt)
+    CU(cudaMemcpyAsync(j->plt, d->plt_table, size_t(MFX_PLT_TABLE_DOUBLES) * 8, cudaMemcpyHostToDevice,
+                       j->stream));
+  return MFX_OK;
+}
+
+static void free_job(mfx_job *j) {
+  if (!j) return;
+  if (j->stream) cudaStreamSynchronize(j->stream);
+  destroy_plan(j->m_r2c);
+  destroy_plan(j->m_c2r);
+  destroy_plan(j->n_c2r);
+  if (j->arena) cudaFree(j->arena);
+  for (auto &e : j->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : j->ev_pool)
+    if (e) cudaEventDestroy(e);
+  if (j->stream) cudaStreamDestroy(j->stream);
+  if (j->eng) {
+    std::lock_guard<std::mutex> lk(j->eng->mu);
+    j->eng->in_use -= std::min(j->eng->in_use, j->arena_bytes);
+  }
+  delete j;
+}
+
+static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
+  TRY(check_desc(d));
+  CU(cudaSetDevice(eng->device));
+  auto *j = new mfx_job();
+  j->eng = eng;
+  j->d = *d;
+  j->N = d->ngrid;
+  j->M = 3 * j->N / 2;
+  j->nh = j->N / 2;
+  j->nk = j->nh + 1;
+  j->mk = j->M / 2 + 1;
+  j->ns = lattice_nshift(d->lattice);
+  j->fp64 = d->precision == MFX_FP64;
+  j->rsize = j->fp64 ? 8 : 4;
+  // per-field scaling of the FP32 form: carry phi(1) as the growth-scaled
+  // potential D+ phi so that Hessians are O(delta) and products stay far from
+  // the FP32 exponent limits; phi2 / phi3 inherit the square / cube.
+  if (!j->fp64) {
+    const double s = std::fabs(d->g1) > 0 ? std::fabs(d->g1) : 1.0;
+    j->scale1 = s;
+    j->scale2 = s * s;
+    j->scale3 = s * s * s;
+  }
+  int rc = MFX_OK;
+  auto fail = [&](int code) {
+    free_job(j);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_error(MFX_ECUDA, "cudaStreamCreate failed"));
+  for (auto &e : j->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(MFX_ECUDA, "cudaEventCreate failed"));
+  j->timed = true;
+  // plans
+  size_t work = 0;
+  if (d->lpt_order >= 2) {
+    if ((rc = make_plan(j->m_r2c, j->M, j->fp64, true)) != MFX_OK) return fail(rc);
+    if ((rc = make_plan(j->m_c2r, j->M, j->fp64, false)) != MFX_OK) return fail(rc);
+    work = std::max(work, std::max(j->m_r2c.work, j->m_c2r.work));
+  }
+  if (d->want_particles) {
+    if ((rc = make_plan(j->n_c2r, j->N, j->fp64, false)) != MFX_OK) return fail(rc);
+    work = std::max(work, j->n_c2r.work);
+  }
+  Layout L = plan_layout(d, work);
+  {
+    std::lock_guard<std::mutex> lk(eng->mu);
+    if (eng->in_use + L.total > eng->budget)
+      return fail(set_error(MFX_EADMIT, "job needs %zu bytes, engine budget has %zu of %zu free", L.total,
+                            eng->budget - std::min(eng->budget, eng->in_use), eng->budget));
+    eng->in_use += L.total;
+  }
+  j->arena_bytes = L.total;
+  cudaError_t e = cudaMalloc(&j->arena, L.total);
+  if (e != cudaSuccess) {
+    j->arena = nullptr;
+    return fail(set_error(MFX_ENOMEM, "cudaMalloc(%zu) for the job arena failed: %s", L.total,
+                          cudaGetErrorString(e)));
+  }
+  char *p = j->arena;
+  j->seeds = (uint32_t *)p;
+  p += L.seeds;
+  j->amp = (double *)p;
+  p += L.amp;
+  j->plt = d->plt ? (double *)p : nullptr;
+  p += L.plt;
+  j->phase = (double2 *)p;
+  p += L.phase;
+  const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
+  j->n_field_bytes = L.n_field;
+  j->m_field_bytes = L.m_field;
+  for (int q = 0; q < nfield; ++q) {
+    j->nf[q] = p;
+    p += align_up(L.n_field);
+  }
+  j->region = p;
+  j->region_bytes = L.region;
+  p += L.region;
+  j->work = L.work_est ? p : nullptr;
+  j->work_bytes = L.work_est;
+  for (int q = 0; q < L.nslots; ++q) j->mslot[q] = j->region + size_t(q) * align_up(L.m_field);
+  j->group = L.group;
+  if (d->want_particles) {
+    char *a = j->region;
+    const size_t np = size_t(j->ns) * j->N * j->N * j->N;
+    j->npart = np;
+    j->pos = a;
+    a += align_up(np * 3 * (d->pos64 ? 8 : 4));
+    j->vel = a;
+    a += align_up(np * 3 * (d->vel64 ? 8 : 4));
+    j->ids = a;
+    a += align_up(np * (d->id64 ? 8 : 4));
+    for (int q = 0; q < 6 * j->group; ++q) {
+      j->asmbuf[q] = a;
+      a += align_up(L.n_field);
+    }
+  }
+  if (j->work) {
+    if (j->m_r2c.valid && cufftSetWorkArea(j->m_r2c.h, j->work) != CUFFT_SUCCESS)
+      return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
+    if (j->m_c2r.valid && cufftSetWorkArea(j->m_c2r.h, j->work) != CUFFT_SUCCESS)
+      return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
+    if (j->n_c2r.valid && cufftSetWorkArea(j->n_c2r.h, j->work) != CUFFT_SUCCESS)
+      return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
+  }
+  for (Plan *pl : {&j->m_r2c, &j->m_c2r, &j->n_c2r})
+    if (pl->valid && cufftSetStream(pl->h, j->stream) != CUFFT_SUCCESS)
+      return fail(set_error(MFX_ECUDA, "cufftSetStream failed"));
+  // phase tables exp(i s_a k_a dx) per sub-lattice and axis (grid_fft.hh:836-839)
+  {
+    const int N = j->N;
+    std::vector<double2> ph(size_t(j->ns) * 3 * N);
+    const double kfac = 2.0 * M_PI / d->boxlen, dx = d->boxlen / N;
+    for (int s = 0; s < j->ns; ++s)
+      for (int ax = 0; ax < 3; ++ax)
+        for (int m = 0; m < N; ++m) {
+          const double km = (double(m) - double(m > N / 2) * N) * kfac;
+          const double th = kShifts[d->lattice][s][ax] * km * dx;
+          ph[(size_t(s) * 3 + ax) * N + m] = make_double2(std::cos(th), std::sin(th));
+        }
+    if (cudaMemcpyAsync(j->phase, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, j->stream) !=
+        cudaSuccess)
+      return fail(set_error(MFX_ECUDA, "phase table upload failed"));
+    if (cudaStreamSynchronize(j->stream) != cudaSuccess)
+      return fail(set_error(MFX_ECUDA, "phase table upload failed"));
+  }
+  if ((rc = upload_tables(j, d)) != MFX_OK) return fail(rc);
+  if (cudaStreamSynchronize(j->stream) != cudaSuccess) return fail(set_error(MFX_ECUDA, "table upload failed"));
+  *out = j;
+  return MFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+#define GUARD_BEGIN try {
+#define GUARD_END                                                       \
+  }                                                                     \
+  catch (const std::bad_alloc &) {                                      \
+    return set_error(MFX_ENOMEM, "host allocation failed");             \
+  }                                                                     \
+  catch (const std::exception &ex) {                                    \
+    return set_error(MFX_EINVAL, "%s", ex.what());                      \
+  }                                                                     \
+  catch (...) {                                                         \
+    return set_error(MFX_EINVAL, "unknown C++ exception");              \
+  }
+
+extern "C" {
+
+size_t mfx_last_error(char *buf, size_t len) {
+  const std::string &s = g_last_error;
+  if (buf && len) {
+    size_t n = std::min(len - 1, s.size());
+    memcpy(buf, s.data(), n);
+    buf[n] = 0;
+  }
+  return s.size();
+}
+
+const char *mfx_version(void) { return "mfx 0.1 (sm_103a)"; }
+
+int mfx_engine_create(const mfx_engine_opts *opts, mfx_engine **out) {
+  GUARD_BEGIN
+  if (!out) return set_error(MFX_EINVAL, "null output pointer");
+  int dev = opts ? opts->device : 0;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+    return set_error(MFX_ECUDA, "no CUDA device available");
+  if (dev < 0 || dev >= count) return set_error(MFX_EINVAL, "device %d out of range", dev);
+  CU(cudaSetDevice(dev));
+  size_t free_b = 0, total_b = 0;
+  CU(cudaMemGetInfo(&free_b, &total_b));
+  auto *e = new mfx_engine();
+  e->device = dev;
+  e->budget = (opts && opts->hbm_budget_bytes) ? opts->hbm_budget_bytes : size_t(double(free_b) * 0.9);
+  *out = e;
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_engine_destroy(mfx_engine *eng) {
+  delete eng;
+  return MFX_OK;
+}
+
+int mfx_job_footprint(mfx_engine *eng, const mfx_job_desc *desc, size_t *bytes) {
+  GUARD_BEGIN
+  TRY(check_desc(desc));
+  if (!bytes) return set_error(MFX_EINVAL, "null output");
+  // FFT work areas are bounded by the largest transform's data size
+  const int M = 3 * desc->ngrid / 2;
+  const size_t rs = desc->precision == MFX_FP64 ? 8 : 4;
+  const size_t work = desc->lpt_order >= 2 ? size_t(M) * M * (M / 2 + 1) * 2 * rs
+                                           : n_field_bytes(desc->ngrid, rs);
+  *bytes = plan_layout(desc, work).total;
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_create(mfx_engine *eng, const mfx_job_desc *desc, mfx_job **out) {
+  GUARD_BEGIN
+  if (!eng || !out) return set_error(MFX_EINVAL, "null argument");
+  return create_job(eng, desc, out);
+  GUARD_END
+}
+
+int mfx_job_upload(mfx_job *job, const mfx_job_desc *desc) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  TRY(check_desc(desc));
+  if (desc->ngrid != job->d.ngrid || desc->amp_table_len != job->d.amp_table_len || desc->plt != job->d.plt)
+    return set_error(MFX_EINVAL, "upload descriptor does not match the job's sizes");
+  job->d.seed_table = desc->seed_table;
+  job->d.amp_table = desc->amp_table;
+  job->d.plt_table = desc->plt_table;
+  return upload_tables(job, desc);
+  GUARD_END
+}
+
+int mfx_job_run(mfx_job *job) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  CU(cudaSetDevice(job->eng->device));
+  return job->fp64 ? run_pipeline<double>(job) : run_pipeline<float>(job);
+  GUARD_END
+}
+
+int mfx_job_run_noise(mfx_job *job, int raw) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  CU(cudaSetDevice(job->eng->device));
+  job->own_launches = 0;
+  int rc = job->fp64 ? launch_noise<double>(job, raw ? 0 : 1, job->nf[0])
+                     : launch_noise<float>(job, raw ? 0 : 1, job->nf[0]);
+  if (rc == MFX_OK) {
+    job->noise_only = true;
+    job->has_run = true;
+  }
+  return rc;
+  GUARD_END
+}
+
+int mfx_job_wait(mfx_job *job, int timeout_ms) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (timeout_ms < 0) {
+    CU(cudaStreamSynchronize(job->stream));
+    return MFX_OK;
+  }
+  // bounded host-side poll; the device work itself never waits
+  for (int waited = 0;; ++waited) {
+    cudaError_t e = cudaStreamQuery(job->stream);
+    if (e == cudaSuccess) return MFX_OK;
+    if (e != cudaErrorNotReady) return set_error(MFX_ECUDA, "job stream: %s", cudaGetErrorString(e));
+    if (waited >= timeout_ms) return set_error(MFX_ETIMEOUT, "job not finished after %d ms", timeout_ms);
+    struct timespec ts = {0, 1000000};
+    nanosleep(&ts, nullptr);
+  }
+  GUARD_END
+}
+
+int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
+  if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has not produced particles");
+  const size_t np = job->npart;
+  if (pos) CU(cudaMemcpyAsync(pos, job->pos, np * 3 * (job->d.pos64 ? 8 : 4), cudaMemcpyDefault, job->stream));
+  if (vel) CU(cudaMemcpyAsync(vel, job->vel, np * 3 * (job->d.vel64 ? 8 : 4), cudaMemcpyDefault, job->stream));
+  if (ids) CU(cudaMemcpyAsync(ids, job->ids, np * (job->d.id64 ? 8 : 4), cudaMemcpyDefault, job->stream));
+  CU(cudaStreamSynchronize(job->stream));
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_particles_device(mfx_job *job, const void **pos, const void **vel, const void **ids, size_t *np) {
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (pos) *pos = job->pos;
+  if (vel) *vel = job->vel;
+  if (ids) *ids = job->ids;
+  if (np) *np = job->npart;
+  return MFX_OK;
+}
+
+int mfx_job_fetch_field(mfx_job *job, int field_id, double *out) {
+  GUARD_BEGIN
+  if (!job || !out) return set_error(MFX_EINVAL, "null argument");
+  if (!job->has_run) return set_error(MFX_ESTATE, "job has not run");
+  int slot = -1;
+  double scale = 1.0;
+  switch (field_id) {
+    case MFX_FIELD_NOISE:
+      if (!job->noise_only) return set_error(MFX_ESTATE, "noise is only kept after mfx_job_run_noise");
+      slot = 0;
+      break;
+    case MFX_FIELD_PHI1: slot = 0; scale = 1.0 / job->scale1; break;
+    case MFX_FIELD_PHI2: slot = 1; scale = 1.0 / job->scale2; break;
+    case MFX_FIELD_PHI3: slot = 2; scale = 1.0 / job->scale3; break;
+    case MFX_FIELD_A3X: slot = 3; scale = 1.0 / job->scale3; break;
+    case MFX_FIELD_A3Y: slot = 4; scale = 1.0 / job->scale3; break;
+    case MFX_FIELD_A3Z: slot = 5; scale = 1.0 / job->scale3; break;
+    default: return set_error(MFX_EINVAL, "unknown field id %d", field_id);
+  }
+  if (field_id != MFX_FIELD_NOISE && job->noise_only) return set_error(MFX_ESTATE, "only the noise was run");
+  if (!job->nf[slot]) return set_error(MFX_EINVAL, "field %d not computed at LPT order %d", field_id, job->d.lpt_order);
+  const size_t nc = size_t(job->N) * job->N * job->nk;
+  CU(cudaStreamSynchronize(job->stream));
+  if (job->fp64) {
+    CU(cudaMemcpy(out, job->nf[slot], nc * 16, cudaMemcpyDeviceToHost));
+    if (scale != 1.0)
+      for (size_t q = 0; q < 2 * nc; ++q) out[q] *= scale;
+  } else {
+    std::vector<float> tmp(2 * nc);
+    CU(cudaMemcpy(tmp.data(), job->nf[slot], nc * 8, cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < 2 * nc; ++q) out[q] = double(tmp[q]) * scale;
+  }
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_stage_times(mfx_job *job, double *ms, int max_stages) {
+  if (!job || !ms) return set_error(MFX_EINVAL, "null argument");
+  if (!job->has_run || job->noise_only) return 0;
+  if (cudaStreamSynchronize(job->stream) != cudaSuccess) return set_error(MFX_ECUDA, "sync failed");
+  int n = 0;
+  for (int s = 0; s < 4 && n < max_stages; ++s) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, job->ev[s], job->ev[s + 1]) != cudaSuccess) t = 0;
+    ms[n++] = t;
+  }
+  return n;
+}
+
+int mfx_job_algorithmic_bytes(mfx_job *job, double *bytes) {
+  if (!job || !bytes) return set_error(MFX_EINVAL, "null argument");
+  // ideal-fused stage model: each stage reads each distinct input once and
+  // writes each output once; FFTs count only their callback inputs/outputs.
+  const double s = double(job->rsize);
+  const double N3 = double(job->N) * job->N * job->N, M3 = double(job->M) * job->M * job->M;
+  const double F = s * N3, P = s * M3;
+  double b = F;  // phi1
+  if (job->d.lpt_order == 2) b += 12 * P + 7 * F;
+  if (job->d.lpt_order == 3) b += 57 * P + 25 * F;
+  if (job->d.want_particles) {
+    const int npot = job->d.lpt_order == 1 ? 1 : (job->d.lpt_order == 2 ? 2 : 6);
+    const double pos_b = job->d.pos64 ? 8 : 4, vel_b = job->d.vel64 ? 8 : 4;
+    b += npot * F + job->ns * (6 * F + 3 * pos_b * N3 + 3 * vel_b * N3 + (job->d.id64 ? 8 : 4) * N3);
+  }
+  *bytes = b;
+  return MFX_OK;
+}
+
+int mfx_job_launch_count(mfx_job *job, int *own, int *ffts) {
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (own) *own = job->own_launches;
+  if (ffts) *ffts = job->fft_execs;
+  return MFX_OK;
+}
+
+int mfx_job_set_profiling(mfx_job *job, int on) {
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  job->prof = on != 0;
+  return MFX_OK;
+}
+
+int mfx_job_kernel_profile(mfx_job *job, int max_entries, char *names, double *ms, double *bytes, int *launches) {
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (cudaStreamSynchronize(job->stream) != cudaSuccess) return set_error(MFX_ECUDA, "sync failed");
+  std::vector<std::string> keys;
+  std::vector<double> t, b;
+  std::vector<int> c;
+  for (const auto &r : job->prof_recs) {
+    float e = 0;
+    if (cudaEventElapsedTime(&e, r.a, r.b) != cudaSuccess) e = 0;
+    size_t q = 0;
+    while (q < keys.size() && keys[q] != r.name) ++q;
+    if (q == keys.size()) {
+      keys.push_back(r.name);
+      t.push_back(0);
+      b.push_back(0);
+      c.push_back(0);
+    }
+    t[q] += e;
+    b[q] += r.bytes;
+    c[q] += 1;
+  }
+  const int n = int(keys.size());
+  for (int q = 0; q < n && q < max_entries; ++q) {
+    if (names) {
+      std::strncpy(names + 32 * q, keys[q].c_str(), 31);
+      names[32 * q + 31] = 0;
+    }
+    if (ms) ms[q] = t[q];
+    if (bytes) bytes[q] = b[q];
+    if (launches) launches[q] = c[q];
+  }
+  return n;
+}
+
+int mfx_job_destroy(mfx_job *job) {
+  free_job(job);
+  return MFX_OK;
+}
+
+int mfx_debug_ranlxd1_words(mfx_engine *eng, unsigned long seed, size_t count, uint64_t *out) {
+  GUARD_BEGIN
+  if (!eng || !out) return set_error(MFX_EINVAL, "null argument");
+  if (seed >= 0x80000000UL) return set_error(MFX_EINVAL, "device seeding takes seeds below 2^31");
+  CU(cudaSetDevice(eng->device));
+  uint64_t *d = nullptr;
+  CU(cudaMalloc(&d, count * 8));
+  k_ranlux_words<<<1, 1>>>(uint32_t(seed), count, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, count * 8, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return set_error(MFX_ECUDA, "ranlux words: %s", cudaGetErrorString(e));
+  return MFX_OK;
+  GUARD_END
+}
+
+}  // extern "C"

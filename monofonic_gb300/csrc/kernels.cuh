@@ -1,0 +1,591 @@
+// Device kernels of the LPT hot path.  Every kernel is templated on the real
+// type R (double: the reference's plain FP64 algorithm; float: the FP32 form).
+//
+// Memory layout (identical to the reference's non-distributed Grid_FFT,
+// grid_fft.cc:40-112): a real field of size n^3 is stored with rows padded to
+// n+2 reals; the same buffer holds the k-space field as n x n x (n/2+1)
+// complex values, kelem(i,j,k) = c[(i*n + j)*(n/2+1) + k].  N-grid fields are
+// the LPT potentials, M-grid (M = 3N/2) fields the Orszag-padded products.
+// FFTs are unnormalised cuFFT transforms; the unitary 1/sqrt(n^3) of the
+// reference (grid_fft.cc:69, 199-270) is folded into the kernel before or
+// after each transform.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ranlxd.cuh"
+
+namespace mfx {
+
+template <typename R> struct Cplx;
+template <> struct Cplx<double> { using T = double2; };
+template <> struct Cplx<float> { using T = float2; };
+
+template <typename R> __device__ __forceinline__ typename Cplx<R>::T mkc(R re, R im) {
+  typename Cplx<R>::T c;
+  c.x = re;
+  c.y = im;
+  return c;
+}
+
+// signed mode index: get_k's i > n/2 -> i - n (grid_fft.hh:281-296)
+__device__ __forceinline__ int signed_idx(int i, int n) { return i > (n >> 1) ? i - n : i; }
+
+// ---------------------------------------------------------------------------
+// compensated FP32 arithmetic (Ogita, Rump & Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26 (2005)): TwoSum and FMA-based TwoProduct.
+// For double the accumulator degenerates to a plain sum (the reference's FP64
+// arithmetic).
+// ---------------------------------------------------------------------------
+template <typename R> struct Acc {
+  R hi, lo;
+  __device__ __forceinline__ Acc(R h = R(0), R l = R(0)) : hi(h), lo(l) {}
+  __device__ __forceinline__ void add(R v);
+  __device__ __forceinline__ void add_prod(R a, R b);       // += a*b
+  __device__ __forceinline__ void add_prod(R c, R a, R b);  // += c*a*b
+  __device__ __forceinline__ R value() const { return hi + lo; }
+};
+
+template <> __device__ __forceinline__ void Acc<double>::add(double v) { hi += v; }
+template <> __device__ __forceinline__ void Acc<double>::add_prod(double a, double b) { hi += a * b; }
+template <> __device__ __forceinline__ void Acc<double>::add_prod(double c, double a, double b) {
+  hi += c * (a * b);
+}
+
+template <> __device__ __forceinline__ void Acc<float>::add(float v) {
+  const float s = hi + v;
+  const float bp = s - hi;
+  const float err = (hi - (s - bp)) + (v - bp);
+  hi = s;
+  lo += err;
+}
+template <> __device__ __forceinline__ void Acc<float>::add_prod(float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  add(p);
+  lo += e;
+}
+template <> __device__ __forceinline__ void Acc<float>::add_prod(float c, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  const float q = c * p;
+  const float e2 = fmaf(c, p, -q) + c * e;
+  add(q);
+  lo += e2;
+}
+
+// ---------------------------------------------------------------------------
+// RANLUX words (device bit-exactness hook)
+// ---------------------------------------------------------------------------
+__global__ void k_ranlux_words(uint32_t seed, size_t count, uint64_t *out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  Ranlxd1 r;
+  r.seed31(seed);
+  for (size_t q = 0; q < count; ++q) out[q] = r.next();
+}
+
+// ---------------------------------------------------------------------------
+// (1) NGenIC white noise -> normalisation -> phi(1)
+//     random_ngenic.cc:84-154, ic_generator.cc:378-383, 509-516
+// One thread per (i,j) column; the column's RANLUX stream is drawn in the
+// reference's order (phase, amplitude with rejection of 0) for every k,
+// Nyquist and DC included.
+// ---------------------------------------------------------------------------
+struct NoiseArgs {
+  const uint32_t *seeds;
+  const double *amp;  // amp[n] = amplitude(kf sqrt n)/(kf^2 n)
+  size_t amp_len;
+  int N;
+  int mode;           // 0: raw noise, 1: normalised noise, 2: phi(1)
+  int fixing;
+  double norm;        // (+-1)/volfac
+  double out_scale;   // extra factor on phi(1) (per-field scaling of the FP32 form)
+};
+
+template <typename R> struct NoiseMath;
+template <> struct NoiseMath<double> {
+  static __device__ __forceinline__ void z(uint64_t a, uint64_t b, double &re, double &im) {
+    const double phase = (double(a) * kTwoM48) * 2 * 3.141592653589793;
+    const double am = sqrt(-log(double(b) * kTwoM48));
+    double s, c;
+    sincos(phase, &s, &c);
+    re = am * c;
+    im = am * s;
+  }
+};
+template <> struct NoiseMath<float> {
+  static __device__ __forceinline__ void z(uint64_t a, uint64_t b, float &re, float &im) {
+    const float ua = float(double(a) * kTwoM48);
+    const float am = sqrtf(-logf(float(double(b) * kTwoM48)));
+    float s, c;
+    sincospif(2.0f * ua, &s, &c);
+    re = am * c;
+    im = am * s;
+  }
+};
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_noise_phi1(NoiseArgs a, typename Cplx<R>::T *out) {
+  using C = typename Cplx<R>::T;
+  const int N = a.N, nh = N >> 1, nk = nh + 1;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= N * N) return;
+  const int i = col / N, j = col - (col / N) * N;
+  const int ii = i > 0 ? N - i : 0, jj = j > 0 ? N - j : 0;
+  const int si = signed_idx(i, N), sj = signed_idx(j, N);
+  Ranlxd1 rng;
+  rng.seed31(a.seeds[col]);
+  C *colp = out + size_t(col) * nk;
+  for (int k = 0; k < nk; ++k) {
+    const uint64_t ua = rng.next();
+    uint64_t ub;
+    do {
+      ub = rng.next();
+    } while (ub == 0);  // the reference rejects 0 and 1; 1 is not representable
+    const bool skip = (i == nh) | (j == nh) | (k == nh) | ((i | j | k) == 0);
+    if (skip) {
+      colp[k] = mkc<R>(R(0), R(0));
+      continue;
+    }
+    // k = 0 plane: only the half that the reference assigns directly writes;
+    // the other half receives the conjugate from its partner column.
+    if (k == 0 && (i > nh || (i == 0 && j > nh))) continue;
+    R re, im;
+    NoiseMath<R>::z(ua, ub, re, im);
+    if (a.mode >= 1) {
+      if (a.fixing) {
+        const R m = sqrt(re * re + im * im);
+        if (m != R(0)) {
+          re /= m;
+          im /= m;
+        }
+      }
+      re *= R(a.norm);
+      im *= R(a.norm);
+      if (a.mode == 2) {
+        const size_t n = size_t(si * si + sj * sj + k * k);
+        const R f = (n < a.amp_len) ? R(-a.amp[n] * a.out_scale) : R(0);
+        re *= f;
+        im *= f;
+      }
+    }
+    colp[k] = mkc<R>(re, im);
+    if (k == 0) out[(size_t(ii) * N + jj) * nk] = mkc<R>(re, -im);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (2) Orszag pad-insert of Hessians: M-grid k-space <- (-g_a g_b) phi * fac
+//     convolution.hh:552-575 with the Hessian functor of convolution.hh:136-157
+// ---------------------------------------------------------------------------
+struct PadArgs {
+  const void *phi;  // N-grid k-space
+  void *out[6];     // M-grid k-space buffers
+  int8_t ca[6], cb[6];
+  int ncomp;
+  int N, M;
+  double kfac, fac;
+};
+
+template <typename R> __global__ void __launch_bounds__(256) k_pad_hessian(PadArgs a) {
+  using C = typename Cplx<R>::T;
+  const int N = a.N, nh = N >> 1, nk = nh + 1, M = a.M, mk = (M >> 1) + 1;
+  const size_t total = size_t(M) * M * mk;
+  const C *phi = reinterpret_cast<const C *>(a.phi);
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int kp = int(idx % mk);
+    const size_t t = idx / mk;
+    const int jp = int(t % M), ip = int(t / M);
+    const bool in = (kp <= nh) && (ip <= nh || ip > N) && (jp <= nh || jp > N);
+    C v = mkc<R>(R(0), R(0));
+    R g[3] = {R(0), R(0), R(0)};
+    if (in) {
+      const int i = ip <= nh ? ip : ip - nh;
+      const int j = jp <= nh ? jp : jp - nh;
+      v = phi[(size_t(i) * N + j) * nk + kp];
+      const R kf = R(a.kfac);
+      g[0] = (i != nh) ? R(signed_idx(i, N)) * kf : R(0);
+      g[1] = (j != nh) ? R(signed_idx(j, N)) * kf : R(0);
+      g[2] = (kp != nh) ? R(kp) * kf : R(0);
+      v.x *= R(a.fac);
+      v.y *= R(a.fac);
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      if (c < a.ncomp) {
+        const R h = -(g[a.ca[c]] * g[a.cb[c]]);
+        reinterpret_cast<C *>(a.out[c])[idx] = mkc<R>(v.x * h, v.y * h);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (3) real-space products on the padded M-grid (convolution.hh:510-514)
+// Elementwise over all M*M*(M+2) reals (the row padding is harmless).
+// Hessian slot order: 0:xx 1:yy 2:zz 3:xy 4:xz 5:yz
+// ---------------------------------------------------------------------------
+struct SrcArgs {
+  const void *h1[6];
+  const void *h2[6];
+  const void *t;    // pairwise-truncated product (phi3a)
+  const void *third;
+  void *hi;         // running sum (phi3 source)
+  void *lo;         // its compensation term (float form)
+  void *out[4];
+  double coef;
+  int init;
+  size_t count;     // number of reals
+};
+
+// phi(2) source, ic_generator.cc:530-534:
+//   xx (yy + zz) + yy zz - xy^2 - xz^2 - yz^2
+template <typename R> __global__ void __launch_bounds__(256) k_src2(SrcArgs a) {
+  const R *H[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) H[c] = reinterpret_cast<const R *>(a.h1[c]);
+  R *out = reinterpret_cast<R *>(a.out[0]);
+  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.count;
+       q += size_t(gridDim.x) * blockDim.x) {
+    const R xx = H[0][q], yy = H[1][q], zz = H[2][q], xy = H[3][q], xz = H[4][q], yz = H[5][q];
+    Acc<R> s;
+    s.add_prod(xx, yy + zz);
+    s.add_prod(yy, zz);
+    s.add_prod(R(-1), xy, xy);
+    s.add_prod(R(-1), xz, xz);
+    s.add_prod(R(-1), yz, yz);
+    out[q] = s.value();
+  }
+}
+
+// out = h1[0] * h1[1] (first pair of a pairwise-dealiased triple product)
+template <typename R> __global__ void __launch_bounds__(256) k_mul(SrcArgs a) {
+  const R *A = reinterpret_cast<const R *>(a.h1[0]);
+  const R *B = reinterpret_cast<const R *>(a.h1[1]);
+  R *out = reinterpret_cast<R *>(a.out[0]);
+  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.count;
+       q += size_t(gridDim.x) * blockDim.x)
+    out[q] = A[q] * B[q];
+}
+
+// (hi, lo) (+)= coef * t * third   (phi3a accumulation, ic_generator.cc:581-585)
+template <typename R> __global__ void __launch_bounds__(256) k_acc3a(SrcArgs a) {
+  const R *T = reinterpret_cast<const R *>(a.t);
+  const R *H = reinterpret_cast<const R *>(a.third);
+  R *hi = reinterpret_cast<R *>(a.hi);
+  R *lo = reinterpret_cast<R *>(a.lo);
+  const R c = R(a.coef);
+  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.count;
+       q += size_t(gridDim.x) * blockDim.x) {
+    Acc<R> s;
+    if (!a.init) {
+      s.hi = hi[q];
+      if (lo) s.lo = lo[q];
+    }
+    s.add_prod(c, T[q], H[q]);
+    hi[q] = s.hi;
+    if (lo) lo[q] = s.lo;
+  }
+}
+
+// phi(3) source completion (phi3b, ic_generator.cc:592-609) and the three
+// transverse A(3) sources (ic_generator.cc:613-628), one pass over the
+// 12 Hessians.
+template <typename R> __global__ void __launch_bounds__(256) k_src3(SrcArgs a) {
+  const R c57 = R(-5.0 / 7.0), c107 = R(10.0 / 7.0);
+  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.count;
+       q += size_t(gridDim.x) * blockDim.x) {
+    R p[6], s[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      p[c] = reinterpret_cast<const R *>(a.h1[c])[q];
+      s[c] = reinterpret_cast<const R *>(a.h2[c])[q];
+    }
+    Acc<R> S(reinterpret_cast<const R *>(a.hi)[q], a.lo ? reinterpret_cast<const R *>(a.lo)[q] : R(0));
+    S.add_prod(c57, p[0], s[1] + s[2]);
+    S.add_prod(c57, p[1], s[2] + s[0]);
+    S.add_prod(c57, p[2], s[0] + s[1]);
+    S.add_prod(c107, p[3], s[3]);
+    S.add_prod(c107, p[4], s[4]);
+    S.add_prod(c107, p[5], s[5]);
+    reinterpret_cast<R *>(a.out[0])[q] = S.value();
+    // A_d with (d, d', d'') cyclic; slot(a,b) of the symmetric Hessian
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+      auto slot = [](int x, int y) {
+        if (x == y) return x;
+        const int lo_ = x < y ? x : y, hi_ = x < y ? y : x;
+        return lo_ == 0 ? (hi_ == 1 ? 3 : 4) : 5;
+      };
+      Acc<R> A;
+      A.add_prod(s[slot(d, d1)], p[slot(d, d2)]);
+      A.add_prod(R(-1), s[slot(d, d2)], p[slot(d, d1)]);
+      A.add_prod(p[slot(d1, d2)], s[slot(d1, d1)] - s[slot(d2, d2)]);
+      A.add_prod(R(-1), s[slot(d1, d2)], p[slot(d1, d1)] - p[slot(d2, d2)]);
+      reinterpret_cast<R *>(a.out[1 + d])[q] = A.value();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (4) unpad (convolution.hh:600-636) + inverse Laplacian (grid_fft.hh:440-449)
+//     N-grid out(i,j,k) = -fac * F(ip,jp,k) / |k|^2, zero on any Nyquist index
+//     and at DC.
+// ---------------------------------------------------------------------------
+struct UnpadArgs {
+  const void *F;  // M-grid k-space
+  void *out;      // N-grid k-space
+  int N, M;
+  double kfac, fac;
+};
+
+template <typename R> __global__ void __launch_bounds__(256) k_unpad_invlap(UnpadArgs a) {
+  using C = typename Cplx<R>::T;
+  const int N = a.N, nh = N >> 1, nk = nh + 1, M = a.M, mk = (M >> 1) + 1;
+  const size_t total = size_t(N) * N * nk;
+  const C *F = reinterpret_cast<const C *>(a.F);
+  C *out = reinterpret_cast<C *>(a.out);
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int k = int(idx % nk);
+    const size_t t = idx / nk;
+    const int j = int(t % N), i = int(t / N);
+    C r = mkc<R>(R(0), R(0));
+    if (i != nh && j != nh && k != nh && (i | j | k) != 0) {
+      const int ip = i > nh ? i + nh : i, jp = j > nh ? j + nh : j;
+      const C v = F[(size_t(ip) * M + jp) * mk + k];
+      const R kf = R(a.kfac);
+      const R kx = R(signed_idx(i, N)) * kf, ky = R(signed_idx(j, N)) * kf, kz = R(k) * kf;
+      const R f = -R(a.fac) / (kx * kx + ky * ky + kz * kz);
+      r = mkc<R>(v.x * f, v.y * f);
+    }
+    out[idx] = r;
+  }
+}
+
+// In-place on an M-grid k-space field: keep the N-grid modes (minus Nyquist)
+// scaled by fac, zero the rest.  Realises unpad -> pad of convolve3's second
+// convolve2 (convolution.hh:525-532).
+struct TruncArgs {
+  void *F;
+  int N, M;
+  double fac;
+};
+
+template <typename R> __global__ void __launch_bounds__(256) k_trunc_repad(TruncArgs a) {
+  using C = typename Cplx<R>::T;
+  const int N = a.N, nh = N >> 1, M = a.M, mk = (M >> 1) + 1;
+  const size_t total = size_t(M) * M * mk;
+  C *F = reinterpret_cast<C *>(a.F);
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int kp = int(idx % mk);
+    const size_t t = idx / mk;
+    const int jp = int(t % M), ip = int(t / M);
+    const bool keep = (kp < nh) && (ip < nh || ip > N) && (jp < nh || jp > N);
+    C v = mkc<R>(R(0), R(0));
+    if (keep) {
+      v = F[idx];
+      v.x *= R(a.fac);
+      v.y *= R(a.fac);
+    }
+    F[idx] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (5) displacement / velocity assembly in k-space (ic_generator.cc:929-1053)
+//     with the per-sub-lattice phase shift of Grid_FFT::shift_field
+//     (grid_fft.hh:832-842, particle_generator.hh:510-522) folded in.
+// ---------------------------------------------------------------------------
+struct AsmArgs {
+  const void *phi[3];   // phi1, phi2, phi3 (N-grid k-space, unscaled)
+  const void *A3[3];
+  const double *plt;    // 4 tables of 64*64*33 (D_r, D_theta, D_phi, alpha^-1) or null
+  const double2 *phase; // [ns][3][N] exp(i s_a k_a dx)
+  void *out[24];        // [shift][pos x,y,z, vel x,y,z]
+  int N, order, nshift, shift0;
+  double kfac, mapratio, boxlen;
+  double g1, g2, g3, g3c, vfac1, vfac2, vfac3;
+  double pfac, vfac;    // lunit/L * 1/sqrt(N^3),  vunit/L * 1/sqrt(N^3)
+  double in_scale1, in_scale2, in_scale3;  // undo per-field scaling
+};
+
+// get_cic_kspace (grid_fft.hh:347-373) on a 64 x 64 x 33 real table
+__device__ __forceinline__ double plt_cic(const double *T, double x, double y, double z) {
+  const int ix = int(floor(x)), iy = int(floor(y)), iz = int(floor(z));
+  const double dx = x - double(ix), tx = 1.0 - dx;
+  const double dy = y - double(iy), ty = 1.0 - dy;
+  const double dz = z - double(iz), tz = 1.0 - dz;
+  const int ix1 = (ix + 1) % 64, iy1 = (iy + 1) % 64, iz1 = min(iz + 1, 32);
+  auto e = [T](int a, int b, int c) { return T[(size_t(a) * 64 + b) * 33 + c]; };
+  double v = 0.0;
+  v += e(ix, iy, iz) * tx * ty * tz;
+  v += e(ix, iy, iz1) * tx * ty * dz;
+  v += e(ix, iy1, iz) * tx * dy * tz;
+  v += e(ix, iy1, iz1) * tx * dy * dz;
+  v += e(ix1, iy, iz) * dx * ty * tz;
+  v += e(ix1, iy, iz1) * dx * ty * dz;
+  v += e(ix1, iy1, iz) * dx * dy * tz;
+  v += e(ix1, iy1, iz1) * dx * dy * dz;
+  return v;
+}
+
+template <typename R, bool PLT>
+__global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
+  using C = typename Cplx<R>::T;
+  const int N = a.N, nh = N >> 1, nk = nh + 1;
+  const size_t total = size_t(N) * N * nk;
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int k = int(idx % nk);
+    const size_t t = idx / nk;
+    const int j = int(t % N), i = int(t / N);
+    R G[3];
+    R vcorr = R(1);
+    if (!PLT) {
+      // op::fourier_gradient (operators.hh:46-56): Nyquist index zeroed
+      const R kf = R(a.kfac);
+      G[0] = (i != nh) ? R(signed_idx(i, N)) * kf : R(0);
+      G[1] = (j != nh) ? R(signed_idx(j, N)) * kf : R(0);
+      G[2] = (k != nh) ? R(k) * kf : R(0);
+    } else {
+      // particle::lattice_gradient::gradient / vfac_corr (particle_plt.hh:551-585)
+      const double x = double(i) * a.mapratio, y = double(j) * a.mapratio, z = double(k) * a.mapratio;
+      const double twopi = 2.0 * 3.141592653589793;
+      const double kx = (x - double(x > 32.0) * 64.0) * twopi;
+      const double ky = (y - double(y > 32.0) * 64.0) * twopi;
+      const double kz = (z - double(z > 32.0) * 64.0) * twopi;
+      const double kr = sqrt(kx * kx + ky * ky + kz * kz);
+      const double kmod = kr / a.mapratio / a.boxlen;
+      const size_t TS = size_t(64) * 64 * 33;
+      const double Dr = plt_cic(a.plt, x, y, z);
+      const double Dt = plt_cic(a.plt + TS, x, y, z);
+      const double Dp = plt_cic(a.plt + 2 * TS, x, y, z);
+      const double al = plt_cic(a.plt + 3 * TS, x, y, z);
+      double st = 0.0, ct = 1.0, sp = 0.0, cp = 1.0;
+      if (kr > 0.0) {
+        const double kperp = sqrt(kx * kx + ky * ky);
+        st = kperp / kr;
+        ct = kz / kr;
+        if (kperp > 0.0) {
+          cp = kx / kperp;
+          sp = ky / kperp;
+        }
+      }
+      G[0] = R(kmod * (Dr * st * cp + Dt * ct * cp - Dp * sp));
+      G[1] = R(kmod * (Dr * st * sp + Dt * ct * sp + Dp * cp));
+      G[2] = R(kmod * (Dr * ct - Dt * st));
+      vcorr = R(1.0 / (1.0 / al));
+    }
+    // phi_tot and its velocity weighting (ic_generator.cc:939-958, 994-1010)
+    const C *p1 = reinterpret_cast<const C *>(a.phi[0]);
+    C f1 = p1[idx];
+    R ps_re = R(a.g1 * a.in_scale1) * f1.x, ps_im = R(a.g1 * a.in_scale1) * f1.y;
+    R vs_re = R(a.vfac1) * ps_re, vs_im = R(a.vfac1) * ps_im;
+    C Ad[3] = {mkc<R>(0, 0), mkc<R>(0, 0), mkc<R>(0, 0)};
+    if (a.order > 1) {
+      const C f2 = reinterpret_cast<const C *>(a.phi[1])[idx];
+      const R s2 = R(a.g2 * a.in_scale2);
+      ps_re += s2 * f2.x;
+      ps_im += s2 * f2.y;
+      vs_re += R(a.vfac2) * (s2 * f2.x);
+      vs_im += R(a.vfac2) * (s2 * f2.y);
+    }
+    if (a.order > 2) {
+      const C f3 = reinterpret_cast<const C *>(a.phi[2])[idx];
+      const R s3 = R(a.g3 * a.in_scale3);
+      ps_re += s3 * f3.x;
+      ps_im += s3 * f3.y;
+      vs_re += R(a.vfac3) * (s3 * f3.x);
+      vs_im += R(a.vfac3) * (s3 * f3.y);
+      const R sa = R(a.g3c * a.in_scale3);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const C v = reinterpret_cast<const C *>(a.A3[d])[idx];
+        Ad[d] = mkc<R>(sa * v.x, sa * v.y);
+      }
+    }
+    const bool dc = (idx == 0);
+    C P[3], V[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+      // i*(G_d phi) + i*(G_d' A_d'' - G_d'' A_d')
+      R tre = G[d] * ps_re, tim = G[d] * ps_im;
+      R vre = G[d] * vs_re, vim = G[d] * vs_im;
+      if (a.order > 2) {
+        const R cre = G[d1] * Ad[d2].x - G[d2] * Ad[d1].x;
+        const R cim = G[d1] * Ad[d2].y - G[d2] * Ad[d1].y;
+        tre += cre;
+        tim += cim;
+        vre += R(a.vfac3) * cre;
+        vim += R(a.vfac3) * cim;
+      }
+      const R pf = R(a.pfac), vf = R(a.vfac) * vcorr;
+      P[d] = dc ? mkc<R>(0, 0) : mkc<R>(-tim * pf, tre * pf);
+      V[d] = dc ? mkc<R>(0, 0) : mkc<R>(-vim * vf, vre * vf);
+    }
+    for (int s = 0; s < a.nshift; ++s) {
+      const double2 *ph = a.phase + size_t(a.shift0 + s) * 3 * N;
+      const double2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
+      // e = ex * ey * ez
+      const double exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
+      const R er = R(exy_re * ez.x - exy_im * ez.y), ei = R(exy_re * ez.y + exy_im * ez.x);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        reinterpret_cast<C *>(a.out[s * 6 + d])[idx] = mkc<R>(P[d].x * er - P[d].y * ei, P[d].x * ei + P[d].y * er);
+        reinterpret_cast<C *>(a.out[s * 6 + 3 + d])[idx] =
+            mkc<R>(V[d].x * er - V[d].y * ei, V[d].x * ei + V[d].y * er);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (6) particle read-out for one sub-lattice shift (particle_generator.hh:212-253,
+//     499-543, 597-639): pos = (idx + s)/N * lunit + Psi, vel = v, ID.
+// ---------------------------------------------------------------------------
+struct PartArgs {
+  const void *f[6];  // real fields (rows padded to N+2): pos x,y,z, vel x,y,z
+  void *pos, *vel, *ids;
+  int N, nshift_total, ishift, pos64, vel64, id64;
+  double sx, sy, sz, lunit;
+  uint64_t id_offset;
+};
+
+template <typename R> __global__ void __launch_bounds__(256) k_particles(PartArgs a) {
+  const int N = a.N;
+  const size_t n3 = size_t(N) * N * N;
+  const size_t rowp = size_t(N + 2);
+  const size_t base = size_t(a.ishift) * n3;
+  const double invN = 1.0 / double(N);
+  for (size_t cell = size_t(blockIdx.x) * blockDim.x + threadIdx.x; cell < n3;
+       cell += size_t(gridDim.x) * blockDim.x) {
+    const int k = int(cell % N);
+    const size_t t = cell / N;
+    const int j = int(t % N), i = int(t / N);
+    const size_t r = (size_t(i) * N + j) * rowp + k;
+    const double q[3] = {(double(i) + a.sx) * invN, (double(j) + a.sy) * invN, (double(k) + a.sz) * invN};
+    const size_t p = base + cell;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double psi = double(reinterpret_cast<const R *>(a.f[d])[r]);
+      const double x = q[d] * a.lunit + psi;
+      if (a.pos64) reinterpret_cast<double *>(a.pos)[3 * p + d] = x;
+      else reinterpret_cast<float *>(a.pos)[3 * p + d] = float(x);
+      const R v = reinterpret_cast<const R *>(a.f[3 + d])[r];
+      if (a.vel64) reinterpret_cast<double *>(a.vel)[3 * p + d] = double(v);
+      else reinterpret_cast<float *>(a.vel)[3 * p + d] = float(v);
+    }
+    if (a.ids) {
+      const uint64_t id = a.id_offset + uint64_t(a.nshift_total) * cell + uint64_t(a.ishift);
+      if (a.id64) reinterpret_cast<uint64_t *>(a.ids)[p] = id;
+      else reinterpret_cast<uint32_t *>(a.ids)[p] = uint32_t(id);
+    }
+  }
+}
+
+}  // namespace mfx

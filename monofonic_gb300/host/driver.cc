@@ -1,0 +1,231 @@
+// Whole-run driver: the in-scope part of ic_generator::run
+// (ic_generator.cc:92-1181) on top of the GPU engine, and the particle
+// output-plugin interface it writes through (output_plugin.hh:33-133).
+//
+// Config keys are the reference's ([setup] GridRes, BoxLength, zstart,
+// LPTorder, ParticleLoad, DoFixing, DoInversion; [random] generator, seed;
+// [cosmology] ...; [output] format, filename).  Two reference compile-time
+// switches become run-time keys: [setup] DoPLT (CMakeLists.txt:111, ENABLE_PLT)
+// and [execution] Precision = double | float (CMakeLists.txt:82-93,
+// CODE_PRECISION; "float" selects the FP32-compensated form).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mfx.h"
+#include "../csrc/common.h"
+#include "config_file.h"
+#include "cosmology.h"
+
+namespace mfx {
+void ngenic_seed_table(long seed, size_t n, uint32_t *t);
+void fill_amp_table(const calculator &c, uint32_t ngrid, double boxlen, double *table, size_t len);
+
+enum class cosmo_species { dm, baryon, neutrino };
+
+// particle::container (particle_container.hh:29-188): interleaved xyz
+struct particle_container {
+  std::vector<float> positions32_, velocities32_;
+  std::vector<double> positions64_, velocities64_;
+  std::vector<uint32_t> ids32_;
+  std::vector<uint64_t> ids64_;
+  size_t get_local_num_particles() const { return std::max(ids32_.size(), ids64_.size()); }
+};
+
+class output_plugin {
+ public:
+  output_plugin(const config_file &cf, const calculator &cc) : cf_(cf), cc_(cc) {
+    fname_ = cf.get_value<std::string>("output", "filename");
+  }
+  virtual ~output_plugin() {}
+  virtual void write_particle_data(const particle_container &pc, const cosmo_species &s, double Omega) = 0;
+  virtual bool has_64bit_reals() const = 0;
+  virtual bool has_64bit_ids() const = 0;
+  virtual double position_unit() const = 0;
+  virtual double velocity_unit() const = 0;
+
+ protected:
+  const config_file &cf_;
+  const calculator &cc_;
+  std::string fname_;
+};
+
+using output_creator = std::unique_ptr<output_plugin> (*)(const config_file &, const calculator &);
+std::map<std::string, output_creator> &get_output_plugin_map() {
+  static std::map<std::string, output_creator> m;
+  return m;
+}
+
+// "binary": one flat little-endian file, positions in Mpc/h and velocities in
+// the Gadget convention (units as output_gadget_hdf5.cc:83-85)
+class binary_output_plugin : public output_plugin {
+ public:
+  binary_output_plugin(const config_file &cf, const calculator &cc) : output_plugin(cf, cc) {
+    const double astart = 1.0 / (1.0 + cf.get_value<double>("setup", "zstart"));
+    lunit_ = cf.get_value<double>("setup", "BoxLength");
+    vunit_ = lunit_ / std::sqrt(astart);
+    b64reals_ = cf.get_value_safe<bool>("output", "UseDoublePrecision", true);
+    b64ids_ = cf.get_value_safe<bool>("output", "UseLongids", true);
+  }
+  void write_particle_data(const particle_container &pc, const cosmo_species &, double Omega) override {
+    FILE *f = std::fopen(fname_.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot open output file '" + fname_ + "'");
+    const char magic[8] = {'M', 'F', 'X', 'I', 'C', '0', '0', '1'};
+    const uint64_t np = pc.get_local_num_particles();
+    const uint32_t rs = b64reals_ ? 8 : 4, is = b64ids_ ? 8 : 4;
+    const double hdr[3] = {lunit_, Omega, cc_.cosmo_param_["h"]};
+    bool ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(&np, 8, 1, f) == 1 && std::fwrite(&rs, 4, 1, f) == 1 &&
+              std::fwrite(&is, 4, 1, f) == 1 && std::fwrite(hdr, 8, 3, f) == 3;
+    if (b64reals_) {
+      ok = ok && std::fwrite(pc.positions64_.data(), 8, 3 * np, f) == 3 * np;
+      ok = ok && std::fwrite(pc.velocities64_.data(), 8, 3 * np, f) == 3 * np;
+    } else {
+      ok = ok && std::fwrite(pc.positions32_.data(), 4, 3 * np, f) == 3 * np;
+      ok = ok && std::fwrite(pc.velocities32_.data(), 4, 3 * np, f) == 3 * np;
+    }
+    if (b64ids_) ok = ok && std::fwrite(pc.ids64_.data(), 8, np, f) == np;
+    else ok = ok && std::fwrite(pc.ids32_.data(), 4, np, f) == np;
+    std::fclose(f);
+    if (!ok) throw std::runtime_error("short write to '" + fname_ + "'");
+  }
+  bool has_64bit_reals() const override { return b64reals_; }
+  bool has_64bit_ids() const override { return b64ids_; }
+  double position_unit() const override { return lunit_; }
+  double velocity_unit() const override { return vunit_; }
+
+ private:
+  double lunit_, vunit_;
+  bool b64reals_, b64ids_;
+};
+
+namespace {
+std::unique_ptr<output_plugin> make_binary(const config_file &cf, const calculator &cc) {
+  return std::make_unique<binary_output_plugin>(cf, cc);
+}
+struct register_binary {
+  register_binary() { get_output_plugin_map()["binary"] = &make_binary; }
+} s_register_binary;
+
+struct Cleanup {
+  mfx_job *job = nullptr;
+  ~Cleanup() {
+    if (job) mfx_job_destroy(job);
+  }
+};
+}  // namespace
+
+int run_config(mfx_engine *eng, const std::string &text) {
+  const config_file cf = config_file::from_text(text);
+  const uint32_t ngrid = cf.get_value<uint32_t>("setup", "GridRes");
+  const double boxlen = cf.get_value<double>("setup", "BoxLength");
+  const double zstart = cf.get_value<double>("setup", "zstart");
+  int order = int(cf.get_value_safe<double>("setup", "LPTorder", 100));
+  order = std::max(1, std::min(3, order));
+  if (ngrid % 2 != 0 && order > 1) throw std::runtime_error("Orszag convolver for LPTorder>1 requires even grid size!");
+  const std::string load = cf.get_value_safe<std::string>("setup", "ParticleLoad", "sc");
+  int lattice;
+  if (load == "sc") lattice = MFX_LATTICE_SC;
+  else if (load == "bcc") lattice = MFX_LATTICE_BCC;
+  else if (load == "fcc") lattice = MFX_LATTICE_FCC;
+  else throw std::runtime_error("ParticleLoad '" + load + "' is not supported by this engine (sc, bcc, fcc)");
+  const std::string gen = cf.get_value<std::string>("random", "generator");
+  if (gen != "NGENIC") throw std::runtime_error("random generator '" + gen + "' is not supported (NGENIC)");
+  const long seed = cf.get_value<long>("random", "seed");
+  const std::string prec = cf.get_value_safe<std::string>("execution", "Precision", "double");
+
+  calculator cc(cf);
+  const double astart = 1.0 / (1.0 + zstart);
+  const double Dplus0 = cc.get_growth_factor(astart), vfac = cc.get_vfact_start();
+  const std::string fmt = cf.get_value<std::string>("output", "format");
+  auto &om = get_output_plugin_map();
+  if (!om.count(fmt)) throw std::runtime_error("Output plug-in '" + fmt + "' not found");
+  auto out = om[fmt](cf, cc);
+
+  std::vector<uint32_t> seeds(size_t(ngrid) * ngrid);
+  ngenic_seed_table(seed, ngrid, seeds.data());
+  const size_t alen = 3 * size_t(ngrid / 2) * (ngrid / 2) + 1;
+  std::vector<double> amp(alen);
+  fill_amp_table(cc, ngrid, boxlen, amp.data(), alen);
+  std::vector<double> plt;
+  const bool do_plt = cf.get_value_safe<bool>("setup", "DoPLT", false);
+  if (do_plt) {
+    plt.resize(MFX_PLT_TABLE_DOUBLES);
+    int rc = mfx_plt_table_build(eng, lattice, plt.data());
+    if (rc != MFX_OK) return rc;
+  }
+  mfx_job_desc d{};
+  d.ngrid = ngrid;
+  d.boxlen = boxlen;
+  d.lpt_order = order;
+  d.lattice = lattice;
+  d.plt = do_plt;
+  d.precision = (prec == "float") ? MFX_FP32C : MFX_FP64;
+  d.fixing = cf.get_value_safe<bool>("setup", "DoFixing", false);
+  d.inversion = cf.get_value_safe<bool>("setup", "DoInversion", false);
+  d.seed_table = seeds.data();
+  d.amp_table = amp.data();
+  d.amp_table_len = alen;
+  d.plt_table = do_plt ? plt.data() : nullptr;
+  d.g1 = -Dplus0;
+  d.g2 = order > 1 ? -3.0 / 7.0 * Dplus0 * Dplus0 : 0.0;
+  d.g3 = order > 2 ? 1.0 / 3.0 * Dplus0 * Dplus0 * Dplus0 : 0.0;
+  d.g3c = order > 2 ? 1.0 / 7.0 * Dplus0 * Dplus0 * Dplus0 : 0.0;
+  d.vfac1 = vfac;
+  d.vfac2 = 2 * vfac;
+  d.vfac3 = 3 * vfac;
+  d.lunit = out->position_unit();
+  d.vunit = out->velocity_unit();
+  d.pos64 = out->has_64bit_reals();
+  d.vel64 = out->has_64bit_reals();
+  d.id64 = out->has_64bit_ids();
+  d.id_offset = 0;
+  d.want_particles = 1;
+  Cleanup cl;
+  int rc = mfx_job_create(eng, &d, &cl.job);
+  if (rc != MFX_OK) return rc;
+  if ((rc = mfx_job_run(cl.job)) != MFX_OK) return rc;
+  if ((rc = mfx_job_wait(cl.job, -1)) != MFX_OK) return rc;
+  particle_container pc;
+  const size_t np = size_t(1 << lattice) * ngrid * ngrid * ngrid;
+  void *pp, *vp, *ip;
+  if (d.pos64) {
+    pc.positions64_.resize(3 * np);
+    pc.velocities64_.resize(3 * np);
+    pp = pc.positions64_.data();
+    vp = pc.velocities64_.data();
+  } else {
+    pc.positions32_.resize(3 * np);
+    pc.velocities32_.resize(3 * np);
+    pp = pc.positions32_.data();
+    vp = pc.velocities32_.data();
+  }
+  if (d.id64) {
+    pc.ids64_.resize(np);
+    ip = pc.ids64_.data();
+  } else {
+    pc.ids32_.resize(np);
+    ip = pc.ids32_.data();
+  }
+  if ((rc = mfx_job_fetch_particles(cl.job, pp, vp, ip)) != MFX_OK) return rc;
+  out->write_particle_data(pc, cosmo_species::dm, cc.cosmo_param_["Omega_m"]);
+  return MFX_OK;
+}
+
+}  // namespace mfx
+
+extern "C" int mfx_run_config(mfx_engine *eng, const char *ini_text) {
+  try {
+    if (!eng || !ini_text) return mfx::set_error(MFX_EINVAL, "null argument");
+    return mfx::run_config(eng, ini_text);
+  } catch (const std::bad_alloc &) {
+    return mfx::set_error(MFX_ENOMEM, "host allocation failed");
+  } catch (const std::exception &ex) {
+    return mfx::set_error(MFX_EINVAL, "%s", ex.what());
+  }
+}

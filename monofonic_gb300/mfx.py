@@ -1,0 +1,374 @@
+"""ctypes binding of libmfx (include/mfx.h) for tests, the bench and Python callers.
+
+The library is built in-tree by ``monofonic_gb300.build``; loading fails loudly
+when it is missing -- there is no CPU fallback for any engine entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+from . import build as _build
+
+MFX_OK, MFX_EINVAL, MFX_ENOMEM, MFX_ECUDA, MFX_ETIMEOUT, MFX_ECANCEL, MFX_ESTATE, MFX_EADMIT = 0, -1, -2, -3, -4, -5, -6, -7
+SC, BCC, FCC = 0, 1, 2
+FP64, FP32C = 0, 1
+FIELD_NOISE, FIELD_PHI1, FIELD_PHI2, FIELD_PHI3, FIELD_A3X, FIELD_A3Y, FIELD_A3Z = range(7)
+PLT_NGRID = 64
+PLT_TABLE_DOUBLES = 4 * 64 * 64 * 33
+
+# every entry point include/mfx.h declares
+EXPORTS = [
+    "mfx_last_error", "mfx_version", "mfx_engine_create", "mfx_engine_destroy", "mfx_job_footprint",
+    "mfx_job_create", "mfx_job_upload", "mfx_job_run", "mfx_job_wait", "mfx_job_fetch_particles",
+    "mfx_job_particles_device", "mfx_job_fetch_field", "mfx_job_run_noise", "mfx_job_stage_times",
+    "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
+    "mfx_job_destroy", "mfx_debug_ranlxd1_words",
+    "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
+    "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
+    "mfx_cosmology_amp_table", "mfx_run_config",
+]
+
+
+class MfxError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("mfx error %d: %s" % (code, msg))
+        self.code = code
+
+
+class EngineOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [
+        ("ngrid", C.c_uint32), ("boxlen", C.c_double), ("lpt_order", C.c_int), ("lattice", C.c_int),
+        ("plt", C.c_int), ("precision", C.c_int), ("fixing", C.c_int), ("inversion", C.c_int),
+        ("seed_table", C.c_void_p), ("amp_table", C.c_void_p), ("amp_table_len", C.c_size_t),
+        ("plt_table", C.c_void_p),
+        ("g1", C.c_double), ("g2", C.c_double), ("g3", C.c_double), ("g3c", C.c_double),
+        ("vfac1", C.c_double), ("vfac2", C.c_double), ("vfac3", C.c_double),
+        ("lunit", C.c_double), ("vunit", C.c_double),
+        ("pos64", C.c_int), ("vel64", C.c_int), ("id64", C.c_int), ("id_offset", C.c_uint64),
+        ("want_particles", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib_path() -> pathlib.Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load libmfx.so (optionally building it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = lib_path()
+    if not p.exists():
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError("libmfx.so not built (%s); run monofonic_gb300.build.build()" % p)
+    L = C.CDLL(str(p))
+    vp, sz, i32, u32, dbl = C.c_void_p, C.c_size_t, C.c_int, C.c_uint32, C.c_double
+    L.mfx_last_error.argtypes = [C.c_char_p, sz]
+    L.mfx_last_error.restype = sz
+    L.mfx_version.restype = C.c_char_p
+    L.mfx_engine_create.argtypes = [C.POINTER(EngineOpts), C.POINTER(vp)]
+    L.mfx_engine_destroy.argtypes = [vp]
+    L.mfx_job_footprint.argtypes = [vp, C.POINTER(JobDesc), C.POINTER(sz)]
+    L.mfx_job_create.argtypes = [vp, C.POINTER(JobDesc), C.POINTER(vp)]
+    L.mfx_job_upload.argtypes = [vp, C.POINTER(JobDesc)]
+    L.mfx_job_run.argtypes = [vp]
+    L.mfx_job_wait.argtypes = [vp, i32]
+    L.mfx_job_fetch_particles.argtypes = [vp, vp, vp, vp]
+    L.mfx_job_particles_device.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(sz)]
+    L.mfx_job_fetch_field.argtypes = [vp, i32, vp]
+    L.mfx_job_run_noise.argtypes = [vp, i32]
+    L.mfx_job_stage_times.argtypes = [vp, C.POINTER(dbl), i32]
+    L.mfx_job_algorithmic_bytes.argtypes = [vp, C.POINTER(dbl)]
+    L.mfx_job_launch_count.argtypes = [vp, C.POINTER(i32), C.POINTER(i32)]
+    L.mfx_job_set_profiling.argtypes = [vp, i32]
+    L.mfx_job_kernel_profile.argtypes = [vp, i32, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i32)]
+    L.mfx_job_destroy.argtypes = [vp]
+    L.mfx_debug_ranlxd1_words.argtypes = [vp, C.c_ulong, sz, vp]
+    L.mfx_ngenic_seed_table.argtypes = [C.c_long, sz, vp]
+    L.mfx_plt_table_build.argtypes = [vp, i32, vp]
+    L.mfx_cosmology_create.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.mfx_cosmology_destroy.argtypes = [vp]
+    L.mfx_cosmology_get.argtypes = [vp, C.c_char_p, C.POINTER(dbl)]
+    L.mfx_cosmology_amplitude.argtypes = [vp, vp, sz, vp]
+    L.mfx_cosmology_transfer.argtypes = [vp, vp, sz, vp]
+    L.mfx_cosmology_growth.argtypes = [vp, dbl, C.POINTER(dbl)]
+    L.mfx_cosmology_amp_table.argtypes = [vp, u32, dbl, vp, sz]
+    L.mfx_run_config.argtypes = [vp, C.c_char_p]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    L = load()
+    buf = C.create_string_buffer(2048)
+    L.mfx_last_error(buf, 2048)
+    return buf.value.decode(errors="replace")
+
+
+def check(rc: int):
+    if rc != MFX_OK:
+        raise MfxError(rc, last_error())
+
+
+# ----------------------------------------------------------------------------
+# host-side plugin logic
+# ----------------------------------------------------------------------------
+def ngenic_seed_table(seed: int, n: int) -> np.ndarray:
+    t = np.zeros(n * n, dtype=np.uint32)
+    check(load().mfx_ngenic_seed_table(seed, n, t.ctypes.data))
+    return t
+
+
+class Cosmology:
+    """cosmology::calculator + transfer plugin built from INI text."""
+
+    def __init__(self, ini_text: str):
+        self._h = C.c_void_p()
+        check(load().mfx_cosmology_create(ini_text.encode(), C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _lib is not None:
+            _lib.mfx_cosmology_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def get(self, name: str) -> float:
+        v = C.c_double()
+        check(load().mfx_cosmology_get(self._h, name.encode(), C.byref(v)))
+        return v.value
+
+    def amplitude(self, k) -> np.ndarray:
+        k = np.ascontiguousarray(k, dtype=np.float64).ravel()
+        out = np.zeros_like(k)
+        check(load().mfx_cosmology_amplitude(self._h, k.ctypes.data, k.size, out.ctypes.data))
+        return out
+
+    def transfer(self, k) -> np.ndarray:
+        k = np.ascontiguousarray(k, dtype=np.float64).ravel()
+        out = np.zeros_like(k)
+        check(load().mfx_cosmology_transfer(self._h, k.ctypes.data, k.size, out.ctypes.data))
+        return out
+
+    def growth(self, a: float) -> float:
+        v = C.c_double()
+        check(load().mfx_cosmology_growth(self._h, a, C.byref(v)))
+        return v.value
+
+    def amp_table(self, n: int, boxlen: float) -> np.ndarray:
+        ln = 3 * (n // 2) ** 2 + 1
+        t = np.zeros(ln)
+        check(load().mfx_cosmology_amp_table(self._h, n, boxlen, t.ctypes.data, ln))
+        return t
+
+
+def ini_text(ngrid, boxlen, zstart, order, seed, lattice="sc", sigma8=0.81, omega_m=0.3, omega_b=0.045,
+             h0=70.0, n_s=0.965, fixing=False, plt=False, precision="double", fmt="binary", filename="ics.bin"):
+    """INI text in monofonIC's config format for the configs this engine serves."""
+    return f"""[setup]
+GridRes = {ngrid}
+BoxLength = {boxlen}
+zstart = {zstart}
+LPTorder = {order}
+ParticleLoad = {lattice}
+DoFixing = {'yes' if fixing else 'no'}
+DoPLT = {'yes' if plt else 'no'}
+[cosmology]
+ParameterSet = none
+Omega_m = {omega_m}
+Omega_b = {omega_b}
+H0 = {h0}
+n_s = {n_s}
+sigma_8 = {sigma8}
+transfer = eisenstein
+ZeroRadiation = true
+m_nu1 = 0
+[random]
+generator = NGENIC
+seed = {seed}
+[execution]
+Precision = {precision}
+[output]
+format = {fmt}
+filename = {filename}
+"""
+
+
+# ----------------------------------------------------------------------------
+# engine / jobs
+# ----------------------------------------------------------------------------
+class Engine:
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self._h = C.c_void_p()
+        opts = EngineOpts(device, hbm_budget_bytes)
+        check(load().mfx_engine_create(C.byref(opts), C.byref(self._h)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h and self._h.value:
+            load().mfx_engine_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def plt_table(self, lattice: int) -> np.ndarray:
+        out = np.zeros(PLT_TABLE_DOUBLES)
+        check(load().mfx_plt_table_build(self._h, lattice, out.ctypes.data))
+        return out.reshape(4, 64, 64, 33)
+
+    def ranlxd1_words(self, seed: int, count: int) -> np.ndarray:
+        out = np.zeros(count, dtype=np.uint64)
+        check(load().mfx_debug_ranlxd1_words(self._h, seed, count, out.ctypes.data))
+        return out
+
+    def run_config(self, text: str):
+        check(load().mfx_run_config(self._h, text.encode()))
+
+
+def lpt_coefficients(dplus: float, vfac: float, order: int) -> dict:
+    """ic_generator.cc:252-269"""
+    return dict(g1=-dplus,
+                g2=(-3.0 / 7.0 * dplus * dplus) if order > 1 else 0.0,
+                g3=(1.0 / 3.0 * dplus ** 3) if order > 2 else 0.0,
+                g3c=(1.0 / 7.0 * dplus ** 3) if order > 2 else 0.0,
+                vfac1=vfac, vfac2=2 * vfac, vfac3=3 * vfac)
+
+
+class Job:
+    """One IC job on the device (mfx_job_*)."""
+
+    def __init__(self, engine: Engine, ngrid, boxlen, order, seed_table, amp_table, coef, lattice=SC,
+                 precision=FP64, plt_table=None, fixing=False, inversion=False, lunit=1.0, vunit=1.0,
+                 pos64=True, vel64=True, id64=True, id_offset=0, want_particles=True):
+        self.engine = engine
+        self.n = ngrid
+        self.lattice = lattice
+        self.precision = precision
+        self.pos64, self.vel64, self.id64 = pos64, vel64, id64
+        self._seed = np.ascontiguousarray(seed_table, dtype=np.uint32)
+        self._amp = np.ascontiguousarray(amp_table, dtype=np.float64)
+        self._plt = None if plt_table is None else np.ascontiguousarray(plt_table, dtype=np.float64)
+        d = JobDesc()
+        d.ngrid, d.boxlen, d.lpt_order, d.lattice = ngrid, boxlen, order, lattice
+        d.plt = 1 if plt_table is not None else 0
+        d.precision = precision
+        d.fixing, d.inversion = int(fixing), int(inversion)
+        d.seed_table = self._seed.ctypes.data
+        d.amp_table = self._amp.ctypes.data
+        d.amp_table_len = self._amp.size
+        d.plt_table = self._plt.ctypes.data if self._plt is not None else None
+        for k in ("g1", "g2", "g3", "g3c", "vfac1", "vfac2", "vfac3"):
+            setattr(d, k, coef[k])
+        d.lunit, d.vunit = lunit, vunit
+        d.pos64, d.vel64, d.id64 = int(pos64), int(vel64), int(id64)
+        d.id_offset = id_offset
+        d.want_particles = int(want_particles)
+        self.desc = d
+        self._h = C.c_void_p()
+        check(load().mfx_job_create(engine.handle, C.byref(d), C.byref(self._h)))
+        self.num_particles = (1 << lattice) * ngrid ** 3
+
+    def close(self):
+        if self._h and self._h.value:
+            load().mfx_job_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def upload(self, seed_table=None, amp_table=None, plt_table=None):
+        if seed_table is not None:
+            np.copyto(self._seed, seed_table)
+        if amp_table is not None:
+            np.copyto(self._amp, amp_table)
+        if plt_table is not None and self._plt is not None:
+            np.copyto(self._plt, plt_table)
+        check(load().mfx_job_upload(self._h, C.byref(self.desc)))
+
+    def run(self, wait=True):
+        check(load().mfx_job_run(self._h))
+        if wait:
+            self.wait()
+
+    def wait(self, timeout_ms=-1):
+        check(load().mfx_job_wait(self._h, timeout_ms))
+
+    def run_noise(self, raw=True):
+        check(load().mfx_job_run_noise(self._h, 1 if raw else 0))
+        self.wait()
+
+    def field(self, fid: int) -> np.ndarray:
+        n = self.n
+        out = np.zeros((n, n, n // 2 + 1), dtype=np.complex128)
+        check(load().mfx_job_fetch_field(self._h, fid, out.ctypes.data))
+        return out
+
+    def particles(self):
+        npart = self.num_particles
+        pos = np.zeros((npart, 3), dtype=np.float64 if self.pos64 else np.float32)
+        vel = np.zeros((npart, 3), dtype=np.float64 if self.vel64 else np.float32)
+        ids = np.zeros(npart, dtype=np.uint64 if self.id64 else np.uint32)
+        check(load().mfx_job_fetch_particles(self._h, pos.ctypes.data, vel.ctypes.data, ids.ctypes.data))
+        return pos, vel, ids
+
+    def fetch_particles_into(self, pos, vel, ids):
+        check(load().mfx_job_fetch_particles(self._h, pos, vel, ids))
+
+    def stage_times(self):
+        ms = (C.c_double * 8)()
+        n = load().mfx_job_stage_times(self._h, ms, 8)
+        if n < 0:
+            check(n)
+        return list(ms)[:n]
+
+    def algorithmic_bytes(self) -> float:
+        b = C.c_double()
+        check(load().mfx_job_algorithmic_bytes(self._h, C.byref(b)))
+        return b.value
+
+    def set_profiling(self, on=True):
+        check(load().mfx_job_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_profile(self):
+        """{name: (ms, algorithmic bytes, launches)} of the last run."""
+        mx = 64
+        names = C.create_string_buffer(32 * mx)
+        ms, by, cnt = (C.c_double * mx)(), (C.c_double * mx)(), (C.c_int * mx)()
+        n = load().mfx_job_kernel_profile(self._h, mx, names, ms, by, cnt)
+        if n < 0:
+            check(n)
+        out = {}
+        for q in range(min(n, mx)):
+            nm = names.raw[32 * q:32 * q + 32].split(b"\0")[0].decode()
+            out[nm] = (ms[q], by[q], cnt[q])
+        return out
+
+    def launch_count(self):
+        a, b = C.c_int(), C.c_int()
+        check(load().mfx_job_launch_count(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value

@@ -1,0 +1,433 @@
+"""ORACLE -- test infrastructure only.
+
+A CPU restatement (numpy/scipy, FP64) of monofonIC's LPT initial-condition hot
+path, written to follow the reference loop by loop so that the GPU engine can be
+checked against it.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg import this module, and only as the checker;
+the product never calls it.
+
+Conventions restated from the reference (file:line within the monofonIC tree):
+
+* k-space layout ``kelem(i,j,k)`` = array[i, j, k] of shape (N, N, N/2+1),
+  i -> k_x, j -> k_y (grid_fft.hh:196-206, 281-296; grid_fft.cc:40-112).
+* Unitary FFTs: r2c and c2r both scaled by 1/sqrt(N^3) (grid_fft.cc:69,
+  199-270) == ``norm="ortho"``.
+* ``get_k``: index i > N/2 maps to i-N, index N/2 stays positive
+  (grid_fft.hh:281-296); ``gradient`` zeroes the index N/2 (grid_fft.hh:376-385).
+* Orszag 3/2 padding, pad factor 1.5^1.5, unpad by sqrt(M^3)/sqrt(N^3) and
+  zeroing of every Nyquist index (convolution.hh:552-651).
+* ``convolve3`` is two pairwise-dealiased ``convolve2`` (convolution.hh:525-532).
+
+The FFT is pocketfft (scipy), not FFTW; results agree with the reference's
+arithmetic to rounding (~1e-15 relative), far inside the 1e-10 parity bar.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import pathlib
+
+import numpy as np
+import scipy.fft as sfft
+
+_HERE = pathlib.Path(__file__).resolve().parent
+_BUILD = _HERE / "_build"
+WORKERS = os.cpu_count() or 1
+
+
+# ----------------------------------------------------------------------------
+# RANLUX / NGenIC (C restatement in oracle/ranlux.c)
+# ----------------------------------------------------------------------------
+def build_lib() -> pathlib.Path:
+    """Compile oracle/ranlux.c into oracle/_build/liboracle_rng.so (if stale)."""
+    src = _HERE / "ranlux.c"
+    out = _BUILD / "liboracle_rng.so"
+    _BUILD.mkdir(exist_ok=True)
+    if not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+        import subprocess
+        tmp = out.with_suffix(".so.tmp%d" % os.getpid())
+        subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-o", str(tmp), str(src), "-lm"])
+        os.replace(tmp, out)
+    return out
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(str(build_lib()))
+        _lib.mfxo_ranlxd1_words.argtypes = [ctypes.c_ulong, ctypes.c_size_t, ctypes.c_void_p]
+        _lib.mfxo_ngenic_seed_table.argtypes = [ctypes.c_long, ctypes.c_size_t, ctypes.c_void_p]
+        _lib.mfxo_ngenic_fill.argtypes = [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    return _lib
+
+
+def ranlxd1_words(seed: int, count: int) -> np.ndarray:
+    out = np.zeros(count, dtype=np.uint64)
+    lib().mfxo_ranlxd1_words(seed, count, out.ctypes.data)
+    return out
+
+
+def ngenic_seed_table(seed: int, n: int) -> np.ndarray:
+    """random_ngenic.cc:39-75"""
+    t = np.zeros(n * n, dtype=np.uint32)
+    lib().mfxo_ngenic_seed_table(seed, n, t.ctypes.data)
+    return t
+
+
+def ngenic_fill(n: int, table: np.ndarray, with_uniforms: bool = False):
+    """random_ngenic.cc:84-154 (non-distributed).  Returns complex (N,N,N/2+1)."""
+    nk = n // 2 + 1
+    out = np.zeros((n, n, nk), dtype=np.complex128)
+    uni = np.zeros((n, n, nk, 2), dtype=np.float64) if with_uniforms else None
+    table = np.ascontiguousarray(table, dtype=np.uint32)
+    lib().mfxo_ngenic_fill(n, table.ctypes.data, out.ctypes.data,
+                           uni.ctypes.data if uni is not None else None)
+    return (out, uni) if with_uniforms else out
+
+
+# ----------------------------------------------------------------------------
+# Grid_FFT helpers
+# ----------------------------------------------------------------------------
+def fft_r2c(r: np.ndarray) -> np.ndarray:
+    """Grid_FFT::FourierTransformForward + ApplyNorm (grid_fft.cc:199-238)."""
+    return sfft.rfftn(r, norm="ortho", workers=WORKERS)
+
+
+def fft_c2r(c: np.ndarray, n: int) -> np.ndarray:
+    """Grid_FFT::FourierTransformBackward + ApplyNorm (grid_fft.cc:241-270)."""
+    return sfft.irfftn(c, s=(n, n, n), norm="ortho", workers=WORKERS)
+
+
+def _signed(n: int, count: int) -> np.ndarray:
+    i = np.arange(count)
+    return (i.astype(np.float64) - (i > n // 2).astype(np.float64) * n)
+
+
+def kvec(n: int, L: float):
+    """get_k<real_t>(i,j,k) components as broadcastable arrays (grid_fft.hh:281-296)."""
+    kfac = 2.0 * np.pi / L
+    kx = (_signed(n, n) * kfac)[:, None, None]
+    ky = (_signed(n, n) * kfac)[None, :, None]
+    kz = (_signed(n, n // 2 + 1) * kfac)[None, None, :]
+    return kx, ky, kz
+
+
+def grad_factors(n: int, L: float):
+    """Imaginary parts of Grid_FFT::gradient for the three axes (grid_fft.hh:376-385):
+    (real(i) - (i>N/2)*N)*kfac, zero at i == N/2."""
+    kfac = 2.0 * np.pi / L
+    g = []
+    for axis, cnt in ((0, n), (1, n), (2, n // 2 + 1)):
+        i = np.arange(cnt)
+        v = np.where(i != n // 2, _signed(n, cnt) * kfac, 0.0)
+        shape = [1, 1, 1]
+        shape[axis] = cnt
+        g.append(v.reshape(shape))
+    return g
+
+
+def kmod2(n: int, L: float):
+    kx, ky, kz = kvec(n, L)
+    return kx * kx + ky * ky + kz * kz
+
+
+def inverse_laplacian(f: np.ndarray, n: int, L: float) -> np.ndarray:
+    """apply_InverseLaplacian in k-space: -x/|k|^2 then zero_DC_mode (grid_fft.hh:440-449, 844-850)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        out = -f / kmod2(n, L)
+    out[0, 0, 0] = 0.0
+    return out
+
+
+# ----------------------------------------------------------------------------
+# Orszag 3/2 convolver (convolution.hh:412-652)
+# ----------------------------------------------------------------------------
+class OrszagConvolver:
+    def __init__(self, n: int, L: float):
+        assert n % 2 == 0
+        self.n, self.L = n, L
+        self.m = 3 * n // 2
+        nh = n // 2
+        i = np.arange(n)
+        self.ip = np.where(i > nh, i + nh, i)
+        self.g = grad_factors(n, L)
+        nyq = np.zeros((n, n, nh + 1), dtype=bool)
+        nyq[nh, :, :] = True
+        nyq[:, nh, :] = True
+        nyq[:, :, nh] = True
+        self.nyq = nyq
+
+    # kfunc builders -----------------------------------------------------
+    def hessian(self, f, a, b):
+        """grad_a * grad_b * f with i*g factors: (i g_a)(i g_b) = -(g_a g_b)."""
+        return -(self.g[a] * self.g[b]) * f
+
+    def sum_of_hessians(self, f, ab1, ab2):
+        """(grad11*grad12 + grad21*grad22) * f (convolution.hh:208-235)."""
+        return (-(self.g[ab1[0]] * self.g[ab1[1]]) + -(self.g[ab2[0]] * self.g[ab2[1]])) * f
+
+    def difference_of_hessians(self, f, ab1, ab2):
+        """(grad11*grad12 - grad21*grad22) * f (convolution.hh:248-275)."""
+        return (-(self.g[ab1[0]] * self.g[ab1[1]]) - -(self.g[ab2[0]] * self.g[ab2[1]])) * f
+
+    # pad / unpad --------------------------------------------------------
+    def pad_insert(self, fk):
+        """convolution.hh:552-575."""
+        n, m = self.n, self.m
+        rfac = np.power(1.5, 1.5)
+        out = np.zeros((m, m, m // 2 + 1), dtype=np.complex128)
+        out[np.ix_(self.ip, self.ip, np.arange(n // 2 + 1))] = fk * rfac
+        return out
+
+    def unpad(self, Fk):
+        """convolution.hh:600-636: divide by sqrt(M^3)/sqrt(N^3), zero Nyquist."""
+        n, m = self.n, self.m
+        rfac = np.sqrt(float(m * m * m)) / np.sqrt(float(n * n * n))
+        out = Fk[np.ix_(self.ip, self.ip, np.arange(n // 2 + 1))] / rfac
+        out[self.nyq] = 0.0
+        return out
+
+    def convolve2(self, k1, k2):
+        """convolution.hh:495-518; returns the unpadded N-grid k-space product."""
+        m = self.m
+        a = fft_c2r(self.pad_insert(k1), m)
+        b = fft_c2r(self.pad_insert(k2), m)
+        b *= a
+        return self.unpad(fft_r2c(b))
+
+    def convolve3(self, k1, k2, k3):
+        """convolution.hh:525-532 (pairwise dealiasing)."""
+        return self.convolve2(self.convolve2(k1, k2), k3)
+
+
+# ----------------------------------------------------------------------------
+# LPT potentials (ic_generator.cc:378-383, 509-658)
+# ----------------------------------------------------------------------------
+def normalise_noise(w: np.ndarray, n: int, L: float, fixing: bool, inversion: bool) -> np.ndarray:
+    """ic_generator.cc:378-383 with volfac from ic_generator.cc:247."""
+    volfac = np.power(L / n / 2.0 / np.pi, 1.5)
+    out = w.copy()
+    if fixing:
+        a = np.abs(out)
+        nz = a != 0.0
+        out[nz] = out[nz] / a[nz]
+    s = -1.0 if inversion else 1.0
+    return s * out / volfac
+
+
+def phi1_from_noise(w: np.ndarray, n: int, L: float, amplitude) -> np.ndarray:
+    """ic_generator.cc:509-516: phi = -delta/k^2 with delta = w*amplitude(|k|)."""
+    kx, ky, kz = kvec(n, L)
+    kmod = np.sqrt(kx * kx + ky * ky + kz * kz)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        amp = amplitude(kmod)
+        phi = -(w * amp) / (kmod * kmod)
+    phi[0, 0, 0] = 0.0
+    return phi
+
+
+def lpt_potentials(phi: np.ndarray, n: int, L: float, order: int):
+    """ic_generator.cc:523-628.  Returns unscaled (phi2, phi3, [A3x, A3y, A3z])."""
+    C = OrszagConvolver(n, L)
+    H, S, D = C.hessian, C.sum_of_hessians, C.difference_of_hessians
+    phi2 = phi3 = None
+    A3 = None
+    if order > 1:
+        phi2 = C.convolve2(H(phi, 0, 0), S(phi, (1, 1), (2, 2)))
+        phi2 = phi2 + C.convolve2(H(phi, 1, 1), H(phi, 2, 2))
+        phi2 = phi2 - C.convolve2(H(phi, 0, 1), H(phi, 0, 1))
+        phi2 = phi2 - C.convolve2(H(phi, 0, 2), H(phi, 0, 2))
+        phi2 = phi2 - C.convolve2(H(phi, 1, 2), H(phi, 1, 2))
+        phi2 = inverse_laplacian(phi2, n, L)
+    if order > 2:
+        phi3 = C.convolve3(H(phi, 0, 0), H(phi, 1, 1), H(phi, 2, 2))
+        phi3 = phi3 + C.convolve3(H(phi, 0, 1), H(phi, 0, 2), H(phi, 1, 2)) * 2.0
+        phi3 = phi3 - C.convolve3(H(phi, 1, 2), H(phi, 1, 2), H(phi, 0, 0))
+        phi3 = phi3 - C.convolve3(H(phi, 0, 2), H(phi, 0, 2), H(phi, 1, 1))
+        phi3 = phi3 - C.convolve3(H(phi, 0, 1), H(phi, 0, 1), H(phi, 2, 2))
+        c57, c107 = -5.0 / 7.0, +10.0 / 7.0
+        phi3 = phi3 + C.convolve2(H(phi, 0, 0), S(phi2, (1, 1), (2, 2))) * c57
+        phi3 = phi3 + C.convolve2(H(phi, 1, 1), S(phi2, (2, 2), (0, 0))) * c57
+        phi3 = phi3 + C.convolve2(H(phi, 2, 2), S(phi2, (0, 0), (1, 1))) * c57
+        phi3 = phi3 + C.convolve2(H(phi, 0, 1), H(phi2, 0, 1)) * c107
+        phi3 = phi3 + C.convolve2(H(phi, 0, 2), H(phi2, 0, 2)) * c107
+        phi3 = phi3 + C.convolve2(H(phi, 1, 2), H(phi2, 1, 2)) * c107
+        phi3 = inverse_laplacian(phi3, n, L)
+        A3 = []
+        for d in range(3):
+            dp, dpp = (d + 1) % 3, (d + 2) % 3
+            a = C.convolve2(H(phi2, d, dp), H(phi, d, dpp))
+            a = a - C.convolve2(H(phi2, d, dpp), H(phi, d, dp))
+            a = a + C.convolve2(H(phi, dp, dpp), D(phi2, (dp, dp), (dpp, dpp)))
+            a = a - C.convolve2(H(phi2, dp, dpp), D(phi, (dp, dp), (dpp, dpp)))
+            A3.append(inverse_laplacian(a, n, L))
+    return phi2, phi3, A3
+
+
+def lpt_coefficients(dplus: float, vfac: float, order: int):
+    """ic_generator.cc:252-269."""
+    g1 = -dplus
+    g2 = (-3.0 / 7.0 * dplus * dplus) if order > 1 else 0.0
+    g3 = (1.0 / 3.0 * dplus * dplus * dplus) if order > 2 else 0.0
+    g3c = (1.0 / 7.0 * dplus * dplus * dplus) if order > 2 else 0.0
+    return dict(g1=g1, g2=g2, g3=g3, g3c=g3c, vfac1=vfac, vfac2=2 * vfac, vfac3=3 * vfac)
+
+
+# ----------------------------------------------------------------------------
+# Displacement / velocity assembly (ic_generator.cc:916-1060)
+# ----------------------------------------------------------------------------
+class FourierGradient:
+    """op::fourier_gradient (operators.hh:38-61): i*k with the Nyquist index zeroed, vfac_corr = 1."""
+
+    def __init__(self, n: int, L: float):
+        self.g = grad_factors(n, L)
+
+    def gradient(self, d):
+        return self.g[d]  # imaginary part
+
+    def vfac_corr(self):
+        return 1.0
+
+
+def _times_i(g, f):
+    """ccomplex_t(0,g) * f."""
+    return 1j * (g * f)
+
+
+def assemble_displacement(d, fields, coef, grad, lunit, L, order):
+    """ic_generator.cc:929-968 for component d; returns the k-space field (DC zeroed)."""
+    phi, phi2, phi3, A3 = fields
+    dp, dpp = (d + 1) % 3, (d + 2) % 3
+    phitot = phi.copy()
+    if order > 1:
+        phitot = phitot + phi2
+    if order > 2:
+        phitot = phitot + phi3
+    tmp = _times_i(grad.gradient(d), phitot)
+    if order > 2:
+        tmp = tmp + (_times_i(grad.gradient(dp), A3[dpp]) - _times_i(grad.gradient(dpp), A3[dp]))
+    tmp = tmp * (lunit / L)
+    tmp[0, 0, 0] = 0.0
+    return tmp
+
+
+def assemble_velocity(d, fields, coef, grad, vunit, L, order):
+    """ic_generator.cc:986-1053 for component d (no baryon / neutrino terms)."""
+    phi, phi2, phi3, A3 = fields
+    dp, dpp = (d + 1) % 3, (d + 2) % 3
+    pv = coef["vfac1"] * phi
+    if order > 1:
+        pv = pv + coef["vfac2"] * phi2
+    if order > 2:
+        pv = pv + coef["vfac3"] * phi3
+    tmp = _times_i(grad.gradient(d), pv)
+    if order > 2:
+        tmp = tmp + coef["vfac3"] * (_times_i(grad.gradient(dp), A3[dpp]) - _times_i(grad.gradient(dpp), A3[dp]))
+    tmp = tmp * grad.vfac_corr()
+    tmp = tmp * (vunit / L)
+    tmp[0, 0, 0] = 0.0
+    return tmp
+
+
+LATTICE_SHIFTS = {
+    # particle_generator.hh:47-54 (SC, BCC, FCC)
+    0: [(0.0, 0.0, 0.0)],
+    1: [(0.0, 0.0, 0.0), (0.5, 0.5, 0.5)],
+    2: [(0.0, 0.0, 0.0), (0.0, 0.5, 0.5), (0.5, 0.0, 0.5), (0.5, 0.5, 0.0)],
+}
+
+
+def shift_field(fr: np.ndarray, s, n: int, L: float) -> np.ndarray:
+    """Grid_FFT::shift_field (grid_fft.hh:832-842): r2c, multiply exp(i k.s dx), c2r."""
+    kx, ky, kz = kvec(n, L)
+    dx = L / n
+    fk = fft_r2c(fr)
+    shift = s[0] * kx * dx + s[1] * ky * dx + s[2] * kz * dx
+    fk = fk * np.exp(1j * shift)
+    return fft_c2r(fk, n)
+
+
+def lattice_read_out(field_r, lattice, n, L, lunit=None):
+    """set_positions (lunit given) / set_velocities (lunit None), particle_generator.hh:499-543, 597-639.
+
+    Returns an (n_s*N^3,) array of this component for all particles, ordered
+    ishift*N^3 + (i*N + j)*N + k."""
+    shifts = LATTICE_SHIFTS[lattice]
+    out = []
+    f = field_r
+    for ish, s in enumerate(shifts):
+        if ish > 0:
+            prev = shifts[ish - 1]
+            f = shift_field(f, (s[0] - prev[0], s[1] - prev[1], s[2] - prev[2]), n, L)
+        if lunit is None:
+            out.append(f.reshape(-1).copy())
+        else:
+            idx = np.arange(n, dtype=np.float64)
+            comp = []
+            for axis in range(3):
+                shape = [1, 1, 1]
+                shape[axis] = n
+                comp.append(((idx + s[axis]) / float(n)).reshape(shape))
+            out.append(comp)
+    return out
+
+
+def particles(fields, coef, grad, lattice, n, L, lunit, vunit, order, id_offset=0):
+    """Positions, velocities and IDs of all particles as the reference's
+    lattice_generator leaves them (particle_generator.hh:212-253, 499-687).
+
+    Returns pos (np_,3), vel (np_,3), ids (np_,) uint64."""
+    shifts = LATTICE_SHIFTS[lattice]
+    ns = len(shifts)
+    n3 = n ** 3
+    pos = np.zeros((ns * n3, 3))
+    vel = np.zeros((ns * n3, 3))
+    for d in range(3):
+        fr = fft_c2r(assemble_displacement(d, fields, coef, grad, lunit, L, order), n)
+        f = fr
+        for ish, s in enumerate(shifts):
+            if ish > 0:
+                prev = shifts[ish - 1]
+                f = shift_field(f, (s[0] - prev[0], s[1] - prev[1], s[2] - prev[2]), n, L)
+            idx = np.arange(n, dtype=np.float64)
+            shape = [1, 1, 1]
+            shape[d] = n
+            q = ((idx + s[d]) / float(n)).reshape(shape)
+            pos[ish * n3:(ish + 1) * n3, d] = (q * lunit + f).reshape(-1)
+    for d in range(3):
+        fr = fft_c2r(assemble_velocity(d, fields, coef, grad, vunit, L, order), n)
+        f = fr
+        for ish, s in enumerate(shifts):
+            if ish > 0:
+                prev = shifts[ish - 1]
+                f = shift_field(f, (s[0] - prev[0], s[1] - prev[1], s[2] - prev[2]), n, L)
+            vel[ish * n3:(ish + 1) * n3, d] = f.reshape(-1)
+    cell = np.arange(n3, dtype=np.uint64)
+    ids = np.zeros(ns * n3, dtype=np.uint64)
+    off = np.uint64(id_offset * ns * n3)
+    for il in range(ns):
+        ids[il * n3:(il + 1) * n3] = off + np.uint64(ns) * cell + np.uint64(il)
+    return pos, vel, ids
+
+
+def run_lpt(n, L, seed_table, amplitude, order, dplus, vfac, lattice=0, lunit=1.0, vunit=1.0,
+            fixing=False, inversion=False, grad=None, want_particles=True):
+    """The whole hot path, ic_generator.cc:288-1064, for one species (dm, no baryons)."""
+    w = ngenic_fill(n, seed_table)
+    w = normalise_noise(w, n, L, fixing, inversion)
+    phi = phi1_from_noise(w, n, L, amplitude)
+    phi2, phi3, A3 = lpt_potentials(phi, n, L, order)
+    c = lpt_coefficients(dplus, vfac, order)
+    phi_s = phi * c["g1"]
+    phi2_s = phi2 * c["g2"] if order > 1 else None
+    phi3_s = phi3 * c["g3"] if order > 2 else None
+    A3_s = [a * c["g3c"] for a in A3] if order > 2 else None
+    res = dict(noise=w, phi=phi_s, phi2=phi2_s, phi3=phi3_s, A3=A3_s, coef=c)
+    if want_particles:
+        g = grad if grad is not None else FourierGradient(n, L)
+        pos, vel, ids = particles((phi_s, phi2_s, phi3_s, A3_s), c, g, lattice, n, L, lunit, vunit, order)
+        res.update(pos=pos, vel=vel, ids=ids)
+    return res

@@ -1,0 +1,178 @@
+"""CPU tests: oracle pinned against golden vectors, host-side plugin logic of
+libmfx against the oracle, and the C ABI surface.  No GPU needed."""
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+GOLDEN = ROOT / "tests" / "golden"
+
+
+# ---------------------------------------------------------------------------
+# C ABI surface
+# ---------------------------------------------------------------------------
+def header_symbols():
+    txt = (ROOT / "include" / "mfx.h").read_text()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(mfx_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(mfxlib):
+    L = mfxlib.load()
+    syms = header_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+    assert set(syms) == set(mfxlib.EXPORTS), set(syms) ^ set(mfxlib.EXPORTS)
+
+
+def test_engine_create_fails_loudly_without_gpu(mfxlib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(mfxlib.MfxError) as e:
+        mfxlib.Engine(0)
+    assert e.value.code == mfxlib.MFX_ECUDA
+
+
+# ---------------------------------------------------------------------------
+# RANLUX / NGenIC
+# ---------------------------------------------------------------------------
+def _py_ranlxd1(seed, count):
+    """Third, pure-Python coding of the ranlxd1 stream (small counts only)."""
+    if seed == 0:
+        seed = 1
+    bits = [(seed >> q) & 1 for q in range(31)]
+    ib, jb = 0, 18
+    y = []
+    for _ in range(12):
+        w = 0
+        for _ in range(48):
+            w = 2 * w + (1 - bits[ib])
+            bits[ib] = bits[ib] ^ bits[jb]
+            ib, jb = (ib + 1) % 31, (jb + 1) % 31
+        y.append(w)
+    out, c = [], 0
+    while len(out) < count:
+        blk = []
+        for _ in range(202):
+            d = y[-5] - y[-12] - c
+            c = 1 if d < 0 else 0
+            d %= 1 << 48
+            y.append(d)
+            y = y[-12:]
+            blk.append(d)
+        out.extend(blk[-12:])
+    return np.array(out[:count], dtype=np.uint64)
+
+
+@pytest.mark.parametrize("seed", [1, 12345, 4242, 2**31 - 2])
+def test_ranlux_three_codings_agree(oracle, seed):
+    a = oracle.ranlxd1_words(seed, 100)
+    b = _py_ranlxd1(seed, 100)
+    assert np.array_equal(a, b)
+    assert np.all(a < 2**48)
+
+
+def test_seed_zero_means_one(oracle):
+    assert np.array_equal(oracle.ranlxd1_words(0, 30), oracle.ranlxd1_words(1, 30))
+
+
+@pytest.mark.parametrize("n,seed", [(16, 12345), (64, 12345), (128, 4242), (96, 1)])
+def test_host_seed_table_matches_oracle(mfxlib, oracle, n, seed):
+    assert np.array_equal(mfxlib.ngenic_seed_table(seed, n), oracle.ngenic_seed_table(seed, n))
+
+
+def test_golden_ranlux_and_seed_table(oracle):
+    g = np.load(GOLDEN / "ngenic_16.npz")
+    assert np.array_equal(oracle.ranlxd1_words(int(g["seed"]), g["words"].size), g["words"])
+    assert np.array_equal(oracle.ngenic_seed_table(int(g["seed"]), 16), g["seed_table"])
+    w = oracle.ngenic_fill(16, g["seed_table"])
+    np.testing.assert_allclose(w, g["noise"], rtol=0, atol=1e-15)
+
+
+def test_noise_hermitian_and_nyquist(oracle):
+    n = 32
+    w = oracle.ngenic_fill(n, oracle.ngenic_seed_table(7, n))
+    nh = n // 2
+    assert np.all(w[nh] == 0) and np.all(w[:, nh] == 0) and np.all(w[:, :, nh] == 0)
+    assert w[0, 0, 0] == 0
+    p = w[:, :, 0]
+    idx = (-np.arange(n)) % n
+    assert np.array_equal(p[np.ix_(idx, idx)], np.conj(p))
+    # unit-variance Gaussian modes: <|z|^2> = 1 (ampl = sqrt(-ln u))
+    m = np.abs(w[1:nh, 1:nh, 1:nh]) ** 2
+    assert abs(m.mean() - 1.0) < 0.05
+
+
+# ---------------------------------------------------------------------------
+# oracle convolver properties
+# ---------------------------------------------------------------------------
+def test_orszag_product_is_exact_for_band_limited_fields(oracle):
+    """For fields with modes |k_i| < N/3 the 3/2-padded product has no aliasing:
+    it equals the exact product truncated to the N-grid."""
+    n, L = 24, 1.0
+    rng = np.random.default_rng(0)
+    r1 = rng.standard_normal((n, n, n))
+    r2 = rng.standard_normal((n, n, n))
+    k1, k2 = oracle.fft_r2c(r1), oracle.fft_r2c(r2)
+    i = np.arange(n)
+    si = np.where(i > n // 2, i - n, i)
+    keep = (np.abs(si)[:, None, None] < n // 4) & (np.abs(si)[None, :, None] < n // 4) & (np.arange(n // 2 + 1)[None, None, :] < n // 4)
+    k1, k2 = k1 * keep, k2 * keep
+    C = oracle.OrszagConvolver(n, L)
+    got = C.convolve2(k1, k2)
+    # with unitary transforms on both grids the padded product equals the
+    # product taken directly on the N-grid (no aliasing for these bands)
+    ref = oracle.fft_r2c(oracle.fft_c2r(k1, n) * oracle.fft_c2r(k2, n))
+    ref[C.nyq] = 0
+    np.testing.assert_allclose(got, ref, atol=1e-12)
+
+
+def test_inverse_laplacian_of_laplacian(oracle):
+    n, L = 16, 10.0
+    rng = np.random.default_rng(1)
+    f = oracle.fft_r2c(rng.standard_normal((n, n, n)))
+    f[0, 0, 0] = 0
+    lap = -oracle.kmod2(n, L) * f
+    np.testing.assert_allclose(oracle.inverse_laplacian(lap, n, L), f, atol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# host cosmology vs the oracle's independent restatement
+# ---------------------------------------------------------------------------
+def test_host_cosmology_matches_oracle(mfxlib):
+    from oracle import cosmo
+    o = cosmo.Cosmology(Om=0.3, Ob=0.045, H0=70.0, n_s=0.965, sigma8=0.81)
+    c = mfxlib.Cosmology(mfxlib.ini_text(64, 100.0, 49.0, 2, 12345))
+    assert c.get("Omega_DE") == pytest.approx(0.7, abs=1e-15)
+    assert c.get("Omega_r") == 0.0
+    k = np.logspace(-4, 2.5, 200)
+    np.testing.assert_allclose(c.transfer(k), o.transfer(k), rtol=1e-13)
+    assert c.get("pnorm") == pytest.approx(o.pnorm, rel=1e-10)
+    np.testing.assert_allclose(c.amplitude(k), o.amplitude(k), rtol=1e-10)
+    for z in (49.0, 24.0, 0.5):
+        a = 1.0 / (1.0 + z)
+        # the reference's own Cash-Karp (eps 1e-10) + log-log spline is good to ~1e-8
+        assert c.growth(a) == pytest.approx(o.growth(a), rel=5e-8)
+    assert c.get("vfact_start") == pytest.approx(o.vfact(1.0 / 50.0), rel=1e-8)
+
+
+def test_amp_table_definition(mfxlib):
+    c = mfxlib.Cosmology(mfxlib.ini_text(32, 100.0, 49.0, 2, 1))
+    t = c.amp_table(32, 100.0)
+    assert t.size == 3 * 16 * 16 + 1 and t[0] == 0.0
+    kf = 2 * np.pi / 100.0
+    n = np.arange(1, t.size)
+    k = kf * np.sqrt(n)
+    np.testing.assert_allclose(t[1:], c.amplitude(k) / (k * k), rtol=1e-14)
+
+
+def test_config_parser_and_errors(mfxlib):
+    with pytest.raises(mfxlib.MfxError):
+        mfxlib.Cosmology("[setup]\nzstart=10\n[cosmology]\ntransfer = CLASS\n")
+    txt = mfxlib.ini_text(32, 50.0, 24.0, 3, 3).replace("Omega_m = 0.3", "Omega_m = 0.31 # trailing comment")
+    c = mfxlib.Cosmology(txt)
+    assert c.get("Omega_m") == 0.31
