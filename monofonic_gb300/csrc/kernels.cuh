@@ -139,9 +139,10 @@ __global__ void __launch_bounds__(128) k_noise_phi1(NoiseArgs a, typename Cplx<R
   for (int k = 0; k < nk; ++k) {
     const uint64_t ua = rng.next();
     uint64_t ub;
+    int tries = 0;
     do {
       ub = rng.next();
-    } while (ub == 0);  // the reference rejects 0 and 1; 1 is not representable
+    } while (ub == 0 && ++tries < 1024);  // the reference rejects 0 and 1; 1 is not representable
     const bool skip = (i == nh) | (j == nh) | (k == nh) | ((i | j | k) == 0);
     if (skip) {
       colp[k] = mkc<R>(R(0), R(0));
