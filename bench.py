@@ -1,0 +1,399 @@
+"""Benchmark of the LPT initial-condition hot path on GB300.
+
+Default workload (one GPU): 3LPT + PLT on a BCC lattice, 256^3 grid,
+2 x 256^3 particles, box 300 Mpc/h, z_start = 24, NGenIC seed 4242, E&H
+transfer function (Omega_m 0.3, Omega_b 0.045, h 0.7, sigma_8 0.81,
+n_s 0.965), FP32-compensated form.  One step = one full pass of the hot path
+(white noise -> phi1/phi2/phi3/A3 -> displacements/velocities -> particles).
+
+  value  particles/s with all inputs resident in HBM (device time, CUDA events
+         on the engine's stream, L2 flushed between steps)
+  e2e    the same through the C ABI with host buffers: every step uploads the
+         seed / amplitude / PLT tables from pinned host memory and copies the
+         particles (f64 positions, f32 velocities, u64 IDs) back to pinned
+         host memory
+  fp64_form  the plain FP64 form of the same workload, for the FP32/FP64 ratio
+  roofline   the dominant own kernel against the measured HBM copy bandwidth
+
+``--impl reference`` times the CPU restatement of the reference path (the
+reference itself cannot be built: it needs FFTW3, GSL and HDF5) on a bounded
+sample of the same workload with all host cores.
+
+Multi-GPU (torchrun): independent replicas, one realisation per rank (seed +
+rank), no data-path collective; value = all ranks' particles / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # name: (ngrid, boxlen, zstart, order, lattice, plt, seed, fixing)
+    "bcc256": (256, 300.0, 24.0, 3, 1, True, 4242, False),
+    "sc64": (64, 100.0, 49.0, 2, 0, False, 12345, False),
+    "fcc768": (768, 1000.0, 24.0, 3, 2, True, 1, True),
+    "fcc384": (384, 1000.0, 24.0, 3, 2, True, 1, True),
+}
+LATNAME = {0: "sc", 1: "bcc", 2: "fcc"}
+
+
+def describe(name, prec):
+    n, L, z, order, lat, plt, seed, fix = WORKLOADS[name]
+    return {"workload": "%dLPT%s %s %d^3 L=%g Mpc/h z=%g seed %d %s" % (
+        order, "+PLT" if plt else "", LATNAME[lat].upper(), n, L, z, seed, prec),
+        "ngrid": n, "boxlen": L, "zstart": z, "lpt_order": order, "lattice": LATNAME[lat], "plt": plt,
+        "seed": seed, "fixing": fix, "particles": (1 << lat) * n ** 3, "precision": prec,
+        "cosmology": "Om=0.3 Ob=0.045 h=0.7 s8=0.81 ns=0.965 E&H", "l2_flush": True}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index, path):
+        self.path = path
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(mfx, name, rank=0):
+    n, L, z, order, lat, plt, seed, fix = WORKLOADS[name]
+    seed = seed + rank
+    cosmo = mfx.Cosmology(mfx.ini_text(n, L, z, order, seed, LATNAME[lat], fixing=fix, plt=plt))
+    dplus, vfac = cosmo.get("dplus_start"), cosmo.get("vfact_start")
+    coef = mfx.lpt_coefficients(dplus, vfac, order)
+    seeds = mfx.ngenic_seed_table(seed, n)
+    amp = cosmo.amp_table(n, L)
+    return dict(n=n, L=L, z=z, order=order, lat=lat, plt=plt, fix=fix, seed=seed, cosmo=cosmo, coef=coef,
+                seeds=seeds, amp=amp, lunit=L, vunit=L / np.sqrt(1.0 / (1.0 + z)))
+
+
+def pinned(nbytes):
+    import torch
+    t = torch.empty(max(1, nbytes), dtype=torch.uint8, pin_memory=True)
+    return t, t.numpy()
+
+
+def l2_flush(buf):
+    buf.add_(1.0)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from monofonic_gb300 import mfx
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    mfx.load(build_if_missing=True)
+    eng = mfx.Engine(local)
+    inp = make_inputs(mfx, args.workload, rank)
+    prec = mfx.FP32C if args.precision == "fp32c" else mfx.FP64
+    plt_tab = eng.plt_table(inp["lat"]) if inp["plt"] else None
+    # pinned host copies of the per-step inputs (uploaded every e2e step)
+    hs_t, hs = pinned(inp["seeds"].nbytes)
+    hs = hs[:inp["seeds"].nbytes].view(np.uint32)
+    hs[:] = inp["seeds"]
+    ha_t, ha = pinned(inp["amp"].nbytes)
+    ha = ha[:inp["amp"].nbytes].view(np.float64)
+    ha[:] = inp["amp"]
+    hp = None
+    if plt_tab is not None:
+        hp_t, hp = pinned(plt_tab.nbytes)
+        hp = hp[:plt_tab.nbytes].view(np.float64).reshape(plt_tab.shape)
+        hp[:] = plt_tab
+    pos64, vel64 = True, (prec == mfx.FP64)
+    job = mfx.Job(eng, inp["n"], inp["L"], inp["order"], hs, ha, inp["coef"], lattice=inp["lat"], precision=prec,
+                  plt_table=hp, fixing=inp["fix"], lunit=inp["lunit"], vunit=inp["vunit"], pos64=pos64,
+                  vel64=vel64, id64=True)
+    npart = job.num_particles
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        job.run()
+    job.set_profiling(True)
+    barrier()
+    clocks = Clocks(local, str(ROOT / "gpurun_out" / ("clocks_rank%d.csv" % rank))) if rank == 0 else None
+    dev_ms, prof_tot = [], {}
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        l2_flush(flush)
+        torch.cuda.synchronize()
+        job.run()
+        dev_ms.append(sum(job.stage_times()))
+        for k, (ms, by, cnt) in job.kernel_profile().items():
+            a = prof_tot.setdefault(k, [0.0, 0.0, 0])
+            a[0] += ms
+            a[1] += by
+            a[2] += cnt
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop() if clocks else None
+    own, ffts = job.launch_count()
+    job.set_profiling(False)
+    ms_step = float(np.mean(dev_ms))
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * npart / (ms_step * 1e-3)
+
+    # ---- e2e through the C ABI with host buffers ----
+    pb_t, pb = pinned(npart * 3 * 8)
+    vb_t, vb = pinned(npart * 3 * (8 if vel64 else 4))
+    ib_t, ib = pinned(npart * 8)
+    h2d = hs.nbytes + ha.nbytes + (hp.nbytes if hp is not None else 0)
+    d2h = pb.nbytes + vb.nbytes + ib.nbytes
+    job.upload(hs, ha, hp)
+    job.run()
+    job.fetch_particles_into(pb.ctypes.data, vb.ctypes.data, ib.ctypes.data)
+    barrier()
+    e2e_t = []
+    for _ in range(args.steps):
+        l2_flush(flush)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        job.upload(hs, ha, hp)
+        job.run(wait=False)
+        job.fetch_particles_into(pb.ctypes.data, vb.ctypes.data, ib.ctypes.data)
+        e2e_t.append(time.perf_counter() - t1)
+    barrier()
+    e2e_s = float(np.mean(e2e_t))
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * npart / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+
+    out = None
+    if rank == 0:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        peak = peaks.get("hbm_gbs", 6800.0)
+        peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+        steps = args.steps
+        kern = {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[2] / steps,
+                    "alg_GBps": (v[1] / (v[0] * 1e-3) / 1e9) if v[0] > 0 else None}
+                for k, v in prof_tot.items()}
+        total_k = sum(v[0] for v in prof_tot.values())
+        for k in kern:
+            kern[k]["share"] = prof_tot[k][0] / total_k if total_k else None
+        own_only = {k: v for k, v in prof_tot.items() if not k.startswith("cufft")}
+        dom = max(own_only, key=lambda k: own_only[k][0])
+        d = prof_tot[dom]
+        achieved = d[1] / (d[0] * 1e-3) / 1e9
+        traffic = None
+        tfile = ROOT / "profiles" / "traffic.json"
+        if tfile.exists():
+            tj = json.loads(tfile.read_text())
+            traffic = tj.get(args.workload + "/" + args.precision, {}).get(dom)
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else "fallback",
+                "traffic": traffic, "alg_bytes_per_launch": d[1] / d[2], "launches": d[2]}
+        fft = {k: v for k, v in prof_tot.items() if k.startswith("cufft")}
+        fft_ms = sum(v[0] for v in fft.values())
+        fft_bytes = sum(v[1] for v in fft.values())
+        alg_total = job.algorithmic_bytes()
+        out = {
+            "metric": "3LPT particles/s (FP32-compensated form) on 1 GB300, 3LPT+PLT BCC 256^3",
+            "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if prec == mfx.FP32C else "f64", "data": "synthetic (NGenIC white noise, seeded)",
+            "config": describe(args.workload, args.precision),
+            "e2e": e2e, "gpu_launches": int(own) * args.steps, "fft_execs_per_step": int(ffts),
+            "roofline": roof,
+            "fft_roofline": {"achieved": fft_bytes / (fft_ms * 1e-3) / 1e9 if fft_ms else None, "peak": peak,
+                             "unit": "GB/s", "share_of_step": fft_ms / total_k if total_k else None},
+            "whole_step_alg": {"bytes": alg_total, "achieved_GBps": alg_total / (ms_step * 1e-3) / 1e9,
+                               "frac": alg_total / (ms_step * 1e-3) / 1e9 / peak},
+            "kernels": kern, "clocks": clk, "wall_s_timed": wall,
+        }
+    job.close()
+    return out, eng, inp, plt_tab
+
+
+def fp64_and_error(args, eng, inp, plt_tab, out):
+    """Times the plain FP64 form of the same workload and states the FP32 form's
+    error against it in units of the mean interparticle spacing."""
+    import torch
+    from monofonic_gb300 import mfx
+    res = {}
+    jobs = {}
+    for prec in (mfx.FP64, mfx.FP32C):
+        j = mfx.Job(eng, inp["n"], inp["L"], inp["order"], inp["seeds"], inp["amp"], inp["coef"], lattice=inp["lat"],
+                    precision=prec, plt_table=plt_tab, fixing=inp["fix"], lunit=inp["lunit"], vunit=inp["vunit"],
+                    pos64=True, vel64=True, id64=True)
+        j.run()
+        if prec == mfx.FP64:
+            ms = []
+            for _ in range(max(1, min(args.steps, 3))):
+                torch.cuda.synchronize()
+                j.run()
+                ms.append(sum(j.stage_times()))
+            res["fp64_form"] = {"value": j.num_particles / (np.mean(ms) * 1e-3), "unit": "particles/s",
+                                "ms_per_step": float(np.mean(ms)), "steps": len(ms)}
+        jobs[prec] = j.particles()
+        j.close()
+    p64, v64, _ = jobs[mfx.FP64]
+    p32, v32, _ = jobs[mfx.FP32C]
+    spacing = inp["L"] / (inp["n"] * 2 ** (inp["lat"] / 3.0))
+    e = (p32 - p64) / spacing
+    res["error_vs_fp64"] = {"psi_rms_spacing": float(np.sqrt(np.mean(e ** 2))), "psi_max_spacing": float(np.max(np.abs(e))),
+                            "vel_rel_l2": float(np.linalg.norm(v32 - v64) / np.linalg.norm(v64)),
+                            "spacing_mpc_h": spacing}
+    res["speedup_fp32c_over_fp64"] = res["fp64_form"]["ms_per_step"] / out["ms_per_step"]
+    return res
+
+
+def oracle_sample(n_sample, name, threads_note):
+    """Times the oracle (CPU restatement, numpy + multi-threaded pocketfft) on the
+    workload's physics at grid n_sample; returns particles/s."""
+    from oracle import cosmo as ocosmo, lpt, plt as oplt
+    n, L, z, order, lat, plt, seed, fix = WORKLOADS[name]
+    c = ocosmo.Cosmology()
+    a = 1.0 / (1.0 + z)
+    dplus, vfac = c.growth(a), c.vfact(a)
+    seeds = lpt.ngenic_seed_table(seed, n_sample)
+    grad = None
+    tab_s = 0.0
+    if plt:
+        t0 = time.perf_counter()
+        tab = oplt.plt_tables(lat)
+        tab_s = time.perf_counter() - t0
+        grad = oplt.PLTGradient(n_sample, L, tab)
+    t0 = time.perf_counter()
+    res = lpt.run_lpt(n_sample, L, seeds, c.amplitude, order, dplus, vfac, lattice=lat, lunit=L,
+                      vunit=L / np.sqrt(a), fixing=fix, grad=grad)
+    dt = time.perf_counter() - t0
+    npart = (1 << lat) * n_sample ** 3
+    return npart / dt, dt, tab_s, res
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    from oracle import lpt
+    lpt.build_lib()
+    n_sample = 128 if WORKLOADS[args.workload][0] >= 128 else WORKLOADS[args.workload][0]
+    vals, dts = [], []
+    tab_s = 0.0
+    for s in range(args.warmup + args.steps):
+        v, dt, ts, _ = oracle_sample(n_sample, args.workload, "")
+        tab_s = max(tab_s, ts)
+        if s >= args.warmup:
+            vals.append(v)
+            dts.append(dt)
+    v = float(np.mean(vals))
+    cores = os.cpu_count()
+    sample = ("full hot path (noise -> 3LPT potentials -> particles, FP64) at %d^3 of the %d^3 workload, "
+              "PLT table build (%.1f s) excluded; CPU restatement (numpy + pocketfft, %d threads for FFTs): "
+              "the reference needs FFTW3/GSL/HDF5, absent on this image" % (n_sample, WORKLOADS[args.workload][0], tab_s, cores))
+    return {"metric": "3LPT particles/s (FP32-compensated form) on 1 GB300, 3LPT+PLT BCC 256^3", "impl": "reference",
+            "value": v, "unit": "particles/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(dts)) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (NGenIC white noise, seeded)",
+            "config": describe(args.workload, args.precision),
+            "cpu_baseline": {"value": v, "unit": "particles/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="bcc256", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    (ROOT / "gpurun_out").mkdir(exist_ok=True)
+    if args.impl == "reference":
+        out = run_reference(args)
+        if out:
+            print(json.dumps(out))
+        return
+    out, eng, inp, plt_tab = run_ours(args)
+    rank, world, _ = dist_env()
+    if rank == 0:
+        if not args.no_fp64 and args.precision == "fp32c":
+            out.update(fp64_and_error(args, eng, inp, plt_tab, out))
+        if not args.no_cpu_baseline and world == 1:
+            from oracle import lpt
+            lpt.build_lib()
+            n_sample = 128 if inp["n"] >= 128 else inp["n"]
+            v, dt, ts, _ = oracle_sample(n_sample, args.workload, "")
+            out["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": os.cpu_count(), "kind": "port",
+                                   "sample": "one full hot-path pass at %d^3 of the %d^3 workload (%.1f s), PLT table build excluded; "
+                                             "CPU restatement in numpy + multi-threaded pocketfft" % (n_sample, inp["n"], dt)}
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

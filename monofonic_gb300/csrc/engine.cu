@@ -126,6 +126,8 @@ struct mfx_job {
   uint32_t *seeds = nullptr;
   double *amp = nullptr;
   double *plt = nullptr;
+  float4 *plt4 = nullptr;  // FP32 form: the PLT tables interleaved per mode
+  std::vector<float4> plt4_host;
   double2 *phase = nullptr;
   void *nf[6] = {};       // phi1, phi2, phi3, A3x, A3y, A3z
   char *region = nullptr; // M-region / assembly union
@@ -201,7 +203,7 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   L.m_field = size_t(M) * M * (M / 2 + 1) * 2 * rs;
   L.seeds = align_up(size_t(N) * N * 4);
   L.amp = align_up(d->amp_table_len * 8);
-  L.plt = d->plt ? align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 8) : 0;
+  L.plt = d->plt ? align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 8) + align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 4) : 0;
   L.phase = align_up(size_t(ns) * 3 * N * sizeof(double2));
   const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
   L.nfields = nfield * align_up(L.n_field);
@@ -476,6 +478,7 @@ template <typename R> static int run_pipeline(mfx_job *j) {
       a.A3[q] = j->nf[3 + q];
     }
     a.plt = j->d.plt ? j->plt : nullptr;
+    a.plt4 = j->d.plt ? j->plt4 : nullptr;
     a.phase = j->phase;
     a.N = N;
     a.order = order;
@@ -541,9 +544,19 @@ static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
   const int N = j->N;
   CU(cudaMemcpyAsync(j->seeds, d->seed_table, size_t(N) * N * 4, cudaMemcpyHostToDevice, j->stream));
   CU(cudaMemcpyAsync(j->amp, d->amp_table, d->amp_table_len * 8, cudaMemcpyHostToDevice, j->stream));
-  if (d->plt)
+  if (d->plt) {
     CU(cudaMemcpyAsync(j->plt, d->plt_table, size_t(MFX_PLT_TABLE_DOUBLES) * 8, cudaMemcpyHostToDevice,
                        j->stream));
+    if (!j->fp64) {
+      // interleave (D_r, D_theta, D_phi, alpha^-1) per mode for the FP32 form
+      const size_t nm = size_t(MFX_PLT_TABLE_DOUBLES) / 4;
+      j->plt4_host.resize(nm);
+      for (size_t q = 0; q < nm; ++q)
+        j->plt4_host[q] = make_float4(float(d->plt_table[q]), float(d->plt_table[nm + q]),
+                                      float(d->plt_table[2 * nm + q]), float(d->plt_table[3 * nm + q]));
+      CU(cudaMemcpyAsync(j->plt4, j->plt4_host.data(), nm * sizeof(float4), cudaMemcpyHostToDevice, j->stream));
+    }
+  }
   return MFX_OK;
 }
 
@@ -631,6 +644,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->amp = (double *)p;
   p += L.amp;
   j->plt = d->plt ? (double *)p : nullptr;
+  j->plt4 = d->plt ? (float4 *)(p + align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 8)) : nullptr;
   p += L.plt;
   j->phase = (double2 *)p;
   p += L.phase;

@@ -405,6 +405,7 @@ struct AsmArgs {
   const void *phi[3];   // phi1, phi2, phi3 (N-grid k-space, unscaled)
   const void *A3[3];
   const double *plt;    // 4 tables of 64*64*33 (D_r, D_theta, D_phi, alpha^-1) or null
+  const float4 *plt4;   // the same tables interleaved per mode in float (FP32 form)
   const double2 *phase; // [ns][3][N] exp(i s_a k_a dx)
   void *out[24];        // [shift][pos x,y,z, vel x,y,z]
   int N, order, nshift, shift0;
@@ -434,6 +435,88 @@ __device__ __forceinline__ double plt_cic(const double *T, double x, double y, d
   return v;
 }
 
+// FP32 form of the PLT gradient: the interpolation point x = i * 64/N is
+// split exactly in integers (ix = floor(64 i / N), dx = (64 i mod N)/N), the
+// direction of the interpolation point's k equals that of the mode's signed
+// index vector, and the four tables are read as one float4 per CIC corner.
+__device__ __forceinline__ void plt_grad_f32(const float4 *T, int i, int j, int k, int N, float kfac, float G[3],
+                                             float &vcorr) {
+  const int ix = (64 * i) / N, iy = (64 * j) / N, iz = (64 * k) / N;
+  const float invN = 1.0f / float(N);
+  const float dx = float((64 * i) % N) * invN, dy = float((64 * j) % N) * invN, dz = float((64 * k) % N) * invN;
+  const float tx = 1.0f - dx, ty = 1.0f - dy, tz = 1.0f - dz;
+  const int ix1 = (ix + 1) & 63, iy1 = (iy + 1) & 63, iz1 = min(iz + 1, 32);
+  auto e = [T](int p, int q, int r) { return __ldg(&T[(p * 64 + q) * 33 + r]); };
+  const float w[8] = {tx * ty * tz, tx * ty * dz, tx * dy * tz, tx * dy * dz,
+                      dx * ty * tz, dx * ty * dz, dx * dy * tz, dx * dy * dz};
+  const float4 c[8] = {e(ix, iy, iz), e(ix, iy, iz1), e(ix, iy1, iz), e(ix, iy1, iz1),
+                       e(ix1, iy, iz), e(ix1, iy, iz1), e(ix1, iy1, iz), e(ix1, iy1, iz1)};
+  float Dr = 0.f, Dt = 0.f, Dp = 0.f, al = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    Dr = fmaf(c[q].x, w[q], Dr);
+    Dt = fmaf(c[q].y, w[q], Dt);
+    Dp = fmaf(c[q].z, w[q], Dp);
+    al = fmaf(c[q].w, w[q], al);
+  }
+  const float sx = float(signed_idx(i, N)), sy = float(signed_idx(j, N)), sz = float(signed_idx(k, N));
+  const float kperp2 = sx * sx + sy * sy;
+  const float kr = sqrtf(kperp2 + sz * sz);
+  float st = 0.f, ct = 1.f, sp = 0.f, cp = 1.f;
+  if (kr > 0.f) {
+    const float kperp = sqrtf(kperp2);
+    st = kperp / kr;
+    ct = sz / kr;
+    if (kperp > 0.f) {
+      cp = sx / kperp;
+      sp = sy / kperp;
+    }
+  }
+  const float kmod = kfac * kr;
+  G[0] = kmod * (Dr * st * cp + Dt * ct * cp - Dp * sp);
+  G[1] = kmod * (Dr * st * sp + Dt * ct * sp + Dp * cp);
+  G[2] = kmod * (Dr * ct - Dt * st);
+  vcorr = al;
+}
+
+// particle::lattice_gradient::gradient / vfac_corr (particle_plt.hh:551-585):
+// the plain form evaluates the reference's FP64 expressions (interpolation
+// point i * 64/N in double, get_cic_kspace on the double tables); the FP32
+// form uses plt_grad_f32.
+template <typename R>
+__device__ __forceinline__ void plt_grad(const AsmArgs &a, int i, int j, int k, int N, R G[3], R &vcorr) {
+  if constexpr (sizeof(R) == 4) {
+    plt_grad_f32(a.plt4, i, j, k, N, float(a.kfac), G, vcorr);
+  } else {
+    const double x = double(i) * a.mapratio, y = double(j) * a.mapratio, z = double(k) * a.mapratio;
+    const double twopi = 2.0 * 3.141592653589793;
+    const double kx = (x - double(x > 32.0) * 64.0) * twopi;
+    const double ky = (y - double(y > 32.0) * 64.0) * twopi;
+    const double kz = (z - double(z > 32.0) * 64.0) * twopi;
+    const double kr = sqrt(kx * kx + ky * ky + kz * kz);
+    const double kmod = kr / a.mapratio / a.boxlen;
+    const size_t TS = size_t(64) * 64 * 33;
+    const double Dr = plt_cic(a.plt, x, y, z);
+    const double Dt = plt_cic(a.plt + TS, x, y, z);
+    const double Dp = plt_cic(a.plt + 2 * TS, x, y, z);
+    const double al = plt_cic(a.plt + 3 * TS, x, y, z);
+    double st = 0.0, ct = 1.0, sp = 0.0, cp = 1.0;
+    if (kr > 0.0) {
+      const double kperp = sqrt(kx * kx + ky * ky);
+      st = kperp / kr;
+      ct = kz / kr;
+      if (kperp > 0.0) {
+        cp = kx / kperp;
+        sp = ky / kperp;
+      }
+    }
+    G[0] = R(kmod * (Dr * st * cp + Dt * ct * cp - Dp * sp));
+    G[1] = R(kmod * (Dr * st * sp + Dt * ct * sp + Dp * cp));
+    G[2] = R(kmod * (Dr * ct - Dt * st));
+    vcorr = R(1.0 / (1.0 / al));
+  }
+}
+
 template <typename R, bool PLT>
 __global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
   using C = typename Cplx<R>::T;
@@ -444,42 +527,42 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
     const int k = int(idx % nk);
     const size_t t = idx / nk;
     const int j = int(t % N), i = int(t / N);
-    R G[3];
-    R vcorr = R(1);
+    // Gp: gradient applied to the displacement, Gv: gradient times vfac_corr
+    // applied to the velocity
+    R Gp[3], Gv[3];
     if (!PLT) {
-      // op::fourier_gradient (operators.hh:46-56): Nyquist index zeroed
+      // op::fourier_gradient (operators.hh:46-56): Nyquist index zeroed, exactly odd in k
       const R kf = R(a.kfac);
-      G[0] = (i != nh) ? R(signed_idx(i, N)) * kf : R(0);
-      G[1] = (j != nh) ? R(signed_idx(j, N)) * kf : R(0);
-      G[2] = (k != nh) ? R(k) * kf : R(0);
+      Gp[0] = (i != nh) ? R(signed_idx(i, N)) * kf : R(0);
+      Gp[1] = (j != nh) ? R(signed_idx(j, N)) * kf : R(0);
+      Gp[2] = (k != nh) ? R(k) * kf : R(0);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) Gv[d] = Gp[d];
     } else {
-      // particle::lattice_gradient::gradient / vfac_corr (particle_plt.hh:551-585)
-      const double x = double(i) * a.mapratio, y = double(j) * a.mapratio, z = double(k) * a.mapratio;
-      const double twopi = 2.0 * 3.141592653589793;
-      const double kx = (x - double(x > 32.0) * 64.0) * twopi;
-      const double ky = (y - double(y > 32.0) * 64.0) * twopi;
-      const double kz = (z - double(z > 32.0) * 64.0) * twopi;
-      const double kr = sqrt(kx * kx + ky * ky + kz * kz);
-      const double kmod = kr / a.mapratio / a.boxlen;
-      const size_t TS = size_t(64) * 64 * 33;
-      const double Dr = plt_cic(a.plt, x, y, z);
-      const double Dt = plt_cic(a.plt + TS, x, y, z);
-      const double Dp = plt_cic(a.plt + 2 * TS, x, y, z);
-      const double al = plt_cic(a.plt + 3 * TS, x, y, z);
-      double st = 0.0, ct = 1.0, sp = 0.0, cp = 1.0;
-      if (kr > 0.0) {
-        const double kperp = sqrt(kx * kx + ky * ky);
-        st = kperp / kr;
-        ct = kz / kr;
-        if (kperp > 0.0) {
-          cp = kx / kperp;
-          sp = ky / kperp;
+      R G[3], vc;
+      plt_grad<R>(a, i, j, k, N, G, vc);
+      if (k == 0) {
+        // On the kz = 0 plane the c2r sees both k and -k.  The interpolated PLT
+        // gradient is not exactly odd where the CIC stencil touches the table's
+        // Nyquist node (stored once, with +k), so the plane would not be
+        // Hermitian and the real field would depend on the FFT library's pass
+        // order.  Taking the odd part makes the input Hermitian; it equals what
+        // a c2c-then-c2r transform of the unsymmetrised plane yields.
+        const int im = i ? N - i : 0, jm = j ? N - j : 0;
+        R Gm[3], vcm;
+        plt_grad<R>(a, im, jm, 0, N, Gm, vcm);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          Gp[d] = R(0.5) * (G[d] - Gm[d]);
+          Gv[d] = R(0.5) * (G[d] * vc - Gm[d] * vcm);
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          Gp[d] = G[d];
+          Gv[d] = G[d] * vc;
         }
       }
-      G[0] = R(kmod * (Dr * st * cp + Dt * ct * cp - Dp * sp));
-      G[1] = R(kmod * (Dr * st * sp + Dt * ct * sp + Dp * cp));
-      G[2] = R(kmod * (Dr * ct - Dt * st));
-      vcorr = R(1.0 / (1.0 / al));
     }
     // phi_tot and its velocity weighting (ic_generator.cc:939-958, 994-1010)
     const C *p1 = reinterpret_cast<const C *>(a.phi[0]);
@@ -515,17 +598,15 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
     for (int d = 0; d < 3; ++d) {
       const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
       // i*(G_d phi) + i*(G_d' A_d'' - G_d'' A_d')
-      R tre = G[d] * ps_re, tim = G[d] * ps_im;
-      R vre = G[d] * vs_re, vim = G[d] * vs_im;
+      R tre = Gp[d] * ps_re, tim = Gp[d] * ps_im;
+      R vre = Gv[d] * vs_re, vim = Gv[d] * vs_im;
       if (a.order > 2) {
-        const R cre = G[d1] * Ad[d2].x - G[d2] * Ad[d1].x;
-        const R cim = G[d1] * Ad[d2].y - G[d2] * Ad[d1].y;
-        tre += cre;
-        tim += cim;
-        vre += R(a.vfac3) * cre;
-        vim += R(a.vfac3) * cim;
+        tre += Gp[d1] * Ad[d2].x - Gp[d2] * Ad[d1].x;
+        tim += Gp[d1] * Ad[d2].y - Gp[d2] * Ad[d1].y;
+        vre += R(a.vfac3) * (Gv[d1] * Ad[d2].x - Gv[d2] * Ad[d1].x);
+        vim += R(a.vfac3) * (Gv[d1] * Ad[d2].y - Gv[d2] * Ad[d1].y);
       }
-      const R pf = R(a.pfac), vf = R(a.vfac) * vcorr;
+      const R pf = R(a.pfac), vf = R(a.vfac);
       P[d] = dc ? mkc<R>(0, 0) : mkc<R>(-tim * pf, tre * pf);
       V[d] = dc ? mkc<R>(0, 0) : mkc<R>(-vim * vf, vre * vf);
     }
@@ -558,34 +639,45 @@ struct PartArgs {
 };
 
 template <typename R> __global__ void __launch_bounds__(256) k_particles(PartArgs a) {
+  // values are staged in shared memory so that the interleaved xyz stores of
+  // a block go out as one contiguous, coalesced run
+  __shared__ double s_pos[256 * 3];
+  __shared__ double s_vel[256 * 3];
   const int N = a.N;
   const size_t n3 = size_t(N) * N * N;
   const size_t rowp = size_t(N + 2);
   const size_t base = size_t(a.ishift) * n3;
   const double invN = 1.0 / double(N);
-  for (size_t cell = size_t(blockIdx.x) * blockDim.x + threadIdx.x; cell < n3;
-       cell += size_t(gridDim.x) * blockDim.x) {
-    const int k = int(cell % N);
-    const size_t t = cell / N;
-    const int j = int(t % N), i = int(t / N);
-    const size_t r = (size_t(i) * N + j) * rowp + k;
-    const double q[3] = {(double(i) + a.sx) * invN, (double(j) + a.sy) * invN, (double(k) + a.sz) * invN};
-    const size_t p = base + cell;
+  const int t = threadIdx.x;
+  for (size_t cell0 = size_t(blockIdx.x) * 256; cell0 < n3; cell0 += size_t(gridDim.x) * 256) {
+    const size_t cell = cell0 + t;
+    if (cell < n3) {
+      const int k = int(cell % N);
+      const size_t tt = cell / N;
+      const int j = int(tt % N), i = int(tt / N);
+      const size_t r = (size_t(i) * N + j) * rowp + k;
+      const double q[3] = {(double(i) + a.sx) * invN, (double(j) + a.sy) * invN, (double(k) + a.sz) * invN};
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const double psi = double(reinterpret_cast<const R *>(a.f[d])[r]);
-      const double x = q[d] * a.lunit + psi;
-      if (a.pos64) reinterpret_cast<double *>(a.pos)[3 * p + d] = x;
-      else reinterpret_cast<float *>(a.pos)[3 * p + d] = float(x);
-      const R v = reinterpret_cast<const R *>(a.f[3 + d])[r];
-      if (a.vel64) reinterpret_cast<double *>(a.vel)[3 * p + d] = double(v);
-      else reinterpret_cast<float *>(a.vel)[3 * p + d] = float(v);
+      for (int d = 0; d < 3; ++d) {
+        s_pos[3 * t + d] = q[d] * a.lunit + double(reinterpret_cast<const R *>(a.f[d])[r]);
+        s_vel[3 * t + d] = double(reinterpret_cast<const R *>(a.f[3 + d])[r]);
+      }
+      if (a.ids) {
+        const uint64_t id = a.id_offset + uint64_t(a.nshift_total) * cell + uint64_t(a.ishift);
+        if (a.id64) reinterpret_cast<uint64_t *>(a.ids)[base + cell] = id;
+        else reinterpret_cast<uint32_t *>(a.ids)[base + cell] = uint32_t(id);
+      }
     }
-    if (a.ids) {
-      const uint64_t id = a.id_offset + uint64_t(a.nshift_total) * cell + uint64_t(a.ishift);
-      if (a.id64) reinterpret_cast<uint64_t *>(a.ids)[p] = id;
-      else reinterpret_cast<uint32_t *>(a.ids)[p] = uint32_t(id);
+    __syncthreads();
+    const size_t cnt = (n3 - cell0) < 256 ? (n3 - cell0) : 256;
+    const size_t o = 3 * (base + cell0);
+    for (size_t q = t; q < 3 * cnt; q += 256) {
+      if (a.pos64) reinterpret_cast<double *>(a.pos)[o + q] = s_pos[q];
+      else reinterpret_cast<float *>(a.pos)[o + q] = float(s_pos[q]);
+      if (a.vel64) reinterpret_cast<double *>(a.vel)[o + q] = s_vel[q];
+      else reinterpret_cast<float *>(a.vel)[o + q] = float(s_vel[q]);
     }
+    __syncthreads();
   }
 }
 

@@ -41,7 +41,8 @@ struct Ranlxd1 {
   MFX_HD void seed31(uint32_t v) {
     if (v == 0) v = 1;
     uint32_t reg = v & 0x7fffffffu;
-#pragma unroll 1
+    // fully unrolled over the 12 words so that w[] stays in registers
+#pragma unroll
     for (int q = 0; q < 12; ++q) {
       uint64_t word = 0;
 #pragma unroll 8

@@ -97,8 +97,25 @@ def fft_r2c(r: np.ndarray) -> np.ndarray:
 
 
 def fft_c2r(c: np.ndarray, n: int) -> np.ndarray:
-    """Grid_FFT::FourierTransformBackward + ApplyNorm (grid_fft.cc:241-270)."""
+    """Grid_FFT::FourierTransformBackward + ApplyNorm (grid_fft.cc:241-270).
+
+    A c2r transform of a kz = 0 (or kz = N/2) plane that is not exactly
+    Hermitian is defined only up to the transform's pass order; with the PLT
+    gradient this happens at modes whose CIC stencil touches the PLT table's
+    Nyquist node.  The oracle takes the Hermitian part of those planes (what a
+    c2c-then-c2r ordering, pocketfft's and FFTW's usual one, computes)."""
+    c = hermitian_planes(c, n)
     return sfft.irfftn(c, s=(n, n, n), norm="ortho", workers=WORKERS)
+
+
+def hermitian_planes(c: np.ndarray, n: int) -> np.ndarray:
+    """(X(k) + conj X(-k)) / 2 on the kz = 0 and kz = N/2 planes."""
+    idx = (-np.arange(c.shape[0])) % c.shape[0]
+    out = c.copy()
+    for kz in (0, c.shape[2] - 1) if (n % 2 == 0) else (0,):
+        p = c[:, :, kz]
+        out[:, :, kz] = 0.5 * (p + np.conj(p[np.ix_(idx, idx)]))
+    return out
 
 
 def _signed(n: int, count: int) -> np.ndarray:

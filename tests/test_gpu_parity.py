@@ -255,6 +255,25 @@ def test_fp32c_error_in_interparticle_spacing(mfxlib, engine, oracle):
     assert np.array_equal(ids, res["ids"])
 
 
+@pytest.mark.parametrize("lattice", [0, 1])
+def test_plt_interpolated_128_fp64_and_fp32(mfxlib, engine, oracle, lattice):
+    """N > 64: the PLT tables are CIC-interpolated between nodes, including the
+    table's Nyquist node; both forms must agree with the oracle."""
+    tab = engine.plt_table(lattice)
+    c = Case(mfxlib, 128, 300.0, 24.0, 3, 4242, lattice=lattice, plt=tab)
+    res = c.oracle(oracle)
+    j = c.job(mfxlib, engine)
+    j.run()
+    check_particles(c, j, res)
+    j.close()
+    j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
+    j.run()
+    pos, vel, _ = j.particles()
+    delta = c.L / (c.n * 2 ** (lattice / 3.0))
+    assert np.sqrt(np.mean(((pos - res["pos"]) / delta) ** 2)) < 1e-6
+    assert rel_l2(vel, res["vel"]) < 2e-6
+
+
 # ---------------------------------------------------------------------------
 # edge cases and errors
 # ---------------------------------------------------------------------------
