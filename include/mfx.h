@@ -151,6 +151,22 @@ int mfx_job_set_profiling(mfx_job *job, int on);
 int mfx_job_kernel_profile(mfx_job *job, int max_entries, char *names, double *ms, double *bytes, int *launches);
 int mfx_job_destroy(mfx_job *job);
 
+/* Allocation-free white-noise fill (no counterpart in the reference): writes
+   the NGenIC noise of RNG_plugin::Fill_Grid -- raw (raw = 1) or normalised /
+   fixed / inverted (raw = 0) -- into a k-space field the caller allocated
+   (out_device, N*N*(N/2+1) complex of double for MFX_FP64 or float for
+   MFX_FP32C), for callers that cannot let a library call cudaMalloc (a host
+   code that owns all of HBM through its own pool, or one running under a
+   device-memory cap).  It allocates nothing; the device copy of the seed table
+   lives in a fixed 4 MiB __device__ array, so ngrid is limited to
+   MFX_NOALLOC_MAX_NGRID and larger sizes are rejected with MFX_EINVAL.  The
+   first call on a device resolves that array's address (make it before any
+   stream capture).  Calls share the array: calls that overlap on the GPU race,
+   so order them on one stream.  `stream` is a cudaStream_t or NULL. */
+#define MFX_NOALLOC_MAX_NGRID 1024
+int mfx_noise_fill_noalloc(mfx_engine *eng, uint32_t ngrid, double boxlen, const uint32_t *seed_table, int raw,
+                           int fixing, int inversion, int precision, void *out_device, void *stream);
+
 /* Debug hook: first `count` 48-bit words of the ranlxd1 stream of `seed`,
    computed on the device (bit-exactness check of the device generator). */
 int mfx_debug_ranlxd1_words(mfx_engine *eng, unsigned long seed, size_t count, uint64_t *out);

@@ -77,7 +77,7 @@ template <> __device__ __forceinline__ void Acc<float>::add_prod(float c, float 
 // ---------------------------------------------------------------------------
 // RANLUX words (device bit-exactness hook)
 // ---------------------------------------------------------------------------
-__global__ void k_ranlux_words(uint32_t seed, size_t count, uint64_t *out) {
+static __global__ void k_ranlux_words(uint32_t seed, size_t count, uint64_t *out) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   Ranlxd1 r;
   r.seed31(seed);

@@ -25,7 +25,7 @@ EXPORTS = [
     "mfx_job_create", "mfx_job_upload", "mfx_job_run", "mfx_job_wait", "mfx_job_fetch_particles",
     "mfx_job_particles_device", "mfx_job_fetch_field", "mfx_job_run_noise", "mfx_job_stage_times",
     "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
-    "mfx_job_destroy", "mfx_debug_ranlxd1_words",
+    "mfx_job_destroy", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
     "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
     "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
     "mfx_cosmology_amp_table", "mfx_run_config",
@@ -96,6 +96,7 @@ def load(build_if_missing: bool = False):
     L.mfx_job_set_profiling.argtypes = [vp, i32]
     L.mfx_job_kernel_profile.argtypes = [vp, i32, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i32)]
     L.mfx_job_destroy.argtypes = [vp]
+    L.mfx_noise_fill_noalloc.argtypes = [vp, u32, dbl, vp, i32, i32, i32, i32, vp, vp]
     L.mfx_debug_ranlxd1_words.argtypes = [vp, C.c_ulong, sz, vp]
     L.mfx_ngenic_seed_table.argtypes = [C.c_long, sz, vp]
     L.mfx_plt_table_build.argtypes = [vp, i32, vp]
