@@ -64,6 +64,21 @@ def dist_env():
     return rank, world, local
 
 
+def replica_throughput(local_ms, local_particles, device="cpu"):
+    """Replicas only: every rank runs its own realisation; the job's time is the
+    slowest rank's and the throughput counts every rank's particles.  Returns
+    (max ms over ranks, total particles / that time)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return local_ms, local_particles / (local_ms * 1e-3)
+    t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(local_particles)], dtype=torch.float64, device=device)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(n.item()) / (float(t.item()) * 1e-3)
+
+
 class Clocks:
     """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
 
@@ -191,12 +206,7 @@ def run_ours(args):
     clk = clocks.stop() if clocks else None
     own, ffts = job.launch_count()
     job.set_profiling(False)
-    ms_step = float(np.mean(dev_ms))
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * npart / (ms_step * 1e-3)
+    ms_step, value = replica_throughput(float(np.mean(dev_ms)), npart, device="cuda")
 
     # ---- e2e through the C ABI with host buffers ----
     pb_t, pb = pinned(npart * 3 * 8)
@@ -218,13 +228,9 @@ def run_ours(args):
         job.fetch_particles_into(pb.ctypes.data, vb.ctypes.data, ib.ctypes.data)
         e2e_t.append(time.perf_counter() - t1)
     barrier()
-    e2e_s = float(np.mean(e2e_t))
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * npart / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+    e2e_ms, e2e_val = replica_throughput(float(np.mean(e2e_t)) * 1e3, npart, device="cuda")
+    e2e = {"value": e2e_val, "unit": "particles/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
 
     out = None
     if rank == 0:
@@ -272,6 +278,241 @@ def run_ours(args):
     return out, eng, inp, plt_tab
 
 
+def ensemble_manifest():
+    """64 independent 2LPT realisations: 32 x 128^3 (seeds 1-32), 24 x 192^3
+    (33-56), 8 x 256^3 (57-64); boxes U[50,500] Mpc/h and sigma_8 U[0.7,0.9]
+    from numpy.random.default_rng(20261203); SC, z = 49."""
+    rng = np.random.default_rng(20261203)
+    boxes = rng.uniform(50.0, 500.0, size=64)
+    s8 = rng.uniform(0.7, 0.9, size=64)
+    sizes = [128] * 32 + [192] * 24 + [256] * 8
+    return [dict(seed=q + 1, ngrid=sizes[q], boxlen=float(boxes[q]), sigma8=float(s8[q]), zstart=49.0, order=2,
+                 lattice="sc") for q in range(64)]
+
+
+def run_ensemble(args):
+    """Config 4: the 64-realisation ensemble as one captured CUDA graph."""
+    import torch
+    from monofonic_gb300 import mfx
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    mfx.load(build_if_missing=True)
+    eng = mfx.Engine(local)
+    man = ensemble_manifest()
+    prec = mfx.FP32C if args.precision == "fp32c" else mfx.FP64
+    specs = []
+    host_bytes = 0
+    for m in man:
+        c = mfx.Cosmology(mfx.ini_text(m["ngrid"], m["boxlen"], m["zstart"], m["order"], m["seed"] + 1000 * rank,
+                                       m["lattice"], sigma8=m["sigma8"]))
+        sp = dict(ngrid=m["ngrid"], boxlen=m["boxlen"], order=m["order"],
+                  seed_table=mfx.ngenic_seed_table(m["seed"] + 1000 * rank, m["ngrid"]),
+                  amp_table=c.amp_table(m["ngrid"], m["boxlen"]),
+                  coef=mfx.lpt_coefficients(c.get("dplus_start"), c.get("vfact_start"), m["order"]),
+                  lattice=mfx.SC, precision=prec, lunit=m["boxlen"],
+                  vunit=m["boxlen"] / np.sqrt(1.0 / (1.0 + m["zstart"])), pos64=True, vel64=(prec == mfx.FP64),
+                  id64=True)
+        host_bytes += sp["seed_table"].nbytes + sp["amp_table"].nbytes
+        specs.append(sp)
+    t0 = time.perf_counter()
+    batch = mfx.Batch(eng, specs)
+    setup_s = time.perf_counter() - t0
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        batch.run()
+        batch.wait()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local, str(ROOT / "gpurun_out" / "clocks_ensemble.csv")) if rank == 0 else None
+    ms = []
+    for _ in range(args.steps):
+        l2_flush(flush)
+        torch.cuda.synchronize()
+        batch.run()
+        ms.append(batch.wait())
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    ms_step = float(np.mean(ms))
+    npart = batch.num_particles
+    # e2e: upload every job's tables from pinned host memory, run the graph,
+    # copy every job's particles back to pinned host memory
+    jobs = [batch.job(q) for q in range(batch.count)]
+    pin = []
+    for q, sp in enumerate(specs):
+        tt, st = pinned(sp["seed_table"].nbytes)
+        st = st[:sp["seed_table"].nbytes].view(np.uint32)
+        st[:] = sp["seed_table"]
+        ta, at = pinned(sp["amp_table"].nbytes)
+        at = at[:sp["amp_table"].nbytes].view(np.float64)
+        at[:] = sp["amp_table"]
+        n = jobs[q].num_particles
+        tp, pb = pinned(n * 24)
+        tv, vb = pinned(n * (8 if prec == mfx.FP64 else 4) * 3)
+        ti, ib = pinned(n * 8)
+        d = batch._descs[q]
+        d.seed_table, d.amp_table = st.ctypes.data, at.ctypes.data
+        pin.append((tt, ta, tp, tv, ti, pb, vb, ib, d))
+    d2h = sum(p[5].nbytes + p[6].nbytes + p[7].nbytes for p in pin)
+    e2e_t = []
+    for s in range(args.steps + 1):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for q, p in enumerate(pin):
+            mfx.check(mfx.load().mfx_job_upload(jobs[q].handle, mfx.C.byref(p[8])))
+        torch.cuda.synchronize()
+        batch.run()
+        batch.wait()
+        for q, p in enumerate(pin):
+            jobs[q].fetch_particles_into(p[5].ctypes.data, p[6].ctypes.data, p[7].ctypes.data)
+        if s > 0:
+            e2e_t.append(time.perf_counter() - t1)
+    e2e_s = float(np.mean(e2e_t))
+    out = {
+        "metric": "ensemble particles/s (64 x 2LPT SC, 128^3/192^3/256^3, one CUDA graph)",
+        "value": world * npart / (ms_step * 1e-3), "unit": "particles/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if prec == mfx.FP32C else "f64",
+        "data": "synthetic (NGenIC white noise, seeds 1-64; boxes and sigma_8 from default_rng(20261203))",
+        "config": {"workload": "ensemble64: 32x128^3 + 24x192^3 + 8x256^3, 2LPT SC z=49, " + args.precision,
+                   "realisations": 64, "particles": npart, "l2_flush": True, "graph_setup_s": setup_s},
+        "e2e": {"value": world * npart / e2e_s, "unit": "particles/s", "h2d_bytes_per_step": int(host_bytes),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
+        "clocks": clk,
+    }
+    batch.close()
+    return out
+
+
+def serving_requests(count, rng_seed=7):
+    """Config 5 request mix: N ~ U{64,128,192,256,384}, LPT order ~ U{1,2,3},
+    lattice ~ U{SC,BCC,FCC} (PLT on for BCC/FCC), sequential seeds, drawn from
+    numpy.random.default_rng(7); box scaled with N (300 Mpc/h at 256^3), z = 24."""
+    rng = np.random.default_rng(rng_seed)
+    out = []
+    for q in range(count):
+        n = int(rng.choice([64, 128, 192, 256, 384]))
+        order = int(rng.integers(1, 4))
+        lat = int(rng.integers(0, 3))
+        out.append(dict(seed=q + 1, ngrid=n, order=order, lattice=lat, plt=lat != 0, boxlen=300.0 * n / 256,
+                        zstart=24.0))
+    return out
+
+
+def run_serving(args):
+    """Config 5: Poisson arrivals into the serving loop; p50/p99 latency and
+    throughput, against the saturated (all-at-once) throughput and the same
+    job list run serially in the plain FP64 form."""
+    import threading
+    import torch
+    from monofonic_gb300 import mfx
+    torch.cuda.set_device(0)
+    mfx.load(build_if_missing=True)
+    eng = mfx.Engine(0)
+    reqs = serving_requests(args.requests)
+    plt = {lat: eng.plt_table(lat) for lat in (1, 2)}
+    cos = {}
+    specs = []
+    for r in reqs:
+        key = (r["ngrid"], r["order"])
+        if key not in cos:
+            cos[key] = mfx.Cosmology(mfx.ini_text(r["ngrid"], r["boxlen"], r["zstart"], r["order"], 1))
+        c = cos[key]
+        specs.append(dict(ngrid=r["ngrid"], boxlen=r["boxlen"], order=r["order"],
+                          seed_table=mfx.ngenic_seed_table(r["seed"], r["ngrid"]),
+                          amp_table=c.amp_table(r["ngrid"], r["boxlen"]),
+                          coef=mfx.lpt_coefficients(c.get("dplus_start"), c.get("vfact_start"), r["order"]),
+                          lattice=r["lattice"], plt_table=plt.get(r["lattice"]), precision=mfx.FP32C,
+                          lunit=r["boxlen"], vunit=r["boxlen"] / np.sqrt(1.0 / (1.0 + r["zstart"])),
+                          pos64=True, vel64=False, id64=True))
+    parts = [(1 << s["lattice"]) * s["ngrid"] ** 3 for s in specs]
+    srv = mfx.Server(eng, max_inflight=args.inflight)
+    # warm the plan pool and the memory pool with one pass over the size classes
+    warm = {}
+    for s in specs:
+        warm.setdefault((s["ngrid"], s["order"], s["lattice"]), s)
+    ts = [srv.submit(s) for s in warm.values()]
+    for t in ts:
+        srv.wait(t)
+        srv.release(t)
+
+    def saturated():
+        t0 = time.perf_counter()
+        tk = [srv.submit(s) for s in specs]
+        lat = []
+        for t in tk:
+            srv.wait(t)
+            lat.append(srv.times(t)[1])
+        span = time.perf_counter() - t0
+        for t in tk:
+            srv.release(t)
+        return span, lat
+
+    sat_span, sat_lat = saturated()
+    sat_tput = sum(parts) / sat_span
+    # Poisson arrivals at a rate giving `load` of the saturated job rate
+    rate = args.load * len(specs) / sat_span
+    rng = np.random.default_rng(11)
+    gaps = rng.exponential(1.0 / rate, size=len(specs))
+    tk = [None] * len(specs)
+    t0 = time.perf_counter()
+
+    def producer():
+        t = t0
+        for q, s in enumerate(specs):
+            t += gaps[q]
+            d = t - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tk[q] = srv.submit(s)
+
+    th = threading.Thread(target=producer)
+    clocks = Clocks(0, str(ROOT / "gpurun_out" / "clocks_serving.csv"))
+    th.start()
+    th.join()
+    lat = []
+    for t in tk:
+        srv.wait(t)
+        lat.append(srv.times(t)[1])
+    span = time.perf_counter() - t0
+    clk = clocks.stop()
+    for t in tk:
+        srv.release(t)
+    srv.close()
+    tput = sum(parts) / span
+    # the same job list in the plain FP64 form, one job at a time
+    serial_s = 0.0
+    if not args.no_fp64:
+        t1 = time.perf_counter()
+        for s in specs:
+            s64 = dict(s, precision=mfx.FP64, vel64=True)
+            j = mfx.Job(eng, s64["ngrid"], s64["boxlen"], s64["order"], s64["seed_table"], s64["amp_table"],
+                        s64["coef"], lattice=s64["lattice"], precision=mfx.FP64, plt_table=s64["plt_table"],
+                        lunit=s64["lunit"], vunit=s64["vunit"])
+            j.run()
+            j.close()
+        serial_s = time.perf_counter() - t1
+    return {
+        "metric": "serving: particles/s and p50/p99 job latency under Poisson arrivals (mixed sizes/orders/lattices)",
+        "value": tput, "unit": "particles/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": span * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (NGenIC white noise, seeds 1..%d; mix from default_rng(7))" % len(specs),
+        "config": {"workload": "serve: %d requests, N in {64..384}, order 1-3, SC/BCC/FCC (+PLT), FP32-compensated"
+                   % len(specs), "arrival_rate_jobs_per_s": rate, "load_vs_saturated": args.load,
+                   "max_inflight": args.inflight, "particles": sum(parts)},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(np.max(lat))},
+        "saturated": {"value": sat_tput, "unit": "particles/s", "span_s": sat_span,
+                      "p50_ms": float(np.percentile(sat_lat, 50)), "p99_ms": float(np.percentile(sat_lat, 99))},
+        "throughput_vs_saturated": tput / sat_tput,
+        "fp64_serial": ({"value": sum(parts) / serial_s, "unit": "particles/s", "span_s": serial_s}
+                        if serial_s else None),
+        "clocks": clk,
+    }
+
+
 def fp64_and_error(args, eng, inp, plt_tab, out):
     """Times the plain FP64 form of the same workload and states the FP32 form's
     error against it in units of the mean interparticle spacing."""
@@ -292,7 +533,9 @@ def fp64_and_error(args, eng, inp, plt_tab, out):
                 ms.append(sum(j.stage_times()))
             res["fp64_form"] = {"value": j.num_particles / (np.mean(ms) * 1e-3), "unit": "particles/s",
                                 "ms_per_step": float(np.mean(ms)), "steps": len(ms)}
-        jobs[prec] = j.particles()
+        # compared particles: all of them up to 64M, else the first 64M
+        count = min(j.num_particles, 1 << 26)
+        jobs[prec] = j.particles_range(0, count)
         j.close()
     p64, v64, _ = jobs[mfx.FP64]
     p32, v32, _ = jobs[mfx.FP32C]
@@ -300,7 +543,7 @@ def fp64_and_error(args, eng, inp, plt_tab, out):
     e = (p32 - p64) / spacing
     res["error_vs_fp64"] = {"psi_rms_spacing": float(np.sqrt(np.mean(e ** 2))), "psi_max_spacing": float(np.max(np.abs(e))),
                             "vel_rel_l2": float(np.linalg.norm(v32 - v64) / np.linalg.norm(v64)),
-                            "spacing_mpc_h": spacing}
+                            "spacing_mpc_h": spacing, "particles_compared": int(count)}
     res["speedup_fp32c_over_fp64"] = res["fp64_form"]["ms_per_step"] / out["ms_per_step"]
     return res
 
@@ -364,7 +607,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bcc256", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="bcc256", choices=sorted(WORKLOADS) + ["ensemble64", "serve"])
+    ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
+    ap.add_argument("--load", type=float, default=0.8, help="serve: arrival rate / saturated job rate")
+    ap.add_argument("--inflight", type=int, default=8, help="serve: max jobs in flight")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
@@ -373,6 +619,14 @@ def main():
     if args.impl == "reference":
         out = run_reference(args)
         if out:
+            print(json.dumps(out))
+        return
+    if args.workload == "serve":
+        print(json.dumps(run_serving(args)))
+        return
+    if args.workload == "ensemble64":
+        out = run_ensemble(args)
+        if dist_env()[0] == 0:
             print(json.dumps(out))
         return
     out, eng, inp, plt_tab = run_ours(args)

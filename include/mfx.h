@@ -126,6 +126,10 @@ int mfx_job_wait(mfx_job *job, int timeout_ms);
    interleaved xyz) into caller buffers; each pointer may be host or device
    memory or NULL to skip. */
 int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids);
+/* Copies particles [first, first + count) only, for output plugins that write
+   a large container in chunks (the reference's plugins write the whole
+   container at once, output_plugin.hh:62-68). */
+int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void *pos, void *vel, void *ids);
 /* Device pointers of the particle arrays (valid until the next run/destroy). */
 int mfx_job_particles_device(mfx_job *job, const void **pos, const void **vel, const void **ids,
                              size_t *num_particles);
@@ -150,6 +154,52 @@ int mfx_job_launch_count(mfx_job *job, int *own_kernels, int *fft_execs);
 int mfx_job_set_profiling(mfx_job *job, int on);
 int mfx_job_kernel_profile(mfx_job *job, int max_entries, char *names, double *ms, double *bytes, int *launches);
 int mfx_job_destroy(mfx_job *job);
+
+/* Autotuner of the FP32 form's fused transforms: times every admissible
+   pencil-tile shape (pencils per CTA of the x/y passes, rows per CTA of the z
+   passes) on the job's own buffers and keeps the fastest for the job and, per
+   grid size, for later jobs of the engine.  Returns the chosen shape (0, 0
+   when the job does not use the fused transforms).  The reference has no
+   tunables: its FFTW plans use FFTW_ESTIMATE (general.hh:87-93). */
+int mfx_job_autotune(mfx_job *job, int *pencils_xy, int *rows_z);
+
+/* Captures the job's whole pipeline into a CUDA graph; later mfx_job_run
+   calls replay it with one cudaGraphLaunch (no per-kernel launch cost).  The
+   reference has no equivalent: it runs the same stages as OpenMP loops and
+   FFTW calls (ic_generator.cc:288-1060).  Stage times and per-launch
+   profiling are not recorded for graph replays. */
+int mfx_job_capture(mfx_job *job);
+
+/* Ensemble of independent realisations (uneven grid sizes, seeds, boxes)
+   run as ONE executable CUDA graph whose parallel branches are the jobs'
+   captured pipelines.  The reference runs one realisation per process
+   invocation (main.cc:73-289).  mfx_batch_wait returns the device time of the
+   whole graph; mfx_batch_job gives access to each job (fetch particles or
+   fields); the batch owns the jobs. */
+typedef struct mfx_batch mfx_batch;
+int mfx_batch_create(mfx_engine *eng, const mfx_job_desc *descs, int count, mfx_batch **out);
+int mfx_batch_run(mfx_batch *b);
+int mfx_batch_wait(mfx_batch *b, double *device_ms);
+int mfx_batch_job(mfx_batch *b, int index, mfx_job **job);
+int mfx_batch_destroy(mfx_batch *b);
+
+/* Serving: a request loop with admission by HBM footprint (no counterpart in
+   the reference, which runs one job per process, main.cc:73-289).  Submitted
+   jobs (their tables are copied) wait in a FIFO queue; an admission thread
+   admits the head as soon as fewer than max_inflight jobs run and its arena
+   fits the engine's HBM budget, and runs it on its own stream, so jobs that
+   arrive while others are on the GPU overlap with them.  Results stay
+   resident until mfx_server_release; mfx_server_job gives the finished job
+   (fetch particles / fields through the mfx_job_* calls).
+   mfx_server_ticket_times: submit -> admit and submit -> done (ms). */
+typedef struct mfx_server mfx_server;
+int mfx_server_create(mfx_engine *eng, int max_inflight, mfx_server **out);
+int mfx_server_submit(mfx_server *s, const mfx_job_desc *desc, uint64_t *ticket);
+int mfx_server_wait(mfx_server *s, uint64_t ticket, int timeout_ms);
+int mfx_server_ticket_times(mfx_server *s, uint64_t ticket, double *queued_ms, double *latency_ms);
+int mfx_server_job(mfx_server *s, uint64_t ticket, mfx_job **job);
+int mfx_server_release(mfx_server *s, uint64_t ticket);
+int mfx_server_destroy(mfx_server *s);
 
 /* Allocation-free white-noise fill (no counterpart in the reference): writes
    the NGenIC noise of RNG_plugin::Fill_Grid -- raw (raw = 1) or normalised /

@@ -22,6 +22,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -32,6 +33,7 @@
 #include "../../include/mfx.h"
 #include "common.h"
 #include "kernels.cuh"
+#include "fused.cuh"
 
 namespace mfx {
 
@@ -96,17 +98,25 @@ static const double kShifts[3][4][3] = {
 
 using namespace mfx;
 
+struct Plan {
+  cufftHandle h = 0;
+  size_t work = 0;
+  bool valid = false;
+  int n = 0;
+  bool fp64 = false, r2c = false;
+};
+
 struct mfx_engine {
   int device = 0;
   size_t budget = 0;
   std::mutex mu;
   size_t in_use = 0;
-};
-
-struct Plan {
-  cufftHandle h = 0;
-  size_t work = 0;
-  bool valid = false;
+  // cuFFT plans returned by finished jobs, reused by later jobs of the same
+  // size class (plan creation is the slowest part of admitting a job)
+  std::vector<Plan> plan_pool;
+  // autotuned pencil-tile shapes of the fused transforms per grid size:
+  // N -> (pencils per CTA of the x/y passes, rows per CTA of the z passes)
+  std::map<int, std::pair<int, int>> ff_tuned;
 };
 
 struct mfx_job {
@@ -114,6 +124,10 @@ struct mfx_job {
   mfx_job_desc d{};
   int N = 0, M = 0, nh = 0, nk = 0, mk = 0, ns = 0, group = 0;
   bool fp64 = true;
+  bool fused = false;          // padded convolutions through fused.cuh
+  int ff_pxy = 16, ff_pz = 8;  // pencils per CTA (x/y passes) and rows per CTA (z passes)
+  void *ff_b = nullptr;        // [N][M][N/2] complex scratch
+  void *ff_d[4] = {};          // [M][M][N/2] complex scratch
   size_t rsize = 8;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[6] = {};
@@ -129,6 +143,7 @@ struct mfx_job {
   float4 *plt4 = nullptr;  // FP32 form: the PLT tables interleaved per mode
   std::vector<float4> plt4_host;
   double2 *phase = nullptr;
+  double *qtab = nullptr;  // [shift][axis][N] unperturbed coordinates times lunit
   void *nf[6] = {};       // phi1, phi2, phi3, A3x, A3y, A3z
   char *region = nullptr; // M-region / assembly union
   size_t region_bytes = 0;
@@ -138,6 +153,9 @@ struct mfx_job {
   void *work = nullptr;
   size_t work_bytes = 0;
   Plan m_r2c, m_c2r, n_c2r;
+  // CUDA graph of the whole pipeline (mfx_job_capture)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
   // accounting
   int own_launches = 0, fft_execs = 0;
   bool has_run = false, noise_only = false;
@@ -173,6 +191,7 @@ struct Layout {
   size_t seeds, amp, plt, phase, nfields, region, work_est, total;
   size_t n_field, m_field, asm_bytes, part_bytes, mregion;
   int nslots, group;
+  size_t ff_b, ff_d;
 };
 
 static size_t n_field_bytes(int N, size_t rs) { return size_t(N) * N * (N / 2 + 1) * 2 * rs; }
@@ -194,6 +213,18 @@ static int check_desc(const mfx_job_desc *d) {
   return MFX_OK;
 }
 
+// FP32 form with a padded length M = 2^a 3^b and N/2 a multiple of 8 can run
+// the padded convolutions through the pruned, fused transforms (fused.cuh);
+// the plain FP64 form and other sizes use cuFFT.  MFX_FUSED=1 selects the
+// fused transforms, MFX_FUSED=0 (the default) cuFFT.
+static bool fused_supported(const mfx_job_desc *d) {
+  if (d->precision != MFX_FP32C || d->lpt_order < 2) return false;
+  const char *env = getenv("MFX_FUSED");
+  if (!env || env[0] != '1') return false;
+  const int N = d->ngrid, M = 3 * N / 2;
+  return (N / 2) % 8 == 0 && ff::supported_length(M) && M <= 2304;
+}
+
 static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   Layout L{};
   const int N = d->ngrid, M = 3 * N / 2;
@@ -204,11 +235,18 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   L.seeds = align_up(size_t(N) * N * 4);
   L.amp = align_up(d->amp_table_len * 8);
   L.plt = d->plt ? align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 8) + align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 4) : 0;
-  L.phase = align_up(size_t(ns) * 3 * N * sizeof(double2));
+  L.phase = align_up(size_t(ns) * 3 * N * sizeof(double2)) + align_up(size_t(ns) * 3 * N * sizeof(double));
   const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
   L.nfields = nfield * align_up(L.n_field);
-  L.nslots = d->lpt_order == 1 ? 0 : (d->lpt_order == 2 ? 7 : (rs == 4 ? 18 : 17));
+  L.nslots = d->lpt_order == 1 ? 0 : (d->lpt_order == 2 ? 7 : 17);
   L.mregion = size_t(L.nslots) * align_up(L.m_field);
+  if (fused_supported(d)) {
+    // pruned-transform scratch: one [N][M][N/2] and up to four [M][M][N/2]
+    const size_t kh = N / 2;
+    L.ff_b = align_up(size_t(N) * M * kh * 8);
+    L.ff_d = align_up(size_t(M) * M * kh * 8);
+    L.mregion += L.ff_b + (d->lpt_order == 3 ? 4 : 1) * L.ff_d;
+  }
   const size_t np = size_t(ns) * N * N * N;
   L.part_bytes = 0;
   if (d->want_particles) {
@@ -253,6 +291,36 @@ static int make_plan(Plan &p, int n, bool fp64, bool r2c) {
 
 static void destroy_plan(Plan &p) {
   if (p.valid) cufftDestroy(p.h);
+  p.valid = false;
+}
+
+static int acquire_plan(mfx_engine *eng, Plan &p, int n, bool fp64, bool r2c) {
+  {
+    std::lock_guard<std::mutex> lk(eng->mu);
+    for (size_t q = 0; q < eng->plan_pool.size(); ++q) {
+      const Plan &c = eng->plan_pool[q];
+      if (c.n == n && c.fp64 == fp64 && c.r2c == r2c) {
+        p = c;
+        eng->plan_pool.erase(eng->plan_pool.begin() + q);
+        return MFX_OK;
+      }
+    }
+  }
+  TRY(make_plan(p, n, fp64, r2c));
+  p.n = n;
+  p.fp64 = fp64;
+  p.r2c = r2c;
+  return MFX_OK;
+}
+
+static void release_plan(mfx_engine *eng, Plan &p) {
+  if (!p.valid) return;
+  std::lock_guard<std::mutex> lk(eng->mu);
+  if (eng->plan_pool.size() < 96) {
+    eng->plan_pool.push_back(p);
+  } else {
+    cufftDestroy(p.h);
+  }
   p.valid = false;
 }
 
@@ -384,6 +452,287 @@ template <typename R> static int unpad_invlap(mfx_job *j, void *F, void *out) {
   return MFX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// pruned, fused transforms of the FP32 form (fused.cuh)
+// ---------------------------------------------------------------------------
+static constexpr size_t kFFSmemCap = 200 * 1024;
+
+static size_t ff_smem(int M, int pencils) { return size_t(M + 2 * M * pencils) * sizeof(float2); }
+
+// largest power-of-two P <= pref whose tile of P*per pencils fits the cap and
+// that divides `count` (the kz extent N/2 for x/y passes, M*M rows for z)
+static int ff_pick(int M, int per, int pref, size_t count) {
+  int p = pref;
+  while (p > 1 && (ff_smem(M, p * per) > kFFSmemCap || count % size_t(p) != 0)) p >>= 1;
+  return p;
+}
+
+template <int P> static void ff_set_attrs() {
+  static int done_dev[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || done_dev[dev]) return;
+  const int cap = int(kFFSmemCap) + 16 * 1024;
+  cudaFuncSetAttribute(ff::k_ff_hess_y<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(ff::k_ff_x_inv<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(ff::k_ff_z_c2r<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(ff::k_ff_z_r2c<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(ff::k_ff_x_fwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  cudaFuncSetAttribute(ff::k_ff_y_fwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
+  done_dev[dev] = 1;
+}
+
+// launches KERNEL<P> with P in {1, 2, 4, 8, 16}
+#define FF_LAUNCH(P, KERNEL, grid, smem, stream, args)           \
+  do {                                                            \
+    switch (P) {                                                  \
+      case 16: ff_set_attrs<16>(); ff::KERNEL<16><<<grid, 256, smem, stream>>>(args); break; \
+      case 8: ff_set_attrs<8>(); ff::KERNEL<8><<<grid, 256, smem, stream>>>(args); break;    \
+      case 4: ff_set_attrs<4>(); ff::KERNEL<4><<<grid, 256, smem, stream>>>(args); break;    \
+      case 2: ff_set_attrs<2>(); ff::KERNEL<2><<<grid, 256, smem, stream>>>(args); break;    \
+      default: ff_set_attrs<1>(); ff::KERNEL<1><<<grid, 256, smem, stream>>>(args); break;   \
+    }                                                             \
+  } while (0)
+
+static void tune_fused(mfx_job *j);
+
+static ff::PassArgs ff_args(mfx_job *j) {
+  ff::PassArgs a{};
+  a.N = j->N;
+  a.M = j->M;
+  a.Kh = j->N / 2;
+  a.kfac = float(2.0 * M_PI / j->d.boxlen);
+  return a;
+}
+
+// c2r of the six padded Hessians of an N-grid field into H[0..5]
+static int ff_hessians(mfx_job *j, const void *phi, void **H) {
+  const int N = j->N, M = j->M, Kh = N / 2;
+  const double M3 = double(M) * M * M;
+  const double bN = double(N) * M * Kh * 8, bM = double(M) * M * Kh * 8;
+  const int pxy = ff_pick(M, 1, j->ff_pxy, Kh), pz = ff_pick(M, 1, j->ff_pz, size_t(M) * M);
+  for (int c = 0; c < 6; ++c) {
+    ff::PassArgs a = ff_args(j);
+    a.in = static_cast<const float2 *>(phi);
+    a.out = static_cast<float2 *>(j->ff_b);
+    a.ca = kHa[c];
+    a.cb = kHb[c];
+    a.fac = float(std::pow(1.5, 1.5) / std::sqrt(M3));
+    KBEGIN(j);
+    FF_LAUNCH(pxy, k_ff_hess_y, dim3(N, Kh / pxy), ff_smem(M, pxy), j->stream, a);
+    KEND(j, "ff_hess_y", double(N) * N * Kh * 8 + bN);
+    ff::PassArgs b = ff_args(j);
+    b.in = static_cast<const float2 *>(j->ff_b);
+    b.out = static_cast<float2 *>(j->ff_d[0]);
+    KBEGIN(j);
+    FF_LAUNCH(pxy, k_ff_x_inv, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, b);
+    KEND(j, "ff_x_inv", bN + bM);
+    ff::PassArgs z = ff_args(j);
+    z.in = static_cast<const float2 *>(j->ff_d[0]);
+    z.rout = static_cast<float *>(H[c]);
+    KBEGIN(j);
+    FF_LAUNCH(pz, k_ff_z_c2r, dim3(M * M / pz), ff_smem(M, pz), j->stream, z);
+    KEND(j, "ff_z_c2r", bM + double(j->m_field_bytes));
+  }
+  return MFX_OK;
+}
+
+// r2c of real-space sources formed from rin (kind ff::SRC_*), unpadded and
+// inverse-Laplacian'd into the N-grid fields outs[0..nout)
+static int ff_sources(mfx_job *j, int kind, const void *const *rin, int nin, int nout, void **outs) {
+  const int N = j->N, M = j->M, Kh = N / 2;
+  const double M3 = double(M) * M * M, N3 = double(N) * N * N;
+  const double bN = double(N) * M * Kh * 8, bM = double(M) * M * Kh * 8;
+  const int pxy = ff_pick(M, 1, j->ff_pxy, Kh), pz = ff_pick(M, nout, j->ff_pz, size_t(M) * M);
+  ff::PassArgs z = ff_args(j);
+  for (int q = 0; q < nin; ++q) z.rin[q] = static_cast<const float *>(rin[q]);
+  for (int o = 0; o < nout; ++o) z.dout[o] = static_cast<float2 *>(j->ff_d[o]);
+  z.kind = kind;
+  z.nout = nout;
+  KBEGIN(j);
+  FF_LAUNCH(pz, k_ff_z_r2c, dim3(M * M / pz), ff_smem(M, pz * nout), j->stream, z);
+  KEND(j, "ff_z_r2c", nin * double(j->m_field_bytes) + nout * bM);
+  for (int o = 0; o < nout; ++o) {
+    ff::PassArgs x = ff_args(j);
+    x.in = static_cast<const float2 *>(j->ff_d[o]);
+    x.out = static_cast<float2 *>(j->ff_b);
+    KBEGIN(j);
+    FF_LAUNCH(pxy, k_ff_x_fwd, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, x);
+    KEND(j, "ff_x_fwd", bM + bN);
+    ff::PassArgs y = ff_args(j);
+    y.in = static_cast<const float2 *>(j->ff_b);
+    y.out = static_cast<float2 *>(outs[o]);
+    y.kind = 0;
+    y.fac = float(1.0 / std::sqrt(M3) / (std::sqrt(M3) / std::sqrt(N3)));
+    KBEGIN(j);
+    FF_LAUNCH(pxy, k_ff_y_fwd, dim3(N, Kh / pxy), ff_smem(M, pxy), j->stream, y);
+    KEND(j, "ff_y_fwd", bN + double(j->n_field_bytes));
+  }
+  return MFX_OK;
+}
+
+// convolve3's first pair: product A*B truncated to the N-grid modes and
+// transformed back to the padded real grid (T)
+static int ff_truncated_pair(mfx_job *j, const void *A, const void *B, void *T) {
+  const int N = j->N, M = j->M, Kh = N / 2;
+  const double M3 = double(M) * M * M, N3 = double(N) * N * N;
+  const double bN = double(N) * M * Kh * 8, bM = double(M) * M * Kh * 8;
+  const int pxy = ff_pick(M, 1, j->ff_pxy, Kh), pz = ff_pick(M, 1, j->ff_pz, size_t(M) * M);
+  ff::PassArgs z = ff_args(j);
+  z.rin[0] = static_cast<const float *>(A);
+  z.rin[1] = static_cast<const float *>(B);
+  z.dout[0] = static_cast<float2 *>(j->ff_d[0]);
+  z.kind = ff::SRC_PAIR;
+  z.nout = 1;
+  KBEGIN(j);
+  FF_LAUNCH(pz, k_ff_z_r2c, dim3(M * M / pz), ff_smem(M, pz), j->stream, z);
+  KEND(j, "ff_z_r2c", 2.0 * double(j->m_field_bytes) + bM);
+  ff::PassArgs x = ff_args(j);
+  x.in = static_cast<const float2 *>(j->ff_d[0]);
+  x.out = static_cast<float2 *>(j->ff_b);
+  KBEGIN(j);
+  FF_LAUNCH(pxy, k_ff_x_fwd, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, x);
+  KEND(j, "ff_x_fwd", bM + bN);
+  ff::PassArgs y = ff_args(j);
+  y.in = static_cast<const float2 *>(j->ff_b);
+  y.out2 = static_cast<float2 *>(j->ff_b);  // each CTA owns its tile: in place
+  y.kind = 1;
+  const double rfac_u = std::sqrt(M3) / std::sqrt(N3), rfac_p = std::pow(1.5, 1.5);
+  y.fac = float((1.0 / std::sqrt(M3) / rfac_u) * rfac_p / std::sqrt(M3));
+  KBEGIN(j);
+  FF_LAUNCH(pxy, k_ff_y_fwd, dim3(N, Kh / pxy), ff_smem(M, pxy), j->stream, y);
+  KEND(j, "ff_y_trunc", 2.0 * bN);
+  ff::PassArgs xi = ff_args(j);
+  xi.in = static_cast<const float2 *>(j->ff_b);
+  xi.out = static_cast<float2 *>(j->ff_d[0]);
+  KBEGIN(j);
+  FF_LAUNCH(pxy, k_ff_x_inv, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, xi);
+  KEND(j, "ff_x_inv", bN + bM);
+  ff::PassArgs zc = ff_args(j);
+  zc.in = static_cast<const float2 *>(j->ff_d[0]);
+  zc.rout = static_cast<float *>(T);
+  KBEGIN(j);
+  FF_LAUNCH(pz, k_ff_z_c2r, dim3(M * M / pz), ff_smem(M, pz), j->stream, zc);
+  KEND(j, "ff_z_c2r", bM + double(j->m_field_bytes));
+  return MFX_OK;
+}
+
+// LPT potentials phi2, phi3, A3 through the fused transforms (FP32 form)
+static int run_potentials_fused(mfx_job *j) {
+  const int order = j->d.lpt_order;
+  void **H1 = &j->mslot[0];
+  TRY(ff_hessians(j, j->nf[0], H1));
+  {
+    const void *rin[6] = {H1[0], H1[1], H1[2], H1[3], H1[4], H1[5]};
+    void *outs[1] = {j->nf[1]};
+    TRY(ff_sources(j, ff::SRC_PHI2, rin, 6, 1, outs));
+  }
+  if (j->timed) CU(cudaEventRecord(j->ev[2], j->stream));
+  if (order >= 3) {
+    void **T = &j->mslot[6];
+    void **H2 = &j->mslot[11];
+    struct Pair { int a, b; };
+    const Pair pr[5] = {{0, 1}, {3, 4}, {5, 5}, {4, 4}, {3, 3}};  // xx*yy, xy*xz, yz^2, xz^2, xy^2
+    for (int t = 0; t < 5; ++t) TRY(ff_truncated_pair(j, H1[pr[t].a], H1[pr[t].b], T[t]));
+    TRY(ff_hessians(j, j->nf[1], H2));
+    const void *rin[17];
+    for (int c = 0; c < 6; ++c) {
+      rin[c] = H1[c];
+      rin[6 + c] = H2[c];
+    }
+    for (int t = 0; t < 5; ++t) rin[12 + t] = T[t];
+    void *outs[4] = {j->nf[2], j->nf[3], j->nf[4], j->nf[5]};
+    TRY(ff_sources(j, ff::SRC_PHI3, rin, 17, 4, outs));
+  }
+  return MFX_OK;
+}
+
+// pencil-tile shapes chosen by mfx_job_autotune for this size class, if any
+static void tune_fused(mfx_job *j) {
+  std::lock_guard<std::mutex> lk(j->eng->mu);
+  auto it = j->eng->ff_tuned.find(j->N);
+  if (it != j->eng->ff_tuned.end()) {
+    j->ff_pxy = it->second.first;
+    j->ff_pz = it->second.second;
+  }
+}
+
+// Times the fused passes for every admissible pencil-tile shape on the job's
+// own buffers and keeps the fastest per size class (engine-wide cache).
+static int autotune_fused(mfx_job *j) {
+  const int N = j->N, M = j->M, Kh = N / 2;
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  auto timed = [&](auto &&launch) -> float {
+    launch();  // warm
+    cudaEventRecord(e0, j->stream);
+    launch();
+    cudaEventRecord(e1, j->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+  };
+  const bool prof = j->prof;
+  j->prof = false;
+  int best_xy = j->ff_pxy, best_z = j->ff_pz;
+  float tbest = 1e30f;
+  for (int p : {16, 8, 4}) {
+    if (ff_pick(M, 1, p, Kh) != p) continue;
+    ff::PassArgs a = ff_args(j);
+    a.in = static_cast<const float2 *>(j->nf[0]);
+    a.out = static_cast<float2 *>(j->ff_b);
+    a.ca = a.cb = 0;
+    a.fac = 1.f;
+    ff::PassArgs b = ff_args(j);
+    b.in = static_cast<const float2 *>(j->ff_b);
+    b.out = static_cast<float2 *>(j->ff_d[0]);
+    ff::PassArgs c = ff_args(j);
+    c.in = static_cast<const float2 *>(j->ff_d[0]);
+    c.out = static_cast<float2 *>(j->ff_b);
+    const float t = timed([&] {
+      FF_LAUNCH(p, k_ff_hess_y, dim3(N, Kh / p), ff_smem(M, p), j->stream, a);
+      FF_LAUNCH(p, k_ff_x_inv, dim3(M, Kh / p), ff_smem(M, p), j->stream, b);
+      FF_LAUNCH(p, k_ff_x_fwd, dim3(M, Kh / p), ff_smem(M, p), j->stream, c);
+    });
+    if (t < tbest) {
+      tbest = t;
+      best_xy = p;
+    }
+  }
+  tbest = 1e30f;
+  for (int p : {16, 8, 4, 2}) {
+    if (ff_pick(M, 1, p, size_t(M) * M) != p) continue;
+    ff::PassArgs zc = ff_args(j);
+    zc.in = static_cast<const float2 *>(j->ff_d[0]);
+    zc.rout = static_cast<float *>(j->mslot[0]);
+    ff::PassArgs zr = ff_args(j);
+    zr.rin[0] = zr.rin[1] = static_cast<const float *>(j->mslot[0]);
+    zr.dout[0] = static_cast<float2 *>(j->ff_d[0]);
+    zr.kind = ff::SRC_PAIR;
+    zr.nout = 1;
+    const float t = timed([&] {
+      FF_LAUNCH(p, k_ff_z_c2r, dim3(M * M / p), ff_smem(M, p), j->stream, zc);
+      FF_LAUNCH(p, k_ff_z_r2c, dim3(M * M / p), ff_smem(M, p), j->stream, zr);
+    });
+    if (t < tbest) {
+      tbest = t;
+      best_z = p;
+    }
+  }
+  j->prof = prof;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(MFX_ECUDA, "autotune: %s", cudaGetErrorString(e));
+  j->ff_pxy = best_xy;
+  j->ff_pz = best_z;
+  std::lock_guard<std::mutex> lk(j->eng->mu);
+  j->eng->ff_tuned[N] = {best_xy, best_z};
+  return MFX_OK;
+}
+
 template <typename R> static int run_pipeline(mfx_job *j) {
   const int order = j->d.lpt_order;
   const size_t mreal = size_t(j->M) * j->M * (j->M + 2);
@@ -396,6 +745,9 @@ template <typename R> static int run_pipeline(mfx_job *j) {
   TRY(launch_noise<R>(j, 2, j->nf[0]));
   if (j->timed) CU(cudaEventRecord(j->ev[1], j->stream));
   void **H1 = &j->mslot[0];
+  if (j->fused) {
+    TRY(run_potentials_fused(j));
+  } else {
   if (order >= 2) {
     TRY(hessians<R>(j, j->nf[0], H1));
     SrcArgs s{};
@@ -409,65 +761,51 @@ template <typename R> static int run_pipeline(mfx_job *j) {
   }
   if (j->timed) CU(cudaEventRecord(j->ev[2], j->stream));
   if (order >= 3) {
-    // phi3a: pairwise dealiased triple products (ic_generator.cc:577-586)
-    struct Tri { int a, b, c; double coef; };
-    const Tri tri[5] = {{0, 1, 2, 1.0}, {3, 4, 5, 2.0}, {5, 5, 0, -1.0}, {4, 4, 1, -1.0}, {3, 3, 2, -1.0}};
-    void *T = j->mslot[6], *hi = j->mslot[7];
-    void *lo = j->fp64 ? nullptr : j->mslot[17];
+    // phi3a: pairwise dealiased triple products (ic_generator.cc:577-586).
+    // The five first-pair products are formed in one pass, each is truncated to
+    // the N-grid modes (r2c, unpad, re-pad, c2r), and one fused kernel combines
+    // them with the third factors, the phi3b terms and the A3 sources.
+    void **T = &j->mslot[6];
+    void **H2 = &j->mslot[11];
     const double M3 = double(j->M) * j->M * j->M, N3 = double(j->N) * j->N * j->N;
     const double rfac_u = std::sqrt(M3) / std::sqrt(N3), rfac_p = std::pow(1.5, 1.5);
-    for (int t = 0; t < 5; ++t) {
+    {
       SrcArgs s{};
-      s.h1[0] = H1[tri[t].a];
-      s.h1[1] = H1[tri[t].b];
-      s.out[0] = T;
+      for (int c = 0; c < 6; ++c) s.h1[c] = H1[c];
+      for (int t = 0; t < 5; ++t) s.out[t] = T[t];
       s.count = mreal;
       KBEGIN(j);
-      k_mul<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(s);
-      KEND(j, "mul_pair", 3.0 * j->m_field_bytes);
-      TRY(exec_fft(j, j->m_r2c, T, true));
+      k_pairs3a<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(s);
+      KEND(j, "pairs3a", 10.0 * j->m_field_bytes);
+    }
+    for (int t = 0; t < 5; ++t) {
+      TRY(exec_fft(j, j->m_r2c, T[t], true));
       TruncArgs ta;
-      ta.F = T;
+      ta.F = T[t];
       ta.N = j->N;
       ta.M = j->M;
       ta.fac = (1.0 / std::sqrt(M3) / rfac_u) * rfac_p / std::sqrt(M3);
       KBEGIN(j);
       k_trunc_repad<R><<<grid_for(size_t(j->M) * j->M * j->mk, 256, nsm), 256, 0, j->stream>>>(ta);
       KEND(j, "trunc_repad", 2.0 * j->m_field_bytes);
-      TRY(exec_fft(j, j->m_c2r, T, false));
-      SrcArgs u{};
-      u.t = T;
-      u.third = H1[tri[t].c];
-      u.hi = hi;
-      u.lo = lo;
-      u.coef = tri[t].coef;
-      u.init = (t == 0);
-      u.count = mreal;
-      KBEGIN(j);
-      k_acc3a<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(u);
-      KEND(j, "acc3a", (u.init ? 3.0 : 4.0) * j->m_field_bytes + (lo ? (u.init ? 1.0 : 2.0) : 0.0) * j->m_field_bytes);
+      TRY(exec_fft(j, j->m_c2r, T[t], false));
     }
-    // phi2 Hessians, then phi3b and A3 sources in one pass
-    void **H2 = &j->mslot[11];
     TRY(hessians<R>(j, j->nf[1], H2));
     SrcArgs s{};
     for (int c = 0; c < 6; ++c) {
       s.h1[c] = H1[c];
       s.h2[c] = H2[c];
     }
-    s.hi = hi;
-    s.lo = lo;
-    s.out[0] = hi;
-    s.out[1] = j->mslot[8];
-    s.out[2] = j->mslot[9];
-    s.out[3] = j->mslot[10];
+    for (int t = 0; t < 5; ++t) s.t[t] = T[t];
+    for (int q = 0; q < 4; ++q) s.out[q] = T[q];  // phi3 source, A3x, A3y, A3z
     s.count = mreal;
     KBEGIN(j);
     k_src3<R><<<grid_for(mreal, 256, nsm), 256, 0, j->stream>>>(s);
-    KEND(j, "src3", (lo ? 18.0 : 17.0) * j->m_field_bytes);
-    TRY(unpad_invlap<R>(j, hi, j->nf[2]));
-    for (int d = 0; d < 3; ++d) TRY(unpad_invlap<R>(j, j->mslot[8 + d], j->nf[3 + d]));
+    KEND(j, "src3", 21.0 * j->m_field_bytes);
+    TRY(unpad_invlap<R>(j, T[0], j->nf[2]));
+    for (int d = 0; d < 3; ++d) TRY(unpad_invlap<R>(j, T[1 + d], j->nf[3 + d]));
   }
+  }  // cuFFT path
   if (j->timed) CU(cudaEventRecord(j->ev[3], j->stream));
   if (j->d.want_particles) {
     const int N = j->N;
@@ -524,9 +862,14 @@ template <typename R> static int run_pipeline(mfx_job *j) {
         p.sy = kShifts[j->d.lattice][s0 + s][1];
         p.sz = kShifts[j->d.lattice][s0 + s][2];
         p.lunit = j->d.lunit;
+        p.qtab = j->qtab + size_t(s0 + s) * 3 * N;
         p.id_offset = j->d.id_offset * uint64_t(j->ns) * uint64_t(N3);
         KBEGIN(j);
-        k_particles<R><<<grid_for(size_t(N) * N * N, 256, nsm), 256, 0, j->stream>>>(p);
+        const unsigned pg = grid_for(size_t(N) * N * N / 4, 256, nsm);
+        if (p.pos64 && p.vel64) k_particles<R, double, double><<<pg, 256, 0, j->stream>>>(p);
+        else if (p.pos64) k_particles<R, double, float><<<pg, 256, 0, j->stream>>>(p);
+        else if (p.vel64) k_particles<R, float, double><<<pg, 256, 0, j->stream>>>(p);
+        else k_particles<R, float, float><<<pg, 256, 0, j->stream>>>(p);
         KEND(j, "particles", N3 * (6.0 * j->rsize + 3.0 * (p.pos64 ? 8 : 4) + 3.0 * (p.vel64 ? 8 : 4) + (p.id64 ? 8 : 4)));
       }
     }
@@ -563,10 +906,22 @@ static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
 static void free_job(mfx_job *j) {
   if (!j) return;
   if (j->stream) cudaStreamSynchronize(j->stream);
-  destroy_plan(j->m_r2c);
-  destroy_plan(j->m_c2r);
-  destroy_plan(j->n_c2r);
-  if (j->arena) cudaFree(j->arena);
+  if (j->gexec) cudaGraphExecDestroy(j->gexec);
+  if (j->graph) cudaGraphDestroy(j->graph);
+  if (j->eng) {
+    release_plan(j->eng, j->m_r2c);
+    release_plan(j->eng, j->m_c2r);
+    release_plan(j->eng, j->n_c2r);
+  } else {
+    destroy_plan(j->m_r2c);
+    destroy_plan(j->m_c2r);
+    destroy_plan(j->n_c2r);
+  }
+  // stream-ordered free: never synchronises other jobs' streams
+  if (j->arena) {
+    cudaFreeAsync(j->arena, j->stream);
+    cudaStreamSynchronize(j->stream);
+  }
   for (auto &e : j->ev)
     if (e) cudaEventDestroy(e);
   for (auto &e : j->ev_pool)
@@ -614,13 +969,20 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->timed = true;
   // plans
   size_t work = 0;
-  if (d->lpt_order >= 2) {
-    if ((rc = make_plan(j->m_r2c, j->M, j->fp64, true)) != MFX_OK) return fail(rc);
-    if ((rc = make_plan(j->m_c2r, j->M, j->fp64, false)) != MFX_OK) return fail(rc);
+  j->fused = fused_supported(d);
+  if (j->fused) {
+    // pencils per CTA: shared memory holds 2 x M x P complex floats
+    j->ff_pxy = (j->M <= 576) ? 16 : 8;
+    j->ff_pz = (j->M <= 576) ? 8 : 4;
+    tune_fused(j);
+  }
+  if (d->lpt_order >= 2 && !j->fused) {
+    if ((rc = acquire_plan(eng, j->m_r2c, j->M, j->fp64, true)) != MFX_OK) return fail(rc);
+    if ((rc = acquire_plan(eng, j->m_c2r, j->M, j->fp64, false)) != MFX_OK) return fail(rc);
     work = std::max(work, std::max(j->m_r2c.work, j->m_c2r.work));
   }
   if (d->want_particles) {
-    if ((rc = make_plan(j->n_c2r, j->N, j->fp64, false)) != MFX_OK) return fail(rc);
+    if ((rc = acquire_plan(eng, j->n_c2r, j->N, j->fp64, false)) != MFX_OK) return fail(rc);
     work = std::max(work, j->n_c2r.work);
   }
   Layout L = plan_layout(d, work);
@@ -632,10 +994,15 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     eng->in_use += L.total;
   }
   j->arena_bytes = L.total;
-  cudaError_t e = cudaMalloc(&j->arena, L.total);
+  // stream-ordered allocation from the device's default pool (kept cached,
+  // see mfx_engine_create): admitting and retiring jobs never synchronises
+  // the device
+  cudaError_t e = cudaMallocAsync(&j->arena, L.total, j->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(j->stream);
   if (e != cudaSuccess) {
     j->arena = nullptr;
-    return fail(set_error(MFX_ENOMEM, "cudaMalloc(%zu) for the job arena failed: %s", L.total,
+    cudaGetLastError();
+    return fail(set_error(MFX_ENOMEM, "allocation of %zu bytes for the job arena failed: %s", L.total,
                           cudaGetErrorString(e)));
   }
   char *p = j->arena;
@@ -647,6 +1014,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->plt4 = d->plt ? (float4 *)(p + align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 8)) : nullptr;
   p += L.plt;
   j->phase = (double2 *)p;
+  j->qtab = (double *)(p + align_up(size_t(j->ns) * 3 * j->N * sizeof(double2)));
   p += L.phase;
   const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
   j->n_field_bytes = L.n_field;
@@ -661,6 +1029,15 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->work = L.work_est ? p : nullptr;
   j->work_bytes = L.work_est;
   for (int q = 0; q < L.nslots; ++q) j->mslot[q] = j->region + size_t(q) * align_up(L.m_field);
+  if (j->fused) {
+    char *f = j->region + size_t(L.nslots) * align_up(L.m_field);
+    j->ff_b = f;
+    f += L.ff_b;
+    for (int q = 0; q < (d->lpt_order == 3 ? 4 : 1); ++q) {
+      j->ff_d[q] = f;
+      f += L.ff_d;
+    }
+  }
   j->group = L.group;
   if (d->want_particles) {
     char *a = j->region;
@@ -700,8 +1077,18 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
           const double th = kShifts[d->lattice][s][ax] * km * dx;
           ph[(size_t(s) * 3 + ax) * N + m] = make_double2(std::cos(th), std::sin(th));
         }
+    // unperturbed lattice coordinates (m + s)/N * lunit, the reference's
+    // get_unit_r_shifted(...)[axis] * lunit (grid_fft.hh:240-250,
+    // particle_generator.hh:529-531)
+    std::vector<double> qt(size_t(j->ns) * 3 * N);
+    for (int s = 0; s < j->ns; ++s)
+      for (int ax = 0; ax < 3; ++ax)
+        for (int m = 0; m < N; ++m)
+          qt[(size_t(s) * 3 + ax) * N + m] = (double(m) + kShifts[d->lattice][s][ax]) / double(N) * d->lunit;
     if (cudaMemcpyAsync(j->phase, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, j->stream) !=
-        cudaSuccess)
+            cudaSuccess ||
+        cudaMemcpyAsync(j->qtab, qt.data(), qt.size() * sizeof(double), cudaMemcpyHostToDevice, j->stream) !=
+            cudaSuccess)
       return fail(set_error(MFX_ECUDA, "phase table upload failed"));
     if (cudaStreamSynchronize(j->stream) != cudaSuccess)
       return fail(set_error(MFX_ECUDA, "phase table upload failed"));
@@ -710,6 +1097,60 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   if (cudaStreamSynchronize(j->stream) != cudaSuccess) return fail(set_error(MFX_ECUDA, "table upload failed"));
   *out = j;
   return MFX_OK;
+}
+
+// Records the job's whole pipeline into a CUDA graph (stream capture on the
+// job stream).  Per-stage events and per-launch profiling stay out of graphs.
+static int capture_pipeline(mfx_job *j, cudaGraph_t *out) {
+  const bool prof = j->prof, timed = j->timed;
+  j->prof = false;
+  j->timed = false;
+  cudaError_t e = cudaStreamBeginCapture(j->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    j->prof = prof;
+    j->timed = timed;
+    return set_error(MFX_ECUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+  }
+  const int rc = j->fp64 ? run_pipeline<double>(j) : run_pipeline<float>(j);
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(j->stream, &g);
+  j->prof = prof;
+  j->timed = timed;
+  j->has_run = false;
+  if (rc != MFX_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return set_error(MFX_ECUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+  *out = g;
+  return MFX_OK;
+}
+
+// An ensemble: independent jobs whose captured pipelines are the parallel
+// branches (child-graph nodes) of one executable graph.
+struct mfx_batch {
+  mfx_engine *eng = nullptr;
+  std::vector<mfx_job *> jobs;
+  std::vector<cudaGraph_t> children;
+  cudaGraph_t parent = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool ran = false;
+};
+
+static void free_batch(mfx_batch *b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->parent) cudaGraphDestroy(b->parent);
+  for (auto g : b->children)
+    if (g) cudaGraphDestroy(g);
+  for (auto j : b->jobs) free_job(j);
+  if (b->e0) cudaEventDestroy(b->e0);
+  if (b->e1) cudaEventDestroy(b->e1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
 }
 
 // ---------------------------------------------------------------------------
@@ -755,6 +1196,13 @@ int mfx_engine_create(const mfx_engine_opts *opts, mfx_engine **out) {
   CU(cudaMemGetInfo(&free_b, &total_b));
   auto *e = new mfx_engine();
   e->device = dev;
+  {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;  // keep freed job arenas cached in the process
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   e->budget = (opts && opts->hbm_budget_bytes) ? opts->hbm_budget_bytes : size_t(double(free_b) * 0.9);
   *out = e;
   return MFX_OK;
@@ -762,6 +1210,8 @@ int mfx_engine_create(const mfx_engine_opts *opts, mfx_engine **out) {
 }
 
 int mfx_engine_destroy(mfx_engine *eng) {
+  if (!eng) return MFX_OK;
+  for (auto &p : eng->plan_pool) destroy_plan(p);
   delete eng;
   return MFX_OK;
 }
@@ -804,7 +1254,42 @@ int mfx_job_run(mfx_job *job) {
   GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
   CU(cudaSetDevice(job->eng->device));
+  if (job->gexec) {
+    CU(cudaGraphLaunch(job->gexec, job->stream));
+    job->has_run = true;
+    job->noise_only = false;
+    return MFX_OK;
+  }
   return job->fp64 ? run_pipeline<double>(job) : run_pipeline<float>(job);
+  GUARD_END
+}
+
+int mfx_job_autotune(mfx_job *job, int *pencils_xy, int *rows_z) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  CU(cudaSetDevice(job->eng->device));
+  if (job->fused) TRY(autotune_fused(job));
+  if (pencils_xy) *pencils_xy = job->fused ? job->ff_pxy : 0;
+  if (rows_z) *rows_z = job->fused ? job->ff_pz : 0;
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_capture(mfx_job *job) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  CU(cudaSetDevice(job->eng->device));
+  if (job->gexec) return MFX_OK;
+  cudaGraph_t g = nullptr;
+  TRY(capture_pipeline(job, &g));
+  cudaError_t e = cudaGraphInstantiate(&job->gexec, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    job->gexec = nullptr;
+    return set_error(MFX_ECUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  }
+  job->graph = g;
+  return MFX_OK;
   GUARD_END
 }
 
@@ -851,6 +1336,27 @@ int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids) {
   if (pos) CU(cudaMemcpyAsync(pos, job->pos, np * 3 * (job->d.pos64 ? 8 : 4), cudaMemcpyDefault, job->stream));
   if (vel) CU(cudaMemcpyAsync(vel, job->vel, np * 3 * (job->d.vel64 ? 8 : 4), cudaMemcpyDefault, job->stream));
   if (ids) CU(cudaMemcpyAsync(ids, job->ids, np * (job->d.id64 ? 8 : 4), cudaMemcpyDefault, job->stream));
+  CU(cudaStreamSynchronize(job->stream));
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void *pos, void *vel, void *ids) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
+  if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has not produced particles");
+  if (first > job->npart || count > job->npart - first)
+    return set_error(MFX_EINVAL, "range [%zu, %zu) outside the %zu particles", first, first + count, job->npart);
+  const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
+  if (pos)
+    CU(cudaMemcpyAsync(pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count, cudaMemcpyDefault,
+                       job->stream));
+  if (vel)
+    CU(cudaMemcpyAsync(vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count, cudaMemcpyDefault,
+                       job->stream));
+  if (ids)
+    CU(cudaMemcpyAsync(ids, static_cast<char *>(job->ids) + is * first, is * count, cudaMemcpyDefault, job->stream));
   CU(cudaStreamSynchronize(job->stream));
   return MFX_OK;
   GUARD_END
@@ -985,6 +1491,82 @@ int mfx_job_destroy(mfx_job *job) {
   return MFX_OK;
 }
 
+int mfx_batch_create(mfx_engine *eng, const mfx_job_desc *descs, int count, mfx_batch **out) {
+  GUARD_BEGIN
+  if (!eng || !descs || !out || count <= 0) return set_error(MFX_EINVAL, "bad arguments");
+  CU(cudaSetDevice(eng->device));
+  auto *b = new mfx_batch();
+  b->eng = eng;
+  auto fail = [&](int rc) {
+    free_batch(b);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess)
+    return fail(set_error(MFX_ECUDA, "batch stream/event creation failed"));
+  if (cudaGraphCreate(&b->parent, 0) != cudaSuccess) return fail(set_error(MFX_ECUDA, "cudaGraphCreate failed"));
+  for (int q = 0; q < count; ++q) {
+    mfx_job *j = nullptr;
+    int rc = create_job(eng, &descs[q], &j);
+    if (rc != MFX_OK) return fail(rc);
+    b->jobs.push_back(j);
+    cudaGraph_t g = nullptr;
+    if ((rc = capture_pipeline(j, &g)) != MFX_OK) return fail(rc);
+    b->children.push_back(g);
+    cudaGraphNode_t node;
+    if (cudaGraphAddChildGraphNode(&node, b->parent, nullptr, 0, g) != cudaSuccess)
+      return fail(set_error(MFX_ECUDA, "cudaGraphAddChildGraphNode failed for job %d", q));
+  }
+  cudaError_t e = cudaGraphInstantiate(&b->exec, b->parent, 0);
+  if (e != cudaSuccess) {
+    b->exec = nullptr;
+    return fail(set_error(MFX_ECUDA, "cudaGraphInstantiate(batch): %s", cudaGetErrorString(e)));
+  }
+  *out = b;
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_batch_run(mfx_batch *b) {
+  GUARD_BEGIN
+  if (!b) return set_error(MFX_EINVAL, "null batch");
+  CU(cudaSetDevice(b->eng->device));
+  CU(cudaEventRecord(b->e0, b->stream));
+  CU(cudaGraphLaunch(b->exec, b->stream));
+  CU(cudaEventRecord(b->e1, b->stream));
+  for (auto j : b->jobs) {
+    j->has_run = true;
+    j->noise_only = false;
+  }
+  b->ran = true;
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_batch_wait(mfx_batch *b, double *device_ms) {
+  GUARD_BEGIN
+  if (!b) return set_error(MFX_EINVAL, "null batch");
+  CU(cudaStreamSynchronize(b->stream));
+  if (device_ms) {
+    float ms = 0;
+    if (b->ran) CU(cudaEventElapsedTime(&ms, b->e0, b->e1));
+    *device_ms = ms;
+  }
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_batch_job(mfx_batch *b, int index, mfx_job **job) {
+  if (!b || !job || index < 0 || index >= int(b->jobs.size())) return set_error(MFX_EINVAL, "bad arguments");
+  *job = b->jobs[index];
+  return MFX_OK;
+}
+
+int mfx_batch_destroy(mfx_batch *b) {
+  free_batch(b);
+  return MFX_OK;
+}
+
 int mfx_debug_ranlxd1_words(mfx_engine *eng, unsigned long seed, size_t count, uint64_t *out) {
   GUARD_BEGIN
   if (!eng || !out) return set_error(MFX_EINVAL, "null argument");
@@ -999,6 +1581,236 @@ int mfx_debug_ranlxd1_words(mfx_engine *eng, unsigned long seed, size_t count, u
   if (e != cudaSuccess) return set_error(MFX_ECUDA, "ranlux words: %s", cudaGetErrorString(e));
   return MFX_OK;
   GUARD_END
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Serving: a request loop with admission by HBM footprint.
+//
+// Requests are copied at submission and queued.  An admission thread admits
+// the queue head as soon as an in-flight slot is free and the job's arena fits
+// the engine's HBM budget (strict FIFO, so large jobs are not starved), runs it
+// on its own stream and keeps its fields and particles resident on the device
+// until the client fetches and releases it.  Admitted jobs overlap on the GPU;
+// arenas come from the stream-ordered pool and FFT plans from the plan pool,
+// so admission and retirement never synchronise the device.  A job's results
+// do not depend on what else runs: every job has its own arena and plans.
+// ---------------------------------------------------------------------------
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <thread>
+
+namespace {
+using clk = std::chrono::steady_clock;
+
+struct Ticket {
+  uint64_t id = 0;
+  mfx_job_desc d{};
+  std::vector<uint32_t> seeds;
+  std::vector<double> amp, plt;
+  size_t footprint = 0;
+  clk::time_point t_submit, t_admit, t_done;
+  int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+  int rc = MFX_OK;
+  std::string err;
+  mfx_job *job = nullptr;
+  cudaEvent_t done = nullptr;
+};
+}  // namespace
+
+struct mfx_server {
+  mfx_engine *eng = nullptr;
+  int max_inflight = 8;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Ticket *> queue;
+  std::map<uint64_t, std::unique_ptr<Ticket>> tickets;
+  std::thread worker;
+  bool stop = false;
+  uint64_t next_id = 1;
+  int inflight = 0;
+};
+
+static double ms_between(clk::time_point a, clk::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+static void server_loop(mfx_server *s) {
+  cudaSetDevice(s->eng->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (!s->stop) {
+    // retire finished jobs (their results stay resident)
+    for (auto &kv : s->tickets) {
+      Ticket *t = kv.second.get();
+      if (t->state != 1) continue;
+      const cudaError_t q = cudaEventQuery(t->done);
+      if (q == cudaErrorNotReady) continue;
+      t->t_done = clk::now();
+      t->state = (q == cudaSuccess) ? 2 : 3;
+      if (q != cudaSuccess) {
+        t->rc = MFX_ECUDA;
+        t->err = cudaGetErrorString(q);
+      }
+      --s->inflight;
+      s->cv.notify_all();
+    }
+    // admit from the queue head while a slot and the HBM budget allow
+    while (!s->queue.empty() && s->inflight < s->max_inflight) {
+      Ticket *t = s->queue.front();
+      bool fits;
+      {
+        std::lock_guard<std::mutex> ek(s->eng->mu);
+        fits = s->eng->in_use + t->footprint <= s->eng->budget;
+      }
+      if (!fits) break;  // wait for running jobs to finish and results to be released
+      s->queue.pop_front();
+      lk.unlock();
+      mfx_job *j = nullptr;
+      int rc = create_job(s->eng, &t->d, &j);
+      std::string err = rc == MFX_OK ? "" : g_last_error;
+      if (rc == MFX_OK) rc = j->fp64 ? run_pipeline<double>(j) : run_pipeline<float>(j);
+      if (rc == MFX_OK && cudaEventRecord(t->done, j->stream) != cudaSuccess) rc = MFX_ECUDA;
+      if (rc != MFX_OK && err.empty()) err = g_last_error;
+      lk.lock();
+      t->t_admit = clk::now();
+      if (rc != MFX_OK) {
+        if (j) free_job(j);
+        t->state = 3;
+        t->rc = rc;
+        t->err = err;
+        t->t_done = t->t_admit;
+        s->cv.notify_all();
+        continue;
+      }
+      t->job = j;
+      t->state = 1;
+      ++s->inflight;
+    }
+    s->cv.wait_for(lk, std::chrono::microseconds(s->inflight > 0 ? 50 : 2000));
+  }
+}
+
+extern "C" {
+
+int mfx_server_create(mfx_engine *eng, int max_inflight, mfx_server **out) {
+  GUARD_BEGIN
+  if (!eng || !out || max_inflight < 1) return set_error(MFX_EINVAL, "bad arguments");
+  auto *s = new mfx_server();
+  s->eng = eng;
+  s->max_inflight = max_inflight;
+  s->worker = std::thread(server_loop, s);
+  *out = s;
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_server_submit(mfx_server *s, const mfx_job_desc *desc, uint64_t *ticket) {
+  GUARD_BEGIN
+  if (!s || !ticket) return set_error(MFX_EINVAL, "null argument");
+  TRY(check_desc(desc));
+  auto t = std::make_unique<Ticket>();
+  t->d = *desc;
+  const size_t n = desc->ngrid;
+  t->seeds.assign(desc->seed_table, desc->seed_table + n * n);
+  t->amp.assign(desc->amp_table, desc->amp_table + desc->amp_table_len);
+  if (desc->plt) t->plt.assign(desc->plt_table, desc->plt_table + MFX_PLT_TABLE_DOUBLES);
+  t->d.seed_table = t->seeds.data();
+  t->d.amp_table = t->amp.data();
+  t->d.plt_table = desc->plt ? t->plt.data() : nullptr;
+  TRY(mfx_job_footprint(s->eng, desc, &t->footprint));
+  if (t->footprint > s->eng->budget)
+    return set_error(MFX_EADMIT, "job footprint %zu exceeds the engine budget %zu", t->footprint, s->eng->budget);
+  CU(cudaSetDevice(s->eng->device));
+  CU(cudaEventCreateWithFlags(&t->done, cudaEventDisableTiming));
+  t->t_submit = clk::now();
+  std::lock_guard<std::mutex> lk(s->mu);
+  t->id = s->next_id++;
+  *ticket = t->id;
+  s->queue.push_back(t.get());
+  s->tickets[t->id] = std::move(t);
+  s->cv.notify_all();
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_server_wait(mfx_server *s, uint64_t ticket, int timeout_ms) {
+  GUARD_BEGIN
+  if (!s) return set_error(MFX_EINVAL, "null server");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
+  Ticket *t = it->second.get();
+  auto pred = [t] { return t->state >= 2; };
+  if (timeout_ms < 0) s->cv.wait(lk, pred);
+  else if (!s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+    return set_error(MFX_ETIMEOUT, "ticket %llu not finished after %d ms", (unsigned long long)ticket, timeout_ms);
+  if (t->state == 3) return set_error(t->rc, "ticket %llu failed: %s", (unsigned long long)ticket, t->err.c_str());
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_server_ticket_times(mfx_server *s, uint64_t ticket, double *queued_ms, double *latency_ms) {
+  if (!s) return set_error(MFX_EINVAL, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket");
+  Ticket *t = it->second.get();
+  if (t->state < 2) return set_error(MFX_ESTATE, "ticket not finished");
+  if (queued_ms) *queued_ms = ms_between(t->t_submit, t->t_admit);
+  if (latency_ms) *latency_ms = ms_between(t->t_submit, t->t_done);
+  return MFX_OK;
+}
+
+int mfx_server_job(mfx_server *s, uint64_t ticket, mfx_job **job) {
+  if (!s || !job) return set_error(MFX_EINVAL, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket");
+  if (it->second->state != 2) return set_error(MFX_ESTATE, "ticket not finished");
+  *job = it->second->job;
+  return MFX_OK;
+}
+
+int mfx_server_release(mfx_server *s, uint64_t ticket) {
+  GUARD_BEGIN
+  if (!s) return set_error(MFX_EINVAL, "null server");
+  std::unique_ptr<Ticket> t;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket");
+    if (it->second->state < 2) return set_error(MFX_ESTATE, "ticket still queued or running");
+    t = std::move(it->second);
+    s->tickets.erase(it);
+  }
+  if (t->job) free_job(t->job);
+  if (t->done) cudaEventDestroy(t->done);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->cv.notify_all();
+  }
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_server_destroy(mfx_server *s) {
+  if (!s) return MFX_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv.notify_all();
+  }
+  if (s->worker.joinable()) s->worker.join();
+  for (auto &kv : s->tickets) {
+    if (kv.second->job) free_job(kv.second->job);
+    if (kv.second->done) cudaEventDestroy(kv.second->done);
+  }
+  delete s;
+  return MFX_OK;
 }
 
 }  // extern "C"

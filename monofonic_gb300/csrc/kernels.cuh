@@ -228,16 +228,11 @@ template <typename R> __global__ void __launch_bounds__(256) k_pad_hessian(PadAr
 // Hessian slot order: 0:xx 1:yy 2:zz 3:xy 4:xz 5:yz
 // ---------------------------------------------------------------------------
 struct SrcArgs {
-  const void *h1[6];
-  const void *h2[6];
-  const void *t;    // pairwise-truncated product (phi3a)
-  const void *third;
-  void *hi;         // running sum (phi3 source)
-  void *lo;         // its compensation term (float form)
-  void *out[4];
-  double coef;
-  int init;
-  size_t count;     // number of reals
+  const void *h1[6];  // Hessians of phi(1)
+  const void *h2[6];  // Hessians of phi(2)
+  const void *t[5];   // pairwise-truncated products of the phi(3a) triples
+  void *out[5];
+  size_t count;       // number of reals
 };
 
 // phi(2) source, ic_generator.cc:530-534:
@@ -260,50 +255,50 @@ template <typename R> __global__ void __launch_bounds__(256) k_src2(SrcArgs a) {
   }
 }
 
-// out = h1[0] * h1[1] (first pair of a pairwise-dealiased triple product)
-template <typename R> __global__ void __launch_bounds__(256) k_mul(SrcArgs a) {
-  const R *A = reinterpret_cast<const R *>(a.h1[0]);
-  const R *B = reinterpret_cast<const R *>(a.h1[1]);
-  R *out = reinterpret_cast<R *>(a.out[0]);
-  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.count;
-       q += size_t(gridDim.x) * blockDim.x)
-    out[q] = A[q] * B[q];
-}
-
-// (hi, lo) (+)= coef * t * third   (phi3a accumulation, ic_generator.cc:581-585)
-template <typename R> __global__ void __launch_bounds__(256) k_acc3a(SrcArgs a) {
-  const R *T = reinterpret_cast<const R *>(a.t);
-  const R *H = reinterpret_cast<const R *>(a.third);
-  R *hi = reinterpret_cast<R *>(a.hi);
-  R *lo = reinterpret_cast<R *>(a.lo);
-  const R c = R(a.coef);
+// First pairs of the five phi(3a) triple products (ic_generator.cc:581-585,
+// convolve3 = convolve2(convolve2(a, b), c), convolution.hh:525-532):
+//   xx*yy, xy*xz, yz*yz, xz*xz, xy*xy   -> out[0..4]
+template <typename R> __global__ void __launch_bounds__(256) k_pairs3a(SrcArgs a) {
+  const R *H[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) H[c] = reinterpret_cast<const R *>(a.h1[c]);
   for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.count;
        q += size_t(gridDim.x) * blockDim.x) {
-    Acc<R> s;
-    if (!a.init) {
-      s.hi = hi[q];
-      if (lo) s.lo = lo[q];
-    }
-    s.add_prod(c, T[q], H[q]);
-    hi[q] = s.hi;
-    if (lo) lo[q] = s.lo;
+    const R xx = H[0][q], yy = H[1][q], xy = H[3][q], xz = H[4][q], yz = H[5][q];
+    reinterpret_cast<R *>(a.out[0])[q] = xx * yy;
+    reinterpret_cast<R *>(a.out[1])[q] = xy * xz;
+    reinterpret_cast<R *>(a.out[2])[q] = yz * yz;
+    reinterpret_cast<R *>(a.out[3])[q] = xz * xz;
+    reinterpret_cast<R *>(a.out[4])[q] = xy * xy;
   }
 }
 
-// phi(3) source completion (phi3b, ic_generator.cc:592-609) and the three
-// transverse A(3) sources (ic_generator.cc:613-628), one pass over the
-// 12 Hessians.
+// Full phi(3) source and the three transverse A(3) sources in one pass over
+// the 12 Hessians and the 5 truncated pair products:
+//   phi3a (ic_generator.cc:581-585): T0 zz + 2 T1 yz - T2 xx - T3 yy - T4 zz
+//   phi3b (ic_generator.cc:592-609): -5/7 sum_i phi_ii (phi2_jj + phi2_kk)
+//                                    +10/7 sum_{i<j} phi_ij phi2_ij
+//   A3_d  (ic_generator.cc:613-628)
+// out[0] = phi3 source, out[1..3] = A3 sources.  Outputs may alias t[] slots
+// (each element is read before it is written by the same thread).
 template <typename R> __global__ void __launch_bounds__(256) k_src3(SrcArgs a) {
   const R c57 = R(-5.0 / 7.0), c107 = R(10.0 / 7.0);
   for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < a.count;
        q += size_t(gridDim.x) * blockDim.x) {
-    R p[6], s[6];
+    R p[6], s[6], T[5];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
       p[c] = reinterpret_cast<const R *>(a.h1[c])[q];
       s[c] = reinterpret_cast<const R *>(a.h2[c])[q];
     }
-    Acc<R> S(reinterpret_cast<const R *>(a.hi)[q], a.lo ? reinterpret_cast<const R *>(a.lo)[q] : R(0));
+#pragma unroll
+    for (int c = 0; c < 5; ++c) T[c] = reinterpret_cast<const R *>(a.t[c])[q];
+    Acc<R> S;
+    S.add_prod(T[0], p[2]);
+    S.add_prod(R(2), T[1], p[5]);
+    S.add_prod(R(-1), T[2], p[0]);
+    S.add_prod(R(-1), T[3], p[1]);
+    S.add_prod(R(-1), T[4], p[2]);
     S.add_prod(c57, p[0], s[1] + s[2]);
     S.add_prod(c57, p[1], s[2] + s[0]);
     S.add_prod(c57, p[2], s[0] + s[1]);
@@ -635,49 +630,85 @@ struct PartArgs {
   void *pos, *vel, *ids;
   int N, nshift_total, ishift, pos64, vel64, id64;
   double sx, sy, sz, lunit;
+  // unperturbed coordinates (m + s_axis)/N * lunit per axis, [3][N], computed on
+  // the host with the reference's expression (grid_fft.hh:240-250)
+  const double *qtab;
   uint64_t id_offset;
 };
 
-template <typename R> __global__ void __launch_bounds__(256) k_particles(PartArgs a) {
-  // values are staged in shared memory so that the interleaved xyz stores of
-  // a block go out as one contiguous, coalesced run
-  __shared__ double s_pos[256 * 3];
-  __shared__ double s_vel[256 * 3];
+// two consecutive reals of a field row (rows padded to N+2 are 8- / 16-byte
+// aligned at even k for float / double)
+template <typename R> __device__ __forceinline__ void load2(const R *p, R &x, R &y);
+template <> __device__ __forceinline__ void load2<float>(const float *p, float &x, float &y) {
+  const float2 v = *reinterpret_cast<const float2 *>(p);
+  x = v.x;
+  y = v.y;
+}
+template <> __device__ __forceinline__ void load2<double>(const double *p, double &x, double &y) {
+  const double2 v = *reinterpret_cast<const double2 *>(p);
+  x = v.x;
+  y = v.y;
+}
+
+// 12 consecutive outputs (4 particles x xyz) with 16-byte vector stores
+__device__ __forceinline__ void store12(double *o, const double *v) {
+#pragma unroll
+  for (int q = 0; q < 6; ++q) reinterpret_cast<double2 *>(o)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+}
+__device__ __forceinline__ void store12(float *o, const double *v) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q)
+    reinterpret_cast<float4 *>(o)[q] =
+        make_float4(float(v[4 * q]), float(v[4 * q + 1]), float(v[4 * q + 2]), float(v[4 * q + 3]));
+}
+
+// One thread per 4 consecutive cells along k (N is a multiple of 4): every
+// store is a 16-byte vector store and a warp writes one contiguous run.
+template <typename R, typename PosT, typename VelT>
+__global__ void __launch_bounds__(256) k_particles(PartArgs a) {
   const int N = a.N;
-  const size_t n3 = size_t(N) * N * N;
+  const size_t n3 = size_t(N) * N * N, nq = n3 / 4;
   const size_t rowp = size_t(N + 2);
   const size_t base = size_t(a.ishift) * n3;
-  const double invN = 1.0 / double(N);
-  const int t = threadIdx.x;
-  for (size_t cell0 = size_t(blockIdx.x) * 256; cell0 < n3; cell0 += size_t(gridDim.x) * 256) {
-    const size_t cell = cell0 + t;
-    if (cell < n3) {
-      const int k = int(cell % N);
-      const size_t tt = cell / N;
-      const int j = int(tt % N), i = int(tt / N);
-      const size_t r = (size_t(i) * N + j) * rowp + k;
-      const double q[3] = {(double(i) + a.sx) * invN, (double(j) + a.sy) * invN, (double(k) + a.sz) * invN};
+  for (size_t g = size_t(blockIdx.x) * blockDim.x + threadIdx.x; g < nq; g += size_t(gridDim.x) * blockDim.x) {
+    const size_t cell = 4 * g;
+    const int k = int(cell % N);
+    const size_t tt = cell / N;
+    const int j = int(tt % N), i = int(tt / N);
+    const size_t r = (size_t(i) * N + j) * rowp + k;
+    double pv[12], vv[12];
+    const double qx = __ldg(&a.qtab[i]), qy = __ldg(&a.qtab[N + j]);
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        s_pos[3 * t + d] = q[d] * a.lunit + double(reinterpret_cast<const R *>(a.f[d])[r]);
-        s_vel[3 * t + d] = double(reinterpret_cast<const R *>(a.f[3 + d])[r]);
-      }
-      if (a.ids) {
-        const uint64_t id = a.id_offset + uint64_t(a.nshift_total) * cell + uint64_t(a.ishift);
-        if (a.id64) reinterpret_cast<uint64_t *>(a.ids)[base + cell] = id;
-        else reinterpret_cast<uint32_t *>(a.ids)[base + cell] = uint32_t(id);
+    for (int d = 0; d < 3; ++d) {
+      const R *fp = reinterpret_cast<const R *>(a.f[d]) + r;
+      const R *fv = reinterpret_cast<const R *>(a.f[3 + d]) + r;
+      R p0, p1, p2, p3, v0, v1, v2, v3;
+      load2<R>(fp, p0, p1);
+      load2<R>(fp + 2, p2, p3);
+      load2<R>(fv, v0, v1);
+      load2<R>(fv + 2, v2, v3);
+      const R ps[4] = {p0, p1, p2, p3}, vs[4] = {v0, v1, v2, v3};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const double q = d == 0 ? qx : (d == 1 ? qy : __ldg(&a.qtab[2 * N + k + c]));
+        pv[3 * c + d] = q + double(ps[c]);
+        vv[3 * c + d] = double(vs[c]);
       }
     }
-    __syncthreads();
-    const size_t cnt = (n3 - cell0) < 256 ? (n3 - cell0) : 256;
-    const size_t o = 3 * (base + cell0);
-    for (size_t q = t; q < 3 * cnt; q += 256) {
-      if (a.pos64) reinterpret_cast<double *>(a.pos)[o + q] = s_pos[q];
-      else reinterpret_cast<float *>(a.pos)[o + q] = float(s_pos[q]);
-      if (a.vel64) reinterpret_cast<double *>(a.vel)[o + q] = s_vel[q];
-      else reinterpret_cast<float *>(a.vel)[o + q] = float(s_vel[q]);
+    store12(reinterpret_cast<PosT *>(a.pos) + 3 * (base + cell), pv);
+    store12(reinterpret_cast<VelT *>(a.vel) + 3 * (base + cell), vv);
+    if (a.ids) {
+      const uint64_t id0 = a.id_offset + uint64_t(a.nshift_total) * cell + uint64_t(a.ishift);
+      const uint64_t st = uint64_t(a.nshift_total);
+      if (a.id64) {
+        ulonglong2 *o = reinterpret_cast<ulonglong2 *>(reinterpret_cast<uint64_t *>(a.ids) + base + cell);
+        o[0] = make_ulonglong2(id0, id0 + st);
+        o[1] = make_ulonglong2(id0 + 2 * st, id0 + 3 * st);
+      } else {
+        *reinterpret_cast<uint4 *>(reinterpret_cast<uint32_t *>(a.ids) + base + cell) =
+            make_uint4(uint32_t(id0), uint32_t(id0 + st), uint32_t(id0 + 2 * st), uint32_t(id0 + 3 * st));
+      }
     }
-    __syncthreads();
   }
 }
 

@@ -23,9 +23,12 @@ PLT_TABLE_DOUBLES = 4 * 64 * 64 * 33
 EXPORTS = [
     "mfx_last_error", "mfx_version", "mfx_engine_create", "mfx_engine_destroy", "mfx_job_footprint",
     "mfx_job_create", "mfx_job_upload", "mfx_job_run", "mfx_job_wait", "mfx_job_fetch_particles",
+    "mfx_job_fetch_particles_range",
     "mfx_job_particles_device", "mfx_job_fetch_field", "mfx_job_run_noise", "mfx_job_stage_times",
     "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
-    "mfx_job_destroy", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
+    "mfx_job_destroy", "mfx_job_autotune", "mfx_job_capture", "mfx_batch_create", "mfx_batch_run", "mfx_batch_wait",
+    "mfx_batch_job", "mfx_batch_destroy", "mfx_server_create", "mfx_server_submit", "mfx_server_wait",
+    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
     "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
     "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
     "mfx_cosmology_amp_table", "mfx_run_config",
@@ -96,6 +99,12 @@ def load(build_if_missing: bool = False):
     L.mfx_job_set_profiling.argtypes = [vp, i32]
     L.mfx_job_kernel_profile.argtypes = [vp, i32, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i32)]
     L.mfx_job_destroy.argtypes = [vp]
+    L.mfx_job_capture.argtypes = [vp]
+    L.mfx_batch_create.argtypes = [vp, C.POINTER(JobDesc), i32, C.POINTER(vp)]
+    L.mfx_batch_run.argtypes = [vp]
+    L.mfx_batch_wait.argtypes = [vp, C.POINTER(dbl)]
+    L.mfx_batch_job.argtypes = [vp, i32, C.POINTER(vp)]
+    L.mfx_batch_destroy.argtypes = [vp]
     L.mfx_noise_fill_noalloc.argtypes = [vp, u32, dbl, vp, i32, i32, i32, i32, vp, vp]
     L.mfx_debug_ranlxd1_words.argtypes = [vp, C.c_ulong, sz, vp]
     L.mfx_ngenic_seed_table.argtypes = [C.c_long, sz, vp]
@@ -340,6 +349,18 @@ class Job:
     def fetch_particles_into(self, pos, vel, ids):
         check(load().mfx_job_fetch_particles(self._h, pos, vel, ids))
 
+    def particles_range(self, first: int, count: int):
+        """Particles [first, first + count) as numpy arrays."""
+        L = load()
+        L.mfx_job_fetch_particles_range.argtypes = [C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p,
+                                                    C.c_void_p]
+        pos = np.zeros((count, 3), dtype=np.float64 if self.pos64 else np.float32)
+        vel = np.zeros((count, 3), dtype=np.float64 if self.vel64 else np.float32)
+        ids = np.zeros(count, dtype=np.uint64 if self.id64 else np.uint32)
+        check(L.mfx_job_fetch_particles_range(self._h, first, count, pos.ctypes.data, vel.ctypes.data,
+                                              ids.ctypes.data))
+        return pos, vel, ids
+
     def stage_times(self):
         ms = (C.c_double * 8)()
         n = load().mfx_job_stage_times(self._h, ms, 8)
@@ -351,6 +372,18 @@ class Job:
         b = C.c_double()
         check(load().mfx_job_algorithmic_bytes(self._h, C.byref(b)))
         return b.value
+
+    def capture(self):
+        """Record the pipeline into a CUDA graph; later run() calls replay it."""
+        check(load().mfx_job_capture(self._h))
+
+    def autotune(self):
+        """Pick the fused transforms' pencil-tile shape; returns (pencils_xy, rows_z)."""
+        L = load()
+        L.mfx_job_autotune.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        a, b = C.c_int(), C.c_int()
+        check(L.mfx_job_autotune(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_profiling(self, on=True):
         check(load().mfx_job_set_profiling(self._h, 1 if on else 0))
@@ -373,3 +406,149 @@ class Job:
         a, b = C.c_int(), C.c_int()
         check(load().mfx_job_launch_count(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+class _JobView(Job):
+    """A job owned by a Batch (not destroyed by this wrapper)."""
+
+    def __init__(self, handle, num_particles, pos64, vel64, id64, n):
+        self._h = handle
+        self.num_particles = num_particles
+        self.pos64, self.vel64, self.id64 = pos64, vel64, id64
+        self.n = n
+
+    def close(self):
+        self._h = C.c_void_p()
+
+
+class Batch:
+    """Ensemble of independent jobs run as one CUDA graph (mfx_batch_*)."""
+
+    def __init__(self, engine: Engine, specs):
+        """specs: list of dicts with the Job() keyword arguments
+        (ngrid, boxlen, order, seed_table, amp_table, coef, lattice, precision, ...)."""
+        self.engine = engine
+        self._keep = []
+        descs = (JobDesc * len(specs))()
+        self._meta = []
+        for q, sp in enumerate(specs):
+            seed = np.ascontiguousarray(sp["seed_table"], dtype=np.uint32)
+            amp = np.ascontiguousarray(sp["amp_table"], dtype=np.float64)
+            plt = sp.get("plt_table")
+            plt = None if plt is None else np.ascontiguousarray(plt, dtype=np.float64)
+            self._keep += [seed, amp, plt]
+            d = descs[q]
+            d.ngrid, d.boxlen, d.lpt_order = sp["ngrid"], sp["boxlen"], sp["order"]
+            d.lattice = sp.get("lattice", SC)
+            d.plt = 1 if plt is not None else 0
+            d.precision = sp.get("precision", FP64)
+            d.fixing, d.inversion = int(sp.get("fixing", False)), int(sp.get("inversion", False))
+            d.seed_table, d.amp_table, d.amp_table_len = seed.ctypes.data, amp.ctypes.data, amp.size
+            d.plt_table = plt.ctypes.data if plt is not None else None
+            for k in ("g1", "g2", "g3", "g3c", "vfac1", "vfac2", "vfac3"):
+                setattr(d, k, sp["coef"][k])
+            d.lunit, d.vunit = sp.get("lunit", 1.0), sp.get("vunit", 1.0)
+            d.pos64, d.vel64, d.id64 = int(sp.get("pos64", True)), int(sp.get("vel64", True)), int(sp.get("id64", True))
+            d.id_offset = sp.get("id_offset", 0)
+            d.want_particles = int(sp.get("want_particles", True))
+            self._meta.append(((1 << d.lattice) * d.ngrid ** 3, bool(d.pos64), bool(d.vel64), bool(d.id64), d.ngrid))
+        self._descs = descs
+        self._h = C.c_void_p()
+        check(load().mfx_batch_create(engine.handle, descs, len(specs), C.byref(self._h)))
+        self.count = len(specs)
+        self.num_particles = sum(m[0] for m in self._meta)
+
+    def run(self):
+        check(load().mfx_batch_run(self._h))
+
+    def wait(self) -> float:
+        ms = C.c_double()
+        check(load().mfx_batch_wait(self._h, C.byref(ms)))
+        return ms.value
+
+    def job(self, q: int) -> Job:
+        h = C.c_void_p()
+        check(load().mfx_batch_job(self._h, q, C.byref(h)))
+        return _JobView(h, *self._meta[q])
+
+    def close(self):
+        if self._h and self._h.value:
+            load().mfx_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request loop with admission by HBM footprint (mfx_server_*)."""
+
+    def __init__(self, engine: Engine, max_inflight: int = 8):
+        L = load()
+        L.mfx_server_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+        L.mfx_server_submit.argtypes = [C.c_void_p, C.POINTER(JobDesc), C.POINTER(C.c_uint64)]
+        L.mfx_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int]
+        L.mfx_server_ticket_times.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.mfx_server_job.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]
+        L.mfx_server_release.argtypes = [C.c_void_p, C.c_uint64]
+        L.mfx_server_destroy.argtypes = [C.c_void_p]
+        self.engine = engine
+        self._h = C.c_void_p()
+        check(L.mfx_server_create(engine.handle, max_inflight, C.byref(self._h)))
+        self._meta = {}
+
+    def submit(self, sp) -> int:
+        """sp: dict of Job() keyword arguments (see Batch)."""
+        seed = np.ascontiguousarray(sp["seed_table"], dtype=np.uint32)
+        amp = np.ascontiguousarray(sp["amp_table"], dtype=np.float64)
+        plt = sp.get("plt_table")
+        plt = None if plt is None else np.ascontiguousarray(plt, dtype=np.float64)
+        d = JobDesc()
+        d.ngrid, d.boxlen, d.lpt_order = sp["ngrid"], sp["boxlen"], sp["order"]
+        d.lattice = sp.get("lattice", SC)
+        d.plt = 1 if plt is not None else 0
+        d.precision = sp.get("precision", FP64)
+        d.fixing, d.inversion = int(sp.get("fixing", False)), int(sp.get("inversion", False))
+        d.seed_table, d.amp_table, d.amp_table_len = seed.ctypes.data, amp.ctypes.data, amp.size
+        d.plt_table = plt.ctypes.data if plt is not None else None
+        for k in ("g1", "g2", "g3", "g3c", "vfac1", "vfac2", "vfac3"):
+            setattr(d, k, sp["coef"][k])
+        d.lunit, d.vunit = sp.get("lunit", 1.0), sp.get("vunit", 1.0)
+        d.pos64, d.vel64, d.id64 = int(sp.get("pos64", True)), int(sp.get("vel64", True)), int(sp.get("id64", True))
+        d.id_offset = sp.get("id_offset", 0)
+        d.want_particles = int(sp.get("want_particles", True))
+        t = C.c_uint64()
+        check(load().mfx_server_submit(self._h, C.byref(d), C.byref(t)))
+        self._meta[t.value] = ((1 << d.lattice) * d.ngrid ** 3, bool(d.pos64), bool(d.vel64), bool(d.id64), d.ngrid)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        check(load().mfx_server_wait(self._h, ticket, timeout_ms))
+
+    def times(self, ticket: int):
+        q, l = C.c_double(), C.c_double()
+        check(load().mfx_server_ticket_times(self._h, ticket, C.byref(q), C.byref(l)))
+        return q.value, l.value
+
+    def job(self, ticket: int) -> Job:
+        h = C.c_void_p()
+        check(load().mfx_server_job(self._h, ticket, C.byref(h)))
+        return _JobView(h, *self._meta[ticket])
+
+    def release(self, ticket: int):
+        check(load().mfx_server_release(self._h, ticket))
+        self._meta.pop(ticket, None)
+
+    def close(self):
+        if self._h and self._h.value:
+            load().mfx_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -274,6 +274,34 @@ def test_plt_interpolated_128_fp64_and_fp32(mfxlib, engine, oracle, lattice):
     assert rel_l2(vel, res["vel"]) < 2e-6
 
 
+@pytest.mark.parametrize("n,lattice,order", [(32, 1, 3), (64, 2, 3), (96, 0, 2)])
+def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, monkeypatch):
+    """FP32 form: the pruned, fused padded transforms against the cuFFT path of
+    the same form (both FP32), field by field, and the autotuner's choice."""
+    tab = engine.plt_table(lattice) if lattice else None
+    c = Case(mfxlib, n, 300.0, 24.0, order, 77, lattice=lattice, plt=tab)
+    fids = [mfxlib.FIELD_PHI1, mfxlib.FIELD_PHI2] + ([mfxlib.FIELD_PHI3, mfxlib.FIELD_A3X, mfxlib.FIELD_A3Y,
+                                                       mfxlib.FIELD_A3Z] if order > 2 else [])
+    monkeypatch.setenv("MFX_FUSED", "1")
+    j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
+    pxy, pz = j.autotune()
+    assert pxy in (4, 8, 16) and pz in (2, 4, 8, 16)
+    j.run()
+    fused = [j.field(f) for f in fids]
+    pf = j.particles()
+    j.close()
+    monkeypatch.setenv("MFX_FUSED", "0")
+    j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
+    j.run()
+    ref = [j.field(f) for f in fids]
+    pr = j.particles()
+    j.close()
+    for a, b in zip(fused, ref):
+        assert rel_l2(a, b) < 5e-6
+    delta = c.L / (c.n * 2 ** (lattice / 3.0))
+    assert np.sqrt(np.mean(((pf[0] - pr[0]) / delta) ** 2)) < 1e-6
+
+
 # ---------------------------------------------------------------------------
 # edge cases and errors
 # ---------------------------------------------------------------------------

@@ -1,0 +1,94 @@
+"""Serving loop: admission by HBM footprint, overlap of concurrent jobs, and
+results that are the same alone and in the mix."""
+import numpy as np
+import pytest
+
+from test_gpu_batch import run_alone, spec
+
+pytestmark = pytest.mark.gpu
+
+_PLT = {}
+
+
+def mixed_specs(mfx, engine, count, seed=7):
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(count):
+        n = int(rng.choice([16, 24, 32, 48]))
+        order = int(rng.integers(1, 4))
+        lat = int(rng.integers(0, 3))
+        prec = mfx.FP32C if q % 2 else mfx.FP64
+        sp = spec(mfx, n, 50.0 * n / 32, 24.0, order, 100 + q, lattice=lat, precision=prec)
+        if lat != 0:
+            if lat not in _PLT:
+                _PLT[lat] = engine.plt_table(lat)
+            sp["plt_table"] = _PLT[lat]
+        out.append(sp)
+    return out
+
+
+def alone(mfx, engine, sp):
+    j = mfx.Job(engine, sp["ngrid"], sp["boxlen"], sp["order"], sp["seed_table"], sp["amp_table"], sp["coef"],
+                lattice=sp["lattice"], precision=sp["precision"], plt_table=sp.get("plt_table"),
+                lunit=sp["lunit"], vunit=sp["vunit"])
+    j.run()
+    out = j.particles()
+    j.close()
+    return out
+
+
+def test_server_results_same_alone_and_in_the_mix(mfxlib, engine):
+    specs = mixed_specs(mfxlib, engine, 10)
+    srv = mfxlib.Server(engine, max_inflight=4)
+    tickets = [srv.submit(sp) for sp in specs]
+    for t in tickets:
+        srv.wait(t, 60000)
+    for t, sp in zip(tickets, specs):
+        got = srv.job(t).particles()
+        ref = alone(mfxlib, engine, sp)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
+        q, lat = srv.times(t)
+        assert 0 <= q <= lat
+        srv.release(t)
+    srv.close()
+
+
+def test_server_admission_by_footprint(mfxlib):
+    import ctypes
+    specs = [spec(mfxlib, 32, 60.0, 24.0, 3, 200 + q) for q in range(4)]
+    # footprint of one job, measured through the ABI
+    probe = mfxlib.Engine(0)
+    j = mfxlib.Job(probe, 32, 60.0, 3, specs[0]["seed_table"], specs[0]["amp_table"], specs[0]["coef"])
+    fp = ctypes.c_size_t()
+    mfxlib.check(mfxlib.load().mfx_job_footprint(probe.handle, ctypes.byref(j.desc), ctypes.byref(fp)))
+    j.close()
+    probe.close()
+    # a budget for about 1.5 jobs: admission must serialise them
+    eng = mfxlib.Engine(0, hbm_budget_bytes=int(fp.value * 1.5))
+    srv = mfxlib.Server(eng, max_inflight=4)
+    tickets = [srv.submit(sp) for sp in specs]
+    ends = []
+    for t in tickets:
+        srv.wait(t, 60000)
+        ends.append(srv.times(t))
+        srv.release(t)  # frees the arena for the next admission
+    # later jobs waited in the queue for memory
+    assert ends[-1][0] > 0.0
+    ref = run_alone(mfxlib, eng, specs[-1])
+    srv.close()
+    eng.close()
+    assert ref[0].shape[0] == 32 ** 3
+
+
+def test_server_wait_timeout_is_an_error_not_a_hang(mfxlib, engine):
+    sp = spec(mfxlib, 64, 100.0, 24.0, 3, 9)
+    srv = mfxlib.Server(engine, max_inflight=1)
+    t = srv.submit(sp)
+    rc = mfxlib.load().mfx_server_wait(srv._h, t, 0)
+    assert rc in (mfxlib.MFX_OK, mfxlib.MFX_ETIMEOUT)
+    srv.wait(t, 60000)
+    srv.release(t)
+    with pytest.raises(mfxlib.MfxError):
+        srv.release(t)
+    srv.close()
