@@ -33,7 +33,7 @@
 #include "../../include/mfx.h"
 #include "common.h"
 #include "kernels.cuh"
-#include "fused.cuh"
+#include "fused_launch.cuh"
 
 namespace mfx {
 
@@ -125,9 +125,10 @@ struct mfx_job {
   int N = 0, M = 0, nh = 0, nk = 0, mk = 0, ns = 0, group = 0;
   bool fp64 = true;
   bool fused = false;          // padded convolutions through fused.cuh
-  int ff_pxy = 16, ff_pz = 8;  // pencils per CTA (x/y passes) and rows per CTA (z passes)
-  void *ff_b = nullptr;        // [N][M][N/2] complex scratch
-  void *ff_d[4] = {};          // [M][M][N/2] complex scratch
+  int ff_pxy = 8, ff_pz = 1;   // pencils per CTA (x/y passes) and rows per CTA (z passes)
+  void *ffB[3] = {};           // B-space [N][M][N/2] complex
+  void *ffC[17] = {};          // C-space [M][M][N/2] complex
+  float2 *ff_tw = nullptr;     // W_M^t, t < M
   size_t rsize = 8;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[6] = {};
@@ -192,6 +193,7 @@ struct Layout {
   size_t n_field, m_field, asm_bytes, part_bytes, mregion;
   int nslots, group;
   size_t ff_b, ff_d;
+  int ff_nc;
 };
 
 static size_t n_field_bytes(int N, size_t rs) { return size_t(N) * N * (N / 2 + 1) * 2 * rs; }
@@ -222,7 +224,7 @@ static bool fused_supported(const mfx_job_desc *d) {
   const char *env = getenv("MFX_FUSED");
   if (!env || env[0] != '1') return false;
   const int N = d->ngrid, M = 3 * N / 2;
-  return (N / 2) % 8 == 0 && ff::supported_length(M) && M <= 2304;
+  return (N / 2) % 8 == 0 && ff::ff_length_supported(M);
 }
 
 static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
@@ -241,11 +243,14 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   L.nslots = d->lpt_order == 1 ? 0 : (d->lpt_order == 2 ? 7 : 17);
   L.mregion = size_t(L.nslots) * align_up(L.m_field);
   if (fused_supported(d)) {
-    // pruned-transform scratch: one [N][M][N/2] and up to four [M][M][N/2]
+    // no real-space M-grid fields: three B-space [N][M][N/2] and 7 (2LPT) or
+    // 17 (3LPT) C-space [M][M][N/2] complex fields, and the twiddles
     const size_t kh = N / 2;
+    L.nslots = 0;
     L.ff_b = align_up(size_t(N) * M * kh * 8);
     L.ff_d = align_up(size_t(M) * M * kh * 8);
-    L.mregion += L.ff_b + (d->lpt_order == 3 ? 4 : 1) * L.ff_d;
+    L.ff_nc = d->lpt_order == 3 ? 17 : 7;
+    L.mregion = 3 * L.ff_b + size_t(L.ff_nc) * L.ff_d + align_up(size_t(M) * 8);
   }
   const size_t np = size_t(ns) * N * N * N;
   L.part_bytes = 0;
@@ -455,196 +460,125 @@ template <typename R> static int unpad_invlap(mfx_job *j, void *F, void *out) {
 // ---------------------------------------------------------------------------
 // pruned, fused transforms of the FP32 form (fused.cuh)
 // ---------------------------------------------------------------------------
-static constexpr size_t kFFSmemCap = 200 * 1024;
-
-static size_t ff_smem(int M, int pencils) { return size_t(M + 2 * M * pencils) * sizeof(float2); }
-
-// largest power-of-two P <= pref whose tile of P*per pencils fits the cap and
-// that divides `count` (the kz extent N/2 for x/y passes, M*M rows for z)
-static int ff_pick(int M, int per, int pref, size_t count) {
-  int p = pref;
-  while (p > 1 && (ff_smem(M, p * per) > kFFSmemCap || count % size_t(p) != 0)) p >>= 1;
-  return p;
-}
-
-template <int P> static void ff_set_attrs() {
-  static int done_dev[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || done_dev[dev]) return;
-  const int cap = int(kFFSmemCap) + 16 * 1024;
-  cudaFuncSetAttribute(ff::k_ff_hess_y<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(ff::k_ff_x_inv<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(ff::k_ff_z_c2r<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(ff::k_ff_z_r2c<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(ff::k_ff_x_fwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  cudaFuncSetAttribute(ff::k_ff_y_fwd<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
-  done_dev[dev] = 1;
-}
-
-// launches KERNEL<P> with P in {1, 2, 4, 8, 16}
-#define FF_LAUNCH(P, KERNEL, grid, smem, stream, args)           \
-  do {                                                            \
-    switch (P) {                                                  \
-      case 16: ff_set_attrs<16>(); ff::KERNEL<16><<<grid, 256, smem, stream>>>(args); break; \
-      case 8: ff_set_attrs<8>(); ff::KERNEL<8><<<grid, 256, smem, stream>>>(args); break;    \
-      case 4: ff_set_attrs<4>(); ff::KERNEL<4><<<grid, 256, smem, stream>>>(args); break;    \
-      case 2: ff_set_attrs<2>(); ff::KERNEL<2><<<grid, 256, smem, stream>>>(args); break;    \
-      default: ff_set_attrs<1>(); ff::KERNEL<1><<<grid, 256, smem, stream>>>(args); break;   \
-    }                                                             \
-  } while (0)
-
 static void tune_fused(mfx_job *j);
 
-static ff::PassArgs ff_args(mfx_job *j) {
-  ff::PassArgs a{};
-  a.N = j->N;
-  a.M = j->M;
-  a.Kh = j->N / 2;
+static ff::FArgs ff_args(mfx_job *j) {
+  ff::FArgs a{};
+  a.tw = j->ff_tw;
   a.kfac = float(2.0 * M_PI / j->d.boxlen);
   return a;
 }
 
-// c2r of the six padded Hessians of an N-grid field into H[0..5]
-static int ff_hessians(mfx_job *j, const void *phi, void **H) {
+static int ff_run(mfx_job *j, int op, int p, const ff::FArgs &a, const char *name, double bytes) {
+  KBEGIN(j);
+  const cudaError_t e = ff::ff_launch(j->M, op, p, a, j->stream);
+  if (e != cudaSuccess) return set_error(MFX_ECUDA, "%s (M = %d, tile %d): %s", name, j->M, p, cudaGetErrorString(e));
+  KEND(j, name, bytes);
+  return MFX_OK;
+}
+
+// the six padded Hessians of an N-grid field into C-space C[0..5]
+static int ff_hessians(mfx_job *j, const void *phi, void *const *C) {
   const int N = j->N, M = j->M, Kh = N / 2;
   const double M3 = double(M) * M * M;
-  const double bN = double(N) * M * Kh * 8, bM = double(M) * M * Kh * 8;
-  const int pxy = ff_pick(M, 1, j->ff_pxy, Kh), pz = ff_pick(M, 1, j->ff_pz, size_t(M) * M);
-  for (int c = 0; c < 6; ++c) {
-    ff::PassArgs a = ff_args(j);
-    a.in = static_cast<const float2 *>(phi);
-    a.out = static_cast<float2 *>(j->ff_b);
-    a.ca = kHa[c];
-    a.cb = kHb[c];
-    a.fac = float(std::pow(1.5, 1.5) / std::sqrt(M3));
-    KBEGIN(j);
-    FF_LAUNCH(pxy, k_ff_hess_y, dim3(N, Kh / pxy), ff_smem(M, pxy), j->stream, a);
-    KEND(j, "ff_hess_y", double(N) * N * Kh * 8 + bN);
-    ff::PassArgs b = ff_args(j);
-    b.in = static_cast<const float2 *>(j->ff_b);
-    b.out = static_cast<float2 *>(j->ff_d[0]);
-    KBEGIN(j);
-    FF_LAUNCH(pxy, k_ff_x_inv, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, b);
-    KEND(j, "ff_x_inv", bN + bM);
-    ff::PassArgs z = ff_args(j);
-    z.in = static_cast<const float2 *>(j->ff_d[0]);
-    z.rout = static_cast<float *>(H[c]);
-    KBEGIN(j);
-    FF_LAUNCH(pz, k_ff_z_c2r, dim3(M * M / pz), ff_smem(M, pz), j->stream, z);
-    KEND(j, "ff_z_c2r", bM + double(j->m_field_bytes));
-  }
+  const double bB = double(N) * M * Kh * 8, bC = double(M) * M * Kh * 8;
+  ff::FArgs y = ff_args(j);
+  y.src[0] = static_cast<const float2 *>(phi);
+  for (int o = 0; o < 3; ++o) y.dst[o] = static_cast<float2 *>(j->ffB[o]);
+  y.ncomp = 3;
+  y.fac = float(std::pow(1.5, 1.5) / std::sqrt(M3));
+  TRY(ff_run(j, ff::FF_Y3, j->ff_pxy, y, "ff_y3", double(N) * N * Kh * 8 + 3 * bB));
+  ff::FArgs x = ff_args(j);
+  for (int o = 0; o < 3; ++o) x.src[o] = static_cast<const float2 *>(j->ffB[o]);
+  for (int c = 0; c < 6; ++c) x.dst[c] = static_cast<float2 *>(C[c]);
+  x.ncomp = 6;
+  x.mode = 0;
+  TRY(ff_run(j, ff::FF_XINV, j->ff_pxy, x, "ff_x6", 3 * bB + 6 * bC));
   return MFX_OK;
 }
 
-// r2c of real-space sources formed from rin (kind ff::SRC_*), unpadded and
-// inverse-Laplacian'd into the N-grid fields outs[0..nout)
-static int ff_sources(mfx_job *j, int kind, const void *const *rin, int nin, int nout, void **outs) {
+// forward x and y transforms of D-space outputs: unpadded and inverse
+// Laplacian'd into N-grid fields (mode 0), or truncated and brought back to
+// C-space (mode 1, convolve3's first pairs)
+static int ff_finish(mfx_job *j, void *D, void *out, int mode) {
   const int N = j->N, M = j->M, Kh = N / 2;
   const double M3 = double(M) * M * M, N3 = double(N) * N * N;
-  const double bN = double(N) * M * Kh * 8, bM = double(M) * M * Kh * 8;
-  const int pxy = ff_pick(M, 1, j->ff_pxy, Kh), pz = ff_pick(M, nout, j->ff_pz, size_t(M) * M);
-  ff::PassArgs z = ff_args(j);
-  for (int q = 0; q < nin; ++q) z.rin[q] = static_cast<const float *>(rin[q]);
-  for (int o = 0; o < nout; ++o) z.dout[o] = static_cast<float2 *>(j->ff_d[o]);
-  z.kind = kind;
-  z.nout = nout;
-  KBEGIN(j);
-  FF_LAUNCH(pz, k_ff_z_r2c, dim3(M * M / pz), ff_smem(M, pz * nout), j->stream, z);
-  KEND(j, "ff_z_r2c", nin * double(j->m_field_bytes) + nout * bM);
-  for (int o = 0; o < nout; ++o) {
-    ff::PassArgs x = ff_args(j);
-    x.in = static_cast<const float2 *>(j->ff_d[o]);
-    x.out = static_cast<float2 *>(j->ff_b);
-    KBEGIN(j);
-    FF_LAUNCH(pxy, k_ff_x_fwd, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, x);
-    KEND(j, "ff_x_fwd", bM + bN);
-    ff::PassArgs y = ff_args(j);
-    y.in = static_cast<const float2 *>(j->ff_b);
-    y.out = static_cast<float2 *>(outs[o]);
-    y.kind = 0;
-    y.fac = float(1.0 / std::sqrt(M3) / (std::sqrt(M3) / std::sqrt(N3)));
-    KBEGIN(j);
-    FF_LAUNCH(pxy, k_ff_y_fwd, dim3(N, Kh / pxy), ff_smem(M, pxy), j->stream, y);
-    KEND(j, "ff_y_fwd", bN + double(j->n_field_bytes));
-  }
-  return MFX_OK;
-}
-
-// convolve3's first pair: product A*B truncated to the N-grid modes and
-// transformed back to the padded real grid (T)
-static int ff_truncated_pair(mfx_job *j, const void *A, const void *B, void *T) {
-  const int N = j->N, M = j->M, Kh = N / 2;
-  const double M3 = double(M) * M * M, N3 = double(N) * N * N;
-  const double bN = double(N) * M * Kh * 8, bM = double(M) * M * Kh * 8;
-  const int pxy = ff_pick(M, 1, j->ff_pxy, Kh), pz = ff_pick(M, 1, j->ff_pz, size_t(M) * M);
-  ff::PassArgs z = ff_args(j);
-  z.rin[0] = static_cast<const float *>(A);
-  z.rin[1] = static_cast<const float *>(B);
-  z.dout[0] = static_cast<float2 *>(j->ff_d[0]);
-  z.kind = ff::SRC_PAIR;
-  z.nout = 1;
-  KBEGIN(j);
-  FF_LAUNCH(pz, k_ff_z_r2c, dim3(M * M / pz), ff_smem(M, pz), j->stream, z);
-  KEND(j, "ff_z_r2c", 2.0 * double(j->m_field_bytes) + bM);
-  ff::PassArgs x = ff_args(j);
-  x.in = static_cast<const float2 *>(j->ff_d[0]);
-  x.out = static_cast<float2 *>(j->ff_b);
-  KBEGIN(j);
-  FF_LAUNCH(pxy, k_ff_x_fwd, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, x);
-  KEND(j, "ff_x_fwd", bM + bN);
-  ff::PassArgs y = ff_args(j);
-  y.in = static_cast<const float2 *>(j->ff_b);
-  y.out2 = static_cast<float2 *>(j->ff_b);  // each CTA owns its tile: in place
-  y.kind = 1;
+  const double bB = double(N) * M * Kh * 8, bC = double(M) * M * Kh * 8;
   const double rfac_u = std::sqrt(M3) / std::sqrt(N3), rfac_p = std::pow(1.5, 1.5);
-  y.fac = float((1.0 / std::sqrt(M3) / rfac_u) * rfac_p / std::sqrt(M3));
-  KBEGIN(j);
-  FF_LAUNCH(pxy, k_ff_y_fwd, dim3(N, Kh / pxy), ff_smem(M, pxy), j->stream, y);
-  KEND(j, "ff_y_trunc", 2.0 * bN);
-  ff::PassArgs xi = ff_args(j);
-  xi.in = static_cast<const float2 *>(j->ff_b);
-  xi.out = static_cast<float2 *>(j->ff_d[0]);
-  KBEGIN(j);
-  FF_LAUNCH(pxy, k_ff_x_inv, dim3(M, Kh / pxy), ff_smem(M, pxy), j->stream, xi);
-  KEND(j, "ff_x_inv", bN + bM);
-  ff::PassArgs zc = ff_args(j);
-  zc.in = static_cast<const float2 *>(j->ff_d[0]);
-  zc.rout = static_cast<float *>(T);
-  KBEGIN(j);
-  FF_LAUNCH(pz, k_ff_z_c2r, dim3(M * M / pz), ff_smem(M, pz), j->stream, zc);
-  KEND(j, "ff_z_c2r", bM + double(j->m_field_bytes));
+  ff::FArgs x = ff_args(j);
+  x.src[0] = static_cast<const float2 *>(D);
+  x.dst[0] = static_cast<float2 *>(j->ffB[0]);
+  x.ncomp = 1;
+  TRY(ff_run(j, ff::FF_XFWD, j->ff_pxy, x, "ff_x_fwd", bC + bB));
+  ff::FArgs y = ff_args(j);
+  y.src[0] = static_cast<const float2 *>(j->ffB[0]);
+  y.ncomp = 1;
+  y.mode = mode;
+  if (mode == 0) {
+    y.dst[0] = static_cast<float2 *>(out);
+    y.fac = float(1.0 / std::sqrt(M3) / rfac_u);
+    TRY(ff_run(j, ff::FF_YFWD, j->ff_pxy, y, "ff_y_fwd", bB + double(j->n_field_bytes)));
+  } else {
+    y.dst[0] = static_cast<float2 *>(j->ffB[0]);  // each CTA owns its tile: in place
+    y.fac = float((1.0 / std::sqrt(M3) / rfac_u) * rfac_p / std::sqrt(M3));
+    TRY(ff_run(j, ff::FF_YFWD, j->ff_pxy, y, "ff_y_trunc", 2 * bB));
+    ff::FArgs xi = ff_args(j);
+    xi.src[0] = static_cast<const float2 *>(j->ffB[0]);
+    xi.dst[0] = static_cast<float2 *>(out);
+    xi.ncomp = 1;
+    xi.mode = 1;
+    TRY(ff_run(j, ff::FF_XINV, j->ff_pxy, xi, "ff_x_inv", bB + bC));
+  }
   return MFX_OK;
 }
 
-// LPT potentials phi2, phi3, A3 through the fused transforms (FP32 form)
+// LPT potentials phi2, phi3, A3 through the fused transforms (FP32 form).
+// C-space slots: ffC[0..5] phi1 Hessians, ffC[6..11] the 2LPT source and the
+// five pair products (then the phi2 Hessians), ffC[12..16] truncated pairs.
 static int run_potentials_fused(mfx_job *j) {
-  const int order = j->d.lpt_order;
-  void **H1 = &j->mslot[0];
-  TRY(ff_hessians(j, j->nf[0], H1));
+  const int order = j->d.lpt_order, M = j->M, Kh = j->N / 2;
+  const double bC = double(M) * M * Kh * 8;
+  void *const *C1 = &j->ffC[0];
+  void *const *D = &j->ffC[6];
+  TRY(ff_hessians(j, j->nf[0], C1));
   {
-    const void *rin[6] = {H1[0], H1[1], H1[2], H1[3], H1[4], H1[5]};
-    void *outs[1] = {j->nf[1]};
-    TRY(ff_sources(j, ff::SRC_PHI2, rin, 6, 1, outs));
+    ff::FArgs z = ff_args(j);
+    for (int c = 0; c < 6; ++c) z.src[c] = static_cast<const float2 *>(C1[c]);
+    const int nout = order >= 3 ? 6 : 1;
+    for (int o = 0; o < nout; ++o) z.dst[o] = static_cast<float2 *>(D[o]);
+    z.mode = order >= 3 ? 1 : 0;
+    TRY(ff_run(j, ff::FF_ZSRC2, j->ff_pz, z, "ff_zsrc2", 6 * bC + nout * bC));
   }
+  TRY(ff_finish(j, D[0], j->nf[1], 0));
   if (j->timed) CU(cudaEventRecord(j->ev[2], j->stream));
   if (order >= 3) {
-    void **T = &j->mslot[6];
-    void **H2 = &j->mslot[11];
-    struct Pair { int a, b; };
-    const Pair pr[5] = {{0, 1}, {3, 4}, {5, 5}, {4, 4}, {3, 3}};  // xx*yy, xy*xz, yz^2, xz^2, xy^2
-    for (int t = 0; t < 5; ++t) TRY(ff_truncated_pair(j, H1[pr[t].a], H1[pr[t].b], T[t]));
-    TRY(ff_hessians(j, j->nf[1], H2));
-    const void *rin[17];
+    void *const *CT = &j->ffC[12];
+    for (int t = 0; t < 5; ++t) TRY(ff_finish(j, D[1 + t], CT[t], 1));
+    void *const *C2 = &j->ffC[6];
+    TRY(ff_hessians(j, j->nf[1], C2));
+    ff::FArgs z = ff_args(j);
     for (int c = 0; c < 6; ++c) {
-      rin[c] = H1[c];
-      rin[6 + c] = H2[c];
+      z.src[c] = static_cast<const float2 *>(C1[c]);
+      z.src[6 + c] = static_cast<const float2 *>(C2[c]);
     }
-    for (int t = 0; t < 5; ++t) rin[12 + t] = T[t];
-    void *outs[4] = {j->nf[2], j->nf[3], j->nf[4], j->nf[5]};
-    TRY(ff_sources(j, ff::SRC_PHI3, rin, 17, 4, outs));
+    for (int t = 0; t < 5; ++t) z.src[12 + t] = static_cast<const float2 *>(CT[t]);
+    for (int o = 0; o < 4; ++o) z.dst[o] = static_cast<float2 *>(CT[o]);  // in place, row by row
+    TRY(ff_run(j, ff::FF_ZSRC3, j->ff_pz, z, "ff_zsrc3", 17 * bC + 4 * bC));
+    for (int o = 0; o < 4; ++o) TRY(ff_finish(j, CT[o], j->nf[2 + o], 0));
   }
   return MFX_OK;
+}
+
+// default tile shapes: the largest x/y tile of at most 512 threads, and two
+// rows per CTA for the z passes where the 17-field rows leave room
+static void ff_default_tiles(mfx_job *j) {
+  j->ff_pxy = 4;
+  for (int p : {16, 8, 4})
+    if (ff::ff_valid(j->M, ff::FF_XFWD, p) && p * ff::ff_maxj(j->M) <= 512) {
+      j->ff_pxy = p;
+      break;
+    }
+  j->ff_pz = j->M <= 576 ? 2 : 1;
 }
 
 // pencil-tile shapes chosen by mfx_job_autotune for this size class, if any
@@ -660,7 +594,7 @@ static void tune_fused(mfx_job *j) {
 // Times the fused passes for every admissible pencil-tile shape on the job's
 // own buffers and keeps the fastest per size class (engine-wide cache).
 static int autotune_fused(mfx_job *j) {
-  const int N = j->N, M = j->M, Kh = N / 2;
+  const int N = j->N, M = j->M;
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
@@ -678,43 +612,32 @@ static int autotune_fused(mfx_job *j) {
   j->prof = false;
   int best_xy = j->ff_pxy, best_z = j->ff_pz;
   float tbest = 1e30f;
+  int rc = MFX_OK;
   for (int p : {16, 8, 4}) {
-    if (ff_pick(M, 1, p, Kh) != p) continue;
-    ff::PassArgs a = ff_args(j);
-    a.in = static_cast<const float2 *>(j->nf[0]);
-    a.out = static_cast<float2 *>(j->ff_b);
-    a.ca = a.cb = 0;
-    a.fac = 1.f;
-    ff::PassArgs b = ff_args(j);
-    b.in = static_cast<const float2 *>(j->ff_b);
-    b.out = static_cast<float2 *>(j->ff_d[0]);
-    ff::PassArgs c = ff_args(j);
-    c.in = static_cast<const float2 *>(j->ff_d[0]);
-    c.out = static_cast<float2 *>(j->ff_b);
+    if (!ff::ff_valid(M, ff::FF_XFWD, p)) continue;
     const float t = timed([&] {
-      FF_LAUNCH(p, k_ff_hess_y, dim3(N, Kh / p), ff_smem(M, p), j->stream, a);
-      FF_LAUNCH(p, k_ff_x_inv, dim3(M, Kh / p), ff_smem(M, p), j->stream, b);
-      FF_LAUNCH(p, k_ff_x_fwd, dim3(M, Kh / p), ff_smem(M, p), j->stream, c);
+      // the Hessian passes of phi1 and one forward x/y pair
+      const int save = j->ff_pxy;
+      j->ff_pxy = p;
+      if (rc == MFX_OK) rc = ff_hessians(j, j->nf[0], &j->ffC[0]);
+      if (rc == MFX_OK) rc = ff_finish(j, j->ffC[0], j->ffC[6], 1);
+      j->ff_pxy = save;
     });
+    if (rc != MFX_OK) break;
     if (t < tbest) {
       tbest = t;
       best_xy = p;
     }
   }
   tbest = 1e30f;
-  for (int p : {16, 8, 4, 2}) {
-    if (ff_pick(M, 1, p, size_t(M) * M) != p) continue;
-    ff::PassArgs zc = ff_args(j);
-    zc.in = static_cast<const float2 *>(j->ff_d[0]);
-    zc.rout = static_cast<float *>(j->mslot[0]);
-    ff::PassArgs zr = ff_args(j);
-    zr.rin[0] = zr.rin[1] = static_cast<const float *>(j->mslot[0]);
-    zr.dout[0] = static_cast<float2 *>(j->ff_d[0]);
-    zr.kind = ff::SRC_PAIR;
-    zr.nout = 1;
+  for (int p : {1, 2}) {
+    if (rc != MFX_OK || !ff::ff_valid(M, ff::FF_ZSRC3, p)) continue;
     const float t = timed([&] {
-      FF_LAUNCH(p, k_ff_z_c2r, dim3(M * M / p), ff_smem(M, p), j->stream, zc);
-      FF_LAUNCH(p, k_ff_z_r2c, dim3(M * M / p), ff_smem(M, p), j->stream, zr);
+      ff::FArgs z = ff_args(j);
+      for (int c = 0; c < 6; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
+      z.dst[0] = static_cast<float2 *>(j->ffC[6]);
+      z.mode = 0;
+      if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC2, p, z, "ff_zsrc2", 0);
     });
     if (t < tbest) {
       tbest = t;
@@ -724,6 +647,7 @@ static int autotune_fused(mfx_job *j) {
   j->prof = prof;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  TRY(rc);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(MFX_ECUDA, "autotune: %s", cudaGetErrorString(e));
   j->ff_pxy = best_xy;
@@ -971,9 +895,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   size_t work = 0;
   j->fused = fused_supported(d);
   if (j->fused) {
-    // pencils per CTA: shared memory holds 2 x M x P complex floats
-    j->ff_pxy = (j->M <= 576) ? 16 : 8;
-    j->ff_pz = (j->M <= 576) ? 8 : 4;
+    ff_default_tiles(j);
     tune_fused(j);
   }
   if (d->lpt_order >= 2 && !j->fused) {
@@ -999,6 +921,18 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   // the device
   cudaError_t e = cudaMallocAsync(&j->arena, L.total, j->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(j->stream);
+  if (e == cudaErrorMemoryAllocation) {
+    // the cached pool may hold freed arenas of other shapes: hand its unused
+    // memory back to the device and try once more
+    cudaGetLastError();
+    j->arena = nullptr;
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+      cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocAsync(&j->arena, L.total, j->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(j->stream);
+  }
   if (e != cudaSuccess) {
     j->arena = nullptr;
     cudaGetLastError();
@@ -1030,13 +964,19 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->work_bytes = L.work_est;
   for (int q = 0; q < L.nslots; ++q) j->mslot[q] = j->region + size_t(q) * align_up(L.m_field);
   if (j->fused) {
-    char *f = j->region + size_t(L.nslots) * align_up(L.m_field);
-    j->ff_b = f;
-    f += L.ff_b;
-    for (int q = 0; q < (d->lpt_order == 3 ? 4 : 1); ++q) {
-      j->ff_d[q] = f;
-      f += L.ff_d;
+    char *f = j->region;
+    for (int q = 0; q < 3; ++q, f += L.ff_b) j->ffB[q] = f;
+    for (int q = 0; q < L.ff_nc; ++q, f += L.ff_d) j->ffC[q] = f;
+    j->ff_tw = reinterpret_cast<float2 *>(f);
+    std::vector<float2> tw(j->M);
+    for (int t = 0; t < j->M; ++t) {
+      const double a = 2.0 * M_PI * double(t) / double(j->M);
+      tw[t] = make_float2(float(std::cos(a)), float(-std::sin(a)));
     }
+    if (cudaMemcpyAsync(j->ff_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, j->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(j->stream) != cudaSuccess)
+      return fail(set_error(MFX_ECUDA, "twiddle upload failed"));
   }
   j->group = L.group;
   if (d->want_particles) {

@@ -1,34 +1,51 @@
 // Pruned, fused 3D transforms for the Orszag-padded convolutions (FP32 form).
 //
 // The padded fields live on the M-grid (M = 3N/2) but their spectra are
-// non-zero only on the N-grid modes.  A 3D transform is done here as three
-// passes of 1D transforms whose pencils skip what is known to be zero, with
-// the pointwise work of the reference's convolver folded into the passes:
+// non-zero only on the N-grid modes, and the z Nyquist plane kz = N/2 is zero
+// in every padded spectrum (phi and every unpadded result zero each Nyquist
+// index).  A 3D transform is done as three passes of 1D transforms whose
+// pencils skip what is known to be zero; nothing on the M-grid is ever stored
+// in real space.  Fields are kept in two mixed layouts (complex float):
 //
-//   c2r of a padded Hessian (convolution.hh:552-575 then the c2r):
-//     Y pass  (i in the N-grid, kz < N/2): reads phi, applies the Hessian
-//             factor -g_a g_b and the pad/normalisation factor, zero-pads the
-//             y modes, inverse FFT along y                        -> B[i][y][kz]
-//     X pass  (y, kz < N/2): zero-pads the x modes, inverse FFT    -> C[x][y][kz]
-//     Z pass  (x, y): rebuilds the Hermitian z pencil from kz < N/2,
-//             inverse FFT, real part                               -> H[x][y][z]
-//   r2c of a real-space product followed by unpad (convolution.hh:600-636):
-//     Z pass  forms the product(s) from the input fields on the fly,
-//             forward FFT, keeps kz < N/2                          -> D[x][y][kz]
-//     X pass  forward FFT along x, keeps the N-grid x modes       -> E[i][y][kz]
-//     Y pass  forward FFT along y, keeps the N-grid y modes, zeroes every
-//             Nyquist index, applies the unpad factor and -1/k^2  -> out[i][j][kz]
-//     (or, for the pairwise truncation of convolve3, truncates and transforms
-//      back along y, then X and Z c2r passes follow)
+//   B-space [N][M][N/2]  kx on the N-grid, y transformed (padded), kz < N/2
+//   C-space [M][M][N/2]  x and y transformed (padded), kz < N/2
 //
-// kz = N/2 (the z Nyquist plane) is identically zero in every padded spectrum
-// (phi and all unpadded results zero every Nyquist index), so pencils only
-// carry kz < N/2.  Each 1D transform is a mixed-radix (4, 2, 3) Stockham FFT in
-// shared memory on P pencils per CTA.
+// and the z transforms of all the fields a source needs are done together, per
+// (x, y) row, inside one CTA, with the real-space products formed in shared
+// memory between the inverse and the forward z transforms:
+//
+//   Y3    phi (N-grid k-space) -> B0 = Y(phi), B1 = Y(ky phi), B2 = Y(ky^2 phi)
+//         (the Hessian factors separate: k_a k_b = (x part)(y part)(z part))
+//   X6    B0..B2 -> the six Hessians -k_a k_b phi in C-space (x inverse FFT)
+//   ZSRC2 per row: six inverse z transforms (three complex, two real pencils
+//         each), the 2LPT source (ic_generator.cc:530-534) and the five
+//         products of convolve3's first pairs (ic_generator.cc:581-609), then
+//         forward z transforms -> D-space (= C-space layout)
+//   XF    D -> E (B-space layout): forward x FFT, keeps the N-grid kx
+//   YF    E -> N-grid k-space: forward y FFT, unpad (zero every Nyquist index,
+//         convolution.hh:600-636), scale, inverse Laplacian (grid_fft.hh:440-449)
+//         or, for the pairs, truncate and transform back along y (B-space)
+//   XI    B-space -> C-space (x inverse FFT) for the truncated pair products
+//   ZSRC3 per row: 17 inverse z transforms (phi1 and phi2 Hessians, the five
+//         truncated pair products), the 3LPT sources phi3a + phi3b and A3
+//         (ic_generator.cc:581-628) with compensated sums, four forward z
+//         transforms -> D-space
+//
+// Each 1D transform is a compile-time mixed-radix Stockham FFT: two or three
+// steps of radix 4..24 butterflies held in registers, with one shared-memory
+// exchange between steps.  The first step reads its inputs straight from
+// global memory (or a shared-memory real row) and the last step writes its
+// outputs straight to their destination, so the x/y passes move each element
+// through shared memory once.
 #pragma once
 #include <stdint.h>
+
+#include <type_traits>
+#include <utility>
 #if defined(__CUDACC__)
 #include <cuda_runtime.h>
+#define MFX_HD __host__ __device__ __forceinline__
+#define MFX_CX __host__ __device__ constexpr
 #else
 // host-only compilation (tests of the transform core on the CPU)
 #include <cmath>
@@ -36,64 +53,78 @@ struct float2 {
   float x, y;
 };
 inline float2 make_float2(float a, float b) { return float2{a, b}; }
-#define __host__
-#define __device__
-#define __forceinline__ inline
+#define MFX_HD inline
+#define MFX_CX constexpr
 #endif
 
 namespace mfx {
 namespace ff {
 
-struct Stages {
-  int n;
-  int r[24];
-};
+// ---------------------------------------------------------------------------
+// compile-time helpers
+// ---------------------------------------------------------------------------
+template <int I> using Ic = std::integral_constant<int, I>;
 
-// radix sequence for L = 2^a 3^b: 4s first, then a 2, then 3s
-__host__ __device__ inline Stages make_stages(int L) {
-  Stages s;
-  s.n = 0;
-  int m = L;
-  while (m % 4 == 0) {
-    s.r[s.n++] = 4;
-    m /= 4;
+template <class F, int... I> MFX_HD void static_for_(F &&f, std::integer_sequence<int, I...>) {
+  (f(Ic<I>{}), ...);
+}
+template <int N, class F> MFX_HD void static_for(F &&f) { static_for_(f, std::make_integer_sequence<int, N>{}); }
+
+// cos / sin by their Taylor series, evaluated by the compiler for the
+// twiddles inside a butterfly (|x| <= pi: the 30th terms are below 1e-40)
+MFX_CX double cx_cos(double x) {
+  double t = 1.0, s = 1.0;
+  for (int k = 1; k <= 30; ++k) {
+    t *= -x * x / double((2 * k - 1) * (2 * k));
+    s += t;
   }
-  if (m % 2 == 0) {
-    s.r[s.n++] = 2;
-    m /= 2;
+  return s;
+}
+MFX_CX double cx_sin(double x) {
+  double t = x, s = x;
+  for (int k = 1; k <= 30; ++k) {
+    t *= -x * x / double((2 * k) * (2 * k + 1));
+    s += t;
   }
-  while (m % 3 == 0) {
-    s.r[s.n++] = 3;
-    m /= 3;
-  }
-  if (m != 1) s.n = -1;  // unsupported length
   return s;
 }
 
-__host__ __device__ inline bool supported_length(int L) { return make_stages(L).n > 0; }
+// W^NUM of W = exp(-2 pi i / DEN), with the quarter turns exact
+template <int NUM, int DEN> struct Tw {
+  static constexpr int n = NUM % DEN;
+  static constexpr bool quarter = (4 * n) % DEN == 0;
+  static constexpr int q = (4 * n) / DEN;
+  static constexpr double ang = -6.283185307179586476925286766559 * double(2 * n > DEN ? n - DEN : n) / double(DEN);
+  static constexpr float c = float(cx_cos(ang)), s = float(cx_sin(ang));
+};
 
-__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+MFX_HD float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+// x * W^NUM (forward) or x * conj(W)^NUM (INV)
+template <int NUM, int DEN, bool INV> MFX_HD float2 twmul(float2 x) {
+  using T = Tw<NUM, DEN>;
+  if constexpr (T::quarter) {
+    constexpr int q = INV ? (4 - T::q) & 3 : T::q;
+    if constexpr (q == 0) return x;
+    else if constexpr (q == 1) return make_float2(x.y, -x.x);  // * (-i)
+    else if constexpr (q == 2) return make_float2(-x.x, -x.y);
+    else return make_float2(-x.y, x.x);  // * (+i)
+  } else {
+    constexpr float c = T::c, s = INV ? -T::s : T::s;
+    return make_float2(x.x * c - x.y * s, x.x * s + x.y * c);
+  }
 }
 
-// One radix-R butterfly (forward: e^{-2 pi i nk/R}; INV: e^{+...})
-template <bool INV> __host__ __device__ __forceinline__ void butterfly(int R, float2 *v) {
-  if (R == 2) {
+// In-register DFT of R points (forward: sum_n v[n] W_R^{nk}; INV: conjugate
+// W, unnormalised).  R = A*B is split as n = A b + a, k = k2 + B k1: B-point
+// DFTs of the A decimated sequences, twiddles W_R^{a k2}, A-point DFTs.
+template <int R, bool INV> MFX_HD void dft(float2 *v) {
+  if constexpr (R == 1) {
+  } else if constexpr (R == 2) {
     const float2 a = v[0], b = v[1];
     v[0] = make_float2(a.x + b.x, a.y + b.y);
     v[1] = make_float2(a.x - b.x, a.y - b.y);
-  } else if (R == 4) {
-    const float2 a = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
-    const float2 b = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
-    const float2 c = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
-    const float2 d = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
-    // forward: y1 = b - i d, y3 = b + i d
-    const float2 id = INV ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);  // (+-i) d
-    v[0] = make_float2(a.x + c.x, a.y + c.y);
-    v[2] = make_float2(a.x - c.x, a.y - c.y);
-    v[1] = make_float2(b.x + id.x, b.y + id.y);
-    v[3] = make_float2(b.x - id.x, b.y - id.y);
-  } else {  // R == 3
+  } else if constexpr (R == 3) {
     const float h = 0.86602540378443864676f;  // sqrt(3)/2
     const float2 s = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
     const float2 d = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
@@ -103,191 +134,174 @@ template <bool INV> __host__ __device__ __forceinline__ void butterfly(int R, fl
     v[0] = make_float2(v[0].x + s.x, v[0].y + s.y);
     v[1] = make_float2(t.x + ihd.x, t.y + ihd.y);
     v[2] = make_float2(t.x - ihd.x, t.y - ihd.y);
+  } else if constexpr (R == 4) {
+    const float2 a = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
+    const float2 b = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
+    const float2 c = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
+    const float2 d = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
+    // forward: y1 = b - i d, y3 = b + i d
+    const float2 id = INV ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+    v[0] = make_float2(a.x + c.x, a.y + c.y);
+    v[2] = make_float2(a.x - c.x, a.y - c.y);
+    v[1] = make_float2(b.x + id.x, b.y + id.y);
+    v[3] = make_float2(b.x - id.x, b.y - id.y);
+  } else {
+    constexpr int A = (R % 4 == 0) ? 4 : ((R % 2 == 0) ? 2 : 3);
+    constexpr int B = R / A;
+    static_assert(A * B == R, "radix must be 2^a 3^b");
+    float2 u[R];
+    static_for<A>([&](auto ai) {
+      constexpr int a = decltype(ai)::value;
+      float2 s[B];
+      static_for<B>([&](auto bi) { s[decltype(bi)::value] = v[A * decltype(bi)::value + a]; });
+      dft<B, INV>(s);
+      static_for<B>([&](auto ki) {
+        constexpr int k = decltype(ki)::value;
+        u[a * B + k] = twmul<a * k, R, INV>(s[k]);
+      });
+    });
+    static_for<B>([&](auto ki) {
+      constexpr int k2 = decltype(ki)::value;
+      float2 s[A];
+      static_for<A>([&](auto ai) { s[decltype(ai)::value] = u[decltype(ai)::value * B + k2]; });
+      dft<A, INV>(s);
+      static_for<A>([&](auto ji) { v[k2 + B * decltype(ji)::value] = s[decltype(ji)::value]; });
+    });
   }
 }
 
-// Stockham stage: x -> y.  Element (n, p) of a tile lives at n*es + p*ps.
-// `t` enumerates (butterfly j, pencil p) pairs; pfast selects which index
-// varies fastest across consecutive t (for bank-conflict-free access).
-template <bool INV>
-__host__ __device__ __forceinline__ void stage_bfly(const float2 *x, float2 *y, const float2 *tw, int L, int R,
-                                                    int Ns, int j, int p, int es, int ps) {
-  const int nb = L / R;
-  const int k = j % Ns;
-  const int tstep = k * (L / (Ns * R));
-  float2 v[4];
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-    if (r < R) v[r] = x[(j + r * nb) * es + p * ps];
-#pragma unroll
-  for (int r = 1; r < 4; ++r) {
-    if (r < R) {
-      float2 w = tw[(r * tstep) % L];
-      if (INV) w.y = -w.y;
-      v[r] = cmul(v[r], w);
-    }
+// Radices of each supported padded length (R3 = 1: two steps).  Every M = 3N/2
+// with N/2 a multiple of 8 and N <= 1024 whose length is 2^a 3^b is listed.
+template <int L> struct Fac;
+MFX_CX int cmax(int a, int b) { return a > b ? a : b; }
+#define MFX_FAC(L, a, b, c)                                                  \
+  template <> struct Fac<L> {                                                \
+    static constexpr int R1 = a, R2 = b, R3 = c;                             \
+    static constexpr int steps = (c > 1) ? 3 : 2;                            \
+    static constexpr int maxJ = cmax(cmax(L / a, L / b), c > 1 ? L / c : 0); \
   }
-  butterfly<INV>(R, v);
-  const int base = (j / Ns) * Ns * R + k;
-#pragma unroll
-  for (int r = 0; r < 4; ++r)
-    if (r < R) y[(base + r * Ns) * es + p * ps] = v[r];
+MFX_FAC(24, 4, 6, 1);
+MFX_FAC(48, 8, 6, 1);
+MFX_FAC(96, 8, 12, 1);
+MFX_FAC(144, 12, 12, 1);
+MFX_FAC(192, 16, 12, 1);
+MFX_FAC(288, 8, 6, 6);
+MFX_FAC(384, 8, 8, 6);
+MFX_FAC(576, 8, 8, 9);
+MFX_FAC(768, 8, 12, 8);
+MFX_FAC(1152, 8, 12, 12);
+MFX_FAC(1536, 16, 12, 8);
+#undef MFX_FAC
+
+// Shared-memory tile of PP pencils of length L.  PF: pencil index fastest
+// (x/y passes, whose pencils are adjacent in global memory); otherwise each
+// pencil is contiguous, padded by one slot per 16 against bank conflicts.
+template <int L, int PP, bool PF> struct Tile {
+  static constexpr int padL = L + (L >> 4);
+  static constexpr int elems = PF ? L * PP : PP * padL;
+  MFX_HD static int at(int q, int n) { return PF ? n * PP + q : q * padL + n + (n >> 4); }
+};
+
+template <int PP, int J, bool PF> MFX_HD void split(int t, int &q, int &j) {
+  if (PF) {
+    q = t % PP;
+    j = t / PP;
+  } else {
+    j = t % J;
+    q = t / J;
+  }
 }
+
+// One Stockham step of radix R after NS points have been combined: task j
+// reads x[j + r L/R], applies W_{NS R}^{r (j mod NS)}, does an R-point DFT and
+// writes y[(j / NS) NS R + (j mod NS) + r NS].  tw[t] = W_L^t.
+template <int L, int R, int NS, bool INV> struct Step {
+  static constexpr int J = L / R;
+  template <class Ld> MFX_HD static void gather(int j, const Ld &ld, const float2 *tw, float2 *v) {
+    static_for<R>([&](auto ri) {
+      constexpr int r = decltype(ri)::value;
+      v[r] = ld(j + r * J);
+    });
+    if constexpr (NS > 1) {
+      const int k = j % NS;
+      constexpr int S = L / (NS * R);
+      static_for<R - 1>([&](auto ri) {
+        constexpr int r = decltype(ri)::value + 1;
+        float2 w = tw[r * k * S];
+        if (INV) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      });
+    }
+    dft<R, INV>(v);
+  }
+  template <class St> MFX_HD static void scatter(int j, const St &st, const float2 *v) {
+    const int k = j % NS, base = (j / NS) * NS * R + k;
+    static_for<R>([&](auto ri) {
+      constexpr int r = decltype(ri)::value;
+      st(base + r * NS, v[r]);
+    });
+  }
+};
 
 #if defined(__CUDACC__)
-// P pencils of length L in shared memory (ping-pong x/y); returns the buffer
-// holding the result.  tw[t] = exp(-2 pi i t / L).
-template <bool INV>
-__device__ float2 *fft_tile(float2 *x, float2 *y, const float2 *tw, int L, int P, int es, int ps, bool pfast) {
-  // radices in make_stages order (4s, then a 2, then 3s), derived from the
-  // remaining length so that no stage table is needed
-  for (int Ns = 1; Ns < L;) {
-    const int m = L / Ns;
-    const int R = (m % 4 == 0) ? 4 : ((m % 2 == 0) ? 2 : 3);
-    const int nb = L / R;
-    for (int t = threadIdx.x; t < nb * P; t += blockDim.x) {
-      int j, p;
-      if (pfast) {
-        p = t % P;
-        j = t / P;
-      } else {
-        j = t % nb;
-        p = t / nb;
-      }
-      stage_bfly<INV>(x, y, tw, L, R, Ns, j, p, es, ps);
-    }
+// PP pencils of length L through one CTA (blockDim.x >= PP * Fac<L>::maxJ;
+// every thread must call it).  ld(q, n) returns input n of pencil q;
+// st(q, k, v) takes output k.  buf holds Tile<L, PP, PF>::elems values.
+// The last step stores after a barrier, so st may write into buf; the caller
+// synchronises before reading what st wrote to shared memory.
+template <int L, int PP, bool PF, bool INV, class Ld, class St>
+__device__ __forceinline__ void pencil_fft(float2 *buf, const float2 *tw, const Ld &ld, const St &st) {
+  using F = Fac<L>;
+  using T = Tile<L, PP, PF>;
+  const int t = threadIdx.x;
+  {
+    using S = Step<L, F::R1, 1, INV>;
+    float2 v[F::R1];
+    int q, j;
+    split<PP, S::J, PF>(t, q, j);
+    const bool act = t < PP * S::J;
+    if (act) S::gather(j, [&](int n) { return ld(q, n); }, tw, v);
     __syncthreads();
-    float2 *tmp = x;
-    x = y;
-    y = tmp;
-    Ns *= R;
+    if (act) S::scatter(j, [&](int n, float2 x) { buf[T::at(q, n)] = x; }, v);
+    __syncthreads();
   }
-  return x;
-}
-
-__device__ __forceinline__ void load_twiddles(float2 *tw, int L) {
-  for (int t = threadIdx.x; t < L; t += blockDim.x) {
-    float s, c;
-    sincospif(-2.0f * float(t) / float(L), &s, &c);
-    tw[t] = make_float2(c, s);
+  if constexpr (F::steps == 3) {
+    using S = Step<L, F::R2, F::R1, INV>;
+    float2 v[F::R2];
+    int q, j;
+    split<PP, S::J, PF>(t, q, j);
+    const bool act = t < PP * S::J;
+    if (act) S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw, v);
+    __syncthreads();
+    if (act) S::scatter(j, [&](int n, float2 x) { buf[T::at(q, n)] = x; }, v);
+    __syncthreads();
+  }
+  {
+    constexpr int RL = F::steps == 3 ? F::R3 : F::R2;
+    using S = Step<L, RL, L / RL, INV>;
+    float2 v[RL];
+    int q, j;
+    split<PP, S::J, PF>(t, q, j);
+    const bool act = t < PP * S::J;
+    if (act) S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw, v);
+    __syncthreads();
+    if (act) S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v);
   }
 }
+#endif
 
+// ---------------------------------------------------------------------------
+// index maps
+// ---------------------------------------------------------------------------
 // N-grid index of padded index ip (convolution.hh:563-572), -1 in the gap
-__device__ __forceinline__ int unpad_index(int ip, int N) {
+MFX_HD int unpad_index(int ip, int N) {
   const int nh = N >> 1;
   return ip <= nh ? ip : (ip > N ? ip - nh : -1);
 }
-__device__ __forceinline__ int sidx(int i, int n) { return i > (n >> 1) ? i - n : i; }
+MFX_HD int sidx(int i, int n) { return i > (n >> 1) ? i - n : i; }
 
-// Buffers (complex float unless noted), Kh = N/2:
-//   phi  N-grid k-space [N][N][N/2+1]
-//   B/E  [N][M][Kh]     after the y transform (x still in N-grid modes)
-//   C/D  [M][M][Kh]     after the x transform
-//   H    real [M][M][M+2] (the in-place padded layout)
-struct PassArgs {
-  const float2 *in;
-  float2 *out;
-  float2 *out2;           // Y-forward truncation: transformed-back tile
-  const float *rin[17];   // Z r2c: input real fields
-  float *rout;            // Z c2r: real output
-  float2 *dout[4];        // Z r2c: outputs
-  int N, M, Kh;
-  int ca, cb;             // Hessian component
-  int kind, nout;         // Z r2c source kind / output count
-  float kfac, fac;
-  float coef;
-};
-
-__device__ __forceinline__ float *smem_base() {
-  extern __shared__ float4 ff_smem[];
-  return reinterpret_cast<float *>(ff_smem);
-}
-
-// c2r, Y pass: Hessian (ca, cb) of phi, padded along y, inverse FFT along y.
-// grid (N, Kh / P).
-template <int P> __global__ void __launch_bounds__(256) k_ff_hess_y(PassArgs a) {
-  const int N = a.N, M = a.M, Kh = a.Kh, nh = N >> 1, nk = nh + 1;
-  float2 *tw = reinterpret_cast<float2 *>(smem_base());
-  float2 *x = tw + M, *y = x + M * P;
-  const int i = blockIdx.x, kz0 = blockIdx.y * P;
-  load_twiddles(tw, M);
-  const float gi = (i != nh) ? float(sidx(i, N)) * a.kfac : 0.f;
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int n = t / P, p = t - (t / P) * P, kz = kz0 + p;
-    const int j = unpad_index(n, N);
-    float2 v = make_float2(0.f, 0.f);
-    if (j >= 0) {
-      v = a.in[(size_t(i) * N + j) * nk + kz];
-      const float g[3] = {gi, (j != nh) ? float(sidx(j, N)) * a.kfac : 0.f, float(kz) * a.kfac};
-      const float h = -(g[a.ca] * g[a.cb]) * a.fac;
-      v.x *= h;
-      v.y *= h;
-    }
-    x[n * P + p] = v;
-  }
-  __syncthreads();
-  const float2 *r = fft_tile<true>(x, y, tw, M, P, P, 1, true);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int n = t / P, p = t - (t / P) * P;
-    a.out[(size_t(i) * M + n) * Kh + kz0 + p] = r[n * P + p];
-  }
-}
-
-// c2r, X pass: zero-pad x, inverse FFT along x.  grid (M, Kh / P).
-template <int P> __global__ void __launch_bounds__(256) k_ff_x_inv(PassArgs a) {
-  const int N = a.N, M = a.M, Kh = a.Kh;
-  float2 *tw = reinterpret_cast<float2 *>(smem_base());
-  float2 *x = tw + M, *y = x + M * P;
-  const int yy = blockIdx.x, kz0 = blockIdx.y * P;
-  load_twiddles(tw, M);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int n = t / P, p = t - (t / P) * P;
-    const int i = unpad_index(n, N);
-    x[n * P + p] = (i >= 0) ? a.in[(size_t(i) * M + yy) * Kh + kz0 + p] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  const float2 *r = fft_tile<true>(x, y, tw, M, P, P, 1, true);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int n = t / P, p = t - (t / P) * P;
-    a.out[(size_t(n) * M + yy) * Kh + kz0 + p] = r[n * P + p];
-  }
-}
-
-// c2r, Z pass: Hermitian z pencil from kz < Kh, inverse FFT, real part into
-// the padded real layout.  grid (M*M / P).
-template <int P> __global__ void __launch_bounds__(256) k_ff_z_c2r(PassArgs a) {
-  const int M = a.M, Kh = a.Kh;
-  float2 *tw = reinterpret_cast<float2 *>(smem_base());
-  float2 *x = tw + M, *y = x + M * P;
-  const size_t r0 = size_t(blockIdx.x) * P;
-  load_twiddles(tw, M);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int p = t / M, n = t - (t / M) * M;
-    float2 v = make_float2(0.f, 0.f);
-    if (n < Kh) {
-      v = a.in[(r0 + p) * Kh + n];
-      if (n == 0) v.y = 0.f;
-    } else if (n > M - Kh) {
-      const float2 c = a.in[(r0 + p) * Kh + (M - n)];
-      v = make_float2(c.x, -c.y);
-    }
-    x[p * M + n] = v;
-  }
-  __syncthreads();
-  const float2 *r = fft_tile<true>(x, y, tw, M, P, 1, M, false);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int p = t / M, n = t - (t / M) * M;
-    a.rout[(r0 + p) * size_t(M + 2) + n] = r[p * M + n].x;
-  }
-}
-
-// sources formed on the fly in the Z r2c pass (slot order of the Hessians:
-// 0 xx 1 yy 2 zz 3 xy 4 xz 5 yz; rin[0..5] = phi1 Hessians, rin[6..11] =
-// phi2 Hessians, rin[12..16] = truncated phi3a pair products)
-enum { SRC_COPY = 0, SRC_PHI2 = 1, SRC_PAIR = 2, SRC_PHI3 = 3 };
-
-__device__ __forceinline__ int hslot(int x, int y) {
+// slot order of the Hessians: 0 xx 1 yy 2 zz 3 xy 4 xz 5 yz
+MFX_HD int hslot(int x, int y) {
   if (x == y) return x;
   const int lo = x < y ? x : y, hi = x < y ? y : x;
   return lo == 0 ? (hi == 1 ? 3 : 4) : 5;
@@ -296,171 +310,405 @@ __device__ __forceinline__ int hslot(int x, int y) {
 // compensated accumulation (Ogita-Rump-Oishi TwoSum / FMA TwoProduct)
 struct Acc32 {
   float hi = 0.f, lo = 0.f;
-  __device__ __forceinline__ void add(float v) {
+  MFX_HD void add(float v) {
     const float s = hi + v, bp = s - hi;
     lo += (hi - (s - bp)) + (v - bp);
     hi = s;
   }
-  __device__ __forceinline__ void add_prod(float c, float a, float b) {
+  MFX_HD void add_prod(float c, float a, float b) {
     const float p = a * b, e = fmaf(a, b, -p), q = c * p, e2 = fmaf(c, p, -q) + c * e;
     add(q);
     lo += e2;
   }
-  __device__ __forceinline__ float value() const { return hi + lo; }
+  MFX_HD float value() const { return hi + lo; }
 };
 
-__device__ __forceinline__ void sources(const PassArgs &a, size_t idx, float *s) {
-  if (a.kind == SRC_COPY) {
-    s[0] = a.rin[0][idx];
-  } else if (a.kind == SRC_PAIR) {
-    s[0] = a.rin[0][idx] * a.rin[1][idx];
-  } else if (a.kind == SRC_PHI2) {
-    // ic_generator.cc:530-534
-    float h[6];
+// 2LPT source (ic_generator.cc:530-534) from the six phi1 Hessians
+MFX_HD float src_phi2(const float *h) {
+  Acc32 S;
+  S.add_prod(1.f, h[0], h[1] + h[2]);
+  S.add_prod(1.f, h[1], h[2]);
+  S.add_prod(-1.f, h[3], h[3]);
+  S.add_prod(-1.f, h[4], h[4]);
+  S.add_prod(-1.f, h[5], h[5]);
+  return S.value();
+}
+
+// phi3a + phi3b (ic_generator.cc:581-609) and A3 (613-628) from the phi1
+// Hessians p, the phi2 Hessians q and the truncated pair products T
+MFX_HD void src_phi3(const float *p, const float *q, const float *T, float *s) {
+  const float c57 = -5.0f / 7.0f, c107 = 10.0f / 7.0f;
+  Acc32 S;
+  S.add_prod(1.f, T[0], p[2]);
+  S.add_prod(2.f, T[1], p[5]);
+  S.add_prod(-1.f, T[2], p[0]);
+  S.add_prod(-1.f, T[3], p[1]);
+  S.add_prod(-1.f, T[4], p[2]);
+  S.add_prod(c57, p[0], q[1] + q[2]);
+  S.add_prod(c57, p[1], q[2] + q[0]);
+  S.add_prod(c57, p[2], q[0] + q[1]);
+  S.add_prod(c107, p[3], q[3]);
+  S.add_prod(c107, p[4], q[4]);
+  S.add_prod(c107, p[5], q[5]);
+  s[0] = S.value();
 #pragma unroll
-    for (int c = 0; c < 6; ++c) h[c] = a.rin[c][idx];
-    Acc32 S;
-    S.add_prod(1.f, h[0], h[1] + h[2]);
-    S.add_prod(1.f, h[1], h[2]);
-    S.add_prod(-1.f, h[3], h[3]);
-    S.add_prod(-1.f, h[4], h[4]);
-    S.add_prod(-1.f, h[5], h[5]);
-    s[0] = S.value();
-  } else {
-    // phi3a + phi3b (ic_generator.cc:581-609) and A3 (613-628)
-    float p[6], q[6], T[5];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      p[c] = a.rin[c][idx];
-      q[c] = a.rin[6 + c][idx];
-    }
-#pragma unroll
-    for (int c = 0; c < 5; ++c) T[c] = a.rin[12 + c][idx];
-    const float c57 = -5.0f / 7.0f, c107 = 10.0f / 7.0f;
-    Acc32 S;
-    S.add_prod(1.f, T[0], p[2]);
-    S.add_prod(2.f, T[1], p[5]);
-    S.add_prod(-1.f, T[2], p[0]);
-    S.add_prod(-1.f, T[3], p[1]);
-    S.add_prod(-1.f, T[4], p[2]);
-    S.add_prod(c57, p[0], q[1] + q[2]);
-    S.add_prod(c57, p[1], q[2] + q[0]);
-    S.add_prod(c57, p[2], q[0] + q[1]);
-    S.add_prod(c107, p[3], q[3]);
-    S.add_prod(c107, p[4], q[4]);
-    S.add_prod(c107, p[5], q[5]);
-    s[0] = S.value();
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
-      Acc32 A;
-      A.add_prod(1.f, q[hslot(d, d1)], p[hslot(d, d2)]);
-      A.add_prod(-1.f, q[hslot(d, d2)], p[hslot(d, d1)]);
-      A.add_prod(1.f, p[hslot(d1, d2)], q[hslot(d1, d1)] - q[hslot(d2, d2)]);
-      A.add_prod(-1.f, q[hslot(d1, d2)], p[hslot(d1, d1)] - p[hslot(d2, d2)]);
-      s[1 + d] = A.value();
-    }
+  for (int d = 0; d < 3; ++d) {
+    const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+    Acc32 A;
+    A.add_prod(1.f, q[hslot(d, d1)], p[hslot(d, d2)]);
+    A.add_prod(-1.f, q[hslot(d, d2)], p[hslot(d, d1)]);
+    A.add_prod(1.f, p[hslot(d1, d2)], q[hslot(d1, d1)] - q[hslot(d2, d2)]);
+    A.add_prod(-1.f, q[hslot(d1, d2)], p[hslot(d1, d1)] - p[hslot(d2, d2)]);
+    s[1 + d] = A.value();
   }
 }
 
-// r2c, Z pass with the real-space product formed on the fly; keeps kz < Kh.
-// grid (M*M / P); nout pencils per row.
-template <int P> __global__ void __launch_bounds__(256) k_ff_z_r2c(PassArgs a) {
-  const int M = a.M, Kh = a.Kh, no = a.nout;
-  float2 *tw = reinterpret_cast<float2 *>(smem_base());
-  float2 *x = tw + M, *y = x + M * P * no;
-  const size_t r0 = size_t(blockIdx.x) * P;
-  load_twiddles(tw, M);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int p = t / M, n = t - (t / M) * M;
-    float s[4];
-    sources(a, (r0 + p) * size_t(M + 2) + n, s);
-    for (int o = 0; o < no; ++o) x[(p * no + o) * M + n] = make_float2(s[o], 0.f);
-  }
+// the five first pairs of convolve3 (ic_generator.cc:581-609):
+// xx*yy, xy*xz, yz^2, xz^2, xy^2
+MFX_HD void pair_products(const float *h, float *t) {
+  t[0] = h[0] * h[1];
+  t[1] = h[3] * h[4];
+  t[2] = h[5] * h[5];
+  t[3] = h[4] * h[4];
+  t[4] = h[3] * h[3];
+}
+
+// Hermitian spectra of two real z pencils packed as A + iB (A[0], B[0] real)
+// and their separation after a forward transform of a + ib
+MFX_HD float2 pack_pair(float2 a, float2 b) { return make_float2(a.x - b.y, a.y + b.x); }
+MFX_HD float2 pack_pair_conj(float2 a, float2 b) { return make_float2(a.x + b.y, b.x - a.y); }
+MFX_HD void unpack_pair(float2 z, float2 zm, float2 &a, float2 &b) {
+  a = make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+  b = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
+}
+
+#if defined(__CUDACC__)
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+struct FArgs {
+  const float2 *src[17];  // inputs per component
+  float2 *dst[6];         // outputs per component
+  const float2 *tw;       // W_M^t, t < M (global)
+  int ncomp;              // components in this launch
+  int mode;               // X6: 0 Hessians from B0..B2, 1 plain; YF: 0 unpad, 1 truncate; ZSRC2: 1 with pairs
+  float kfac, fac;
+};
+
+template <int M> struct Dims {
+  static constexpr int N = 2 * M / 3, nh = N / 2, Kh = N / 2, nk = N / 2 + 1;
+};
+
+__device__ __forceinline__ float2 *ff_smem() {
+  extern __shared__ float4 ff_smem4[];
+  return reinterpret_cast<float2 *>(ff_smem4);
+}
+
+template <int M> __device__ __forceinline__ void load_tw(float2 *tw, const float2 *g) {
+  for (int t = threadIdx.x; t < M; t += blockDim.x) tw[t] = g[t];
   __syncthreads();
-  const float2 *r = fft_tile<false>(x, y, tw, M, P * no, 1, M, false);
-  for (int t = threadIdx.x; t < Kh * P * no; t += blockDim.x) {
-    const int q = t / Kh, k = t - (t / Kh) * Kh;
-    const int p = q / no, o = q - (q / no) * no;
-    a.dout[o][(r0 + p) * Kh + k] = r[q * M + k];
-  }
 }
 
-// r2c, X pass: forward FFT along x, keep the N-grid x modes.  grid (M, Kh / P).
-template <int P> __global__ void __launch_bounds__(256) k_ff_x_fwd(PassArgs a) {
-  const int N = a.N, M = a.M, Kh = a.Kh;
-  float2 *tw = reinterpret_cast<float2 *>(smem_base());
-  float2 *x = tw + M, *y = x + M * P;
-  const int yy = blockIdx.x, kz0 = blockIdx.y * P;
-  load_twiddles(tw, M);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int n = t / P, p = t - (t / P) * P;
-    x[n * P + p] = a.in[(size_t(n) * M + yy) * Kh + kz0 + p];
-  }
-  __syncthreads();
-  const float2 *r = fft_tile<false>(x, y, tw, M, P, P, 1, true);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int n = t / P, p = t - (t / P) * P;
-    const int i = unpad_index(n, N);
-    if (i >= 0) a.out[(size_t(i) * M + yy) * Kh + kz0 + p] = r[n * P + p];
-  }
+// CTAs per SM the register allocation is sized for: as many as leave each
+// thread at least 64 registers, at most four
+MFX_CX int min_blocks(int threads) {
+  return 65536 / (threads * 64) < 1 ? 1 : (65536 / (threads * 64) > 4 ? 4 : 65536 / (threads * 64));
 }
 
-// r2c, Y pass: forward FFT along y, keep the N-grid y modes.
-//  kind 0: unpad (zero every Nyquist index), scale, inverse Laplacian
-//          (grid_fft.hh:440-449) -> N-grid k-space out
-//  kind 1: truncation of convolve3's first pair: zero outside the N-grid
-//          modes and on Nyquist, scale, inverse FFT along y -> out2 [N][M][Kh]
-// grid (N, Kh / P).
-template <int P> __global__ void __launch_bounds__(256) k_ff_y_fwd(PassArgs a) {
-  const int N = a.N, M = a.M, Kh = a.Kh, nh = N >> 1, nk = nh + 1;
-  float2 *tw = reinterpret_cast<float2 *>(smem_base());
-  float2 *x = tw + M, *y = x + M * P;
+template <int M, int P> struct XY {
+  static constexpr int threads = P * Fac<M>::maxJ;
+  static constexpr int minb = min_blocks(threads);
+  static constexpr size_t smem = size_t(M + Tile<M, P, true>::elems) * sizeof(float2);
+};
+
+// Y3: B_o = inverse-y of fac (ky)^o phi, o < ncomp, padded in y.  grid (N, Kh/P)
+// (element offsets fit 32 bits for every supported size: N <= 1024)
+template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y3(FArgs a) {
+  using D = Dims<M>;
+  float2 *tw = ff_smem(), *buf = tw + M;
+  load_tw<M>(tw, a.tw);
   const int i = blockIdx.x, kz0 = blockIdx.y * P;
-  load_twiddles(tw, M);
-  for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-    const int n = t / P, p = t - (t / P) * P;
-    x[n * P + p] = a.in[(size_t(i) * M + n) * Kh + kz0 + p];
+  const float2 *src = a.src[0] + (unsigned(i) * D::N * D::nk + kz0);
+#pragma unroll 1
+  for (int o = 0; o < a.ncomp; ++o) {
+    float2 *out = a.dst[o] + (unsigned(i) * M * D::Kh + kz0);
+    pencil_fft<M, P, true, true>(
+        buf, tw,
+        [&](int q, int n) -> float2 {
+          const int j = unpad_index(n, D::N);
+          if (j < 0) return make_float2(0.f, 0.f);
+          const float2 v = src[unsigned(j) * D::nk + q];
+          float f = a.fac;
+          if (o > 0) {
+            const float gy = (j != D::nh) ? float(sidx(j, D::N)) * a.kfac : 0.f;
+            f *= (o == 1) ? gy : gy * gy;
+          }
+          return make_float2(v.x * f, v.y * f);
+        },
+        [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+  }
+}
+
+// X inverse into C-space.  mode 0: the six Hessians from B0 = Y(phi),
+// B1 = Y(ky phi), B2 = Y(ky^2 phi) (slot order xx yy zz xy xz yz, factor
+// -k_a k_b split into its x and z parts); mode 1: component c of src[c].
+// grid (M, Kh/P)
+template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_x_inv(FArgs a) {
+  using D = Dims<M>;
+  float2 *tw = ff_smem(), *buf = tw + M;
+  load_tw<M>(tw, a.tw);
+  const int yy = blockIdx.x, kz0 = blockIdx.y * P;
+  const unsigned off = unsigned(yy) * D::Kh + kz0;
+#pragma unroll 1
+  for (int c = 0; c < a.ncomp; ++c) {
+    // c: 0 xx <- -gx^2 B0, 1 yy <- -B2, 2 zz <- -gz^2 B0, 3 xy <- -gx B1, 4 xz <- -gx gz B0, 5 yz <- -gz B1
+    const int s = a.mode ? c : (c == 1 ? 2 : ((c == 3 || c == 5) ? 1 : 0));
+    const float2 *src = a.src[s] + off;
+    float2 *out = a.dst[c] + off;
+    pencil_fft<M, P, true, true>(
+        buf, tw,
+        [&](int q, int n) -> float2 {
+          const int i = unpad_index(n, D::N);
+          if (i < 0) return make_float2(0.f, 0.f);
+          float2 v = src[unsigned(i) * M * D::Kh + q];
+          if (a.mode == 0) {
+            const float gx = (i != D::nh) ? float(sidx(i, D::N)) * a.kfac : 0.f;
+            const float gz = float(kz0 + q) * a.kfac;
+            const float f = c == 0 ? -gx * gx : c == 1 ? -1.f : c == 2 ? -gz * gz : c == 3 ? -gx : c == 4 ? -gx * gz : -gz;
+            v.x *= f;
+            v.y *= f;
+          }
+          return v;
+        },
+        [&](int q, int n, float2 v) { out[unsigned(n) * M * D::Kh + q] = v; });
+  }
+}
+
+// X forward: C-space layout -> B-space layout, keeping the N-grid kx.
+// grid (M, Kh/P)
+template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_x_fwd(FArgs a) {
+  using D = Dims<M>;
+  float2 *tw = ff_smem(), *buf = tw + M;
+  load_tw<M>(tw, a.tw);
+  const int yy = blockIdx.x, kz0 = blockIdx.y * P;
+  const unsigned off = unsigned(yy) * D::Kh + kz0;
+#pragma unroll 1
+  for (int c = 0; c < a.ncomp; ++c) {
+    const float2 *src = a.src[c] + off;
+    float2 *dst = a.dst[c] + off;
+    pencil_fft<M, P, true, false>(
+        buf, tw, [&](int q, int n) { return src[unsigned(n) * M * D::Kh + q]; },
+        [&](int q, int k, float2 v) {
+          const int i = unpad_index(k, D::N);
+          if (i >= 0) dst[unsigned(i) * M * D::Kh + q] = v;
+        });
+  }
+}
+
+// Y forward.  MODE 0: keep the N-grid ky, zero every Nyquist index and the
+// mean, scale by fac / -k^2 -> N-grid k-space (kz = N/2 plane zeroed);
+// MODE 1: truncation of a convolve3 pair (zero outside the N-grid modes and on
+// Nyquist, scale by fac) and inverse y transform -> B-space (may be in place).
+// grid (N, Kh/P, ncomp)
+template <int M, int P, int MODE>
+__global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y_fwd(FArgs a) {
+  using D = Dims<M>;
+  using T = Tile<M, P, true>;
+  float2 *tw = ff_smem(), *buf = tw + M;
+  load_tw<M>(tw, a.tw);
+  // one component per grid z: no loop whose invariants the compiler would keep live
+  const int i = blockIdx.x, kz0 = blockIdx.y * P, c = blockIdx.z;
+  const float2 *src = a.src[c] + (unsigned(i) * M * D::Kh + kz0);
+  float2 *dst = a.dst[c];
+  if constexpr (MODE == 0) {
+    const float kx = float(sidx(i, D::N)) * a.kfac;
+    float2 *out = dst + unsigned(i) * D::N * D::nk + kz0;
+    pencil_fft<M, P, true, false>(
+        buf, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
+        [&](int q, int k, float2 v) {
+          const int j = unpad_index(k, D::N);
+          if (j < 0) return;
+          const int kz = kz0 + q;
+          float2 r = make_float2(0.f, 0.f);
+          if (i != D::nh && j != D::nh && (i | j | kz) != 0) {
+            const float ky = float(sidx(j, D::N)) * a.kfac, kk = float(kz) * a.kfac;
+            const float f = -a.fac * __frcp_rn(kx * kx + ky * ky + kk * kk);
+            r = make_float2(v.x * f, v.y * f);
+          }
+          out[unsigned(j) * D::nk + q] = r;
+        });
+    if (blockIdx.y == 0)
+      for (int j = threadIdx.x; j < D::N; j += blockDim.x)
+        dst[(unsigned(i) * D::N + j) * D::nk + D::nh] = make_float2(0.f, 0.f);
+  } else {
+    float2 *out = dst + (unsigned(i) * M * D::Kh + kz0);
+    const bool row_kept = i != D::nh;
+    pencil_fft<M, P, true, false>(
+        buf, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
+        [&](int q, int k, float2 v) {
+          const int j = unpad_index(k, D::N);
+          const bool keep = row_kept && j >= 0 && j != D::nh;
+          buf[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
+        });
+    __syncthreads();
+    pencil_fft<M, P, true, true>(
+        buf, tw, [&](int q, int n) { return buf[T::at(q, n)]; },
+        [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+  }
+}
+
+// Z row kernels: RW rows per CTA; NIN real inputs per row (C-space spectra,
+// kz < Kh), paired into complex pencils of G per round; NOUT real sources per
+// row written back as D-space spectra (kz < Kh).
+template <int M, int RW, int G, int NIN> struct ZR {
+  static constexpr int nin_pad = NIN + (NIN & 1);
+  static constexpr int threads = G * Fac<M>::maxJ;
+  static constexpr size_t smem =
+      size_t(M) * sizeof(float2) + size_t(RW) * nin_pad * M * sizeof(float) + size_t(Tile<M, G, false>::elems) * sizeof(float2);
+};
+
+// inverse z transforms of NIN C-space inputs of RW rows into h[w][c][z]
+template <int M, int RW, int G, int NIN>
+__device__ __forceinline__ void z_inverse(const FArgs &a, size_t r0, float *h, float2 *buf, const float2 *tw) {
+  using D = Dims<M>;
+  constexpr int NPI = RW * (ZR<M, RW, G, NIN>::nin_pad / 2);  // complex pencils
+  constexpr int NP = ZR<M, RW, G, NIN>::nin_pad;
+#pragma unroll 1
+  for (int g0 = 0; g0 < NPI; g0 += G) {
+    pencil_fft<M, G, false, true>(
+        buf, tw,
+        [&](int q, int n) -> float2 {
+          const int g = g0 + q;
+          if (g >= NPI) return make_float2(0.f, 0.f);
+          const int w = g / (NP / 2), c0 = 2 * (g - w * (NP / 2)), c1 = c0 + 1;
+          const size_t row = (r0 + w) * D::Kh;
+          int m;
+          bool conj;
+          if (n < D::Kh) {
+            m = n;
+            conj = false;
+          } else if (n > M - D::Kh) {
+            m = M - n;
+            conj = true;
+          } else {
+            return make_float2(0.f, 0.f);
+          }
+          float2 va = a.src[c0][row + m];
+          float2 vb = c1 < NIN ? a.src[c1][row + m] : make_float2(0.f, 0.f);
+          if (m == 0) {
+            va.y = 0.f;
+            vb.y = 0.f;
+          }
+          return conj ? pack_pair_conj(va, vb) : pack_pair(va, vb);
+        },
+        [&](int q, int n, float2 v) {
+          const int g = g0 + q;
+          if (g >= NPI) return;
+          const int w = g / (NP / 2), c0 = 2 * (g - w * (NP / 2));
+          h[(w * NP + c0) * M + n] = v.x;
+          h[(w * NP + c0 + 1) * M + n] = v.y;
+        });
   }
   __syncthreads();
-  float2 *r = fft_tile<false>(x, y, tw, M, P, P, 1, true);
-  float2 *other = (r == x) ? y : x;
-  if (a.kind == 0) {
-    for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-      const int n = t / P, p = t - (t / P) * P, kz = kz0 + p;
-      const int j = unpad_index(n, N);
-      if (j < 0) continue;
-      float2 v = make_float2(0.f, 0.f);
-      if (i != nh && j != nh && (i | j | kz) != 0) {
-        const float kx = float(sidx(i, N)) * a.kfac, ky = float(sidx(j, N)) * a.kfac, kzz = float(kz) * a.kfac;
-        const float f = -a.fac / (kx * kx + ky * ky + kzz * kzz);
-        v = r[n * P + p];
-        v.x *= f;
-        v.y *= f;
-      }
-      a.out[(size_t(i) * N + j) * nk + kz] = v;
-    }
-    if (blockIdx.y == 0)  // the kz = N/2 plane of this row is zero
-      for (int j = threadIdx.x; j < N; j += blockDim.x) a.out[(size_t(i) * N + j) * nk + nh] = make_float2(0.f, 0.f);
-  } else {
-    for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-      const int n = t / P, p = t - (t / P) * P;
-      const int j = unpad_index(n, N);
-      float2 v = make_float2(0.f, 0.f);
-      if (j >= 0 && j != nh && i != nh) {
-        v = r[n * P + p];
-        v.x *= a.fac;
-        v.y *= a.fac;
-      }
-      r[n * P + p] = v;
+}
+
+// forward z transforms of NOUT real sources per row held in h[w][o][z]
+// (o < NOUT, row stride NP) and the kz < Kh spectra written to dst[o]
+template <int M, int RW, int G, int NP, int NOUT>
+__device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float *h, float2 *buf, const float2 *tw) {
+  using D = Dims<M>;
+  using T = Tile<M, G, false>;
+  constexpr int NR = RW * NOUT;        // real outputs
+  constexpr int NPO = (NR + 1) / 2;    // complex pencils
+#pragma unroll 1
+  for (int g0 = 0; g0 < NPO; g0 += G) {
+    pencil_fft<M, G, false, false>(
+        buf, tw,
+        [&](int q, int n) -> float2 {
+          const int g = g0 + q;
+          if (g >= NPO) return make_float2(0.f, 0.f);
+          const int f0 = 2 * g, f1 = f0 + 1;
+          const float re = h[((f0 / NOUT) * NP + f0 % NOUT) * M + n];
+          const float im = f1 < NR ? h[((f1 / NOUT) * NP + f1 % NOUT) * M + n] : 0.f;
+          return make_float2(re, im);
+        },
+        [&](int q, int k, float2 v) { buf[T::at(q, k)] = v; });
+    __syncthreads();
+    for (int t = threadIdx.x; t < G * D::Kh; t += blockDim.x) {
+      const int q = t / D::Kh, k = t - q * D::Kh, g = g0 + q;
+      if (g >= NPO) continue;
+      const float2 z = buf[T::at(q, k)], zm = buf[T::at(q, k == 0 ? 0 : M - k)];
+      float2 sa, sb;
+      unpack_pair(z, zm, sa, sb);
+      const int f0 = 2 * g, f1 = f0 + 1;
+      a.dst[f0 % NOUT][(r0 + f0 / NOUT) * D::Kh + k] = sa;
+      if (f1 < NR) a.dst[f1 % NOUT][(r0 + f1 / NOUT) * D::Kh + k] = sb;
     }
     __syncthreads();
-    const float2 *b = fft_tile<true>(r, other, tw, M, P, P, 1, true);
-    for (int t = threadIdx.x; t < M * P; t += blockDim.x) {
-      const int n = t / P, p = t - (t / P) * P;
-      a.out2[(size_t(i) * M + n) * Kh + kz0 + p] = b[n * P + p];
+  }
+}
+
+// ZSRC2: phi1 Hessians (src[0..5], C-space) -> 2LPT source (dst[0]) and, with
+// mode 1, the five first-pair products of convolve3 (dst[1..5]).
+// grid (M*M / RW)
+template <int M, int RW, int G> __global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads) k_ff_zsrc2(FArgs a) {
+  constexpr int NP = 6;
+  float2 *tw = ff_smem();
+  float *h = reinterpret_cast<float *>(tw + M);
+  float2 *buf = reinterpret_cast<float2 *>(h + RW * NP * M);
+  load_tw<M>(tw, a.tw);
+  const size_t r0 = size_t(blockIdx.x) * RW;
+  z_inverse<M, RW, G, 6>(a, r0, h, buf, tw);
+  for (int t = threadIdx.x; t < RW * M; t += blockDim.x) {
+    const int w = t / M, n = t - w * M;
+    float *hr = h + size_t(w) * NP * M + n;
+    float v[6], s[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = hr[c * M];
+    s[0] = src_phi2(v);
+    pair_products(v, s + 1);
+    hr[0] = s[0];
+    if (a.mode) {
+#pragma unroll
+      for (int c = 1; c < 6; ++c) hr[c * M] = s[c];
     }
   }
+  __syncthreads();
+  if (a.mode)
+    z_forward<M, RW, G, NP, 6>(a, r0, h, buf, tw);
+  else
+    z_forward<M, RW, G, NP, 1>(a, r0, h, buf, tw);
+}
+
+// ZSRC3: phi1 Hessians src[0..5], phi2 Hessians src[6..11] and the truncated
+// pair products src[12..16] (C-space) -> phi3 source (dst[0]) and A3 (dst[1..3]).
+// The outputs may alias inputs: each CTA reads its rows whole before writing.
+// grid (M*M / RW)
+template <int M, int RW, int G> __global__ void __launch_bounds__(ZR<M, RW, G, 17>::threads) k_ff_zsrc3(FArgs a) {
+  constexpr int NP = ZR<M, RW, G, 17>::nin_pad;  // 18
+  float2 *tw = ff_smem();
+  float *h = reinterpret_cast<float *>(tw + M);
+  float2 *buf = reinterpret_cast<float2 *>(h + RW * NP * M);
+  load_tw<M>(tw, a.tw);
+  const size_t r0 = size_t(blockIdx.x) * RW;
+  z_inverse<M, RW, G, 17>(a, r0, h, buf, tw);
+  for (int t = threadIdx.x; t < RW * M; t += blockDim.x) {
+    const int w = t / M, n = t - w * M;
+    float *hr = h + size_t(w) * NP * M + n;
+    float p[6], q[6], T5[5], s[4];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      p[c] = hr[c * M];
+      q[c] = hr[(6 + c) * M];
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c) T5[c] = hr[(12 + c) * M];
+    src_phi3(p, q, T5, s);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) hr[c * M] = s[c];
+  }
+  __syncthreads();
+  z_forward<M, RW, G, NP, 4>(a, r0, h, buf, tw);
 }
 #endif
 

@@ -1,0 +1,160 @@
+// Host-side launchers of the fused transforms (fused.cuh), one instantiation
+// per padded length M (the ff_m*.cu translation units compile them in
+// parallel).  ff_launch_m<M> launches one pass with pencil tile `p`: pencils
+// per CTA for the x/y passes (4, 8 or 16), rows per CTA for the z passes.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fused.cuh"
+
+namespace mfx {
+namespace ff {
+
+enum FFOp { FF_Y3 = 0, FF_XINV = 1, FF_XFWD = 2, FF_YFWD = 3, FF_ZSRC2 = 4, FF_ZSRC3 = 5, FF_NOPS = 6 };
+
+// complex pencils per round of the z passes: as many as fit 512 threads
+template <int M, int RW, int NIN> struct ZG {
+  static constexpr int npi = RW * ((NIN + (NIN & 1)) / 2);
+  static constexpr int cap = 512 / Fac<M>::maxJ > 0 ? 512 / Fac<M>::maxJ : 1;
+  static constexpr int G = npi < cap ? npi : cap;
+};
+
+constexpr size_t kFFSmemMax = 227 * 1024;
+
+template <int M, int RW> constexpr bool ff_z_fits() {
+  return ZR<M, RW, ZG<M, RW, 6>::G, 6>::smem <= kFFSmemMax && ZR<M, RW, ZG<M, RW, 17>::G, 17>::smem <= kFFSmemMax;
+}
+
+template <int M> bool ff_valid_m(int op, int p) {
+  constexpr int Kh = M / 3;
+  if (op == FF_ZSRC2 || op == FF_ZSRC3) return (p == 1 && ff_z_fits<M, 1>()) || (p == 2 && ff_z_fits<M, 2>());
+  if (op < 0 || op >= FF_NOPS) return false;
+  return (p == 4 || p == 8 || p == 16) && Kh % p == 0 && p * Fac<M>::maxJ <= 1024 &&
+         (size_t(M) + size_t(M) * p) * sizeof(float2) <= kFFSmemMax;
+}
+
+// lets a kernel instance use up to 227 KB of dynamic shared memory; the
+// static flag is per expansion site, i.e. per kernel instance, and per device
+#define MFX_FF_ALLOW_SMEM(kernel)                                                               \
+  do {                                                                                          \
+    static int done_[64] = {};                                                                  \
+    int dev_ = 0;                                                                               \
+    cudaGetDevice(&dev_);                                                                       \
+    if (dev_ >= 0 && dev_ < 64 && !done_[dev_]) {                                               \
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024); \
+      done_[dev_] = 1;                                                                          \
+    }                                                                                           \
+  } while (0)
+
+template <int M, int P> cudaError_t ff_launch_xy(int op, const FArgs &a, cudaStream_t s) {
+  if constexpr (P * Fac<M>::maxJ > 1024 || (M / 3) % P != 0) {
+    return cudaErrorInvalidConfiguration;
+  } else {
+    constexpr int N = 2 * M / 3, Kh = M / 3;
+    using X = XY<M, P>;
+    const dim3 gy(N, Kh / P), gx(M, Kh / P), gyc(N, Kh / P, a.ncomp);
+    switch (op) {
+      case FF_Y3:
+        MFX_FF_ALLOW_SMEM((k_ff_y3<M, P>));
+        k_ff_y3<M, P><<<gy, X::threads, X::smem, s>>>(a);
+        break;
+      case FF_XINV:
+        MFX_FF_ALLOW_SMEM((k_ff_x_inv<M, P>));
+        k_ff_x_inv<M, P><<<gx, X::threads, X::smem, s>>>(a);
+        break;
+      case FF_XFWD:
+        MFX_FF_ALLOW_SMEM((k_ff_x_fwd<M, P>));
+        k_ff_x_fwd<M, P><<<gx, X::threads, X::smem, s>>>(a);
+        break;
+      case FF_YFWD:
+        if (a.mode == 0) {
+          MFX_FF_ALLOW_SMEM((k_ff_y_fwd<M, P, 0>));
+          k_ff_y_fwd<M, P, 0><<<gyc, X::threads, X::smem, s>>>(a);
+        } else {
+          MFX_FF_ALLOW_SMEM((k_ff_y_fwd<M, P, 1>));
+          k_ff_y_fwd<M, P, 1><<<gyc, X::threads, X::smem, s>>>(a);
+        }
+        break;
+      default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  }
+}
+
+template <int M, int RW> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStream_t s) {
+  if constexpr (!ff_z_fits<M, RW>()) {
+    return cudaErrorInvalidConfiguration;
+  } else {
+  const unsigned grid = unsigned(size_t(M) * M / RW);
+  if (op == FF_ZSRC2) {
+    constexpr int G = ZG<M, RW, 6>::G;
+    using Z = ZR<M, RW, G, 6>;
+    MFX_FF_ALLOW_SMEM((k_ff_zsrc2<M, RW, G>));
+    k_ff_zsrc2<M, RW, G><<<grid, Z::threads, Z::smem, s>>>(a);
+  } else {
+    constexpr int G = ZG<M, RW, 17>::G;
+    using Z = ZR<M, RW, G, 17>;
+    MFX_FF_ALLOW_SMEM((k_ff_zsrc3<M, RW, G>));
+    k_ff_zsrc3<M, RW, G><<<grid, Z::threads, Z::smem, s>>>(a);
+  }
+  return cudaGetLastError();
+  }
+}
+
+template <int M> cudaError_t ff_launch_m(int op, int p, const FArgs &a, cudaStream_t s) {
+  if (!ff_valid_m<M>(op, p)) return cudaErrorInvalidConfiguration;
+  if (op == FF_ZSRC2 || op == FF_ZSRC3) return p == 1 ? ff_launch_z<M, 1>(op, a, s) : ff_launch_z<M, 2>(op, a, s);
+  switch (p) {
+    case 4: return ff_launch_xy<M, 4>(op, a, s);
+    case 8: return ff_launch_xy<M, 8>(op, a, s);
+    default: return ff_launch_xy<M, 16>(op, a, s);
+  }
+}
+
+// per-M entry points (defined in the ff_m*.cu units)
+#define MFX_FF_LENGTHS(X) X(24) X(48) X(96) X(144) X(192) X(288) X(384) X(576) X(768) X(1152) X(1536)
+#define MFX_FF_DECL(M)                                                        \
+  cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s); \
+  bool ff_valid_##M(int op, int p);
+MFX_FF_LENGTHS(MFX_FF_DECL)
+#undef MFX_FF_DECL
+
+#define MFX_FF_DEFINE(M)                                                                                     \
+  cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s) { return ff_launch_m<M>(op, p, a, s); } \
+  bool ff_valid_##M(int op, int p) { return ff_valid_m<M>(op, p); }
+
+inline bool ff_length_supported(int M) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return true;
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return false;
+}
+
+inline int ff_maxj(int M) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return Fac<L>::maxJ;
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return 0;
+}
+
+inline bool ff_valid(int M, int op, int p) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return ff_valid_##L(op, p);
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return false;
+}
+
+inline cudaError_t ff_launch(int M, int op, int p, const FArgs &a, cudaStream_t s) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return ff_launch_##L(op, p, a, s);
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ff
+}  // namespace mfx

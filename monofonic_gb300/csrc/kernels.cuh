@@ -103,6 +103,8 @@ struct NoiseArgs {
 };
 
 template <typename R> struct NoiseMath;
+// Box-Muller of two 48-bit uniforms (the FP32 form uses it too: a uniform
+// within 2^-25 of 1 rounds to 1.0f, and logf(1) = 0 would zero the mode)
 template <> struct NoiseMath<double> {
   static __device__ __forceinline__ void z(uint64_t a, uint64_t b, double &re, double &im) {
     const double phase = (double(a) * kTwoM48) * 2 * 3.141592653589793;
@@ -113,17 +115,6 @@ template <> struct NoiseMath<double> {
     im = am * s;
   }
 };
-template <> struct NoiseMath<float> {
-  static __device__ __forceinline__ void z(uint64_t a, uint64_t b, float &re, float &im) {
-    const float ua = float(double(a) * kTwoM48);
-    const float am = sqrtf(-logf(float(double(b) * kTwoM48)));
-    float s, c;
-    sincospif(2.0f * ua, &s, &c);
-    re = am * c;
-    im = am * s;
-  }
-};
-
 template <typename R>
 __global__ void __launch_bounds__(128) k_noise_phi1(NoiseArgs a, typename Cplx<R>::T *out) {
   using C = typename Cplx<R>::T;
@@ -151,27 +142,28 @@ __global__ void __launch_bounds__(128) k_noise_phi1(NoiseArgs a, typename Cplx<R
     // k = 0 plane: only the half that the reference assigns directly writes;
     // the other half receives the conjugate from its partner column.
     if (k == 0 && (i > nh || (i == 0 && j > nh))) continue;
-    R re, im;
-    NoiseMath<R>::z(ua, ub, re, im);
+    // the mode is formed in FP64 in both forms and rounded once at the end
+    double re, im;
+    NoiseMath<double>::z(ua, ub, re, im);
     if (a.mode >= 1) {
       if (a.fixing) {
-        const R m = sqrt(re * re + im * im);
-        if (m != R(0)) {
+        const double m = sqrt(re * re + im * im);
+        if (m != 0.0) {
           re /= m;
           im /= m;
         }
       }
-      re *= R(a.norm);
-      im *= R(a.norm);
+      re *= a.norm;
+      im *= a.norm;
       if (a.mode == 2) {
         const size_t n = size_t(si * si + sj * sj + k * k);
-        const R f = (n < a.amp_len) ? R(-a.amp[n] * a.out_scale) : R(0);
+        const double f = (n < a.amp_len) ? -a.amp[n] * a.out_scale : 0.0;
         re *= f;
         im *= f;
       }
     }
-    colp[k] = mkc<R>(re, im);
-    if (k == 0) out[(size_t(ii) * N + jj) * nk] = mkc<R>(re, -im);
+    colp[k] = mkc<R>(R(re), R(im));
+    if (k == 0) out[(size_t(ii) * N + jj) * nk] = mkc<R>(R(re), R(-im));
   }
 }
 

@@ -349,6 +349,13 @@ class Job:
     def fetch_particles_into(self, pos, vel, ids):
         check(load().mfx_job_fetch_particles(self._h, pos, vel, ids))
 
+    def fetch_particles_range_into(self, first: int, count: int, pos, vel, ids):
+        """Copies particles [first, first + count) to host (or device) addresses."""
+        L = load()
+        L.mfx_job_fetch_particles_range.argtypes = [C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p,
+                                                    C.c_void_p]
+        check(L.mfx_job_fetch_particles_range(self._h, first, count, pos, vel, ids))
+
     def particles_range(self, first: int, count: int):
         """Particles [first, first + count) as numpy arrays."""
         L = load()

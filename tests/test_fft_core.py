@@ -1,5 +1,6 @@
-"""The mixed-radix Stockham core of the fused transforms (fused.cuh), built
-for the host, against numpy's FFT for every padded length the engine uses."""
+"""The compile-time pencil FFT of the fused transforms (fused.cuh), built for
+the host and run step by step as the CTA runs it, against numpy's FFT for
+every padded length the engine supports, in both shared-memory layouts."""
 import pathlib
 import subprocess
 
@@ -16,7 +17,7 @@ def harness(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("L", [12, 48, 96, 192, 288, 384, 576, 1152])
+@pytest.mark.parametrize("L", [24, 48, 96, 144, 192, 288, 384, 576, 768, 1152, 1536])
 @pytest.mark.parametrize("inv", [0, 1])
 @pytest.mark.parametrize("layout", [0, 1])
 def test_stockham_matches_numpy(harness, L, inv, layout):
