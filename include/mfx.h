@@ -130,6 +130,12 @@ int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids);
    a large container in chunks (the reference's plugins write the whole
    container at once, output_plugin.hh:62-68). */
 int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void *pos, void *vel, void *ids);
+/* Re-runs the displacement / velocity assembly and the particle stage
+   (ic_generator.cc:937-1030) on the potentials of the last mfx_job_run,
+   combining only the LPT orders in orders_mask (bit n-1: order n, 1..7), so
+   that each order's displacement and velocity can be read on its own (the
+   per-order error statement of the FP32 form).  Not capturable in a graph. */
+int mfx_job_assemble(mfx_job *job, int orders_mask);
 /* Device pointers of the particle arrays (valid until the next run/destroy). */
 int mfx_job_particles_device(mfx_job *job, const void **pos, const void **vel, const void **ids,
                              size_t *num_particles);
@@ -155,6 +161,12 @@ int mfx_job_set_profiling(mfx_job *job, int on);
 int mfx_job_kernel_profile(mfx_job *job, int max_entries, char *names, double *ms, double *bytes, int *launches);
 int mfx_job_destroy(mfx_job *job);
 
+/* Sets the pencil-tile shape of the fused transforms by hand (the choice
+   mfx_job_autotune makes by timing): pencils per CTA of the x/y passes
+   (4, 8 or 16) and rows per CTA of the z passes (1 or 2).  MFX_EINVAL for a
+   shape the padded length does not admit, MFX_ESTATE for a job without the
+   fused transforms. */
+int mfx_job_set_tiles(mfx_job *job, int pencils_xy, int rows_z);
 /* Autotuner of the FP32 form's fused transforms: times every admissible
    pencil-tile shape (pencils per CTA of the x/y passes, rows per CTA of the z
    passes) on the job's own buffers and keeps the fastest for the job and, per

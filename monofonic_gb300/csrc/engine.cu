@@ -131,6 +131,7 @@ struct mfx_job {
   float2 *ff_tw = nullptr;     // W_M^t, t < M
   size_t rsize = 8;
   cudaStream_t stream = nullptr;
+  cudaStream_t xfer[4] = {};  // particle downloads, split across copy streams
   cudaEvent_t ev[6] = {};
   bool timed = false;
   // arena
@@ -192,7 +193,7 @@ struct Layout {
   size_t seeds, amp, plt, phase, nfields, region, work_est, total;
   size_t n_field, m_field, asm_bytes, part_bytes, mregion;
   int nslots, group;
-  size_t ff_b, ff_d;
+  size_t ff_b, ff_d, ff_tw;
   int ff_nc;
 };
 
@@ -250,7 +251,9 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
     L.ff_b = align_up(size_t(N) * M * kh * 8);
     L.ff_d = align_up(size_t(M) * M * kh * 8);
     L.ff_nc = d->lpt_order == 3 ? 17 : 7;
-    L.mregion = 3 * L.ff_b + size_t(L.ff_nc) * L.ff_d + align_up(size_t(M) * 8);
+    L.mregion = 3 * L.ff_b + size_t(L.ff_nc) * L.ff_d;
+    // the twiddles outlive the run: not in the region the particles reuse
+    L.ff_tw = align_up(size_t(M) * 8);
   }
   const size_t np = size_t(ns) * N * N * N;
   L.part_bytes = 0;
@@ -269,7 +272,7 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   L.asm_bytes = d->want_particles ? L.part_bytes + size_t(6 * group) * align_up(L.n_field) : 0;
   L.region = std::max(L.mregion, L.asm_bytes);
   L.work_est = align_up(work_bytes);
-  L.total = L.seeds + L.amp + L.plt + L.phase + L.nfields + L.region + L.work_est;
+  L.total = L.seeds + L.amp + L.plt + L.phase + L.ff_tw + L.nfields + L.region + L.work_est;
   return L;
 }
 
@@ -657,6 +660,82 @@ static int autotune_fused(mfx_job *j) {
   return MFX_OK;
 }
 
+// Displacement / velocity assembly and particles (ic_generator.cc:937-1030):
+// the LPT orders in `mask` (bit n-1: order n) are combined, the others left out.
+template <typename R> static int assemble_stage(mfx_job *j, int mask) {
+  const int order = j->d.lpt_order;
+  const int nsm = num_sm();
+  const int N = j->N;
+  const double N3 = double(N) * N * N;
+  AsmArgs a{};
+  for (int q = 0; q < 3; ++q) {
+    a.phi[q] = j->nf[q];
+    a.A3[q] = j->nf[3 + q];
+  }
+  a.plt = j->d.plt ? j->plt : nullptr;
+  a.plt4 = j->d.plt ? j->plt4 : nullptr;
+  a.phase = j->phase;
+  a.N = N;
+  a.order = order;
+  a.kfac = 2.0 * M_PI / j->d.boxlen;
+  a.mapratio = double(MFX_PLT_NGRID) / double(N);
+  a.boxlen = j->d.boxlen;
+  a.g1 = j->d.g1;
+  a.g2 = j->d.g2;
+  a.g3 = j->d.g3;
+  a.g3c = j->d.g3c;
+  a.vfac1 = j->d.vfac1;
+  a.vfac2 = j->d.vfac2;
+  a.vfac3 = j->d.vfac3;
+  if (!(mask & 1)) a.g1 = a.vfac1 = 0.0;
+  if (!(mask & 2)) a.g2 = a.vfac2 = 0.0;
+  if (!(mask & 4)) a.g3 = a.g3c = a.vfac3 = 0.0;
+  a.pfac = j->d.lunit / j->d.boxlen / std::sqrt(N3);
+  a.vfac = j->d.vunit / j->d.boxlen / std::sqrt(N3);
+  a.in_scale1 = 1.0 / j->scale1;
+  a.in_scale2 = 1.0 / j->scale2;
+  a.in_scale3 = 1.0 / j->scale3;
+  const size_t total = size_t(N) * N * j->nk;
+  for (int s0 = 0; s0 < j->ns; s0 += j->group) {
+    const int g = std::min(j->group, j->ns - s0);
+    a.shift0 = s0;
+    a.nshift = g;
+    for (int q = 0; q < 6 * g; ++q) a.out[q] = j->asmbuf[q];
+    KBEGIN(j);
+    if (a.plt) k_assemble<R, true><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(a);
+    else k_assemble<R, false><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(a);
+    KEND(j, "assemble", ((order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) + 6.0 * g) * j->n_field_bytes);
+    for (int s = 0; s < g; ++s) {
+      for (int q = 0; q < 6; ++q) TRY(exec_fft(j, j->n_c2r, j->asmbuf[s * 6 + q], false));
+      PartArgs p{};
+      for (int q = 0; q < 6; ++q) p.f[q] = j->asmbuf[s * 6 + q];
+      p.pos = j->pos;
+      p.vel = j->vel;
+      p.ids = j->ids;
+      p.N = N;
+      p.nshift_total = j->ns;
+      p.ishift = s0 + s;
+      p.pos64 = j->d.pos64;
+      p.vel64 = j->d.vel64;
+      p.id64 = j->d.id64;
+      p.sx = kShifts[j->d.lattice][s0 + s][0];
+      p.sy = kShifts[j->d.lattice][s0 + s][1];
+      p.sz = kShifts[j->d.lattice][s0 + s][2];
+      p.lunit = j->d.lunit;
+      p.qtab = j->qtab + size_t(s0 + s) * 3 * N;
+      p.id_offset = j->d.id_offset * uint64_t(j->ns) * uint64_t(N3);
+      KBEGIN(j);
+      const unsigned pg = grid_for(size_t(N) * N * N / 4, 256, nsm);
+      if (p.pos64 && p.vel64) k_particles<R, double, double><<<pg, 256, 0, j->stream>>>(p);
+      else if (p.pos64) k_particles<R, double, float><<<pg, 256, 0, j->stream>>>(p);
+      else if (p.vel64) k_particles<R, float, double><<<pg, 256, 0, j->stream>>>(p);
+      else k_particles<R, float, float><<<pg, 256, 0, j->stream>>>(p);
+      KEND(j, "particles", N3 * (6.0 * j->rsize + 3.0 * (p.pos64 ? 8 : 4) + 3.0 * (p.vel64 ? 8 : 4) + (p.id64 ? 8 : 4)));
+    }
+  }
+  return MFX_OK;
+}
+
 template <typename R> static int run_pipeline(mfx_job *j) {
   const int order = j->d.lpt_order;
   const size_t mreal = size_t(j->M) * j->M * (j->M + 2);
@@ -731,73 +810,7 @@ template <typename R> static int run_pipeline(mfx_job *j) {
   }
   }  // cuFFT path
   if (j->timed) CU(cudaEventRecord(j->ev[3], j->stream));
-  if (j->d.want_particles) {
-    const int N = j->N;
-    const double N3 = double(N) * N * N;
-    AsmArgs a{};
-    for (int q = 0; q < 3; ++q) {
-      a.phi[q] = j->nf[q];
-      a.A3[q] = j->nf[3 + q];
-    }
-    a.plt = j->d.plt ? j->plt : nullptr;
-    a.plt4 = j->d.plt ? j->plt4 : nullptr;
-    a.phase = j->phase;
-    a.N = N;
-    a.order = order;
-    a.kfac = 2.0 * M_PI / j->d.boxlen;
-    a.mapratio = double(MFX_PLT_NGRID) / double(N);
-    a.boxlen = j->d.boxlen;
-    a.g1 = j->d.g1;
-    a.g2 = j->d.g2;
-    a.g3 = j->d.g3;
-    a.g3c = j->d.g3c;
-    a.vfac1 = j->d.vfac1;
-    a.vfac2 = j->d.vfac2;
-    a.vfac3 = j->d.vfac3;
-    a.pfac = j->d.lunit / j->d.boxlen / std::sqrt(N3);
-    a.vfac = j->d.vunit / j->d.boxlen / std::sqrt(N3);
-    a.in_scale1 = 1.0 / j->scale1;
-    a.in_scale2 = 1.0 / j->scale2;
-    a.in_scale3 = 1.0 / j->scale3;
-    const size_t total = size_t(N) * N * j->nk;
-    for (int s0 = 0; s0 < j->ns; s0 += j->group) {
-      const int g = std::min(j->group, j->ns - s0);
-      a.shift0 = s0;
-      a.nshift = g;
-      for (int q = 0; q < 6 * g; ++q) a.out[q] = j->asmbuf[q];
-      KBEGIN(j);
-      if (a.plt) k_assemble<R, true><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(a);
-      else k_assemble<R, false><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(a);
-      KEND(j, "assemble", ((order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) + 6.0 * g) * j->n_field_bytes);
-      for (int s = 0; s < g; ++s) {
-        for (int q = 0; q < 6; ++q) TRY(exec_fft(j, j->n_c2r, j->asmbuf[s * 6 + q], false));
-        PartArgs p{};
-        for (int q = 0; q < 6; ++q) p.f[q] = j->asmbuf[s * 6 + q];
-        p.pos = j->pos;
-        p.vel = j->vel;
-        p.ids = j->ids;
-        p.N = N;
-        p.nshift_total = j->ns;
-        p.ishift = s0 + s;
-        p.pos64 = j->d.pos64;
-        p.vel64 = j->d.vel64;
-        p.id64 = j->d.id64;
-        p.sx = kShifts[j->d.lattice][s0 + s][0];
-        p.sy = kShifts[j->d.lattice][s0 + s][1];
-        p.sz = kShifts[j->d.lattice][s0 + s][2];
-        p.lunit = j->d.lunit;
-        p.qtab = j->qtab + size_t(s0 + s) * 3 * N;
-        p.id_offset = j->d.id_offset * uint64_t(j->ns) * uint64_t(N3);
-        KBEGIN(j);
-        const unsigned pg = grid_for(size_t(N) * N * N / 4, 256, nsm);
-        if (p.pos64 && p.vel64) k_particles<R, double, double><<<pg, 256, 0, j->stream>>>(p);
-        else if (p.pos64) k_particles<R, double, float><<<pg, 256, 0, j->stream>>>(p);
-        else if (p.vel64) k_particles<R, float, double><<<pg, 256, 0, j->stream>>>(p);
-        else k_particles<R, float, float><<<pg, 256, 0, j->stream>>>(p);
-        KEND(j, "particles", N3 * (6.0 * j->rsize + 3.0 * (p.pos64 ? 8 : 4) + 3.0 * (p.vel64 ? 8 : 4) + (p.id64 ? 8 : 4)));
-      }
-    }
-  }
+  if (j->d.want_particles) TRY(assemble_stage<R>(j, 7));
   if (j->timed) CU(cudaEventRecord(j->ev[4], j->stream));
   j->has_run = true;
   j->noise_only = false;
@@ -850,6 +863,8 @@ static void free_job(mfx_job *j) {
     if (e) cudaEventDestroy(e);
   for (auto &e : j->ev_pool)
     if (e) cudaEventDestroy(e);
+  for (auto &x : j->xfer)
+    if (x) cudaStreamDestroy(x);
   if (j->stream) cudaStreamDestroy(j->stream);
   if (j->eng) {
     std::lock_guard<std::mutex> lk(j->eng->mu);
@@ -950,6 +965,8 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->phase = (double2 *)p;
   j->qtab = (double *)(p + align_up(size_t(j->ns) * 3 * j->N * sizeof(double2)));
   p += L.phase;
+  j->ff_tw = L.ff_tw ? reinterpret_cast<float2 *>(p) : nullptr;
+  p += L.ff_tw;
   const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
   j->n_field_bytes = L.n_field;
   j->m_field_bytes = L.m_field;
@@ -967,7 +984,6 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     char *f = j->region;
     for (int q = 0; q < 3; ++q, f += L.ff_b) j->ffB[q] = f;
     for (int q = 0; q < L.ff_nc; ++q, f += L.ff_d) j->ffC[q] = f;
-    j->ff_tw = reinterpret_cast<float2 *>(f);
     std::vector<float2> tw(j->M);
     for (int t = 0; t < j->M; ++t) {
       const double a = 2.0 * M_PI * double(t) / double(j->M);
@@ -1204,6 +1220,36 @@ int mfx_job_run(mfx_job *job) {
   GUARD_END
 }
 
+int mfx_job_assemble(mfx_job *job, int orders_mask) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
+  if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has no potentials (run it first)");
+  if (orders_mask < 1 || orders_mask > 7) return set_error(MFX_EINVAL, "orders_mask %d outside 1..7", orders_mask);
+  CU(cudaSetDevice(job->eng->device));
+  job->ev_next = 0;
+  job->prof_recs.clear();
+  TRY(job->fp64 ? assemble_stage<double>(job, orders_mask) : assemble_stage<float>(job, orders_mask));
+  CU(cudaStreamSynchronize(job->stream));
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_set_tiles(mfx_job *job, int pencils_xy, int rows_z) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->fused) return set_error(MFX_ESTATE, "job does not use the fused transforms");
+  if (!ff::ff_valid(job->M, ff::FF_XFWD, pencils_xy))
+    return set_error(MFX_EINVAL, "x/y tile of %d pencils not admissible for M = %d", pencils_xy, job->M);
+  if (!ff::ff_valid(job->M, ff::FF_ZSRC3, rows_z) || !ff::ff_valid(job->M, ff::FF_ZSRC2, rows_z))
+    return set_error(MFX_EINVAL, "z tile of %d rows not admissible for M = %d", rows_z, job->M);
+  if (job->gexec) return set_error(MFX_ESTATE, "job already captured into a graph");
+  job->ff_pxy = pencils_xy;
+  job->ff_pz = rows_z;
+  return MFX_OK;
+  GUARD_END
+}
+
 int mfx_job_autotune(mfx_job *job, int *pencils_xy, int *rows_z) {
   GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
@@ -1267,17 +1313,55 @@ int mfx_job_wait(mfx_job *job, int timeout_ms) {
   GUARD_END
 }
 
+// Downloads after the job's work: each copy is cut into pieces of at least
+// 32 MB spread over four copy streams (one stream's copies do not fill the
+// host link), all waiting on the job stream, and joined before returning.
+struct Xfer {
+  void *dst;
+  const void *src;
+  size_t bytes;
+};
+static int download(mfx_job *j, const Xfer *xs, int n) {
+  for (auto &x : j->xfer)
+    if (!x) CU(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+  cudaEvent_t ready = nullptr;
+  CU(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  cudaError_t e = cudaEventRecord(ready, j->stream);
+  for (auto &x : j->xfer)
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(x, ready, 0);
+  size_t total = 0;
+  for (int q = 0; q < n; ++q) total += xs[q].dst ? xs[q].bytes : 0;
+  const size_t piece = std::max<size_t>(size_t(32) << 20, (total + 7) / 8);
+  int s = 0;
+  for (int q = 0; q < n && e == cudaSuccess; ++q) {
+    if (!xs[q].dst) continue;
+    for (size_t off = 0; off < xs[q].bytes && e == cudaSuccess; off += piece) {
+      const size_t len = std::min(piece, xs[q].bytes - off);
+      e = cudaMemcpyAsync(static_cast<char *>(xs[q].dst) + off, static_cast<const char *>(xs[q].src) + off, len,
+                          cudaMemcpyDefault, j->xfer[s]);
+      s = (s + 1) % 4;
+    }
+  }
+  for (auto &x : j->xfer) {
+    const cudaError_t f = cudaStreamSynchronize(x);
+    if (e == cudaSuccess) e = f;
+  }
+  cudaEventDestroy(ready);
+  if (e != cudaSuccess) return set_error(MFX_ECUDA, "particle download: %s", cudaGetErrorString(e));
+  return MFX_OK;
+}
+
 int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids) {
   GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
   if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
   if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has not produced particles");
+  CU(cudaSetDevice(job->eng->device));
   const size_t np = job->npart;
-  if (pos) CU(cudaMemcpyAsync(pos, job->pos, np * 3 * (job->d.pos64 ? 8 : 4), cudaMemcpyDefault, job->stream));
-  if (vel) CU(cudaMemcpyAsync(vel, job->vel, np * 3 * (job->d.vel64 ? 8 : 4), cudaMemcpyDefault, job->stream));
-  if (ids) CU(cudaMemcpyAsync(ids, job->ids, np * (job->d.id64 ? 8 : 4), cudaMemcpyDefault, job->stream));
-  CU(cudaStreamSynchronize(job->stream));
-  return MFX_OK;
+  const Xfer xs[3] = {{pos, job->pos, np * 3 * (job->d.pos64 ? 8 : 4)},
+                      {vel, job->vel, np * 3 * (job->d.vel64 ? 8 : 4)},
+                      {ids, job->ids, np * (job->d.id64 ? 8 : 4)}};
+  return download(job, xs, 3);
   GUARD_END
 }
 
@@ -1288,17 +1372,12 @@ int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void
   if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has not produced particles");
   if (first > job->npart || count > job->npart - first)
     return set_error(MFX_EINVAL, "range [%zu, %zu) outside the %zu particles", first, first + count, job->npart);
+  CU(cudaSetDevice(job->eng->device));
   const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
-  if (pos)
-    CU(cudaMemcpyAsync(pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count, cudaMemcpyDefault,
-                       job->stream));
-  if (vel)
-    CU(cudaMemcpyAsync(vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count, cudaMemcpyDefault,
-                       job->stream));
-  if (ids)
-    CU(cudaMemcpyAsync(ids, static_cast<char *>(job->ids) + is * first, is * count, cudaMemcpyDefault, job->stream));
-  CU(cudaStreamSynchronize(job->stream));
-  return MFX_OK;
+  const Xfer xs[3] = {{pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
+                      {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
+                      {ids, static_cast<char *>(job->ids) + is * first, is * count}};
+  return download(job, xs, 3);
   GUARD_END
 }
 

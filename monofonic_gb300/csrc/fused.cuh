@@ -565,6 +565,9 @@ template <int M, int RW, int G, int NIN> struct ZR {
   static constexpr int threads = G * Fac<M>::maxJ;
   static constexpr size_t smem =
       size_t(M) * sizeof(float2) + size_t(RW) * nin_pad * M * sizeof(float) + size_t(Tile<M, G, false>::elems) * sizeof(float2);
+  // CTAs per SM: by registers (64 each) and by shared memory (228 KB per SM)
+  static constexpr int by_smem = int(233472 / (smem + 1024));
+  static constexpr int minb = min_blocks(threads) < by_smem ? min_blocks(threads) : (by_smem < 1 ? 1 : by_smem);
 };
 
 // inverse z transforms of NIN C-space inputs of RW rows into h[w][c][z]
@@ -614,12 +617,13 @@ __device__ __forceinline__ void z_inverse(const FArgs &a, size_t r0, float *h, f
 
 // forward z transforms of NOUT real sources per row held in h[w][o][z]
 // (o < NOUT, row stride NP) and the kz < Kh spectra written to dst[o]
-template <int M, int RW, int G, int NP, int NOUT>
+template <int M, int RW, int G0, int NP, int NOUT>
 __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float *h, float2 *buf, const float2 *tw) {
   using D = Dims<M>;
-  using T = Tile<M, G, false>;
   constexpr int NR = RW * NOUT;        // real outputs
   constexpr int NPO = (NR + 1) / 2;    // complex pencils
+  constexpr int G = G0 < NPO ? G0 : NPO;
+  using T = Tile<M, G, false>;
 #pragma unroll 1
   for (int g0 = 0; g0 < NPO; g0 += G) {
     pencil_fft<M, G, false, false>(
@@ -651,7 +655,8 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
 // ZSRC2: phi1 Hessians (src[0..5], C-space) -> 2LPT source (dst[0]) and, with
 // mode 1, the five first-pair products of convolve3 (dst[1..5]).
 // grid (M*M / RW)
-template <int M, int RW, int G> __global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads) k_ff_zsrc2(FArgs a) {
+template <int M, int RW, int G>
+__global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads, ZR<M, RW, G, 6>::minb) k_ff_zsrc2(FArgs a) {
   constexpr int NP = 6;
   float2 *tw = ff_smem();
   float *h = reinterpret_cast<float *>(tw + M);
@@ -684,7 +689,8 @@ template <int M, int RW, int G> __global__ void __launch_bounds__(ZR<M, RW, G, 6
 // pair products src[12..16] (C-space) -> phi3 source (dst[0]) and A3 (dst[1..3]).
 // The outputs may alias inputs: each CTA reads its rows whole before writing.
 // grid (M*M / RW)
-template <int M, int RW, int G> __global__ void __launch_bounds__(ZR<M, RW, G, 17>::threads) k_ff_zsrc3(FArgs a) {
+template <int M, int RW, int G>
+__global__ void __launch_bounds__(ZR<M, RW, G, 17>::threads, ZR<M, RW, G, 17>::minb) k_ff_zsrc3(FArgs a) {
   constexpr int NP = ZR<M, RW, G, 17>::nin_pad;  // 18
   float2 *tw = ff_smem();
   float *h = reinterpret_cast<float *>(tw + M);

@@ -12,11 +12,19 @@ namespace ff {
 
 enum FFOp { FF_Y3 = 0, FF_XINV = 1, FF_XFWD = 2, FF_YFWD = 3, FF_ZSRC2 = 4, FF_ZSRC3 = 5, FF_NOPS = 6 };
 
-// complex pencils per round of the z passes: as many as fit 512 threads
+// complex pencils per round of the z passes: the largest divisor of the row
+// tile's pencil count that keeps the CTA within 256 threads (small CTAs, so
+// that the barriers of one leave the SM to the others)
+constexpr int zg_pick(int npi, int cap) {
+  int g = 1;
+  for (int d = 1; d <= npi; ++d)
+    if (npi % d == 0 && d <= cap) g = d;
+  return g;
+}
 template <int M, int RW, int NIN> struct ZG {
   static constexpr int npi = RW * ((NIN + (NIN & 1)) / 2);
-  static constexpr int cap = 512 / Fac<M>::maxJ > 0 ? 512 / Fac<M>::maxJ : 1;
-  static constexpr int G = npi < cap ? npi : cap;
+  static constexpr int cap = 256 / Fac<M>::maxJ > 0 ? 256 / Fac<M>::maxJ : 1;
+  static constexpr int G = zg_pick(npi, cap);
 };
 
 constexpr size_t kFFSmemMax = 227 * 1024;

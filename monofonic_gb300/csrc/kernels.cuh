@@ -102,9 +102,9 @@ struct NoiseArgs {
   double out_scale;   // extra factor on phi(1) (per-field scaling of the FP32 form)
 };
 
+// Box-Muller of two 48-bit uniforms u_a = a 2^-48, u_b = b 2^-48
+// (random_ngenic.cc:117-121): z = sqrt(-ln u_b) exp(2 pi i u_a).
 template <typename R> struct NoiseMath;
-// Box-Muller of two 48-bit uniforms (the FP32 form uses it too: a uniform
-// within 2^-25 of 1 rounds to 1.0f, and logf(1) = 0 would zero the mode)
 template <> struct NoiseMath<double> {
   static __device__ __forceinline__ void z(uint64_t a, uint64_t b, double &re, double &im) {
     const double phase = (double(a) * kTwoM48) * 2 * 3.141592653589793;
@@ -115,6 +115,28 @@ template <> struct NoiseMath<double> {
     im = am * s;
   }
 };
+// The FP32 form keeps the variates' 48 bits where float would drop them:
+// ln u_b as log1p(-(1 - u_b)) with 1 - u_b taken exactly from the integer when
+// u_b >= 1/2 (a plain float u_b within 2^-25 of 1 rounds to 1 and would zero
+// the mode), and the phase pi x, x = 2 u_a, split as x_hi + x_lo with the
+// small part applied to the sine and cosine to first order (|pi x_lo| < 4e-7).
+template <> struct NoiseMath<float> {
+  static __device__ __forceinline__ void z(uint64_t a, uint64_t b, float &re, float &im) {
+    const float lnu = (b < (uint64_t(1) << 47)) ? logf(float(b) * 3.5527136788005009e-15f)  // 2^-48
+                                                : log1pf(-float((uint64_t(1) << 48) - b) * 3.5527136788005009e-15f);
+    const float am = sqrtf(-lnu);
+    const uint64_t ahi = a & ~((uint64_t(1) << 24) - 1);
+    const float xh = float(ahi) * 7.1054273576010019e-15f;     // 2^-47: x = a 2^-47 in [0, 2)
+    const float xl = float(a - ahi) * 7.1054273576010019e-15f;  // < 2^-23
+    float s, c;
+    sincospif(xh, &s, &c);
+    const float pxl = 3.14159265358979f * xl;
+    const float s1 = fmaf(pxl, c, s), c1 = fmaf(-pxl, s, c);
+    re = am * c1;
+    im = am * s1;
+  }
+};
+
 template <typename R>
 __global__ void __launch_bounds__(128) k_noise_phi1(NoiseArgs a, typename Cplx<R>::T *out) {
   using C = typename Cplx<R>::T;
@@ -142,28 +164,27 @@ __global__ void __launch_bounds__(128) k_noise_phi1(NoiseArgs a, typename Cplx<R
     // k = 0 plane: only the half that the reference assigns directly writes;
     // the other half receives the conjugate from its partner column.
     if (k == 0 && (i > nh || (i == 0 && j > nh))) continue;
-    // the mode is formed in FP64 in both forms and rounded once at the end
-    double re, im;
-    NoiseMath<double>::z(ua, ub, re, im);
+    R re, im;
+    NoiseMath<R>::z(ua, ub, re, im);
     if (a.mode >= 1) {
       if (a.fixing) {
-        const double m = sqrt(re * re + im * im);
-        if (m != 0.0) {
+        const R m = sqrt(re * re + im * im);
+        if (m != R(0)) {
           re /= m;
           im /= m;
         }
       }
-      re *= a.norm;
-      im *= a.norm;
+      re *= R(a.norm);
+      im *= R(a.norm);
       if (a.mode == 2) {
         const size_t n = size_t(si * si + sj * sj + k * k);
-        const double f = (n < a.amp_len) ? -a.amp[n] * a.out_scale : 0.0;
+        const R f = (n < a.amp_len) ? R(-a.amp[n] * a.out_scale) : R(0);
         re *= f;
         im *= f;
       }
     }
-    colp[k] = mkc<R>(R(re), R(im));
-    if (k == 0) out[(size_t(ii) * N + jj) * nk] = mkc<R>(R(re), R(-im));
+    colp[k] = mkc<R>(re, im);
+    if (k == 0) out[(size_t(ii) * N + jj) * nk] = mkc<R>(re, -im);
   }
 }
 

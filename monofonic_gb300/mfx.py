@@ -23,7 +23,7 @@ PLT_TABLE_DOUBLES = 4 * 64 * 64 * 33
 EXPORTS = [
     "mfx_last_error", "mfx_version", "mfx_engine_create", "mfx_engine_destroy", "mfx_job_footprint",
     "mfx_job_create", "mfx_job_upload", "mfx_job_run", "mfx_job_wait", "mfx_job_fetch_particles",
-    "mfx_job_fetch_particles_range",
+    "mfx_job_fetch_particles_range", "mfx_job_assemble", "mfx_job_set_tiles",
     "mfx_job_particles_device", "mfx_job_fetch_field", "mfx_job_run_noise", "mfx_job_stage_times",
     "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
     "mfx_job_destroy", "mfx_job_autotune", "mfx_job_capture", "mfx_batch_create", "mfx_batch_run", "mfx_batch_wait",
@@ -348,6 +348,19 @@ class Job:
 
     def fetch_particles_into(self, pos, vel, ids):
         check(load().mfx_job_fetch_particles(self._h, pos, vel, ids))
+
+    def set_tiles(self, pencils_xy: int, rows_z: int):
+        """Pencil-tile shape of the fused transforms (what autotune() picks)."""
+        L = load()
+        L.mfx_job_set_tiles.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        check(L.mfx_job_set_tiles(self._h, int(pencils_xy), int(rows_z)))
+
+    def assemble(self, orders_mask: int):
+        """Re-assemble the particles from the last run's potentials with only the
+        LPT orders in orders_mask (bit n-1: order n)."""
+        L = load()
+        L.mfx_job_assemble.argtypes = [C.c_void_p, C.c_int]
+        check(L.mfx_job_assemble(self._h, int(orders_mask)))
 
     def fetch_particles_range_into(self, first: int, count: int, pos, vel, ids):
         """Copies particles [first, first + count) to host (or device) addresses."""

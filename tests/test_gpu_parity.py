@@ -302,6 +302,62 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     assert np.sqrt(np.mean(((pf[0] - pr[0]) / delta) ** 2)) < 1e-6
 
 
+@pytest.mark.parametrize("n,lattice", [(64, 2), (48, 2)])
+def test_fused_rerun_is_identical(mfxlib, engine, n, lattice, monkeypatch):
+    """A second run of the same job (the particle stage reuses the padded
+    transforms' buffers in between) reproduces the first bit for bit, for every
+    admissible tile shape."""
+    monkeypatch.setenv("MFX_FUSED", "1")
+    c = Case(mfxlib, n, 300.0, 24.0, 3, 4242, lattice=lattice, plt=engine.plt_table(lattice))
+    fids = [mfxlib.FIELD_PHI2, mfxlib.FIELD_PHI3, mfxlib.FIELD_A3Y]
+    first = None
+    for pxy in (4, 8, 16):
+        for pz in (1, 2):
+            j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
+            try:
+                j.set_tiles(pxy, pz)
+            except RuntimeError:
+                j.close()
+                continue
+            j.run()
+            a = [j.field(f) for f in fids] + [j.particles()[0]]
+            j.run()
+            b = [j.field(f) for f in fids] + [j.particles()[0]]
+            j.close()
+            for x, y in zip(a, b):
+                assert np.all(np.isfinite(x)) and np.array_equal(x, y)
+            if first is None:
+                first = a
+            for x, y in zip(a[:-1], first[:-1]):  # tiles change only the summation order
+                assert rel_l2(x, y) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_assemble_per_order_is_linear(mfxlib, engine, precision):
+    """mfx_job_assemble: the displacements and velocities of the orders taken
+    one at a time add up to those of the full assembly."""
+    prec = mfxlib.FP64 if precision == "fp64" else mfxlib.FP32C
+    c = Case(mfxlib, 32, 300.0, 24.0, 3, 4242, lattice=1, plt=engine.plt_table(1))
+    j = c.job(mfxlib, engine, precision=prec)
+    j.run()
+    pos, vel, ids = j.particles()
+    q = lattice_q(c.n, c.lattice, c.lunit)
+    psi, v = np.zeros_like(pos), np.zeros_like(vel, dtype=np.float64)
+    for m in (1, 2, 4):
+        j.assemble(m)
+        p, vv, ii = j.particles()
+        assert np.array_equal(ii, ids)
+        psi += p - q
+        v += vv
+    j.assemble(7)
+    p7, v7, _ = j.particles()
+    j.close()
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert rel_l2(psi, pos - q) < tol
+    assert rel_l2(v, vel.astype(np.float64)) < tol
+    assert np.array_equal(p7, pos) and np.array_equal(v7, vel)
+
+
 # ---------------------------------------------------------------------------
 # edge cases and errors
 # ---------------------------------------------------------------------------
