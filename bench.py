@@ -184,6 +184,7 @@ def run_ours(args):
                   plt_table=hp, fixing=inp["fix"], lunit=inp["lunit"], vunit=inp["vunit"], pos64=pos64,
                   vel64=vel64, id64=True)
     npart = job.num_particles
+    tiles = job.autotune() if prec == mfx.FP32C else None  # pencil tiles of the fused transforms (untimed)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
 
     def barrier():
@@ -289,6 +290,7 @@ def run_ours(args):
             "whole_step_alg": {"bytes": alg_total, "achieved_GBps": alg_total / (ms_step * 1e-3) / 1e9,
                                "frac": alg_total / (ms_step * 1e-3) / 1e9 / peak},
             "kernels": kern, "clocks": clk, "wall_s_timed": wall,
+            "fused_tiles": {"pencils_xy": tiles[0], "rows_z": tiles[1]} if tiles else None,
         }
     job.close()
     return out, eng, inp, plt_tab

@@ -129,6 +129,7 @@ struct mfx_job {
   void *ffB[3] = {};           // B-space [N][M][N/2] complex
   void *ffC[17] = {};          // C-space [M][M][N/2] complex
   float2 *ff_tw = nullptr;     // W_M^t, t < M
+  int *dstatus = nullptr;      // device status word: nonzero when a kernel's bounded wait ran out
   size_t rsize = 8;
   cudaStream_t stream = nullptr;
   cudaStream_t xfer[4] = {};  // particle downloads, split across copy streams
@@ -193,7 +194,7 @@ struct Layout {
   size_t seeds, amp, plt, phase, nfields, region, work_est, total;
   size_t n_field, m_field, asm_bytes, part_bytes, mregion;
   int nslots, group;
-  size_t ff_b, ff_d, ff_tw;
+  size_t ff_b, ff_d, ff_tw, status;
   int ff_nc;
 };
 
@@ -216,14 +217,14 @@ static int check_desc(const mfx_job_desc *d) {
   return MFX_OK;
 }
 
-// FP32 form with a padded length M = 2^a 3^b and N/2 a multiple of 8 can run
-// the padded convolutions through the pruned, fused transforms (fused.cuh);
-// the plain FP64 form and other sizes use cuFFT.  MFX_FUSED=1 selects the
-// fused transforms, MFX_FUSED=0 (the default) cuFFT.
+// The FP32 form runs the padded convolutions through the pruned, fused
+// transforms (fused.cuh) for every padded length they are built for; the
+// plain FP64 form and other sizes use cuFFT.  MFX_FUSED=0 in the environment
+// sends the FP32 form through cuFFT as well (for comparisons).
 static bool fused_supported(const mfx_job_desc *d) {
   if (d->precision != MFX_FP32C || d->lpt_order < 2) return false;
   const char *env = getenv("MFX_FUSED");
-  if (!env || env[0] != '1') return false;
+  if (env && env[0] == '0') return false;
   const int N = d->ngrid, M = 3 * N / 2;
   return (N / 2) % 8 == 0 && ff::ff_length_supported(M);
 }
@@ -254,6 +255,7 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
     L.mregion = 3 * L.ff_b + size_t(L.ff_nc) * L.ff_d;
     // the twiddles outlive the run: not in the region the particles reuse
     L.ff_tw = align_up(size_t(M) * 8);
+    L.status = align_up(sizeof(int));
   }
   const size_t np = size_t(ns) * N * N * N;
   L.part_bytes = 0;
@@ -272,7 +274,7 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   L.asm_bytes = d->want_particles ? L.part_bytes + size_t(6 * group) * align_up(L.n_field) : 0;
   L.region = std::max(L.mregion, L.asm_bytes);
   L.work_est = align_up(work_bytes);
-  L.total = L.seeds + L.amp + L.plt + L.phase + L.ff_tw + L.nfields + L.region + L.work_est;
+  L.total = L.seeds + L.amp + L.plt + L.phase + L.ff_tw + L.status + L.nfields + L.region + L.work_est;
   return L;
 }
 
@@ -468,6 +470,7 @@ static void tune_fused(mfx_job *j);
 static ff::FArgs ff_args(mfx_job *j) {
   ff::FArgs a{};
   a.tw = j->ff_tw;
+  a.status = j->dstatus;
   a.kfac = float(2.0 * M_PI / j->d.boxlen);
   return a;
 }
@@ -572,8 +575,8 @@ static int run_potentials_fused(mfx_job *j) {
   return MFX_OK;
 }
 
-// default tile shapes: the largest x/y tile of at most 512 threads, and two
-// rows per CTA for the z passes where the 17-field rows leave room
+// default tile shapes: the largest x/y tile of at most 512 threads, and one
+// row per step of the persistent z passes (two fit one CTA per SM only)
 static void ff_default_tiles(mfx_job *j) {
   j->ff_pxy = 4;
   for (int p : {16, 8, 4})
@@ -581,7 +584,7 @@ static void ff_default_tiles(mfx_job *j) {
       j->ff_pxy = p;
       break;
     }
-  j->ff_pz = j->M <= 576 ? 2 : 1;
+  j->ff_pz = 1;
 }
 
 // pencil-tile shapes chosen by mfx_job_autotune for this size class, if any
@@ -635,12 +638,19 @@ static int autotune_fused(mfx_job *j) {
   tbest = 1e30f;
   for (int p : {1, 2}) {
     if (rc != MFX_OK || !ff::ff_valid(M, ff::FF_ZSRC3, p)) continue;
+    // the z pass that dominates the job: ZSRC3 (3LPT) or ZSRC2 (2LPT)
     const float t = timed([&] {
       ff::FArgs z = ff_args(j);
-      for (int c = 0; c < 6; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
-      z.dst[0] = static_cast<float2 *>(j->ffC[6]);
-      z.mode = 0;
-      if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC2, p, z, "ff_zsrc2", 0);
+      if (j->d.lpt_order >= 3) {
+        for (int c = 0; c < 17; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
+        for (int o = 0; o < 4; ++o) z.dst[o] = static_cast<float2 *>(j->ffC[12 + o]);
+        if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC3, p, z, "ff_zsrc3", 0);
+      } else {
+        for (int c = 0; c < 6; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
+        z.dst[0] = static_cast<float2 *>(j->ffC[6]);
+        z.mode = 0;
+        if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC2, p, z, "ff_zsrc2", 0);
+      }
     });
     if (t < tbest) {
       tbest = t;
@@ -967,6 +977,10 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   p += L.phase;
   j->ff_tw = L.ff_tw ? reinterpret_cast<float2 *>(p) : nullptr;
   p += L.ff_tw;
+  j->dstatus = L.status ? reinterpret_cast<int *>(p) : nullptr;
+  p += L.status;
+  if (j->dstatus && (cudaMemsetAsync(j->dstatus, 0, sizeof(int), j->stream) != cudaSuccess))
+    return fail(set_error(MFX_ECUDA, "status word reset failed"));
   const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
   j->n_field_bytes = L.n_field;
   j->m_field_bytes = L.m_field;
@@ -1294,17 +1308,27 @@ int mfx_job_run_noise(mfx_job *job, int raw) {
   GUARD_END
 }
 
+// the device status word of a finished job: a kernel whose bounded wait for
+// its own asynchronous copies ran out set it and left its work undone
+static int check_status(mfx_job *job) {
+  if (!job->dstatus) return MFX_OK;
+  int st = 0;
+  CU(cudaMemcpy(&st, job->dstatus, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st) return set_error(MFX_ETIMEOUT, "a fused-transform kernel timed out waiting for its staged inputs");
+  return MFX_OK;
+}
+
 int mfx_job_wait(mfx_job *job, int timeout_ms) {
   GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
   if (timeout_ms < 0) {
     CU(cudaStreamSynchronize(job->stream));
-    return MFX_OK;
+    return check_status(job);
   }
-  // bounded host-side poll; the device work itself never waits
+  // bounded host-side poll
   for (int waited = 0;; ++waited) {
     cudaError_t e = cudaStreamQuery(job->stream);
-    if (e == cudaSuccess) return MFX_OK;
+    if (e == cudaSuccess) return check_status(job);
     if (e != cudaErrorNotReady) return set_error(MFX_ECUDA, "job stream: %s", cudaGetErrorString(e));
     if (waited >= timeout_ms) return set_error(MFX_ETIMEOUT, "job not finished after %d ms", timeout_ms);
     struct timespec ts = {0, 1000000};

@@ -246,11 +246,18 @@ template <int L, int R, int NS, bool INV> struct Step {
 #if defined(__CUDACC__)
 // PP pencils of length L through one CTA (blockDim.x >= PP * Fac<L>::maxJ;
 // every thread must call it).  ld(q, n) returns input n of pencil q;
-// st(q, k, v) takes output k.  buf holds Tile<L, PP, PF>::elems values.
-// The last step stores after a barrier, so st may write into buf; the caller
-// synchronises before reading what st wrote to shared memory.
+// st(q, k, v) takes output k.  buf and buf2 each hold Tile<L, PP, PF>::elems
+// values; the steps alternate between them, so that a step's reads and the
+// next step's writes never share a buffer (one barrier per exchange).  ld may
+// read either buffer; st may write obuf() (the buffer the last step does not
+// read); the caller synchronises before reading what st wrote to shared
+// memory.
+template <int L> __device__ __forceinline__ float2 *obuf(float2 *buf, float2 *buf2) {
+  return Fac<L>::steps == 3 ? buf : buf2;
+}
+
 template <int L, int PP, bool PF, bool INV, class Ld, class St>
-__device__ __forceinline__ void pencil_fft(float2 *buf, const float2 *tw, const Ld &ld, const St &st) {
+__device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const float2 *tw, const Ld &ld, const St &st) {
   using F = Fac<L>;
   using T = Tile<L, PP, PF>;
   const int t = threadIdx.x;
@@ -261,20 +268,22 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, const float2 *tw, const 
     split<PP, S::J, PF>(t, q, j);
     const bool act = t < PP * S::J;
     if (act) S::gather(j, [&](int n) { return ld(q, n); }, tw, v);
-    __syncthreads();
+    __syncthreads();  // ld may read buf; an earlier call's last step may still read it
     if (act) S::scatter(j, [&](int n, float2 x) { buf[T::at(q, n)] = x; }, v);
     __syncthreads();
   }
+  float2 *src = buf;
   if constexpr (F::steps == 3) {
     using S = Step<L, F::R2, F::R1, INV>;
     float2 v[F::R2];
     int q, j;
     split<PP, S::J, PF>(t, q, j);
-    const bool act = t < PP * S::J;
-    if (act) S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw, v);
+    if (t < PP * S::J) {
+      S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw, v);
+      S::scatter(j, [&](int n, float2 x) { buf2[T::at(q, n)] = x; }, v);
+    }
     __syncthreads();
-    if (act) S::scatter(j, [&](int n, float2 x) { buf[T::at(q, n)] = x; }, v);
-    __syncthreads();
+    src = buf2;
   }
   {
     constexpr int RL = F::steps == 3 ? F::R3 : F::R2;
@@ -282,10 +291,10 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, const float2 *tw, const 
     float2 v[RL];
     int q, j;
     split<PP, S::J, PF>(t, q, j);
-    const bool act = t < PP * S::J;
-    if (act) S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw, v);
-    __syncthreads();
-    if (act) S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v);
+    if (t < PP * S::J) {
+      S::gather(j, [&](int n) { return src[T::at(q, n)]; }, tw, v);
+      S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v);
+    }
   }
 }
 #endif
@@ -390,6 +399,7 @@ struct FArgs {
   const float2 *src[17];  // inputs per component
   float2 *dst[6];         // outputs per component
   const float2 *tw;       // W_M^t, t < M (global)
+  int *status;            // set to nonzero by a kernel whose bounded wait ran out
   int ncomp;              // components in this launch
   int mode;               // X6: 0 Hessians from B0..B2, 1 plain; YF: 0 unpad, 1 truncate; ZSRC2: 1 with pairs
   float kfac, fac;
@@ -418,14 +428,14 @@ MFX_CX int min_blocks(int threads) {
 template <int M, int P> struct XY {
   static constexpr int threads = P * Fac<M>::maxJ;
   static constexpr int minb = min_blocks(threads);
-  static constexpr size_t smem = size_t(M + Tile<M, P, true>::elems) * sizeof(float2);
+  static constexpr size_t smem = size_t(M + 2 * Tile<M, P, true>::elems) * sizeof(float2);
 };
 
 // Y3: B_o = inverse-y of fac (ky)^o phi, o < ncomp, padded in y.  grid (N, Kh/P)
 // (element offsets fit 32 bits for every supported size: N <= 1024)
 template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y3(FArgs a) {
   using D = Dims<M>;
-  float2 *tw = ff_smem(), *buf = tw + M;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
   load_tw<M>(tw, a.tw);
   const int i = blockIdx.x, kz0 = blockIdx.y * P;
   const float2 *src = a.src[0] + (unsigned(i) * D::N * D::nk + kz0);
@@ -433,7 +443,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<
   for (int o = 0; o < a.ncomp; ++o) {
     float2 *out = a.dst[o] + (unsigned(i) * M * D::Kh + kz0);
     pencil_fft<M, P, true, true>(
-        buf, tw,
+        buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int j = unpad_index(n, D::N);
           if (j < 0) return make_float2(0.f, 0.f);
@@ -455,7 +465,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<
 // grid (M, Kh/P)
 template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_x_inv(FArgs a) {
   using D = Dims<M>;
-  float2 *tw = ff_smem(), *buf = tw + M;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
   load_tw<M>(tw, a.tw);
   const int yy = blockIdx.x, kz0 = blockIdx.y * P;
   const unsigned off = unsigned(yy) * D::Kh + kz0;
@@ -466,7 +476,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<
     const float2 *src = a.src[s] + off;
     float2 *out = a.dst[c] + off;
     pencil_fft<M, P, true, true>(
-        buf, tw,
+        buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int i = unpad_index(n, D::N);
           if (i < 0) return make_float2(0.f, 0.f);
@@ -488,7 +498,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<
 // grid (M, Kh/P)
 template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_x_fwd(FArgs a) {
   using D = Dims<M>;
-  float2 *tw = ff_smem(), *buf = tw + M;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
   load_tw<M>(tw, a.tw);
   const int yy = blockIdx.x, kz0 = blockIdx.y * P;
   const unsigned off = unsigned(yy) * D::Kh + kz0;
@@ -497,7 +507,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<
     const float2 *src = a.src[c] + off;
     float2 *dst = a.dst[c] + off;
     pencil_fft<M, P, true, false>(
-        buf, tw, [&](int q, int n) { return src[unsigned(n) * M * D::Kh + q]; },
+        buf, buf2, tw, [&](int q, int n) { return src[unsigned(n) * M * D::Kh + q]; },
         [&](int q, int k, float2 v) {
           const int i = unpad_index(k, D::N);
           if (i >= 0) dst[unsigned(i) * M * D::Kh + q] = v;
@@ -514,7 +524,7 @@ template <int M, int P, int MODE>
 __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y_fwd(FArgs a) {
   using D = Dims<M>;
   using T = Tile<M, P, true>;
-  float2 *tw = ff_smem(), *buf = tw + M;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
   load_tw<M>(tw, a.tw);
   // one component per grid z: no loop whose invariants the compiler would keep live
   const int i = blockIdx.x, kz0 = blockIdx.y * P, c = blockIdx.z;
@@ -524,7 +534,7 @@ __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y_fwd(
     const float kx = float(sidx(i, D::N)) * a.kfac;
     float2 *out = dst + unsigned(i) * D::N * D::nk + kz0;
     pencil_fft<M, P, true, false>(
-        buf, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
+        buf, buf2, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
         [&](int q, int k, float2 v) {
           const int j = unpad_index(k, D::N);
           if (j < 0) return;
@@ -543,48 +553,108 @@ __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y_fwd(
   } else {
     float2 *out = dst + (unsigned(i) * M * D::Kh + kz0);
     const bool row_kept = i != D::nh;
+    float2 *mid = obuf<M>(buf, buf2);
     pencil_fft<M, P, true, false>(
-        buf, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
+        buf, buf2, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
         [&](int q, int k, float2 v) {
           const int j = unpad_index(k, D::N);
           const bool keep = row_kept && j >= 0 && j != D::nh;
-          buf[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
+          mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
         });
     __syncthreads();
     pencil_fft<M, P, true, true>(
-        buf, tw, [&](int q, int n) { return buf[T::at(q, n)]; },
+        buf, buf2, tw, [&](int q, int n) { return mid[T::at(q, n)]; },
         [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
   }
 }
 
-// Z row kernels: RW rows per CTA; NIN real inputs per row (C-space spectra,
-// kz < Kh), paired into complex pencils of G per round; NOUT real sources per
-// row written back as D-space spectra (kz < Kh).
+// ---------------------------------------------------------------------------
+// z row kernels (persistent): each CTA walks rows blockIdx.x, + gridDim.x, ...
+// RW rows at a time.  The NIN C-space input spectra of the next row group are
+// fetched into shared memory by bulk asynchronous copies (one thread issues
+// them, an mbarrier counts the bytes) while the current group is transformed,
+// so global latency stays off the FFT critical path.  Inverse z transforms
+// (fields paired into complex pencils, G per round) fill h[w][c][z]; the
+// sources are formed in place; NOUT real sources per row go through forward z
+// transforms and their kz < Kh spectra to global memory (D-space).
+// ---------------------------------------------------------------------------
+constexpr int kMbarSpins = 1 << 20;  // bounded mbarrier wait (try_wait suspends between polls)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  for (int it = 0; it < kMbarSpins; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// global -> shared bulk copy (16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
 template <int M, int RW, int G, int NIN> struct ZR {
+  using D = Dims<M>;
   static constexpr int nin_pad = NIN + (NIN & 1);
   static constexpr int threads = G * Fac<M>::maxJ;
-  static constexpr size_t smem =
-      size_t(M) * sizeof(float2) + size_t(RW) * nin_pad * M * sizeof(float) + size_t(Tile<M, G, false>::elems) * sizeof(float2);
+  static constexpr int srow = NIN * D::Kh;  // float2 per row in the stage
+  static constexpr size_t head = 32;        // two mbarriers and a status word
+  static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(2 * RW * srow) * sizeof(float2) +
+                                 size_t(RW) * nin_pad * M * sizeof(float) +
+                                 size_t(2 * Tile<M, G, false>::elems) * sizeof(float2);
   // CTAs per SM: by registers (64 each) and by shared memory (228 KB per SM)
   static constexpr int by_smem = int(233472 / (smem + 1024));
   static constexpr int minb = min_blocks(threads) < by_smem ? min_blocks(threads) : (by_smem < 1 ? 1 : by_smem);
 };
 
-// inverse z transforms of NIN C-space inputs of RW rows into h[w][c][z]
-template <int M, int RW, int G, int NIN>
-__device__ __forceinline__ void z_inverse(const FArgs &a, size_t r0, float *h, float2 *buf, const float2 *tw) {
+// issues the bulk copies of row group g (RW rows x NIN spectra) into stage
+template <int M, int RW, int NIN>
+__device__ __forceinline__ void z_fetch(const FArgs &a, size_t g, float2 *stage, uint64_t *bar) {
   using D = Dims<M>;
-  constexpr int NPI = RW * (ZR<M, RW, G, NIN>::nin_pad / 2);  // complex pencils
+  constexpr uint32_t bytes = uint32_t(D::Kh) * sizeof(float2);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the stage was last read by the generic proxy
+  mbar_expect_tx(bar, bytes * RW * NIN);
+  for (int w = 0; w < RW; ++w)
+    for (int c = 0; c < NIN; ++c)
+      bulk_g2s(stage + (w * NIN + c) * D::Kh, a.src[c] + (g * RW + w) * D::Kh, bytes, bar);
+}
+
+// inverse z transforms of the staged spectra into h[w][c][z]
+template <int M, int RW, int G, int NIN>
+__device__ __forceinline__ void z_inverse(const float2 *stage, float *h, float2 *buf, float2 *buf2, const float2 *tw) {
+  using D = Dims<M>;
   constexpr int NP = ZR<M, RW, G, NIN>::nin_pad;
+  constexpr int NPI = RW * (NP / 2);  // complex pencils
 #pragma unroll 1
   for (int g0 = 0; g0 < NPI; g0 += G) {
     pencil_fft<M, G, false, true>(
-        buf, tw,
+        buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int g = g0 + q;
           if (g >= NPI) return make_float2(0.f, 0.f);
           const int w = g / (NP / 2), c0 = 2 * (g - w * (NP / 2)), c1 = c0 + 1;
-          const size_t row = (r0 + w) * D::Kh;
           int m;
           bool conj;
           if (n < D::Kh) {
@@ -596,8 +666,9 @@ __device__ __forceinline__ void z_inverse(const FArgs &a, size_t r0, float *h, f
           } else {
             return make_float2(0.f, 0.f);
           }
-          float2 va = a.src[c0][row + m];
-          float2 vb = c1 < NIN ? a.src[c1][row + m] : make_float2(0.f, 0.f);
+          const float2 *row = stage + w * NIN * D::Kh;
+          float2 va = row[c0 * D::Kh + m];
+          float2 vb = c1 < NIN ? row[c1 * D::Kh + m] : make_float2(0.f, 0.f);
           if (m == 0) {
             va.y = 0.f;
             vb.y = 0.f;
@@ -618,16 +689,18 @@ __device__ __forceinline__ void z_inverse(const FArgs &a, size_t r0, float *h, f
 // forward z transforms of NOUT real sources per row held in h[w][o][z]
 // (o < NOUT, row stride NP) and the kz < Kh spectra written to dst[o]
 template <int M, int RW, int G0, int NP, int NOUT>
-__device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float *h, float2 *buf, const float2 *tw) {
+__device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float *h, float2 *buf, float2 *buf2,
+                                          const float2 *tw) {
   using D = Dims<M>;
-  constexpr int NR = RW * NOUT;        // real outputs
-  constexpr int NPO = (NR + 1) / 2;    // complex pencils
+  constexpr int NR = RW * NOUT;      // real outputs
+  constexpr int NPO = (NR + 1) / 2;  // complex pencils
   constexpr int G = G0 < NPO ? G0 : NPO;
   using T = Tile<M, G, false>;
+  float2 *ob = obuf<M>(buf, buf2);
 #pragma unroll 1
   for (int g0 = 0; g0 < NPO; g0 += G) {
     pencil_fft<M, G, false, false>(
-        buf, tw,
+        buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int g = g0 + q;
           if (g >= NPO) return make_float2(0.f, 0.f);
@@ -636,12 +709,12 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
           const float im = f1 < NR ? h[((f1 / NOUT) * NP + f1 % NOUT) * M + n] : 0.f;
           return make_float2(re, im);
         },
-        [&](int q, int k, float2 v) { buf[T::at(q, k)] = v; });
+        [&](int q, int k, float2 v) { ob[T::at(q, k)] = v; });
     __syncthreads();
     for (int t = threadIdx.x; t < G * D::Kh; t += blockDim.x) {
       const int q = t / D::Kh, k = t - q * D::Kh, g = g0 + q;
       if (g >= NPO) continue;
-      const float2 z = buf[T::at(q, k)], zm = buf[T::at(q, k == 0 ? 0 : M - k)];
+      const float2 z = ob[T::at(q, k)], zm = ob[T::at(q, k == 0 ? 0 : M - k)];
       float2 sa, sb;
       unpack_pair(z, zm, sa, sb);
       const int f0 = 2 * g, f1 = f0 + 1;
@@ -652,55 +725,83 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
   }
 }
 
+// the persistent row loop shared by ZSRC2 and ZSRC3; `sources(h_row, n)`
+// forms the sources of one element in place
+template <int M, int RW, int G, int NIN, int NOUT, class Src>
+__device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
+  using Z = ZR<M, RW, G, NIN>;
+  constexpr int NP = Z::nin_pad;
+  char *base = reinterpret_cast<char *>(ff_smem());
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base);
+  volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
+  float2 *tw = reinterpret_cast<float2 *>(base + Z::head);
+  float2 *stage = tw + M;  // two buffers of RW * srow
+  float *h = reinterpret_cast<float *>(stage + 2 * RW * Z::srow);
+  float2 *buf = reinterpret_cast<float2 *>(h + RW * NP * M);
+  float2 *buf2 = buf + Tile<M, G, false>::elems;
+  const size_t ngroups = size_t(M) * M / RW;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    *flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  load_tw<M>(tw, a.tw);  // includes a barrier
+  size_t g = blockIdx.x;
+  if (threadIdx.x == 0 && g < ngroups) z_fetch<M, RW, NIN>(a, g, stage, &bar[0]);
+#pragma unroll 1
+  for (uint32_t it = 0; g < ngroups; ++it, g += gridDim.x) {
+    const int b = it & 1;
+    const size_t gn = g + gridDim.x;
+    if (threadIdx.x == 0) {
+      if (gn < ngroups) z_fetch<M, RW, NIN>(a, gn, stage + (b ^ 1) * RW * Z::srow, &bar[b ^ 1]);
+      if (!mbar_wait_bounded(&bar[b], (it >> 1) & 1)) *flag = 1;
+    }
+    __syncthreads();
+    if (*flag) {
+      // the copies did not land: report, let those in flight finish (bounded), leave
+      if (threadIdx.x == 0) {
+        if (a.status) atomicExch(a.status, 1);
+        mbar_wait_bounded(&bar[b], (it >> 1) & 1);
+        if (gn < ngroups) mbar_wait_bounded(&bar[b ^ 1], ((it + 1) >> 1) & 1);
+      }
+      return;
+    }
+    z_inverse<M, RW, G, NIN>(stage + b * RW * Z::srow, h, buf, buf2, tw);
+    for (int t = threadIdx.x; t < RW * M; t += blockDim.x) {
+      const int w = t / M, n = t - w * M;
+      sources(h + size_t(w) * NP * M + n);
+    }
+    __syncthreads();
+    z_forward<M, RW, G, NP, NOUT>(a, g * RW, h, buf, buf2, tw);
+  }
+}
+
 // ZSRC2: phi1 Hessians (src[0..5], C-space) -> 2LPT source (dst[0]) and, with
 // mode 1, the five first-pair products of convolve3 (dst[1..5]).
-// grid (M*M / RW)
-template <int M, int RW, int G>
+template <int M, int RW, int G, int MODE>
 __global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads, ZR<M, RW, G, 6>::minb) k_ff_zsrc2(FArgs a) {
-  constexpr int NP = 6;
-  float2 *tw = ff_smem();
-  float *h = reinterpret_cast<float *>(tw + M);
-  float2 *buf = reinterpret_cast<float2 *>(h + RW * NP * M);
-  load_tw<M>(tw, a.tw);
-  const size_t r0 = size_t(blockIdx.x) * RW;
-  z_inverse<M, RW, G, 6>(a, r0, h, buf, tw);
-  for (int t = threadIdx.x; t < RW * M; t += blockDim.x) {
-    const int w = t / M, n = t - w * M;
-    float *hr = h + size_t(w) * NP * M + n;
+  z_rows<M, RW, G, 6, MODE ? 6 : 1>(a, [&](float *hr) {
     float v[6], s[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) v[c] = hr[c * M];
     s[0] = src_phi2(v);
-    pair_products(v, s + 1);
     hr[0] = s[0];
-    if (a.mode) {
+    if (MODE) {
+      pair_products(v, s + 1);
 #pragma unroll
       for (int c = 1; c < 6; ++c) hr[c * M] = s[c];
     }
-  }
-  __syncthreads();
-  if (a.mode)
-    z_forward<M, RW, G, NP, 6>(a, r0, h, buf, tw);
-  else
-    z_forward<M, RW, G, NP, 1>(a, r0, h, buf, tw);
+  });
 }
 
 // ZSRC3: phi1 Hessians src[0..5], phi2 Hessians src[6..11] and the truncated
 // pair products src[12..16] (C-space) -> phi3 source (dst[0]) and A3 (dst[1..3]).
-// The outputs may alias inputs: each CTA reads its rows whole before writing.
-// grid (M*M / RW)
+// The outputs may alias inputs: a row's spectra are staged before any of its
+// outputs is written.
 template <int M, int RW, int G>
 __global__ void __launch_bounds__(ZR<M, RW, G, 17>::threads, ZR<M, RW, G, 17>::minb) k_ff_zsrc3(FArgs a) {
-  constexpr int NP = ZR<M, RW, G, 17>::nin_pad;  // 18
-  float2 *tw = ff_smem();
-  float *h = reinterpret_cast<float *>(tw + M);
-  float2 *buf = reinterpret_cast<float2 *>(h + RW * NP * M);
-  load_tw<M>(tw, a.tw);
-  const size_t r0 = size_t(blockIdx.x) * RW;
-  z_inverse<M, RW, G, 17>(a, r0, h, buf, tw);
-  for (int t = threadIdx.x; t < RW * M; t += blockDim.x) {
-    const int w = t / M, n = t - w * M;
-    float *hr = h + size_t(w) * NP * M + n;
+  z_rows<M, RW, G, 17, 4>(a, [&](float *hr) {
     float p[6], q[6], T5[5], s[4];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -712,9 +813,7 @@ __global__ void __launch_bounds__(ZR<M, RW, G, 17>::threads, ZR<M, RW, G, 17>::m
     src_phi3(p, q, T5, s);
 #pragma unroll
     for (int c = 0; c < 4; ++c) hr[c * M] = s[c];
-  }
-  __syncthreads();
-  z_forward<M, RW, G, NP, 4>(a, r0, h, buf, tw);
+  });
 }
 #endif
 

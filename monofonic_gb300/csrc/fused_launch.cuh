@@ -90,23 +90,44 @@ template <int M, int P> cudaError_t ff_launch_xy(int op, const FArgs &a, cudaStr
   }
 }
 
+// persistent grid of a z-row kernel: as many CTAs as fit on the device at once
+template <class K> static unsigned ff_persistent_grid(K kernel, int threads, size_t smem, size_t groups) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1) per = 1;
+  const size_t g = size_t(nsm > 0 ? nsm : 1) * size_t(per);
+  return unsigned(g < groups ? g : groups);
+}
+
 template <int M, int RW> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStream_t s) {
   if constexpr (!ff_z_fits<M, RW>()) {
     return cudaErrorInvalidConfiguration;
   } else {
-  const unsigned grid = unsigned(size_t(M) * M / RW);
-  if (op == FF_ZSRC2) {
-    constexpr int G = ZG<M, RW, 6>::G;
-    using Z = ZR<M, RW, G, 6>;
-    MFX_FF_ALLOW_SMEM((k_ff_zsrc2<M, RW, G>));
-    k_ff_zsrc2<M, RW, G><<<grid, Z::threads, Z::smem, s>>>(a);
-  } else {
-    constexpr int G = ZG<M, RW, 17>::G;
-    using Z = ZR<M, RW, G, 17>;
-    MFX_FF_ALLOW_SMEM((k_ff_zsrc3<M, RW, G>));
-    k_ff_zsrc3<M, RW, G><<<grid, Z::threads, Z::smem, s>>>(a);
-  }
-  return cudaGetLastError();
+    const size_t groups = size_t(M) * M / RW;
+    if (op == FF_ZSRC2) {
+      constexpr int G = ZG<M, RW, 6>::G;
+      using Z = ZR<M, RW, G, 6>;
+      if (a.mode) {
+        MFX_FF_ALLOW_SMEM((k_ff_zsrc2<M, RW, G, 1>));
+        static unsigned grid = 0;  // per instance; devices of one kind
+        if (!grid) grid = ff_persistent_grid(k_ff_zsrc2<M, RW, G, 1>, Z::threads, Z::smem, groups);
+        k_ff_zsrc2<M, RW, G, 1><<<grid, Z::threads, Z::smem, s>>>(a);
+      } else {
+        MFX_FF_ALLOW_SMEM((k_ff_zsrc2<M, RW, G, 0>));
+        static unsigned grid = 0;
+        if (!grid) grid = ff_persistent_grid(k_ff_zsrc2<M, RW, G, 0>, Z::threads, Z::smem, groups);
+        k_ff_zsrc2<M, RW, G, 0><<<grid, Z::threads, Z::smem, s>>>(a);
+      }
+    } else {
+      constexpr int G = ZG<M, RW, 17>::G;
+      using Z = ZR<M, RW, G, 17>;
+      MFX_FF_ALLOW_SMEM((k_ff_zsrc3<M, RW, G>));
+      static unsigned grid = 0;
+      if (!grid) grid = ff_persistent_grid(k_ff_zsrc3<M, RW, G>, Z::threads, Z::smem, groups);
+      k_ff_zsrc3<M, RW, G><<<grid, Z::threads, Z::smem, s>>>(a);
+    }
+    return cudaGetLastError();
   }
 }
 
