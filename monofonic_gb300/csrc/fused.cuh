@@ -414,6 +414,10 @@ __device__ __forceinline__ float2 *ff_smem() {
   return reinterpret_cast<float2 *>(ff_smem4);
 }
 
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
 template <int M> __device__ __forceinline__ void load_tw(float2 *tw, const float2 *g) {
   for (int t = threadIdx.x; t < M; t += blockDim.x) tw[t] = g[t];
   __syncthreads();
@@ -425,164 +429,247 @@ MFX_CX int min_blocks(int threads) {
   return 65536 / (threads * 64) < 1 ? 1 : (65536 / (threads * 64) > 4 ? 4 : 65536 / (threads * 64));
 }
 
-template <int M, int P> struct XY {
+// ---------------------------------------------------------------------------
+// x/y passes (persistent): each CTA walks units blockIdx.x, + gridDim.x, ...
+// A unit is one tile of P adjacent kz pencils (one outer index, one kz block,
+// one input field).  The tile's input rows (P complex each, a fixed stride
+// apart in global memory) are staged into shared memory with cp.async while
+// the previous unit is transformed, and the first FFT step gathers from the
+// stage.  Element offsets fit 32 bits for every supported size (N <= 1024).
+// ---------------------------------------------------------------------------
+template <int CHUNK> __device__ __forceinline__ void cp_async(void *dst, const void *src) {
+  if constexpr (CHUNK == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// stages ROWS rows of P complex (row r at src + r * stride) as stage[r * P + q]
+template <int P, int ROWS, int CHUNK>
+__device__ __forceinline__ void stage_rows(float2 *stage, const float2 *src, unsigned stride) {
+  constexpr int per_row = P * 8 / CHUNK, E = CHUNK / 8;
+  for (int t = threadIdx.x; t < ROWS * per_row; t += blockDim.x) {
+    const int r = t / per_row, c = t - r * per_row;
+    cp_async<CHUNK>(stage + r * P + c * E, src + r * stride + c * E);
+  }
+}
+
+template <int M, int P, int ROWS> struct XY {
   static constexpr int threads = P * Fac<M>::maxJ;
   static constexpr int minb = min_blocks(threads);
-  static constexpr size_t smem = size_t(M + 2 * Tile<M, P, true>::elems) * sizeof(float2);
+  static constexpr size_t smem = size_t(M + 2 * Tile<M, P, true>::elems + 2 * ROWS * P) * sizeof(float2);
 };
 
-// Y3: B_o = inverse-y of fac (ky)^o phi, o < ncomp, padded in y.  grid (N, Kh/P)
-// (element offsets fit 32 bits for every supported size: N <= 1024)
-template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y3(FArgs a) {
-  using D = Dims<M>;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
-  load_tw<M>(tw, a.tw);
-  const int i = blockIdx.x, kz0 = blockIdx.y * P;
-  const float2 *src = a.src[0] + (unsigned(i) * D::N * D::nk + kz0);
+// The persistent unit loop: fetch(u, stage) issues unit u's copies,
+// work(u, stage) transforms it.
+template <class Fetch, class Work>
+__device__ __forceinline__ void xy_units(unsigned units, unsigned stage_elems, float2 *stage0, const Fetch &fetch,
+                                         const Work &work) {
+  unsigned u = blockIdx.x;
+  if (u < units) fetch(u, stage0);
+  cp_async_commit();
 #pragma unroll 1
-  for (int o = 0; o < a.ncomp; ++o) {
-    float2 *out = a.dst[o] + (unsigned(i) * M * D::Kh + kz0);
-    pencil_fft<M, P, true, true>(
-        buf, buf2, tw,
-        [&](int q, int n) -> float2 {
-          const int j = unpad_index(n, D::N);
-          if (j < 0) return make_float2(0.f, 0.f);
-          const float2 v = src[unsigned(j) * D::nk + q];
-          float f = a.fac;
-          if (o > 0) {
-            const float gy = (j != D::nh) ? float(sidx(j, D::N)) * a.kfac : 0.f;
-            f *= (o == 1) ? gy : gy * gy;
-          }
-          return make_float2(v.x * f, v.y * f);
-        },
-        [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+  for (unsigned it = 0; u < units; ++it, u += gridDim.x) {
+    float2 *cur = stage0 + (it & 1) * stage_elems, *nxt = stage0 + ((it & 1) ^ 1) * stage_elems;
+    const unsigned un = u + gridDim.x;
+    if (un < units) fetch(un, nxt);
+    cp_async_commit();
+    cp_async_wait_prev();
+    __syncthreads();
+    work(u, cur);
+    __syncthreads();  // the stage just read is the next fetch's target
   }
+}
+
+// Y3: B_o = inverse-y of fac (ky)^o phi, o < 3, padded in y.
+// units: (i < N) x (Kh/P kz blocks); input rows j < N of phi (8-byte aligned)
+template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::threads, XY<M, P, 2 * M / 3>::minb)
+    k_ff_y3(FArgs a) {
+  using D = Dims<M>;
+  constexpr int ROWS = D::N, KB = D::Kh / P;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems, *stage = buf2 + Tile<M, P, true>::elems;
+  load_tw<M>(tw, a.tw);
+  xy_units(
+      unsigned(D::N * KB), ROWS * P, stage,
+      [&](unsigned u, float2 *st) {
+        const unsigned i = u / KB, kz0 = (u % KB) * P;
+        stage_rows<P, ROWS, 8>(st, a.src[0] + (i * D::N * D::nk + kz0), D::nk);
+      },
+      [&](unsigned u, const float2 *st) {
+        const unsigned i = u / KB, kz0 = (u % KB) * P;
+#pragma unroll 1
+        for (int o = 0; o < 3; ++o) {
+          float2 *out = a.dst[o] + (i * M * D::Kh + kz0);
+          pencil_fft<M, P, true, true>(
+              buf, buf2, tw,
+              [&](int q, int n) -> float2 {
+                const int j = unpad_index(n, D::N);
+                if (j < 0) return make_float2(0.f, 0.f);
+                const float2 v = st[j * P + q];
+                float f = a.fac;
+                if (o > 0) {
+                  const float gy = (j != D::nh) ? float(sidx(j, D::N)) * a.kfac : 0.f;
+                  f *= (o == 1) ? gy : gy * gy;
+                }
+                return make_float2(v.x * f, v.y * f);
+              },
+              [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+        }
+      });
 }
 
 // X inverse into C-space.  mode 0: the six Hessians from B0 = Y(phi),
-// B1 = Y(ky phi), B2 = Y(ky^2 phi) (slot order xx yy zz xy xz yz, factor
-// -k_a k_b split into its x and z parts); mode 1: component c of src[c].
-// grid (M, Kh/P)
-template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_x_inv(FArgs a) {
+// B1 = Y(ky phi), B2 = Y(ky^2 phi) (slot order xx yy zz xy xz yz; the factor
+// -k_a k_b splits into its x and z parts): a unit stages one B tile and makes
+// every Hessian that derives from it (B0: xx zz xz, B1: xy yz, B2: yy).
+// mode 1: component c of src[c] (units also run over c < ncomp).
+// units: (y < M) x (Kh/P kz blocks) x (3 sources | ncomp); input rows i < N
+template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::threads, XY<M, P, 2 * M / 3>::minb)
+    k_ff_x_inv(FArgs a) {
   using D = Dims<M>;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
+  constexpr int ROWS = D::N, KB = D::Kh / P;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems, *stage = buf2 + Tile<M, P, true>::elems;
   load_tw<M>(tw, a.tw);
-  const int yy = blockIdx.x, kz0 = blockIdx.y * P;
-  const unsigned off = unsigned(yy) * D::Kh + kz0;
+  const unsigned nsrc = a.mode ? unsigned(a.ncomp) : 3u;
+  xy_units(
+      unsigned(M * KB) * nsrc, ROWS * P, stage,
+      [&](unsigned u, float2 *st) {
+        const unsigned s = u % nsrc, t = u / nsrc, yy = t / KB, kz0 = (t % KB) * P;
+        stage_rows<P, ROWS, 16>(st, a.src[s] + (yy * D::Kh + kz0), unsigned(M * D::Kh));
+      },
+      [&](unsigned u, const float2 *st) {
+        const unsigned s = u % nsrc, t = u / nsrc, yy = t / KB, kz0 = (t % KB) * P;
+        const unsigned off = yy * D::Kh + kz0;
+        // components made from source s: mode 0: B0 -> xx zz xz, B1 -> xy yz, B2 -> yy
+        const int ncs = a.mode ? 1 : (s == 0 ? 3 : (s == 1 ? 2 : 1));
 #pragma unroll 1
-  for (int c = 0; c < a.ncomp; ++c) {
-    // c: 0 xx <- -gx^2 B0, 1 yy <- -B2, 2 zz <- -gz^2 B0, 3 xy <- -gx B1, 4 xz <- -gx gz B0, 5 yz <- -gz B1
-    const int s = a.mode ? c : (c == 1 ? 2 : ((c == 3 || c == 5) ? 1 : 0));
-    const float2 *src = a.src[s] + off;
-    float2 *out = a.dst[c] + off;
-    pencil_fft<M, P, true, true>(
-        buf, buf2, tw,
-        [&](int q, int n) -> float2 {
-          const int i = unpad_index(n, D::N);
-          if (i < 0) return make_float2(0.f, 0.f);
-          float2 v = src[unsigned(i) * M * D::Kh + q];
-          if (a.mode == 0) {
-            const float gx = (i != D::nh) ? float(sidx(i, D::N)) * a.kfac : 0.f;
-            const float gz = float(kz0 + q) * a.kfac;
-            const float f = c == 0 ? -gx * gx : c == 1 ? -1.f : c == 2 ? -gz * gz : c == 3 ? -gx : c == 4 ? -gx * gz : -gz;
-            v.x *= f;
-            v.y *= f;
-          }
-          return v;
-        },
-        [&](int q, int n, float2 v) { out[unsigned(n) * M * D::Kh + q] = v; });
-  }
+        for (int k = 0; k < ncs; ++k) {
+          const int c = a.mode ? int(s) : (s == 0 ? 2 * k : (s == 1 ? (k == 0 ? 3 : 5) : 1));
+          float2 *out = a.dst[c] + off;
+          pencil_fft<M, P, true, true>(
+              buf, buf2, tw,
+              [&](int q, int n) -> float2 {
+                const int i = unpad_index(n, D::N);
+                if (i < 0) return make_float2(0.f, 0.f);
+                float2 v = st[i * P + q];
+                if (a.mode == 0) {
+                  const float gx = (i != D::nh) ? float(sidx(i, D::N)) * a.kfac : 0.f;
+                  const float gz = float(kz0 + q) * a.kfac;
+                  const float f = c == 0 ? -gx * gx : c == 1 ? -1.f : c == 2 ? -gz * gz : c == 3 ? -gx : c == 4 ? -gx * gz : -gz;
+                  v.x *= f;
+                  v.y *= f;
+                }
+                return v;
+              },
+              [&](int q, int n, float2 v) { out[unsigned(n) * M * D::Kh + q] = v; });
+        }
+      });
 }
 
 // X forward: C-space layout -> B-space layout, keeping the N-grid kx.
-// grid (M, Kh/P)
-template <int M, int P> __global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_x_fwd(FArgs a) {
+// units: (y < M) x (Kh/P kz blocks) x (c < ncomp); input rows n < M
+template <int M, int P> __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_x_fwd(FArgs a) {
   using D = Dims<M>;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
+  constexpr int ROWS = M, KB = D::Kh / P;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems, *stage = buf2 + Tile<M, P, true>::elems;
   load_tw<M>(tw, a.tw);
-  const int yy = blockIdx.x, kz0 = blockIdx.y * P;
-  const unsigned off = unsigned(yy) * D::Kh + kz0;
-#pragma unroll 1
-  for (int c = 0; c < a.ncomp; ++c) {
-    const float2 *src = a.src[c] + off;
-    float2 *dst = a.dst[c] + off;
-    pencil_fft<M, P, true, false>(
-        buf, buf2, tw, [&](int q, int n) { return src[unsigned(n) * M * D::Kh + q]; },
-        [&](int q, int k, float2 v) {
-          const int i = unpad_index(k, D::N);
-          if (i >= 0) dst[unsigned(i) * M * D::Kh + q] = v;
-        });
-  }
+  const unsigned nc = unsigned(a.ncomp);
+  xy_units(
+      unsigned(M * KB) * nc, ROWS * P, stage,
+      [&](unsigned u, float2 *st) {
+        const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
+        stage_rows<P, ROWS, 16>(st, a.src[c] + (yy * D::Kh + kz0), unsigned(M * D::Kh));
+      },
+      [&](unsigned u, const float2 *st) {
+        const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
+        float2 *dst = a.dst[c] + (yy * D::Kh + kz0);
+        pencil_fft<M, P, true, false>(
+            buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
+            [&](int q, int k, float2 v) {
+              const int i = unpad_index(k, D::N);
+              if (i >= 0) dst[unsigned(i) * M * D::Kh + q] = v;
+            });
+      });
 }
 
 // Y forward.  MODE 0: keep the N-grid ky, zero every Nyquist index and the
 // mean, scale by fac / -k^2 -> N-grid k-space (kz = N/2 plane zeroed);
 // MODE 1: truncation of a convolve3 pair (zero outside the N-grid modes and on
-// Nyquist, scale by fac) and inverse y transform -> B-space (may be in place).
-// grid (N, Kh/P, ncomp)
+// Nyquist, scale by fac) and inverse y transform -> B-space (may be in place:
+// a unit's tile is staged whole before any of its outputs is written, and no
+// other unit touches it).
+// units: (i < N) x (Kh/P kz blocks) x (c < ncomp); input rows n < M
 template <int M, int P, int MODE>
-__global__ void __launch_bounds__(XY<M, P>::threads, XY<M, P>::minb) k_ff_y_fwd(FArgs a) {
+__global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_y_fwd(FArgs a) {
   using D = Dims<M>;
   using T = Tile<M, P, true>;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems;
+  constexpr int ROWS = M, KB = D::Kh / P;
+  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + T::elems, *stage = buf2 + T::elems;
   load_tw<M>(tw, a.tw);
-  // one component per grid z: no loop whose invariants the compiler would keep live
-  const int i = blockIdx.x, kz0 = blockIdx.y * P, c = blockIdx.z;
-  const float2 *src = a.src[c] + (unsigned(i) * M * D::Kh + kz0);
-  float2 *dst = a.dst[c];
-  if constexpr (MODE == 0) {
-    const float kx = float(sidx(i, D::N)) * a.kfac;
-    float2 *out = dst + unsigned(i) * D::N * D::nk + kz0;
-    pencil_fft<M, P, true, false>(
-        buf, buf2, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
-        [&](int q, int k, float2 v) {
-          const int j = unpad_index(k, D::N);
-          if (j < 0) return;
-          const int kz = kz0 + q;
-          float2 r = make_float2(0.f, 0.f);
-          if (i != D::nh && j != D::nh && (i | j | kz) != 0) {
-            const float ky = float(sidx(j, D::N)) * a.kfac, kk = float(kz) * a.kfac;
-            const float f = -a.fac * __frcp_rn(kx * kx + ky * ky + kk * kk);
-            r = make_float2(v.x * f, v.y * f);
-          }
-          out[unsigned(j) * D::nk + q] = r;
-        });
-    if (blockIdx.y == 0)
-      for (int j = threadIdx.x; j < D::N; j += blockDim.x)
-        dst[(unsigned(i) * D::N + j) * D::nk + D::nh] = make_float2(0.f, 0.f);
-  } else {
-    float2 *out = dst + (unsigned(i) * M * D::Kh + kz0);
-    const bool row_kept = i != D::nh;
-    float2 *mid = obuf<M>(buf, buf2);
-    pencil_fft<M, P, true, false>(
-        buf, buf2, tw, [&](int q, int n) { return src[unsigned(n) * D::Kh + q]; },
-        [&](int q, int k, float2 v) {
-          const int j = unpad_index(k, D::N);
-          const bool keep = row_kept && j >= 0 && j != D::nh;
-          mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
-        });
-    __syncthreads();
-    pencil_fft<M, P, true, true>(
-        buf, buf2, tw, [&](int q, int n) { return mid[T::at(q, n)]; },
-        [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
-  }
+  const unsigned nc = unsigned(a.ncomp);
+  xy_units(
+      unsigned(D::N * KB) * nc, ROWS * P, stage,
+      [&](unsigned u, float2 *st) {
+        const unsigned c = u % nc, t = u / nc, i = t / KB, kz0 = (t % KB) * P;
+        stage_rows<P, ROWS, 16>(st, a.src[c] + (i * M * D::Kh + kz0), unsigned(D::Kh));
+      },
+      [&](unsigned u, const float2 *st) {
+        const unsigned c = u % nc, t = u / nc, i = t / KB, kz0 = (t % KB) * P;
+        float2 *dst = a.dst[c];
+        if constexpr (MODE == 0) {
+          const float kx = float(sidx(int(i), D::N)) * a.kfac;
+          float2 *out = dst + i * D::N * D::nk + kz0;
+          pencil_fft<M, P, true, false>(
+              buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
+              [&](int q, int k, float2 v) {
+                const int j = unpad_index(k, D::N);
+                if (j < 0) return;
+                const int kz = int(kz0) + q;
+                float2 r = make_float2(0.f, 0.f);
+                if (int(i) != D::nh && j != D::nh && (int(i) | j | kz) != 0) {
+                  const float ky = float(sidx(j, D::N)) * a.kfac, kk = float(kz) * a.kfac;
+                  const float f = -a.fac * __frcp_rn(kx * kx + ky * ky + kk * kk);
+                  r = make_float2(v.x * f, v.y * f);
+                }
+                out[unsigned(j) * D::nk + q] = r;
+              });
+          if (kz0 == 0)
+            for (int j = threadIdx.x; j < D::N; j += blockDim.x)
+              dst[(i * D::N + j) * D::nk + D::nh] = make_float2(0.f, 0.f);
+        } else {
+          float2 *out = dst + (i * M * D::Kh + kz0);
+          const bool row_kept = int(i) != D::nh;
+          float2 *mid = obuf<M>(buf, buf2);
+          pencil_fft<M, P, true, false>(
+              buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
+              [&](int q, int k, float2 v) {
+                const int j = unpad_index(k, D::N);
+                const bool keep = row_kept && j >= 0 && j != D::nh;
+                mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
+              });
+          __syncthreads();
+          pencil_fft<M, P, true, true>(
+              buf, buf2, tw, [&](int q, int n) { return mid[T::at(q, n)]; },
+              [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+        }
+      });
 }
 
 // ---------------------------------------------------------------------------
 // z row kernels (persistent): each CTA walks rows blockIdx.x, + gridDim.x, ...
 // RW rows at a time.  The NIN C-space input spectra of the next row group are
 // fetched into shared memory by bulk asynchronous copies (one thread issues
-// them, an mbarrier counts the bytes) while the current group is transformed,
-// so global latency stays off the FFT critical path.  Inverse z transforms
+// them, an mbarrier counts the bytes) while the current group's sources and
+// forward transforms run, so global latency stays off the FFT critical path
+// (one stage only: shared memory is what bounds the CTAs per SM).  Inverse z transforms
 // (fields paired into complex pencils, G per round) fill h[w][c][z]; the
 // sources are formed in place; NOUT real sources per row go through forward z
 // transforms and their kz < Kh spectra to global memory (D-space).
 // ---------------------------------------------------------------------------
 constexpr int kMbarSpins = 1 << 20;  // bounded mbarrier wait (try_wait suspends between polls)
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
@@ -621,7 +708,7 @@ template <int M, int RW, int G, int NIN> struct ZR {
   static constexpr int threads = G * Fac<M>::maxJ;
   static constexpr int srow = NIN * D::Kh;  // float2 per row in the stage
   static constexpr size_t head = 32;        // two mbarriers and a status word
-  static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(2 * RW * srow) * sizeof(float2) +
+  static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(RW * srow) * sizeof(float2) +
                                  size_t(RW) * nin_pad * M * sizeof(float) +
                                  size_t(2 * Tile<M, G, false>::elems) * sizeof(float2);
   // CTAs per SM: by registers (64 each) and by shared memory (228 KB per SM)
@@ -725,8 +812,10 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
   }
 }
 
-// the persistent row loop shared by ZSRC2 and ZSRC3; `sources(h_row, n)`
-// forms the sources of one element in place
+// the persistent row loop shared by ZSRC2 and ZSRC3; `sources(h_row)` forms
+// the sources of one element in place.  One stage: the next group's copies are
+// issued as soon as the inverse transforms have read the current one, and
+// land while the sources and the forward transforms run.
 template <int M, int RW, int G, int NIN, int NOUT, class Src>
 __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
   using Z = ZR<M, RW, G, NIN>;
@@ -735,39 +824,34 @@ __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
   uint64_t *bar = reinterpret_cast<uint64_t *>(base);
   volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
   float2 *tw = reinterpret_cast<float2 *>(base + Z::head);
-  float2 *stage = tw + M;  // two buffers of RW * srow
-  float *h = reinterpret_cast<float *>(stage + 2 * RW * Z::srow);
+  float2 *stage = tw + M;  // RW * srow
+  float *h = reinterpret_cast<float *>(stage + RW * Z::srow);
   float2 *buf = reinterpret_cast<float2 *>(h + RW * NP * M);
   float2 *buf2 = buf + Tile<M, G, false>::elems;
   const size_t ngroups = size_t(M) * M / RW;
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    mbar_init(bar, 1);
     *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   load_tw<M>(tw, a.tw);  // includes a barrier
   size_t g = blockIdx.x;
-  if (threadIdx.x == 0 && g < ngroups) z_fetch<M, RW, NIN>(a, g, stage, &bar[0]);
+  if (threadIdx.x == 0 && g < ngroups) z_fetch<M, RW, NIN>(a, g, stage, bar);
 #pragma unroll 1
   for (uint32_t it = 0; g < ngroups; ++it, g += gridDim.x) {
-    const int b = it & 1;
     const size_t gn = g + gridDim.x;
-    if (threadIdx.x == 0) {
-      if (gn < ngroups) z_fetch<M, RW, NIN>(a, gn, stage + (b ^ 1) * RW * Z::srow, &bar[b ^ 1]);
-      if (!mbar_wait_bounded(&bar[b], (it >> 1) & 1)) *flag = 1;
-    }
+    if (threadIdx.x == 0 && !mbar_wait_bounded(bar, it & 1)) *flag = 1;
     __syncthreads();
     if (*flag) {
-      // the copies did not land: report, let those in flight finish (bounded), leave
+      // the copies did not land: report, let them finish (bounded), leave
       if (threadIdx.x == 0) {
         if (a.status) atomicExch(a.status, 1);
-        mbar_wait_bounded(&bar[b], (it >> 1) & 1);
-        if (gn < ngroups) mbar_wait_bounded(&bar[b ^ 1], ((it + 1) >> 1) & 1);
+        mbar_wait_bounded(bar, it & 1);
       }
       return;
     }
-    z_inverse<M, RW, G, NIN>(stage + b * RW * Z::srow, h, buf, buf2, tw);
+    z_inverse<M, RW, G, NIN>(stage, h, buf, buf2, tw);  // ends with a barrier: the stage is free
+    if (threadIdx.x == 0 && gn < ngroups) z_fetch<M, RW, NIN>(a, gn, stage, bar);
     for (int t = threadIdx.x; t < RW * M; t += blockDim.x) {
       const int w = t / M, n = t - w * M;
       sources(h + size_t(w) * NP * M + n);

@@ -38,7 +38,7 @@ template <int M> bool ff_valid_m(int op, int p) {
   if (op == FF_ZSRC2 || op == FF_ZSRC3) return (p == 1 && ff_z_fits<M, 1>()) || (p == 2 && ff_z_fits<M, 2>());
   if (op < 0 || op >= FF_NOPS) return false;
   return (p == 4 || p == 8 || p == 16) && Kh % p == 0 && p * Fac<M>::maxJ <= 1024 &&
-         (size_t(M) + size_t(M) * p) * sizeof(float2) <= kFFSmemMax;
+         (size_t(M) + 4 * size_t(M) * p) * sizeof(float2) <= kFFSmemMax;
 }
 
 // lets a kernel instance use up to 227 KB of dynamic shared memory; the
@@ -54,50 +54,56 @@ template <int M> bool ff_valid_m(int op, int p) {
     }                                                                                           \
   } while (0)
 
+// persistent grid: as many CTAs as fit on the device at once, at most `units`
+template <class K> static unsigned ff_persistent_grid(K kernel, int threads, size_t smem, size_t units) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1) per = 1;
+  const size_t g = size_t(nsm > 0 ? nsm : 1) * size_t(per);
+  return unsigned(g < units ? g : units);
+}
+
+// launches a persistent kernel instance; the grid is computed once per
+// instance (the devices of one engine are of one kind)
+#define MFX_FF_PERSISTENT(kernel, threads, smem, units, stream, args)                   \
+  do {                                                                              \
+    MFX_FF_ALLOW_SMEM(kernel);                                                      \
+    static unsigned grid_ = 0;                                                      \
+    if (!grid_) grid_ = ff_persistent_grid(kernel, threads, smem, size_t(1) << 40); \
+    const unsigned g_ = grid_ < (units) ? grid_ : unsigned(units);                   \
+    kernel<<<g_, threads, smem, stream>>>(args);                                    \
+  } while (0)
+
 template <int M, int P> cudaError_t ff_launch_xy(int op, const FArgs &a, cudaStream_t s) {
-  if constexpr (P * Fac<M>::maxJ > 1024 || (M / 3) % P != 0) {
+  if constexpr (P * Fac<M>::maxJ > 1024 || (M / 3) % P != 0 || XY<M, P, M>::smem > kFFSmemMax) {
     return cudaErrorInvalidConfiguration;
   } else {
-    constexpr int N = 2 * M / 3, Kh = M / 3;
-    using X = XY<M, P>;
-    const dim3 gy(N, Kh / P), gx(M, Kh / P), gyc(N, Kh / P, a.ncomp);
+    constexpr int N = 2 * M / 3, KB = (M / 3) / P;
+    using XN = XY<M, P, N>;
+    using XM = XY<M, P, M>;
+    const size_t nc = size_t(a.ncomp > 0 ? a.ncomp : 1);
     switch (op) {
       case FF_Y3:
-        MFX_FF_ALLOW_SMEM((k_ff_y3<M, P>));
-        k_ff_y3<M, P><<<gy, X::threads, X::smem, s>>>(a);
+        MFX_FF_PERSISTENT((k_ff_y3<M, P>), XN::threads, XN::smem, size_t(N) * KB, s, a);
         break;
       case FF_XINV:
-        MFX_FF_ALLOW_SMEM((k_ff_x_inv<M, P>));
-        k_ff_x_inv<M, P><<<gx, X::threads, X::smem, s>>>(a);
+        MFX_FF_PERSISTENT((k_ff_x_inv<M, P>), XN::threads, XN::smem, size_t(M) * KB * (a.mode ? nc : 3), s, a);
         break;
       case FF_XFWD:
-        MFX_FF_ALLOW_SMEM((k_ff_x_fwd<M, P>));
-        k_ff_x_fwd<M, P><<<gx, X::threads, X::smem, s>>>(a);
+        MFX_FF_PERSISTENT((k_ff_x_fwd<M, P>), XM::threads, XM::smem, size_t(M) * KB * nc, s, a);
         break;
       case FF_YFWD:
-        if (a.mode == 0) {
-          MFX_FF_ALLOW_SMEM((k_ff_y_fwd<M, P, 0>));
-          k_ff_y_fwd<M, P, 0><<<gyc, X::threads, X::smem, s>>>(a);
-        } else {
-          MFX_FF_ALLOW_SMEM((k_ff_y_fwd<M, P, 1>));
-          k_ff_y_fwd<M, P, 1><<<gyc, X::threads, X::smem, s>>>(a);
-        }
+        if (a.mode == 0)
+          MFX_FF_PERSISTENT((k_ff_y_fwd<M, P, 0>), XM::threads, XM::smem, size_t(N) * KB * nc, s, a);
+        else
+          MFX_FF_PERSISTENT((k_ff_y_fwd<M, P, 1>), XM::threads, XM::smem, size_t(N) * KB * nc, s, a);
         break;
       default:
         return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
   }
-}
-
-// persistent grid of a z-row kernel: as many CTAs as fit on the device at once
-template <class K> static unsigned ff_persistent_grid(K kernel, int threads, size_t smem, size_t groups) {
-  int dev = 0, nsm = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1) per = 1;
-  const size_t g = size_t(nsm > 0 ? nsm : 1) * size_t(per);
-  return unsigned(g < groups ? g : groups);
 }
 
 template <int M, int RW> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStream_t s) {
@@ -108,24 +114,14 @@ template <int M, int RW> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStr
     if (op == FF_ZSRC2) {
       constexpr int G = ZG<M, RW, 6>::G;
       using Z = ZR<M, RW, G, 6>;
-      if (a.mode) {
-        MFX_FF_ALLOW_SMEM((k_ff_zsrc2<M, RW, G, 1>));
-        static unsigned grid = 0;  // per instance; devices of one kind
-        if (!grid) grid = ff_persistent_grid(k_ff_zsrc2<M, RW, G, 1>, Z::threads, Z::smem, groups);
-        k_ff_zsrc2<M, RW, G, 1><<<grid, Z::threads, Z::smem, s>>>(a);
-      } else {
-        MFX_FF_ALLOW_SMEM((k_ff_zsrc2<M, RW, G, 0>));
-        static unsigned grid = 0;
-        if (!grid) grid = ff_persistent_grid(k_ff_zsrc2<M, RW, G, 0>, Z::threads, Z::smem, groups);
-        k_ff_zsrc2<M, RW, G, 0><<<grid, Z::threads, Z::smem, s>>>(a);
-      }
+      if (a.mode)
+        MFX_FF_PERSISTENT((k_ff_zsrc2<M, RW, G, 1>), Z::threads, Z::smem, groups, s, a);
+      else
+        MFX_FF_PERSISTENT((k_ff_zsrc2<M, RW, G, 0>), Z::threads, Z::smem, groups, s, a);
     } else {
       constexpr int G = ZG<M, RW, 17>::G;
       using Z = ZR<M, RW, G, 17>;
-      MFX_FF_ALLOW_SMEM((k_ff_zsrc3<M, RW, G>));
-      static unsigned grid = 0;
-      if (!grid) grid = ff_persistent_grid(k_ff_zsrc3<M, RW, G>, Z::threads, Z::smem, groups);
-      k_ff_zsrc3<M, RW, G><<<grid, Z::threads, Z::smem, s>>>(a);
+      MFX_FF_PERSISTENT((k_ff_zsrc3<M, RW, G>), Z::threads, Z::smem, groups, s, a);
     }
     return cudaGetLastError();
   }
