@@ -184,7 +184,13 @@ def run_ours(args):
                   plt_table=hp, fixing=inp["fix"], lunit=inp["lunit"], vunit=inp["vunit"], pos64=pos64,
                   vel64=vel64, id64=True)
     npart = job.num_particles
-    tiles = job.autotune() if prec == mfx.FP32C else None  # pencil tiles of the fused transforms (untimed)
+    tiles = None
+    if prec == mfx.FP32C:
+        if args.tiles:  # fixed pencil tiles (profiling runs), else the autotuner's (untimed)
+            tiles = tuple(int(x) for x in args.tiles.split(","))
+            job.set_tiles(*tiles)
+        else:
+            tiles = job.autotune()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
 
     def barrier():
@@ -216,6 +222,9 @@ def run_ours(args):
     job.set_profiling(False)
     ms_step, value = replica_throughput(float(np.mean(dev_ms)), npart, device="cuda")
 
+    if args.no_e2e:  # profiling runs: the device-timed steps only
+        job.close()
+        return None, eng, inp, plt_tab
     # ---- e2e through the C ABI with host buffers ----
     # particles come back in chunks of at most 128M (a bounded pinned buffer),
     # the way an output plugin drains them
@@ -643,6 +652,8 @@ def main():
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end pass and the report")
+    ap.add_argument("--tiles", default="", help="fused-transform tiles 'PXY,PZ' instead of the autotuner's")
     args = ap.parse_args()
     (ROOT / "gpurun_out").mkdir(exist_ok=True)
     if args.impl == "reference":
@@ -660,7 +671,9 @@ def main():
         return
     out, eng, inp, plt_tab = run_ours(args)
     rank, world, _ = dist_env()
-    if rank == 0:
+    if out is None:  # --no-e2e profiling run
+        print(json.dumps({"profiling_run": True, "workload": args.workload}))
+    elif rank == 0:
         if not args.no_fp64 and args.precision == "fp32c":
             out.update(fp64_and_error(args, eng, inp, plt_tab, out))
         if not args.no_cpu_baseline and world == 1:

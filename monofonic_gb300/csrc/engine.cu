@@ -104,6 +104,8 @@ struct Plan {
   bool valid = false;
   int n = 0;
   bool fp64 = false, r2c = false;
+  int batch = 1;            // transforms per execution
+  long long dist_bytes = 0; // distance between consecutive transforms' buffers
 };
 
 struct mfx_engine {
@@ -281,19 +283,27 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
 // ---------------------------------------------------------------------------
 // cuFFT plans (in-place, padded rows as in the reference's Grid_FFT)
 // ---------------------------------------------------------------------------
-static int make_plan(Plan &p, int n, bool fp64, bool r2c) {
+// batch > 1: `batch` in-place transforms whose buffers lie dist_bytes apart
+static int make_plan(Plan &p, int n, bool fp64, bool r2c, int batch = 1, long long dist_bytes = 0) {
   CF(cufftCreate(&p.h));
   CF(cufftSetAutoAllocation(p.h, 0));
   long long dims[3] = {n, n, n};
   long long rembed[3] = {n, n, n + 2};
   long long cembed[3] = {n, n, n / 2 + 1};
+  const long long rs = fp64 ? 8 : 4;
   long long rdist = (long long)n * n * (n + 2), cdist = (long long)n * n * (n / 2 + 1);
+  if (batch > 1) {
+    rdist = dist_bytes / rs;
+    cdist = dist_bytes / (2 * rs);
+  }
   cufftType t = fp64 ? (r2c ? CUFFT_D2Z : CUFFT_Z2D) : (r2c ? CUFFT_R2C : CUFFT_C2R);
   size_t ws = 0;
   if (r2c)
-    CF(cufftMakePlanMany64(p.h, 3, dims, rembed, 1, rdist, cembed, 1, cdist, t, 1, &ws));
+    CF(cufftMakePlanMany64(p.h, 3, dims, rembed, 1, rdist, cembed, 1, cdist, t, batch, &ws));
   else
-    CF(cufftMakePlanMany64(p.h, 3, dims, cembed, 1, cdist, rembed, 1, rdist, t, 1, &ws));
+    CF(cufftMakePlanMany64(p.h, 3, dims, cembed, 1, cdist, rembed, 1, rdist, t, batch, &ws));
+  p.batch = batch;
+  p.dist_bytes = dist_bytes;
   p.work = ws;
   p.valid = true;
   return MFX_OK;
@@ -304,19 +314,20 @@ static void destroy_plan(Plan &p) {
   p.valid = false;
 }
 
-static int acquire_plan(mfx_engine *eng, Plan &p, int n, bool fp64, bool r2c) {
+static int acquire_plan(mfx_engine *eng, Plan &p, int n, bool fp64, bool r2c, int batch = 1,
+                        long long dist_bytes = 0) {
   {
     std::lock_guard<std::mutex> lk(eng->mu);
     for (size_t q = 0; q < eng->plan_pool.size(); ++q) {
       const Plan &c = eng->plan_pool[q];
-      if (c.n == n && c.fp64 == fp64 && c.r2c == r2c) {
+      if (c.n == n && c.fp64 == fp64 && c.r2c == r2c && c.batch == batch && c.dist_bytes == dist_bytes) {
         p = c;
         eng->plan_pool.erase(eng->plan_pool.begin() + q);
         return MFX_OK;
       }
     }
   }
-  TRY(make_plan(p, n, fp64, r2c));
+  TRY(make_plan(p, n, fp64, r2c, batch, dist_bytes));
   p.n = n;
   p.fp64 = fp64;
   p.r2c = r2c;
@@ -349,7 +360,7 @@ static int exec_fft(mfx_job *j, Plan &p, void *buf, bool r2c) {
   j->fft_execs++;
   const bool m = (&p != &j->n_c2r);
   kend_prof(j, m ? (r2c ? "cufft_r2c_M" : "cufft_c2r_M") : "cufft_c2r_N",
-            2.0 * double(m ? j->m_field_bytes : j->n_field_bytes));
+            2.0 * double(m ? j->m_field_bytes : j->n_field_bytes) * p.batch);
   return MFX_OK;
 }
 
@@ -716,7 +727,7 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
     else k_assemble<R, false><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(a);
     KEND(j, "assemble", ((order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) + 6.0 * g) * j->n_field_bytes);
     for (int s = 0; s < g; ++s) {
-      for (int q = 0; q < 6; ++q) TRY(exec_fft(j, j->n_c2r, j->asmbuf[s * 6 + q], false));
+      TRY(exec_fft(j, j->n_c2r, j->asmbuf[s * 6], false));  // the six components (batched)
       PartArgs p{};
       for (int q = 0; q < 6; ++q) p.f[q] = j->asmbuf[s * 6 + q];
       p.pos = j->pos;
@@ -929,7 +940,10 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     work = std::max(work, std::max(j->m_r2c.work, j->m_c2r.work));
   }
   if (d->want_particles) {
-    if ((rc = acquire_plan(eng, j->n_c2r, j->N, j->fp64, false)) != MFX_OK) return fail(rc);
+    // the six assembled components of a sub-lattice lie one padded field apart:
+    // one batched c2r per sub-lattice
+    const long long nfb = (long long)align_up(n_field_bytes(j->N, j->rsize));
+    if ((rc = acquire_plan(eng, j->n_c2r, j->N, j->fp64, false, 6, nfb)) != MFX_OK) return fail(rc);
     work = std::max(work, j->n_c2r.work);
   }
   Layout L = plan_layout(d, work);
@@ -1190,11 +1204,13 @@ int mfx_job_footprint(mfx_engine *eng, const mfx_job_desc *desc, size_t *bytes) 
   GUARD_BEGIN
   TRY(check_desc(desc));
   if (!bytes) return set_error(MFX_EINVAL, "null output");
-  // FFT work areas are bounded by the largest transform's data size
+  // FFT work areas are bounded by the largest transform's data size: the
+  // padded cuFFT transforms (plain form), the batch of six N-grid c2r
   const int M = 3 * desc->ngrid / 2;
   const size_t rs = desc->precision == MFX_FP64 ? 8 : 4;
-  const size_t work = desc->lpt_order >= 2 ? size_t(M) * M * (M / 2 + 1) * 2 * rs
-                                           : n_field_bytes(desc->ngrid, rs);
+  size_t work = desc->want_particles ? 6 * n_field_bytes(desc->ngrid, rs) : 0;
+  if (desc->lpt_order >= 2 && !fused_supported(desc))
+    work = std::max(work, size_t(M) * M * (M / 2 + 1) * 2 * rs);
   *bytes = plan_layout(desc, work).total;
   return MFX_OK;
   GUARD_END

@@ -728,7 +728,8 @@ __device__ __forceinline__ void z_fetch(const FArgs &a, size_t g, float2 *stage,
       bulk_g2s(stage + (w * NIN + c) * D::Kh, a.src[c] + (g * RW + w) * D::Kh, bytes, bar);
 }
 
-// inverse z transforms of the staged spectra into h[w][c][z]
+// inverse z transforms of the staged spectra into the pair-interleaved
+// scratch h2[w * NP/2 + c/2][z] (float2: field c in x for even c, y for odd c)
 template <int M, int RW, int G, int NIN>
 __device__ __forceinline__ void z_inverse(const float2 *stage, float *h, float2 *buf, float2 *buf2, const float2 *tw) {
   using D = Dims<M>;
@@ -765,16 +766,15 @@ __device__ __forceinline__ void z_inverse(const float2 *stage, float *h, float2 
         [&](int q, int n, float2 v) {
           const int g = g0 + q;
           if (g >= NPI) return;
-          const int w = g / (NP / 2), c0 = 2 * (g - w * (NP / 2));
-          h[(w * NP + c0) * M + n] = v.x;
-          h[(w * NP + c0 + 1) * M + n] = v.y;
+          // fields (c0, c0 + 1) of row w are pair g of h2[g][z] = (x: c0, y: c0 + 1)
+          reinterpret_cast<float2 *>(h)[g * M + n] = v;
         });
   }
   __syncthreads();
 }
 
-// forward z transforms of NOUT real sources per row held in h[w][o][z]
-// (o < NOUT, row stride NP) and the kz < Kh spectra written to dst[o]
+// forward z transforms of NOUT real sources per row held in the pair scratch
+// (source o of row w in field slot o) and the kz < Kh spectra written to dst[o]
 template <int M, int RW, int G0, int NP, int NOUT>
 __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float *h, float2 *buf, float2 *buf2,
                                           const float2 *tw) {
@@ -791,10 +791,18 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
         [&](int q, int n) -> float2 {
           const int g = g0 + q;
           if (g >= NPO) return make_float2(0.f, 0.f);
-          const int f0 = 2 * g, f1 = f0 + 1;
-          const float re = h[((f0 / NOUT) * NP + f0 % NOUT) * M + n];
-          const float im = f1 < NR ? h[((f1 / NOUT) * NP + f1 % NOUT) * M + n] : 0.f;
-          return make_float2(re, im);
+          if constexpr (NOUT % 2 == 0) {
+            // sources (2g', 2g'+1) of one row share a pair slot
+            const int w = g / (NOUT / 2), o = 2 * (g - w * (NOUT / 2));
+            return reinterpret_cast<const float2 *>(h)[(w * (NP / 2) + o / 2) * M + n];
+          } else {
+            const int f0 = 2 * g, f1 = f0 + 1;
+            auto at = [&](int f) {
+              const int w = f / NOUT, o = f % NOUT;
+              return h[((w * (NP / 2) + o / 2) * M + n) * 2 + (o & 1)];
+            };
+            return make_float2(at(f0), f1 < NR ? at(f1) : 0.f);
+          }
         },
         [&](int q, int k, float2 v) { ob[T::at(q, k)] = v; });
     __syncthreads();
@@ -812,8 +820,8 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
   }
 }
 
-// the persistent row loop shared by ZSRC2 and ZSRC3; `sources(h_row)` forms
-// the sources of one element in place.  One stage: the next group's copies are
+// the persistent row loop shared by ZSRC2 and ZSRC3; `sources(pairs)` forms
+// the sources of one element in place (pairs[p * M]: fields 2p, 2p + 1).  One stage: the next group's copies are
 // issued as soon as the inverse transforms have read the current one, and
 // land while the sources and the forward transforms run.
 template <int M, int RW, int G, int NIN, int NOUT, class Src>
@@ -854,7 +862,7 @@ __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
     if (threadIdx.x == 0 && gn < ngroups) z_fetch<M, RW, NIN>(a, gn, stage, bar);
     for (int t = threadIdx.x; t < RW * M; t += blockDim.x) {
       const int w = t / M, n = t - w * M;
-      sources(h + size_t(w) * NP * M + n);
+      sources(reinterpret_cast<float2 *>(h) + size_t(w) * (NP / 2) * M + n);
     }
     __syncthreads();
     z_forward<M, RW, G, NP, NOUT>(a, g * RW, h, buf, buf2, tw);
@@ -865,16 +873,21 @@ __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
 // mode 1, the five first-pair products of convolve3 (dst[1..5]).
 template <int M, int RW, int G, int MODE>
 __global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads, ZR<M, RW, G, 6>::minb) k_ff_zsrc2(FArgs a) {
-  z_rows<M, RW, G, 6, MODE ? 6 : 1>(a, [&](float *hr) {
+  z_rows<M, RW, G, 6, MODE ? 6 : 1>(a, [&](float2 *hp) {
     float v[6], s[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) v[c] = hr[c * M];
+    for (int c = 0; c < 3; ++c) {
+      const float2 x = hp[c * M];
+      v[2 * c] = x.x;
+      v[2 * c + 1] = x.y;
+    }
     s[0] = src_phi2(v);
-    hr[0] = s[0];
     if (MODE) {
       pair_products(v, s + 1);
 #pragma unroll
-      for (int c = 1; c < 6; ++c) hr[c * M] = s[c];
+      for (int c = 0; c < 3; ++c) hp[c * M] = make_float2(s[2 * c], s[2 * c + 1]);
+    } else {
+      hp[0].x = s[0];
     }
   });
 }
@@ -885,18 +898,17 @@ __global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads, ZR<M, RW, G, 6>::min
 // outputs is written.
 template <int M, int RW, int G>
 __global__ void __launch_bounds__(ZR<M, RW, G, 17>::threads, ZR<M, RW, G, 17>::minb) k_ff_zsrc3(FArgs a) {
-  z_rows<M, RW, G, 17, 4>(a, [&](float *hr) {
-    float p[6], q[6], T5[5], s[4];
+  z_rows<M, RW, G, 17, 4>(a, [&](float2 *hp) {
+    float f[18], s[4];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      p[c] = hr[c * M];
-      q[c] = hr[(6 + c) * M];
+    for (int c = 0; c < 9; ++c) {
+      const float2 x = hp[c * M];
+      f[2 * c] = x.x;
+      f[2 * c + 1] = x.y;
     }
-#pragma unroll
-    for (int c = 0; c < 5; ++c) T5[c] = hr[(12 + c) * M];
-    src_phi3(p, q, T5, s);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) hr[c * M] = s[c];
+    src_phi3(f, f + 6, f + 12, s);
+    hp[0] = make_float2(s[0], s[1]);
+    hp[M] = make_float2(s[2], s[3]);
   });
 }
 #endif
