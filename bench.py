@@ -44,6 +44,8 @@ WORKLOADS = {
     "sc64": (64, 100.0, 49.0, 2, 0, False, 12345, False),
     "fcc768": (768, 1000.0, 24.0, 3, 2, True, 1, True),
     "fcc384": (384, 1000.0, 24.0, 3, 2, True, 1, True),
+    # the 256^3 BCC physics at 128^3 (L scaled): profiling captures of every kernel
+    "bcc128": (128, 150.0, 24.0, 3, 1, True, 4242, False),
 }
 LATNAME = {0: "sc", 1: "bcc", 2: "fcc"}
 
