@@ -131,6 +131,7 @@ struct mfx_job {
   void *ffB[3] = {};           // B-space [N][M][N/2] complex
   void *ffC[17] = {};          // C-space [M][M][N/2] complex
   float2 *ff_tw = nullptr;     // W_M^t, t < M
+  float2 *ff_twn = nullptr;    // W_N^t, t < N (fused assembly)
   int *dstatus = nullptr;      // device status word: nonzero when a kernel's bounded wait ran out
   size_t rsize = 8;
   cudaStream_t stream = nullptr;
@@ -256,7 +257,7 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
     L.ff_nc = d->lpt_order == 3 ? 17 : 7;
     L.mregion = 3 * L.ff_b + size_t(L.ff_nc) * L.ff_d;
     // the twiddles outlive the run: not in the region the particles reuse
-    L.ff_tw = align_up(size_t(M) * 8);
+    L.ff_tw = align_up(size_t(M) * 8) + align_up(size_t(N) * 8);
     L.status = align_up(sizeof(int));
   }
   const size_t np = size_t(ns) * N * N * N;
@@ -683,6 +684,56 @@ static int autotune_fused(mfx_job *j) {
 
 // Displacement / velocity assembly and particles (ic_generator.cc:937-1030):
 // the LPT orders in `mask` (bit n-1: order n) are combined, the others left out.
+// Fused assembly of the FP32 form (fused_asm.cuh): per sub-lattice, the
+// assembly with the inverse x transform, the inverse y transform, and the
+// inverse z transform with the particle read-out; the six components live in
+// the first six assembly buffers.
+static int assemble_fused(mfx_job *j, const AsmArgs &as) {
+  const int N = j->N, ns = j->ns, order = j->d.lpt_order;
+  const double qf = double(N) * N * (N / 2) * 8;  // one component field
+  const double nfb = double(j->n_field_bytes);
+  const double N3 = double(N) * N * N;
+  const double pb = N3 * (3.0 * (j->d.pos64 ? 8 : 4) + 3.0 * (j->d.vel64 ? 8 : 4) + (j->d.id64 ? 8 : 4));
+  // velocity / displacement magnitude ratio of the assembly: vfac * vunit / lunit
+  const double vfmax = std::max({std::fabs(as.vfac1), std::fabs(as.vfac2), std::fabs(as.vfac3)});
+  const double ratio = (vfmax > 0 && as.pfac != 0) ? vfmax * std::fabs(as.vfac / as.pfac) : 1.0;
+  const float vscale = float(ratio > 0 ? 1.0 / ratio : 1.0);
+  for (int s = 0; s < ns; ++s) {
+    ff::FAArgs fa{};
+    fa.as = as;
+    for (int c = 0; c < 6; ++c) fa.q[c] = static_cast<float2 *>(j->asmbuf[c]);
+    fa.tw = j->ff_twn;
+    fa.status = j->dstatus;
+    fa.shift = s;
+    fa.pos = j->pos;
+    fa.vel = j->vel;
+    fa.ids = j->ids;
+    fa.pos64 = j->d.pos64;
+    fa.vel64 = j->d.vel64;
+    fa.id64 = j->d.id64;
+    fa.nshift_total = ns;
+    fa.qtab = j->qtab + size_t(s) * 3 * N;
+    fa.id_offset = j->d.id_offset * uint64_t(ns) * uint64_t(N3);
+    fa.vscale = vscale;
+    fa.vunscale = 1.0 / double(vscale);
+    const bool plt = as.plt != nullptr;
+    const struct {
+      int op;
+      const char *name;
+      double bytes;
+    } passes[3] = {{ff::FA_X, "fa_x", (order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) * nfb + 6 * qf},
+                   {ff::FA_Y, "fa_y", 12 * qf},
+                   {ff::FA_Z, "fa_z", 6 * qf + pb}};
+    for (const auto &ps : passes) {
+      KBEGIN(j);
+      const cudaError_t e = ff::fa_launch(j->M, ps.op, plt, fa, j->stream);
+      if (e != cudaSuccess) return set_error(MFX_ECUDA, "%s (N = %d): %s", ps.name, N, cudaGetErrorString(e));
+      KEND(j, ps.name, ps.bytes);
+    }
+  }
+  return MFX_OK;
+}
+
 template <typename R> static int assemble_stage(mfx_job *j, int mask) {
   const int order = j->d.lpt_order;
   const int nsm = num_sm();
@@ -716,6 +767,7 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
   a.in_scale1 = 1.0 / j->scale1;
   a.in_scale2 = 1.0 / j->scale2;
   a.in_scale3 = 1.0 / j->scale3;
+  if (j->fused) return assemble_fused(j, a);
   const size_t total = size_t(N) * N * j->nk;
   for (int s0 = 0; s0 < j->ns; s0 += j->group) {
     const int g = std::min(j->group, j->ns - s0);
@@ -939,7 +991,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     if ((rc = acquire_plan(eng, j->m_c2r, j->M, j->fp64, false)) != MFX_OK) return fail(rc);
     work = std::max(work, std::max(j->m_r2c.work, j->m_c2r.work));
   }
-  if (d->want_particles) {
+  if (d->want_particles && !j->fused) {
     // the six assembled components of a sub-lattice lie one padded field apart:
     // one batched c2r per sub-lattice
     const long long nfb = (long long)align_up(n_field_bytes(j->N, j->rsize));
@@ -990,6 +1042,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->qtab = (double *)(p + align_up(size_t(j->ns) * 3 * j->N * sizeof(double2)));
   p += L.phase;
   j->ff_tw = L.ff_tw ? reinterpret_cast<float2 *>(p) : nullptr;
+  j->ff_twn = L.ff_tw ? reinterpret_cast<float2 *>(p + align_up(size_t(j->M) * 8)) : nullptr;
   p += L.ff_tw;
   j->dstatus = L.status ? reinterpret_cast<int *>(p) : nullptr;
   p += L.status;
@@ -1012,15 +1065,17 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     char *f = j->region;
     for (int q = 0; q < 3; ++q, f += L.ff_b) j->ffB[q] = f;
     for (int q = 0; q < L.ff_nc; ++q, f += L.ff_d) j->ffC[q] = f;
-    std::vector<float2> tw(j->M);
-    for (int t = 0; t < j->M; ++t) {
-      const double a = 2.0 * M_PI * double(t) / double(j->M);
-      tw[t] = make_float2(float(std::cos(a)), float(-std::sin(a)));
+    for (const int L : {j->M, j->N}) {
+      std::vector<float2> tw(L);
+      for (int t = 0; t < L; ++t) {
+        const double a = 2.0 * M_PI * double(t) / double(L);
+        tw[t] = make_float2(float(std::cos(a)), float(-std::sin(a)));
+      }
+      if (cudaMemcpyAsync(L == j->M ? j->ff_tw : j->ff_twn, tw.data(), tw.size() * sizeof(float2),
+                          cudaMemcpyHostToDevice, j->stream) != cudaSuccess ||
+          cudaStreamSynchronize(j->stream) != cudaSuccess)
+        return fail(set_error(MFX_ECUDA, "twiddle upload failed"));
     }
-    if (cudaMemcpyAsync(j->ff_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, j->stream) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(j->stream) != cudaSuccess)
-      return fail(set_error(MFX_ECUDA, "twiddle upload failed"));
   }
   j->group = L.group;
   if (d->want_particles) {
@@ -1208,9 +1263,9 @@ int mfx_job_footprint(mfx_engine *eng, const mfx_job_desc *desc, size_t *bytes) 
   // padded cuFFT transforms (plain form), the batch of six N-grid c2r
   const int M = 3 * desc->ngrid / 2;
   const size_t rs = desc->precision == MFX_FP64 ? 8 : 4;
-  size_t work = desc->want_particles ? 6 * n_field_bytes(desc->ngrid, rs) : 0;
-  if (desc->lpt_order >= 2 && !fused_supported(desc))
-    work = std::max(work, size_t(M) * M * (M / 2 + 1) * 2 * rs);
+  const bool fused = fused_supported(desc);
+  size_t work = (desc->want_particles && !fused) ? 6 * n_field_bytes(desc->ngrid, rs) : 0;
+  if (desc->lpt_order >= 2 && !fused) work = std::max(work, size_t(M) * M * (M / 2 + 1) * 2 * rs);
   *bytes = plan_layout(desc, work).total;
   return MFX_OK;
   GUARD_END

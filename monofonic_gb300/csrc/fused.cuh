@@ -170,8 +170,9 @@ template <int R, bool INV> MFX_HD void dft(float2 *v) {
   }
 }
 
-// Radices of each supported padded length (R3 = 1: two steps).  Every M = 3N/2
-// with N/2 a multiple of 8 and N <= 1024 whose length is 2^a 3^b is listed.
+// Radices of each supported length (R3 = 1: two steps): every padded length
+// M = 3N/2 with N/2 a multiple of 8 and N <= 1024 whose length is 2^a 3^b, and
+// the matching N-grid lengths of the assembly passes.
 template <int L> struct Fac;
 MFX_CX int cmax(int a, int b) { return a > b ? a : b; }
 #define MFX_FAC(L, a, b, c)                                                  \
@@ -180,7 +181,14 @@ MFX_CX int cmax(int a, int b) { return a > b ? a : b; }
     static constexpr int steps = (c > 1) ? 3 : 2;                            \
     static constexpr int maxJ = cmax(cmax(L / a, L / b), c > 1 ? L / c : 0); \
   }
+MFX_FAC(16, 4, 4, 1);
 MFX_FAC(24, 4, 6, 1);
+MFX_FAC(32, 4, 8, 1);
+MFX_FAC(64, 8, 8, 1);
+MFX_FAC(128, 16, 8, 1);
+MFX_FAC(256, 16, 16, 1);
+MFX_FAC(512, 8, 8, 8);
+MFX_FAC(1024, 16, 8, 8);
 MFX_FAC(48, 8, 6, 1);
 MFX_FAC(96, 8, 12, 1);
 MFX_FAC(144, 12, 12, 1);

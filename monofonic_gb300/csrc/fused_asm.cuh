@@ -1,0 +1,240 @@
+// Fused displacement / velocity assembly and particle read-out (FP32 form).
+//
+// One sub-lattice s at a time, the six real components (Psi_x,y,z, v_x,y,z)
+// that the reference assembles in k-space and transforms back one by one
+// (ic_generator.cc:929-1053, then particle_generator.hh:499-687) are produced
+// by three passes of the pencil FFT of fused.cuh, the N-grid counterpart of
+// the padded passes:
+//
+//   ASM1  units (j, kz block): every mode (i, j, kz) of the tile is assembled
+//         (asm_mode: PLT gradient, phi sum, A3 curl, sub-lattice phase) into
+//         shared memory and transformed back along x           -> Q[c][x][j][kz]
+//   ASM2  units (x, kz block, c): inverse y transform, in place -> Q[c][x][y][kz]
+//   ASM3  rows (x, y), persistent, spectra staged by bulk copies: inverse z
+//         transforms of the three component pairs, then q + Psi (FP64), v and
+//         the IDs of the row's N particles with 16-byte vector stores
+//
+// kz runs over [0, N/2): the kz = N/2 plane of every component is zero (the
+// potentials' Nyquist planes are), and the kz = 0 plane is Hermitian (asm_mode
+// takes the odd part of the PLT gradient there), so the z pass is a c2r.
+#pragma once
+#include "fused.cuh"
+#include "kernels.cuh"
+
+namespace mfx {
+namespace ff {
+
+struct FAArgs {
+  AsmArgs as;             // potentials, PLT tables, phases, coefficients
+  float2 *q[6];           // component fields [N][N][N/2] (ASM1 output, ASM2 in place, ASM3 input)
+  const float2 *tw;       // W_N^t, t < N
+  int *status;            // set when a bounded wait ran out
+  int shift;              // sub-lattice
+  // particle output (particle_generator.hh:212-253, 499-543, 597-639)
+  void *pos, *vel, *ids;
+  int pos64, vel64, id64, nshift_total;
+  const double *qtab;     // [3][N] unperturbed coordinates of this sub-lattice
+  uint64_t id_offset;
+  // The velocity components are carried times vscale and multiplied by
+  // vunscale = 1 / vscale at the read-out: the z pass pairs v_x with Psi_z in
+  // one complex FFT, whose FP32 rounding follows the larger of the two, so
+  // both are brought to the displacements' magnitude.
+  float vscale;
+  double vunscale;
+};
+
+// tile shapes per N: pencils P of ASM1 (P2 of ASM2), components CG per
+// assembly round (6 / CG rounds re-assemble the tile), rows RW of the z pass
+template <int N> struct FA {
+  static constexpr int maxJ = Fac<N>::maxJ;
+  static constexpr int P = 4;
+  static constexpr int P2 = (8 * maxJ <= 256) ? 8 : 4;
+  static constexpr int CG = (6 * P * maxJ <= 512) ? 6 : ((3 * P * maxJ <= 1024) ? 3 : 2);
+  static constexpr int RW = (256 / (3 * maxJ)) >= 8 ? 8 : ((256 / (3 * maxJ)) >= 4 ? 4 : ((256 / (3 * maxJ)) >= 2 ? 2 : 1));
+  static constexpr int Kh = N / 2, nk = N / 2 + 1;
+  static constexpr int t1 = CG * P * maxJ;  // ASM1 threads
+  static constexpr int t2 = P2 * maxJ;      // ASM2 threads
+  static constexpr int t3 = 3 * RW * maxJ;  // ASM3 threads
+  static constexpr int nbuf = Fac<N>::steps == 3 ? 2 : 1;
+  static constexpr size_t s1 = size_t(N + nbuf * Tile<N, CG * P, true>::elems) * sizeof(float2);
+  static constexpr size_t s2 = size_t(N + nbuf * Tile<N, P2, true>::elems + 2 * N * P2) * sizeof(float2);
+  static constexpr size_t head = 32;
+  static constexpr size_t s3 = head + size_t(N) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
+                               size_t(RW * 3 * N) * sizeof(float2) + size_t(2 * Tile<N, 3 * RW, false>::elems) * sizeof(float2);
+};
+
+// ASM1: assembly of the tile's modes and the inverse x transform
+template <int N, bool PLT>
+__global__ void __launch_bounds__(FA<N>::t1, min_blocks(FA<N>::t1)) k_fa_x(FAArgs a) {
+  using F = FA<N>;
+  constexpr int P = F::P, CG = F::CG, PP = CG * P, KB = F::Kh / P;
+  float2 *tw = ff_smem(), *buf = tw + N, *buf2 = buf + (F::nbuf == 2 ? Tile<N, PP, true>::elems : 0);
+  load_tw<N>(tw, a.tw);
+#pragma unroll 1
+  for (unsigned u = blockIdx.x; u < unsigned(N * KB); u += gridDim.x) {
+    const int j = int(u / KB), kz0 = int(u % KB) * P;
+#pragma unroll 1
+    for (int g0 = 0; g0 < 6; g0 += CG) {
+      // the tile's modes, components g0 .. g0 + CG - 1, PF layout: buf[i][c][p]
+      for (int t = threadIdx.x; t < N * P; t += blockDim.x) {
+        const int i = t / P, p = t - (t / P) * P, kz = kz0 + p;
+        const size_t idx = (size_t(i) * N + j) * F::nk + kz;
+        float2 Pm[3], Vm[3];
+        asm_mode<float, PLT>(a.as, i, j, kz, idx, Pm, Vm);
+        float er, ei;
+        lattice_phase<float>(a.as, a.shift, i, j, kz, er, ei);
+#pragma unroll
+        for (int c = 0; c < CG; ++c) {
+          const int cc = g0 + c;
+          float2 v = cc < 3 ? Pm[cc] : Vm[cc - 3];
+          if (cc >= 3) {
+            v.x *= a.vscale;
+            v.y *= a.vscale;
+          }
+          buf[i * PP + c * P + p] = make_float2(v.x * er - v.y * ei, v.x * ei + v.y * er);
+        }
+      }
+      __syncthreads();
+      pencil_fft<N, PP, true, true>(
+          buf, buf2, tw, [&](int q, int n) { return buf[n * PP + q]; },
+          [&](int q, int x, float2 v) {
+            const int c = q / P, p = q - (q / P) * P;
+            a.q[g0 + c][(unsigned(x) * N + j) * F::Kh + kz0 + p] = v;
+          });
+      __syncthreads();  // the next round assembles into buf
+    }
+  }
+}
+
+// ASM2: inverse y transforms of the six components, in place
+template <int N>
+__global__ void __launch_bounds__(FA<N>::t2, min_blocks(FA<N>::t2)) k_fa_y(FAArgs a) {
+  using F = FA<N>;
+  constexpr int P = F::P2, KB = F::Kh / P;
+  float2 *tw = ff_smem(), *buf = tw + N, *buf2 = buf + (F::nbuf == 2 ? Tile<N, P, true>::elems : 0),
+         *stage = buf + F::nbuf * Tile<N, P, true>::elems;
+  load_tw<N>(tw, a.tw);
+  xy_units(
+      unsigned(N * KB * 6), N * P, stage,
+      [&](unsigned u, float2 *st) {
+        const unsigned c = u % 6, t = u / 6, x = t / KB, kz0 = (t % KB) * P;
+        stage_rows<P, N, 16>(st, a.q[c] + (x * N * F::Kh + kz0), unsigned(F::Kh));
+      },
+      [&](unsigned u, const float2 *st) {
+        const unsigned c = u % 6, t = u / 6, x = t / KB, kz0 = (t % KB) * P;
+        float2 *out = a.q[c] + (x * N * F::Kh + kz0);
+        pencil_fft<N, P, true, true>(
+            buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
+            [&](int q, int y, float2 v) { out[unsigned(y) * F::Kh + q] = v; });
+      });
+}
+
+// ASM3: inverse z transforms (c2r, component pairs (0,1), (2,3), (4,5)) and the
+// particles of RW rows at a time
+template <int N>
+__global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
+  using F = FA<N>;
+  constexpr int RW = F::RW, Kh = F::Kh, G = 3 * RW;
+  char *base = reinterpret_cast<char *>(ff_smem());
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base);
+  volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
+  float2 *tw = reinterpret_cast<float2 *>(base + F::head);
+  float2 *stage = tw + N;            // [w][c][Kh]
+  float2 *h2 = stage + RW * 6 * Kh;  // [w][pair][z]
+  float2 *buf = h2 + RW * 3 * N;
+  float2 *buf2 = buf + Tile<N, G, false>::elems;
+  const size_t ngroups = size_t(N) * N / RW;
+  constexpr uint32_t rowbytes = uint32_t(Kh) * sizeof(float2);
+  auto fetch = [&](size_t g) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, rowbytes * 6 * RW);
+    for (int w = 0; w < RW; ++w)
+      for (int c = 0; c < 6; ++c) bulk_g2s(stage + (w * 6 + c) * Kh, a.q[c] + (g * RW + w) * Kh, rowbytes, bar);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    *flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  load_tw<N>(tw, a.tw);
+  size_t g = blockIdx.x;
+  if (threadIdx.x == 0 && g < ngroups) fetch(g);
+  const size_t n3 = size_t(N) * N * N, pbase = size_t(a.shift) * n3;
+#pragma unroll 1
+  for (uint32_t it = 0; g < ngroups; ++it, g += gridDim.x) {
+    const size_t gn = g + gridDim.x;
+    if (threadIdx.x == 0 && !mbar_wait_bounded(bar, it & 1)) *flag = 1;
+    __syncthreads();
+    if (*flag) {
+      // the copies did not land: report, let them finish (bounded), leave
+      if (threadIdx.x == 0) {
+        if (a.status) atomicExch(a.status, 1);
+        mbar_wait_bounded(bar, it & 1);
+      }
+      return;
+    }
+    pencil_fft<N, G, false, true>(
+        buf, buf2, tw,
+        [&](int q, int n) -> float2 {
+          const int w = q / 3, c0 = 2 * (q - w * 3);
+          int m;
+          bool conj;
+          if (n < Kh) {
+            m = n;
+            conj = false;
+          } else if (n > N - Kh) {
+            m = N - n;
+            conj = true;
+          } else {
+            return make_float2(0.f, 0.f);
+          }
+          const float2 *row = stage + w * 6 * Kh;
+          float2 va = row[c0 * Kh + m], vb = row[(c0 + 1) * Kh + m];
+          if (m == 0) {
+            va.y = 0.f;
+            vb.y = 0.f;
+          }
+          return conj ? pack_pair_conj(va, vb) : pack_pair(va, vb);
+        },
+        [&](int q, int z, float2 v) { h2[q * N + z] = v; });
+    __syncthreads();  // the stage is free, the components are in h2
+    if (threadIdx.x == 0 && gn < ngroups) fetch(gn);
+    for (int t = threadIdx.x; t < RW * (N / 4); t += blockDim.x) {
+      const int w = t / (N / 4), z0 = 4 * (t - w * (N / 4));
+      const size_t row = g * RW + w, cell = row * N + z0;
+      const int x = int(row / N), y = int(row - size_t(x) * N);
+      const float2 *hw = h2 + w * 3 * N;
+      double pv[12], vv[12];
+      const double qx = a.qtab[x], qy = a.qtab[N + y];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float2 a0 = hw[z0 + c], a1 = hw[N + z0 + c], a2 = hw[2 * N + z0 + c];
+        pv[3 * c + 0] = qx + double(a0.x);
+        pv[3 * c + 1] = qy + double(a0.y);
+        pv[3 * c + 2] = a.qtab[2 * N + z0 + c] + double(a1.x);
+        vv[3 * c + 0] = double(a1.y) * a.vunscale;
+        vv[3 * c + 1] = double(a2.x) * a.vunscale;
+        vv[3 * c + 2] = double(a2.y) * a.vunscale;
+      }
+      if (a.pos64) store12(reinterpret_cast<double *>(a.pos) + 3 * (pbase + cell), pv);
+      else store12(reinterpret_cast<float *>(a.pos) + 3 * (pbase + cell), pv);
+      if (a.vel64) store12(reinterpret_cast<double *>(a.vel) + 3 * (pbase + cell), vv);
+      else store12(reinterpret_cast<float *>(a.vel) + 3 * (pbase + cell), vv);
+      if (a.ids) {
+        const uint64_t st = uint64_t(a.nshift_total), id0 = a.id_offset + st * cell + uint64_t(a.shift);
+        if (a.id64) {
+          ulonglong2 *o = reinterpret_cast<ulonglong2 *>(reinterpret_cast<uint64_t *>(a.ids) + pbase + cell);
+          o[0] = make_ulonglong2(id0, id0 + st);
+          o[1] = make_ulonglong2(id0 + 2 * st, id0 + 3 * st);
+        } else {
+          *reinterpret_cast<uint4 *>(reinterpret_cast<uint32_t *>(a.ids) + pbase + cell) =
+              make_uint4(uint32_t(id0), uint32_t(id0 + st), uint32_t(id0 + 2 * st), uint32_t(id0 + 3 * st));
+        }
+      }
+    }
+    __syncthreads();  // h2 is rewritten by the next group
+  }
+}
+
+}  // namespace ff
+}  // namespace mfx

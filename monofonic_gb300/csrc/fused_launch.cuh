@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "fused.cuh"
+#include "fused_asm.cuh"
 
 namespace mfx {
 namespace ff {
@@ -137,16 +138,47 @@ template <int M> cudaError_t ff_launch_m(int op, int p, const FArgs &a, cudaStre
   }
 }
 
+// the fused assembly passes on the N-grid (N = 2M/3) of padded length M
+enum FAOp { FA_X = 0, FA_Y = 1, FA_Z = 2 };
+
+template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cudaStream_t s) {
+  constexpr int N = 2 * M / 3;
+  using F = FA<N>;
+  if constexpr (F::s1 > kFFSmemMax || F::s2 > kFFSmemMax || F::s3 > kFFSmemMax || F::t1 > 1024) {
+    return cudaErrorInvalidConfiguration;
+  } else {
+    switch (op) {
+      case FA_X:
+        if (plt) MFX_FF_PERSISTENT((k_fa_x<N, true>), F::t1, F::s1, size_t(N) * (F::Kh / F::P), s, a);
+        else MFX_FF_PERSISTENT((k_fa_x<N, false>), F::t1, F::s1, size_t(N) * (F::Kh / F::P), s, a);
+        break;
+      case FA_Y:
+        MFX_FF_PERSISTENT((k_fa_y<N>), F::t2, F::s2, size_t(N) * (F::Kh / F::P2) * 6, s, a);
+        break;
+      case FA_Z:
+        MFX_FF_PERSISTENT((k_fa_z<N>), F::t3, F::s3, size_t(N) * N / F::RW, s, a);
+        break;
+      default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  }
+}
+
 // per-M entry points (defined in the ff_m*.cu units)
 #define MFX_FF_LENGTHS(X) X(24) X(48) X(96) X(144) X(192) X(288) X(384) X(576) X(768) X(1152) X(1536)
-#define MFX_FF_DECL(M)                                                        \
-  cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s); \
+#define MFX_FF_DECL(M)                                                            \
+  cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s);     \
+  cudaError_t fa_launch_##M(int op, bool plt, const FAArgs &a, cudaStream_t s); \
   bool ff_valid_##M(int op, int p);
 MFX_FF_LENGTHS(MFX_FF_DECL)
 #undef MFX_FF_DECL
 
 #define MFX_FF_DEFINE(M)                                                                                     \
   cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s) { return ff_launch_m<M>(op, p, a, s); } \
+  cudaError_t fa_launch_##M(int op, bool plt, const FAArgs &a, cudaStream_t s) {                               \
+    return fa_launch_m<M>(op, plt, a, s);                                                                      \
+  }                                                                                                            \
   bool ff_valid_##M(int op, int p) { return ff_valid_m<M>(op, p); }
 
 inline bool ff_length_supported(int M) {
@@ -171,6 +203,14 @@ inline bool ff_valid(int M, int op, int p) {
   MFX_FF_LENGTHS(MFX_FF_CASE)
 #undef MFX_FF_CASE
   return false;
+}
+
+inline cudaError_t fa_launch(int M, int op, bool plt, const FAArgs &a, cudaStream_t s) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return fa_launch_##L(op, plt, a, s);
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return cudaErrorInvalidValue;
 }
 
 inline cudaError_t ff_launch(int M, int op, int p, const FArgs &a, cudaStream_t s) {

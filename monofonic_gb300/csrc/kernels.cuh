@@ -525,6 +525,108 @@ __device__ __forceinline__ void plt_grad(const AsmArgs &a, int i, int j, int k, 
   }
 }
 
+// One k-space mode of the displacement (P) and velocity (V) components before
+// the sub-lattice phase (ic_generator.cc:929-1053): idx = (i N + j)(N/2+1) + k.
+template <typename R, bool PLT>
+__device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, size_t idx,
+                                         typename Cplx<R>::T P[3], typename Cplx<R>::T V[3]) {
+  using C = typename Cplx<R>::T;
+  const int N = a.N, nh = N >> 1;
+  // Gp: gradient applied to the displacement, Gv: gradient times vfac_corr
+  // applied to the velocity
+  R Gp[3], Gv[3];
+  if (!PLT) {
+    // op::fourier_gradient (operators.hh:46-56): Nyquist index zeroed, exactly odd in k
+    const R kf = R(a.kfac);
+    Gp[0] = (i != nh) ? R(signed_idx(i, N)) * kf : R(0);
+    Gp[1] = (j != nh) ? R(signed_idx(j, N)) * kf : R(0);
+    Gp[2] = (k != nh) ? R(k) * kf : R(0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) Gv[d] = Gp[d];
+  } else {
+    R G[3], vc;
+    plt_grad<R>(a, i, j, k, N, G, vc);
+    if (k == 0) {
+      // On the kz = 0 plane the c2r sees both k and -k.  The interpolated PLT
+      // gradient is not exactly odd where the CIC stencil touches the table's
+      // Nyquist node (stored once, with +k), so the plane would not be
+      // Hermitian and the real field would depend on the FFT library's pass
+      // order.  Taking the odd part makes the input Hermitian; it equals what
+      // a c2c-then-c2r transform of the unsymmetrised plane yields.
+      const int im = i ? N - i : 0, jm = j ? N - j : 0;
+      R Gm[3], vcm;
+      plt_grad<R>(a, im, jm, 0, N, Gm, vcm);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Gp[d] = R(0.5) * (G[d] - Gm[d]);
+        Gv[d] = R(0.5) * (G[d] * vc - Gm[d] * vcm);
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Gp[d] = G[d];
+        Gv[d] = G[d] * vc;
+      }
+    }
+  }
+  // phi_tot and its velocity weighting (ic_generator.cc:939-958, 994-1010)
+  const C *p1 = reinterpret_cast<const C *>(a.phi[0]);
+  C f1 = p1[idx];
+  R ps_re = R(a.g1 * a.in_scale1) * f1.x, ps_im = R(a.g1 * a.in_scale1) * f1.y;
+  R vs_re = R(a.vfac1) * ps_re, vs_im = R(a.vfac1) * ps_im;
+  C Ad[3] = {mkc<R>(0, 0), mkc<R>(0, 0), mkc<R>(0, 0)};
+  if (a.order > 1) {
+    const C f2 = reinterpret_cast<const C *>(a.phi[1])[idx];
+    const R s2 = R(a.g2 * a.in_scale2);
+    ps_re += s2 * f2.x;
+    ps_im += s2 * f2.y;
+    vs_re += R(a.vfac2) * (s2 * f2.x);
+    vs_im += R(a.vfac2) * (s2 * f2.y);
+  }
+  if (a.order > 2) {
+    const C f3 = reinterpret_cast<const C *>(a.phi[2])[idx];
+    const R s3 = R(a.g3 * a.in_scale3);
+    ps_re += s3 * f3.x;
+    ps_im += s3 * f3.y;
+    vs_re += R(a.vfac3) * (s3 * f3.x);
+    vs_im += R(a.vfac3) * (s3 * f3.y);
+    const R sa = R(a.g3c * a.in_scale3);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const C v = reinterpret_cast<const C *>(a.A3[d])[idx];
+      Ad[d] = mkc<R>(sa * v.x, sa * v.y);
+    }
+  }
+  const bool dc = (idx == 0);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+    // i*(G_d phi) + i*(G_d' A_d'' - G_d'' A_d')
+    R tre = Gp[d] * ps_re, tim = Gp[d] * ps_im;
+    R vre = Gv[d] * vs_re, vim = Gv[d] * vs_im;
+    if (a.order > 2) {
+      tre += Gp[d1] * Ad[d2].x - Gp[d2] * Ad[d1].x;
+      tim += Gp[d1] * Ad[d2].y - Gp[d2] * Ad[d1].y;
+      vre += R(a.vfac3) * (Gv[d1] * Ad[d2].x - Gv[d2] * Ad[d1].x);
+      vim += R(a.vfac3) * (Gv[d1] * Ad[d2].y - Gv[d2] * Ad[d1].y);
+    }
+    const R pf = R(a.pfac), vf = R(a.vfac);
+    P[d] = dc ? mkc<R>(0, 0) : mkc<R>(-tim * pf, tre * pf);
+    V[d] = dc ? mkc<R>(0, 0) : mkc<R>(-vim * vf, vre * vf);
+  }
+}
+
+// the phase of sub-lattice s at mode (i, j, k): exp(i s.k dx) (grid_fft.hh:836-839)
+template <typename R>
+__device__ __forceinline__ void lattice_phase(const AsmArgs &a, int s, int i, int j, int k, R &er, R &ei) {
+  const int N = a.N;
+  const double2 *ph = a.phase + size_t(s) * 3 * N;
+  const double2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
+  const double exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
+  er = R(exy_re * ez.x - exy_im * ez.y);
+  ei = R(exy_re * ez.y + exy_im * ez.x);
+}
+
 template <typename R, bool PLT>
 __global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
   using C = typename Cplx<R>::T;
@@ -535,95 +637,11 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
     const int k = int(idx % nk);
     const size_t t = idx / nk;
     const int j = int(t % N), i = int(t / N);
-    // Gp: gradient applied to the displacement, Gv: gradient times vfac_corr
-    // applied to the velocity
-    R Gp[3], Gv[3];
-    if (!PLT) {
-      // op::fourier_gradient (operators.hh:46-56): Nyquist index zeroed, exactly odd in k
-      const R kf = R(a.kfac);
-      Gp[0] = (i != nh) ? R(signed_idx(i, N)) * kf : R(0);
-      Gp[1] = (j != nh) ? R(signed_idx(j, N)) * kf : R(0);
-      Gp[2] = (k != nh) ? R(k) * kf : R(0);
-#pragma unroll
-      for (int d = 0; d < 3; ++d) Gv[d] = Gp[d];
-    } else {
-      R G[3], vc;
-      plt_grad<R>(a, i, j, k, N, G, vc);
-      if (k == 0) {
-        // On the kz = 0 plane the c2r sees both k and -k.  The interpolated PLT
-        // gradient is not exactly odd where the CIC stencil touches the table's
-        // Nyquist node (stored once, with +k), so the plane would not be
-        // Hermitian and the real field would depend on the FFT library's pass
-        // order.  Taking the odd part makes the input Hermitian; it equals what
-        // a c2c-then-c2r transform of the unsymmetrised plane yields.
-        const int im = i ? N - i : 0, jm = j ? N - j : 0;
-        R Gm[3], vcm;
-        plt_grad<R>(a, im, jm, 0, N, Gm, vcm);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          Gp[d] = R(0.5) * (G[d] - Gm[d]);
-          Gv[d] = R(0.5) * (G[d] * vc - Gm[d] * vcm);
-        }
-      } else {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          Gp[d] = G[d];
-          Gv[d] = G[d] * vc;
-        }
-      }
-    }
-    // phi_tot and its velocity weighting (ic_generator.cc:939-958, 994-1010)
-    const C *p1 = reinterpret_cast<const C *>(a.phi[0]);
-    C f1 = p1[idx];
-    R ps_re = R(a.g1 * a.in_scale1) * f1.x, ps_im = R(a.g1 * a.in_scale1) * f1.y;
-    R vs_re = R(a.vfac1) * ps_re, vs_im = R(a.vfac1) * ps_im;
-    C Ad[3] = {mkc<R>(0, 0), mkc<R>(0, 0), mkc<R>(0, 0)};
-    if (a.order > 1) {
-      const C f2 = reinterpret_cast<const C *>(a.phi[1])[idx];
-      const R s2 = R(a.g2 * a.in_scale2);
-      ps_re += s2 * f2.x;
-      ps_im += s2 * f2.y;
-      vs_re += R(a.vfac2) * (s2 * f2.x);
-      vs_im += R(a.vfac2) * (s2 * f2.y);
-    }
-    if (a.order > 2) {
-      const C f3 = reinterpret_cast<const C *>(a.phi[2])[idx];
-      const R s3 = R(a.g3 * a.in_scale3);
-      ps_re += s3 * f3.x;
-      ps_im += s3 * f3.y;
-      vs_re += R(a.vfac3) * (s3 * f3.x);
-      vs_im += R(a.vfac3) * (s3 * f3.y);
-      const R sa = R(a.g3c * a.in_scale3);
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const C v = reinterpret_cast<const C *>(a.A3[d])[idx];
-        Ad[d] = mkc<R>(sa * v.x, sa * v.y);
-      }
-    }
-    const bool dc = (idx == 0);
     C P[3], V[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
-      // i*(G_d phi) + i*(G_d' A_d'' - G_d'' A_d')
-      R tre = Gp[d] * ps_re, tim = Gp[d] * ps_im;
-      R vre = Gv[d] * vs_re, vim = Gv[d] * vs_im;
-      if (a.order > 2) {
-        tre += Gp[d1] * Ad[d2].x - Gp[d2] * Ad[d1].x;
-        tim += Gp[d1] * Ad[d2].y - Gp[d2] * Ad[d1].y;
-        vre += R(a.vfac3) * (Gv[d1] * Ad[d2].x - Gv[d2] * Ad[d1].x);
-        vim += R(a.vfac3) * (Gv[d1] * Ad[d2].y - Gv[d2] * Ad[d1].y);
-      }
-      const R pf = R(a.pfac), vf = R(a.vfac);
-      P[d] = dc ? mkc<R>(0, 0) : mkc<R>(-tim * pf, tre * pf);
-      V[d] = dc ? mkc<R>(0, 0) : mkc<R>(-vim * vf, vre * vf);
-    }
+    asm_mode<R, PLT>(a, i, j, k, idx, P, V);
     for (int s = 0; s < a.nshift; ++s) {
-      const double2 *ph = a.phase + size_t(a.shift0 + s) * 3 * N;
-      const double2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
-      // e = ex * ey * ez
-      const double exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
-      const R er = R(exy_re * ez.x - exy_im * ez.y), ei = R(exy_re * ez.y + exy_im * ez.x);
+      R er, ei;
+      lattice_phase<R>(a, a.shift0 + s, i, j, k, er, ei);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         reinterpret_cast<C *>(a.out[s * 6 + d])[idx] = mkc<R>(P[d].x * er - P[d].y * ei, P[d].x * ei + P[d].y * er);

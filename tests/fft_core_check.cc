@@ -87,7 +87,14 @@ int main(int argc, char **argv) {
   }
   int rc = 2;
   switch (L) {
+    case 16: rc = run<16>(PP, inv, pf, data); break;
     case 24: rc = run<24>(PP, inv, pf, data); break;
+    case 32: rc = run<32>(PP, inv, pf, data); break;
+    case 64: rc = run<64>(PP, inv, pf, data); break;
+    case 128: rc = run<128>(PP, inv, pf, data); break;
+    case 256: rc = run<256>(PP, inv, pf, data); break;
+    case 512: rc = run<512>(PP, inv, pf, data); break;
+    case 1024: rc = run<1024>(PP, inv, pf, data); break;
     case 48: rc = run<48>(PP, inv, pf, data); break;
     case 96: rc = run<96>(PP, inv, pf, data); break;
     case 144: rc = run<144>(PP, inv, pf, data); break;

@@ -17,7 +17,7 @@ def harness(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("L", [24, 48, 96, 144, 192, 288, 384, 576, 768, 1152, 1536])
+@pytest.mark.parametrize("L", [16, 24, 32, 48, 64, 96, 128, 144, 192, 256, 288, 384, 512, 576, 768, 1024, 1152, 1536])
 @pytest.mark.parametrize("inv", [0, 1])
 @pytest.mark.parametrize("layout", [0, 1])
 def test_stockham_matches_numpy(harness, L, inv, layout):

@@ -298,8 +298,11 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     j.close()
     for a, b in zip(fused, ref):
         assert rel_l2(a, b) < 5e-6
+    # particles: fused assembly (own x/y/z passes) against cuFFT's c2r + read-out
     delta = c.L / (c.n * 2 ** (lattice / 3.0))
     assert np.sqrt(np.mean(((pf[0] - pr[0]) / delta) ** 2)) < 1e-6
+    assert rel_l2(pf[1].astype(np.float64), pr[1].astype(np.float64)) < 5e-6
+    assert np.array_equal(pf[2], pr[2])
 
 
 @pytest.mark.parametrize("n,lattice", [(64, 2), (48, 2)])
