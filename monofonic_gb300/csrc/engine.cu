@@ -149,6 +149,7 @@ struct mfx_job {
   float4 *plt4 = nullptr;  // FP32 form: the PLT tables interleaved per mode
   std::vector<float4> plt4_host;
   double2 *phase = nullptr;
+  float2 *phase32 = nullptr;  // the phase tables rounded to float (FP32 form)
   double *qtab = nullptr;  // [shift][axis][N] unperturbed coordinates times lunit
   void *nf[6] = {};       // phi1, phi2, phi3, A3x, A3y, A3z
   char *region = nullptr; // M-region / assembly union
@@ -242,7 +243,8 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   L.seeds = align_up(size_t(N) * N * 4);
   L.amp = align_up(d->amp_table_len * 8);
   L.plt = d->plt ? align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 8) + align_up(size_t(MFX_PLT_TABLE_DOUBLES) * 4) : 0;
-  L.phase = align_up(size_t(ns) * 3 * N * sizeof(double2)) + align_up(size_t(ns) * 3 * N * sizeof(double));
+  L.phase = align_up(size_t(ns) * 3 * N * sizeof(double2)) + align_up(size_t(ns) * 3 * N * sizeof(double)) +
+            align_up(size_t(ns) * 3 * N * sizeof(float2));
   const int nfield = d->lpt_order == 1 ? 1 : (d->lpt_order == 2 ? 2 : 6);
   L.nfields = nfield * align_up(L.n_field);
   L.nslots = d->lpt_order == 1 ? 0 : (d->lpt_order == 2 ? 7 : 17);
@@ -716,6 +718,7 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
     fa.id_offset = j->d.id_offset * uint64_t(ns) * uint64_t(N3);
     fa.vscale = vscale;
     fa.vunscale = 1.0 / double(vscale);
+    fa.vunscale_f = float(fa.vunscale);
     const bool plt = as.plt != nullptr;
     const struct {
       int op;
@@ -747,6 +750,7 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
   a.plt = j->d.plt ? j->plt : nullptr;
   a.plt4 = j->d.plt ? j->plt4 : nullptr;
   a.phase = j->phase;
+  a.phase32 = j->phase32;
   a.N = N;
   a.order = order;
   a.kfac = 2.0 * M_PI / j->d.boxlen;
@@ -1040,6 +1044,8 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   p += L.plt;
   j->phase = (double2 *)p;
   j->qtab = (double *)(p + align_up(size_t(j->ns) * 3 * j->N * sizeof(double2)));
+  j->phase32 = (float2 *)(p + align_up(size_t(j->ns) * 3 * j->N * sizeof(double2)) +
+                          align_up(size_t(j->ns) * 3 * j->N * sizeof(double)));
   p += L.phase;
   j->ff_tw = L.ff_tw ? reinterpret_cast<float2 *>(p) : nullptr;
   j->ff_twn = L.ff_tw ? reinterpret_cast<float2 *>(p + align_up(size_t(j->M) * 8)) : nullptr;
@@ -1124,7 +1130,11 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
       for (int ax = 0; ax < 3; ++ax)
         for (int m = 0; m < N; ++m)
           qt[(size_t(s) * 3 + ax) * N + m] = (double(m) + kShifts[d->lattice][s][ax]) / double(N) * d->lunit;
+    std::vector<float2> ph32(ph.size());
+    for (size_t q = 0; q < ph.size(); ++q) ph32[q] = make_float2(float(ph[q].x), float(ph[q].y));
     if (cudaMemcpyAsync(j->phase, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, j->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(j->phase32, ph32.data(), ph32.size() * sizeof(float2), cudaMemcpyHostToDevice, j->stream) !=
             cudaSuccess ||
         cudaMemcpyAsync(j->qtab, qt.data(), qt.size() * sizeof(double), cudaMemcpyHostToDevice, j->stream) !=
             cudaSuccess)

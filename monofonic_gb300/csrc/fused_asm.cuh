@@ -41,6 +41,7 @@ struct FAArgs {
   // both are brought to the displacements' magnitude.
   float vscale;
   double vunscale;
+  float vunscale_f;  // the same in float (velocities stored as float)
 };
 
 // tile shapes per N: pencils P of ASM1 (P2 of ASM2), components CG per
@@ -204,7 +205,10 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
       const size_t row = g * RW + w, cell = row * N + z0;
       const int x = int(row / N), y = int(row - size_t(x) * N);
       const float2 *hw = h2 + w * 3 * N;
-      double pv[12], vv[12];
+      // q + Psi in FP64; the velocities stay in float unless stored in FP64
+      // (FP64 arithmetic and conversions are slow on this part)
+      double pv[12];
+      float vv[12];
       const double qx = a.qtab[x], qy = a.qtab[N + y];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
@@ -212,14 +216,22 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
         pv[3 * c + 0] = qx + double(a0.x);
         pv[3 * c + 1] = qy + double(a0.y);
         pv[3 * c + 2] = a.qtab[2 * N + z0 + c] + double(a1.x);
-        vv[3 * c + 0] = double(a1.y) * a.vunscale;
-        vv[3 * c + 1] = double(a2.x) * a.vunscale;
-        vv[3 * c + 2] = double(a2.y) * a.vunscale;
+        vv[3 * c + 0] = a1.y;
+        vv[3 * c + 1] = a2.x;
+        vv[3 * c + 2] = a2.y;
       }
       if (a.pos64) store12(reinterpret_cast<double *>(a.pos) + 3 * (pbase + cell), pv);
       else store12(reinterpret_cast<float *>(a.pos) + 3 * (pbase + cell), pv);
-      if (a.vel64) store12(reinterpret_cast<double *>(a.vel) + 3 * (pbase + cell), vv);
-      else store12(reinterpret_cast<float *>(a.vel) + 3 * (pbase + cell), vv);
+      if (a.vel64) {
+        double vd[12];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) vd[c] = double(vv[c]) * a.vunscale;
+        store12(reinterpret_cast<double *>(a.vel) + 3 * (pbase + cell), vd);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 12; ++c) vv[c] *= a.vunscale_f;
+        store12(reinterpret_cast<float *>(a.vel) + 3 * (pbase + cell), vv);
+      }
       if (a.ids) {
         const uint64_t st = uint64_t(a.nshift_total), id0 = a.id_offset + st * cell + uint64_t(a.shift);
         if (a.id64) {

@@ -415,6 +415,7 @@ struct AsmArgs {
   const double *plt;    // 4 tables of 64*64*33 (D_r, D_theta, D_phi, alpha^-1) or null
   const float4 *plt4;   // the same tables interleaved per mode in float (FP32 form)
   const double2 *phase; // [ns][3][N] exp(i s_a k_a dx)
+  const float2 *phase32; // the same rounded to float (FP32 form)
   void *out[24];        // [shift][pos x,y,z, vel x,y,z]
   int N, order, nshift, shift0;
   double kfac, mapratio, boxlen;
@@ -467,17 +468,19 @@ __device__ __forceinline__ void plt_grad_f32(const float4 *T, int i, int j, int 
     Dp = fmaf(c[q].z, w[q], Dp);
     al = fmaf(c[q].w, w[q], al);
   }
+  // angles of k from reciprocal square roots (no IEEE divisions)
   const float sx = float(signed_idx(i, N)), sy = float(signed_idx(j, N)), sz = float(signed_idx(k, N));
-  const float kperp2 = sx * sx + sy * sy;
-  const float kr = sqrtf(kperp2 + sz * sz);
-  float st = 0.f, ct = 1.f, sp = 0.f, cp = 1.f;
-  if (kr > 0.f) {
-    const float kperp = sqrtf(kperp2);
-    st = kperp / kr;
-    ct = sz / kr;
-    if (kperp > 0.f) {
-      cp = sx / kperp;
-      sp = sy / kperp;
+  const float kperp2 = sx * sx + sy * sy, kr2 = kperp2 + sz * sz;
+  float st = 0.f, ct = 1.f, sp = 0.f, cp = 1.f, kr = 0.f;
+  if (kr2 > 0.f) {
+    const float rkr = rsqrtf(kr2);
+    kr = kr2 * rkr;
+    ct = sz * rkr;
+    if (kperp2 > 0.f) {
+      const float rkp = rsqrtf(kperp2);
+      st = kperp2 * rkp * rkr;
+      cp = sx * rkp;
+      sp = sy * rkp;
     }
   }
   const float kmod = kfac * kr;
@@ -616,10 +619,21 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
   }
 }
 
-// the phase of sub-lattice s at mode (i, j, k): exp(i s.k dx) (grid_fft.hh:836-839)
+// the phase of sub-lattice s at mode (i, j, k): exp(i s.k dx) (grid_fft.hh:836-839);
+// the FP32 form multiplies the float tables (FP64 arithmetic is slow here)
 template <typename R>
 __device__ __forceinline__ void lattice_phase(const AsmArgs &a, int s, int i, int j, int k, R &er, R &ei) {
   const int N = a.N;
+  if constexpr (sizeof(R) == 4) {
+    if (a.phase32) {
+      const float2 *ph = a.phase32 + size_t(s) * 3 * N;
+      const float2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
+      const float exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
+      er = exy_re * ez.x - exy_im * ez.y;
+      ei = exy_re * ez.y + exy_im * ez.x;
+      return;
+    }
+  }
   const double2 *ph = a.phase + size_t(s) * 3 * N;
   const double2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
   const double exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
@@ -686,6 +700,10 @@ __device__ __forceinline__ void store12(double *o, const double *v) {
 #pragma unroll
   for (int q = 0; q < 6; ++q) reinterpret_cast<double2 *>(o)[q] = make_double2(v[2 * q], v[2 * q + 1]);
 }
+__device__ __forceinline__ void store12(float *o, const float *v) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) reinterpret_cast<float4 *>(o)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
 __device__ __forceinline__ void store12(float *o, const double *v) {
 #pragma unroll
   for (int q = 0; q < 3; ++q)
@@ -707,7 +725,8 @@ __global__ void __launch_bounds__(256) k_particles(PartArgs a) {
     const size_t tt = cell / N;
     const int j = int(tt % N), i = int(tt / N);
     const size_t r = (size_t(i) * N + j) * rowp + k;
-    double pv[12], vv[12];
+    double pv[12];
+    VelT vv[12];  // velocities never pass through FP64 when stored as float
     const double qx = __ldg(&a.qtab[i]), qy = __ldg(&a.qtab[N + j]);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -723,7 +742,7 @@ __global__ void __launch_bounds__(256) k_particles(PartArgs a) {
       for (int c = 0; c < 4; ++c) {
         const double q = d == 0 ? qx : (d == 1 ? qy : __ldg(&a.qtab[2 * N + k + c]));
         pv[3 * c + d] = q + double(ps[c]);
-        vv[3 * c + d] = double(vs[c]);
+        vv[3 * c + d] = VelT(vs[c]);
       }
     }
     store12(reinterpret_cast<PosT *>(a.pos) + 3 * (base + cell), pv);
