@@ -163,16 +163,21 @@ int mfx_job_destroy(mfx_job *job);
 
 /* Sets the pencil-tile shape of the fused transforms by hand (the choice
    mfx_job_autotune makes by timing): pencils per CTA of the x/y passes
-   (4, 8 or 16) and rows per CTA of the z passes (1 or 2).  MFX_EINVAL for a
-   shape the padded length does not admit, MFX_ESTATE for a job without the
-   fused transforms. */
+   (4, 8 or 16) and the z passes' shape: 1 or 2 rows per CTA, or 3 for one
+   row per CTA and as many pencils per transform as one CTA per SM holds
+   (the wide shape of the long padded lengths), for both z passes (2LPT and
+   3LPT sources).  MFX_EINVAL for a shape the padded length does not admit,
+   MFX_ESTATE for a job without the fused transforms. */
 int mfx_job_set_tiles(mfx_job *job, int pencils_xy, int rows_z);
 /* Autotuner of the FP32 form's fused transforms: times every admissible
-   pencil-tile shape (pencils per CTA of the x/y passes, rows per CTA of the z
-   passes) on the job's own buffers and keeps the fastest for the job and, per
-   grid size, for later jobs of the engine.  Returns the chosen shape (0, 0
-   when the job does not use the fused transforms).  The reference has no
-   tunables: its FFTW plans use FFTW_ESTIMATE (general.hh:87-93). */
+   pencil-tile shape (pencils per CTA of the x/y passes; the z shape of the
+   2LPT and, for 3LPT jobs, the 3LPT source pass, each on its own) on the
+   job's own buffers and keeps the fastest for the job and, per grid size,
+   for later jobs of the engine.  Call it before mfx_job_run: it overwrites
+   the job's buffers.  Returns the x/y tile and the z shape of the job's last
+   source pass (0, 0 when the job does not use the fused transforms).  The
+   reference has no tunables: its FFTW plans use FFTW_ESTIMATE
+   (general.hh:87-93). */
 int mfx_job_autotune(mfx_job *job, int *pencils_xy, int *rows_z);
 
 /* Captures the job's whole pipeline into a CUDA graph; later mfx_job_run

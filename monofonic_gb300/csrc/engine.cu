@@ -118,7 +118,10 @@ struct mfx_engine {
   std::vector<Plan> plan_pool;
   // autotuned pencil-tile shapes of the fused transforms per grid size:
   // N -> (pencils per CTA of the x/y passes, rows per CTA of the z passes)
-  std::map<int, std::pair<int, int>> ff_tuned;
+  struct FFTiles {
+    int pxy, pz, pz2;
+  };
+  std::map<int, FFTiles> ff_tuned;  // per grid size: x/y tile, ZSRC3 and ZSRC2 shapes
 };
 
 struct mfx_job {
@@ -127,7 +130,7 @@ struct mfx_job {
   int N = 0, M = 0, nh = 0, nk = 0, mk = 0, ns = 0, group = 0;
   bool fp64 = true;
   bool fused = false;          // padded convolutions through fused.cuh
-  int ff_pxy = 8, ff_pz = 1;   // pencils per CTA (x/y passes) and rows per CTA (z passes)
+  int ff_pxy = 8, ff_pz = 1, ff_pz2 = 1;  // pencils per CTA (x/y passes), ZSRC3 / ZSRC2 shapes (1, 2 rows; 3 wide)
   void *ffB[3] = {};           // B-space [N][M][N/2] complex
   void *ffC[17] = {};          // C-space [M][M][N/2] complex
   float2 *ff_tw = nullptr;     // W_M^t, t < M
@@ -233,7 +236,10 @@ static bool fused_supported(const mfx_job_desc *d) {
   return (N / 2) % 8 == 0 && ff::ff_length_supported(M);
 }
 
-static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
+// group_all: hold every sub-lattice's assembled components at once even where
+// that grows the region beyond the padded fields (the fused assembly then
+// assembles each mode once for all sub-lattices)
+static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes, bool group_all = false) {
   Layout L{};
   const int N = d->ngrid, M = 3 * N / 2;
   const size_t rs = d->precision == MFX_FP64 ? 8 : 4;
@@ -273,7 +279,7 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes) {
   int group = ns;
   if (d->want_particles) {
     size_t full = L.part_bytes + size_t(6 * ns) * align_up(L.n_field);
-    if (L.mregion > 0 && full > L.mregion) group = 1;
+    if (L.mregion > 0 && full > L.mregion && !group_all) group = 1;
   }
   L.group = group;
   L.asm_bytes = d->want_particles ? L.part_bytes + size_t(6 * group) * align_up(L.n_field) : 0;
@@ -567,7 +573,7 @@ static int run_potentials_fused(mfx_job *j) {
     const int nout = order >= 3 ? 6 : 1;
     for (int o = 0; o < nout; ++o) z.dst[o] = static_cast<float2 *>(D[o]);
     z.mode = order >= 3 ? 1 : 0;
-    TRY(ff_run(j, ff::FF_ZSRC2, j->ff_pz, z, "ff_zsrc2", 6 * bC + nout * bC));
+    TRY(ff_run(j, ff::FF_ZSRC2, j->ff_pz2, z, "ff_zsrc2", 6 * bC + nout * bC));
   }
   TRY(ff_finish(j, D[0], j->nf[1], 0));
   if (j->timed) CU(cudaEventRecord(j->ev[2], j->stream));
@@ -606,8 +612,9 @@ static void tune_fused(mfx_job *j) {
   std::lock_guard<std::mutex> lk(j->eng->mu);
   auto it = j->eng->ff_tuned.find(j->N);
   if (it != j->eng->ff_tuned.end()) {
-    j->ff_pxy = it->second.first;
-    j->ff_pz = it->second.second;
+    j->ff_pxy = it->second.pxy;
+    j->ff_pz = it->second.pz;
+    j->ff_pz2 = it->second.pz2;
   }
 }
 
@@ -630,7 +637,7 @@ static int autotune_fused(mfx_job *j) {
   };
   const bool prof = j->prof;
   j->prof = false;
-  int best_xy = j->ff_pxy, best_z = j->ff_pz;
+  int best_xy = j->ff_pxy;
   float tbest = 1e30f;
   int rc = MFX_OK;
   for (int p : {16, 8, 4}) {
@@ -649,26 +656,33 @@ static int autotune_fused(mfx_job *j) {
       best_xy = p;
     }
   }
-  tbest = 1e30f;
-  for (int p : {1, 2}) {
-    if (rc != MFX_OK || !ff::ff_valid(M, ff::FF_ZSRC3, p)) continue;
-    // the z pass that dominates the job: ZSRC3 (3LPT) or ZSRC2 (2LPT)
-    const float t = timed([&] {
-      ff::FArgs z = ff_args(j);
-      if (j->d.lpt_order >= 3) {
-        for (int c = 0; c < 17; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
-        for (int o = 0; o < 4; ++o) z.dst[o] = static_cast<float2 *>(j->ffC[12 + o]);
-        if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC3, p, z, "ff_zsrc3", 0);
-      } else {
-        for (int c = 0; c < 6; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
-        z.dst[0] = static_cast<float2 *>(j->ffC[6]);
-        z.mode = 0;
-        if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC2, p, z, "ff_zsrc2", 0);
+  // the z passes, each shape timed on the job's own fields: ZSRC2 always,
+  // ZSRC3 for 3LPT jobs
+  int best_z2 = j->ff_pz2, best_z3 = j->ff_pz;
+  for (int op : {ff::FF_ZSRC2, ff::FF_ZSRC3}) {
+    if (op == ff::FF_ZSRC3 && j->d.lpt_order < 3) continue;
+    tbest = 1e30f;
+    for (int p : {1, 2, 3}) {
+      if (rc != MFX_OK || !ff::ff_valid(M, op, p)) continue;
+      const float t = timed([&] {
+        ff::FArgs z = ff_args(j);
+        if (op == ff::FF_ZSRC3) {
+          for (int c = 0; c < 17; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
+          for (int o = 0; o < 4; ++o) z.dst[o] = static_cast<float2 *>(j->ffC[12 + o]);
+          if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC3, p, z, "ff_zsrc3", 0);
+        } else {
+          // the 3LPT form's ZSRC2 (mode 1: the five pair products as well)
+          for (int c = 0; c < 6; ++c) z.src[c] = static_cast<const float2 *>(j->ffC[c]);
+          const int nout = j->d.lpt_order >= 3 ? 6 : 1;
+          for (int o = 0; o < nout; ++o) z.dst[o] = static_cast<float2 *>(j->ffC[6 + o]);
+          z.mode = nout > 1 ? 1 : 0;
+          if (rc == MFX_OK) rc = ff_run(j, ff::FF_ZSRC2, p, z, "ff_zsrc2", 0);
+        }
+      });
+      if (t < tbest) {
+        tbest = t;
+        (op == ff::FF_ZSRC3 ? best_z3 : best_z2) = p;
       }
-    });
-    if (t < tbest) {
-      tbest = t;
-      best_z = p;
     }
   }
   j->prof = prof;
@@ -678,9 +692,10 @@ static int autotune_fused(mfx_job *j) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(MFX_ECUDA, "autotune: %s", cudaGetErrorString(e));
   j->ff_pxy = best_xy;
-  j->ff_pz = best_z;
+  j->ff_pz = best_z3;
+  j->ff_pz2 = best_z2;
   std::lock_guard<std::mutex> lk(j->eng->mu);
-  j->eng->ff_tuned[N] = {best_xy, best_z};
+  j->eng->ff_tuned[N] = {best_xy, best_z3, best_z2};
   return MFX_OK;
 }
 
@@ -700,38 +715,46 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   const double vfmax = std::max({std::fabs(as.vfac1), std::fabs(as.vfac2), std::fabs(as.vfac3)});
   const double ratio = (vfmax > 0 && as.pfac != 0) ? vfmax * std::fabs(as.vfac / as.pfac) : 1.0;
   const float vscale = float(ratio > 0 ? 1.0 / ratio : 1.0);
-  for (int s = 0; s < ns; ++s) {
-    ff::FAArgs fa{};
-    fa.as = as;
-    for (int c = 0; c < 6; ++c) fa.q[c] = static_cast<float2 *>(j->asmbuf[c]);
-    fa.tw = j->ff_twn;
-    fa.status = j->dstatus;
-    fa.shift = s;
-    fa.pos = j->pos;
-    fa.vel = j->vel;
-    fa.ids = j->ids;
-    fa.pos64 = j->d.pos64;
-    fa.vel64 = j->d.vel64;
-    fa.id64 = j->d.id64;
-    fa.nshift_total = ns;
-    fa.qtab = j->qtab + size_t(s) * 3 * N;
-    fa.id_offset = j->d.id_offset * uint64_t(ns) * uint64_t(N3);
-    fa.vscale = vscale;
-    fa.vunscale = 1.0 / double(vscale);
-    fa.vunscale_f = float(fa.vunscale);
-    const bool plt = as.plt != nullptr;
-    const struct {
-      int op;
-      const char *name;
-      double bytes;
-    } passes[3] = {{ff::FA_X, "fa_x", (order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) * nfb + 6 * qf},
-                   {ff::FA_Y, "fa_y", 12 * qf},
-                   {ff::FA_Z, "fa_z", 6 * qf + pb}};
-    for (const auto &ps : passes) {
-      KBEGIN(j);
-      const cudaError_t e = ff::fa_launch(j->M, ps.op, plt, fa, j->stream);
-      if (e != cudaSuccess) return set_error(MFX_ECUDA, "%s (N = %d): %s", ps.name, N, cudaGetErrorString(e));
-      KEND(j, ps.name, ps.bytes);
+  // all sub-lattices from one assembly when their components fit the buffers;
+  // MFX_FA_KEEP=0 in the environment assembles per sub-lattice (for comparisons)
+  const char *env = getenv("MFX_FA_KEEP");
+  const bool keep = !(env && env[0] == '0');
+  const int nsub = (keep && ns > 1 && ff::fa_keep(j->M) && j->group >= ns) ? ns : 1;
+  const bool plt = as.plt != nullptr;
+  ff::FAArgs fa{};
+  fa.as = as;
+  fa.tw = j->ff_twn;
+  fa.status = j->dstatus;
+  fa.pos = j->pos;
+  fa.vel = j->vel;
+  fa.ids = j->ids;
+  fa.pos64 = j->d.pos64;
+  fa.vel64 = j->d.vel64;
+  fa.id64 = j->d.id64;
+  fa.nshift_total = ns;
+  fa.id_offset = j->d.id_offset * uint64_t(ns) * uint64_t(N3);
+  fa.vscale = vscale;
+  fa.vunscale = 1.0 / double(vscale);
+  fa.vunscale_f = float(fa.vunscale);
+  auto pass = [&](int op, const char *name, double bytes) -> int {
+    KBEGIN(j);
+    const cudaError_t e = ff::fa_launch(j->M, op, plt, fa, j->stream);
+    if (e != cudaSuccess) return set_error(MFX_ECUDA, "%s (N = %d): %s", name, N, cudaGetErrorString(e));
+    KEND(j, name, bytes);
+    return MFX_OK;
+  };
+  const double in_b = (order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) * nfb;
+  for (int s0 = 0; s0 < ns; s0 += nsub) {
+    fa.shift = s0;
+    fa.nsub = nsub;
+    for (int q = 0; q < 6 * nsub; ++q) fa.qx[q] = static_cast<float2 *>(j->asmbuf[q]);
+    TRY(pass(ff::FA_X, "fa_x", in_b + 6 * nsub * qf));
+    for (int s = 0; s < nsub; ++s) {
+      fa.shift = s0 + s;
+      for (int c = 0; c < 6; ++c) fa.q[c] = static_cast<float2 *>(j->asmbuf[6 * s + c]);
+      fa.qtab = j->qtab + size_t(s0 + s) * 3 * N;
+      TRY(pass(ff::FA_Y, "fa_y", 12 * qf));
+      TRY(pass(ff::FA_Z, "fa_z", 6 * qf + pb));
     }
   }
   return MFX_OK;
@@ -1005,6 +1028,13 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   Layout L = plan_layout(d, work);
   {
     std::lock_guard<std::mutex> lk(eng->mu);
+    // the fused assembly emits all sub-lattices from one assembly of each mode
+    // when their components are held together: worth the extra memory while
+    // the engine budget has it
+    if (j->fused && d->want_particles && L.group < j->ns && ff::fa_keep(j->M)) {
+      const Layout La = plan_layout(d, work, true);
+      if (eng->in_use + La.total <= eng->budget) L = La;
+    }
     if (eng->in_use + L.total > eng->budget)
       return fail(set_error(MFX_EADMIT, "job needs %zu bytes, engine budget has %zu of %zu free", L.total,
                             eng->budget - std::min(eng->budget, eng->in_use), eng->budget));
@@ -1341,6 +1371,7 @@ int mfx_job_set_tiles(mfx_job *job, int pencils_xy, int rows_z) {
   if (job->gexec) return set_error(MFX_ESTATE, "job already captured into a graph");
   job->ff_pxy = pencils_xy;
   job->ff_pz = rows_z;
+  job->ff_pz2 = rows_z;
   return MFX_OK;
   GUARD_END
 }
@@ -1351,7 +1382,7 @@ int mfx_job_autotune(mfx_job *job, int *pencils_xy, int *rows_z) {
   CU(cudaSetDevice(job->eng->device));
   if (job->fused) TRY(autotune_fused(job));
   if (pencils_xy) *pencils_xy = job->fused ? job->ff_pxy : 0;
-  if (rows_z) *rows_z = job->fused ? job->ff_pz : 0;
+  if (rows_z) *rows_z = job->fused ? (job->d.lpt_order >= 3 ? job->ff_pz : job->ff_pz2) : 0;
   return MFX_OK;
   GUARD_END
 }

@@ -259,12 +259,14 @@ template <int L, int R, int NS, bool INV> struct Step {
 // next step's writes never share a buffer (one barrier per exchange).  ld may
 // read either buffer; st may write obuf() (the buffer the last step does not
 // read); the caller synchronises before reading what st wrote to shared
-// memory.
+// memory.  LDB = false: ld reads neither buffer and nothing but an earlier
+// call of the same shape reads buf, which then needs no barrier before the
+// first step's writes when that call's last step read buf2 (three steps).
 template <int L> __device__ __forceinline__ float2 *obuf(float2 *buf, float2 *buf2) {
   return Fac<L>::steps == 3 ? buf : buf2;
 }
 
-template <int L, int PP, bool PF, bool INV, class Ld, class St>
+template <int L, int PP, bool PF, bool INV, bool LDB = true, class Ld, class St>
 __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const float2 *tw, const Ld &ld, const St &st) {
   using F = Fac<L>;
   using T = Tile<L, PP, PF>;
@@ -276,7 +278,8 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
     split<PP, S::J, PF>(t, q, j);
     const bool act = t < PP * S::J;
     if (act) S::gather(j, [&](int n) { return ld(q, n); }, tw, v);
-    __syncthreads();  // ld may read buf; an earlier call's last step may still read it
+    // ld may read buf; an earlier call's last step may still read it
+    if constexpr (LDB || F::steps != 3) __syncthreads();
     if (act) S::scatter(j, [&](int n, float2 x) { buf[T::at(q, n)] = x; }, v);
     __syncthreads();
   }
@@ -710,7 +713,9 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                : "memory");
 }
 
-template <int M, int RW, int G, int NIN> struct ZR {
+// z-pass shape: RW rows per group, G pencils per transform; WIDE: one CTA per
+// SM by shared memory and registers (the wide shape of the long lengths)
+template <int M, int RW, int G, int NIN, bool WIDE = false> struct ZR {
   using D = Dims<M>;
   static constexpr int nin_pad = NIN + (NIN & 1);
   static constexpr int threads = G * Fac<M>::maxJ;
@@ -721,7 +726,8 @@ template <int M, int RW, int G, int NIN> struct ZR {
                                  size_t(2 * Tile<M, G, false>::elems) * sizeof(float2);
   // CTAs per SM: by registers (64 each) and by shared memory (228 KB per SM)
   static constexpr int by_smem = int(233472 / (smem + 1024));
-  static constexpr int minb = min_blocks(threads) < by_smem ? min_blocks(threads) : (by_smem < 1 ? 1 : by_smem);
+  static constexpr int minb =
+      WIDE ? 1 : (min_blocks(threads) < by_smem ? min_blocks(threads) : (by_smem < 1 ? 1 : by_smem));
 };
 
 // issues the bulk copies of row group g (RW rows x NIN spectra) into stage
@@ -745,7 +751,7 @@ __device__ __forceinline__ void z_inverse(const float2 *stage, float *h, float2 
   constexpr int NPI = RW * (NP / 2);  // complex pencils
 #pragma unroll 1
   for (int g0 = 0; g0 < NPI; g0 += G) {
-    pencil_fft<M, G, false, true>(
+    pencil_fft<M, G, false, true, false>(
         buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int g = g0 + q;
@@ -794,7 +800,7 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
   float2 *ob = obuf<M>(buf, buf2);
 #pragma unroll 1
   for (int g0 = 0; g0 < NPO; g0 += G) {
-    pencil_fft<M, G, false, false>(
+    pencil_fft<M, G, false, false, false>(
         buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int g = g0 + q;
@@ -879,8 +885,8 @@ __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
 
 // ZSRC2: phi1 Hessians (src[0..5], C-space) -> 2LPT source (dst[0]) and, with
 // mode 1, the five first-pair products of convolve3 (dst[1..5]).
-template <int M, int RW, int G, int MODE>
-__global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads, ZR<M, RW, G, 6>::minb) k_ff_zsrc2(FArgs a) {
+template <int M, int RW, int G, int MODE, bool WIDE>
+__global__ void __launch_bounds__(ZR<M, RW, G, 6, WIDE>::threads, ZR<M, RW, G, 6, WIDE>::minb) k_ff_zsrc2(FArgs a) {
   z_rows<M, RW, G, 6, MODE ? 6 : 1>(a, [&](float2 *hp) {
     float v[6], s[6];
 #pragma unroll
@@ -904,8 +910,8 @@ __global__ void __launch_bounds__(ZR<M, RW, G, 6>::threads, ZR<M, RW, G, 6>::min
 // pair products src[12..16] (C-space) -> phi3 source (dst[0]) and A3 (dst[1..3]).
 // The outputs may alias inputs: a row's spectra are staged before any of its
 // outputs is written.
-template <int M, int RW, int G>
-__global__ void __launch_bounds__(ZR<M, RW, G, 17>::threads, ZR<M, RW, G, 17>::minb) k_ff_zsrc3(FArgs a) {
+template <int M, int RW, int G, bool WIDE>
+__global__ void __launch_bounds__(ZR<M, RW, G, 17, WIDE>::threads, ZR<M, RW, G, 17, WIDE>::minb) k_ff_zsrc3(FArgs a) {
   z_rows<M, RW, G, 17, 4>(a, [&](float2 *hp) {
     float f[18], s[4];
 #pragma unroll

@@ -26,7 +26,9 @@ namespace ff {
 
 struct FAArgs {
   AsmArgs as;             // potentials, PLT tables, phases, coefficients
-  float2 *q[6];           // component fields [N][N][N/2] (ASM1 output, ASM2 in place, ASM3 input)
+  float2 *q[6];           // component fields [N][N][N/2] of sub-lattice `shift` (ASM2 in place, ASM3 input)
+  float2 *qx[24];         // ASM1 output: component c of sub-lattice shift + s at qx[6 s + c], s < nsub
+  int nsub;               // sub-lattices ASM1 emits from one assembly of each mode (1 unless FA::keep)
   const float2 *tw;       // W_N^t, t < N
   int *status;            // set when a bounded wait ran out
   int shift;              // sub-lattice
@@ -58,51 +60,92 @@ template <int N> struct FA {
   static constexpr int t3 = 3 * RW * maxJ;  // ASM3 threads
   static constexpr int nbuf = Fac<N>::steps == 3 ? 2 : 1;
   static constexpr size_t s1 = size_t(N + nbuf * Tile<N, CG * P, true>::elems) * sizeof(float2);
+  // ASM1 keeping each mode's six pre-phase components in shared memory, to emit
+  // every sub-lattice from one assembly: component group CGK (the largest
+  // divisor of 6 up to CG whose tiles fit beside the kept components)
+  template <int cg>
+  static constexpr size_t s1k_of = size_t(N + nbuf * Tile<N, cg * P, true>::elems + 6 * N * P) * sizeof(float2);
+  static constexpr size_t kKeepMax = 200 * 1024;
+  static constexpr int CGK = (CG >= 6 && s1k_of<6> <= kKeepMax)   ? 6
+                             : (CG >= 3 && s1k_of<3> <= kKeepMax) ? 3
+                             : (CG >= 2 && s1k_of<2> <= kKeepMax) ? 2
+                                                                  : 1;
+  static constexpr bool keep = s1k_of<CGK> <= kKeepMax;
+  static constexpr int t1k = CGK * P * maxJ;
+  static constexpr size_t s1k = s1k_of<CGK>;
   static constexpr size_t s2 = size_t(N + nbuf * Tile<N, P2, true>::elems + 2 * N * P2) * sizeof(float2);
   static constexpr size_t head = 32;
   static constexpr size_t s3 = head + size_t(N) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
                                size_t(RW * 3 * N) * sizeof(float2) + size_t(2 * Tile<N, 3 * RW, false>::elems) * sizeof(float2);
 };
 
-// ASM1: assembly of the tile's modes and the inverse x transform
-template <int N, bool PLT>
-__global__ void __launch_bounds__(FA<N>::t1, min_blocks(FA<N>::t1)) k_fa_x(FAArgs a) {
+// ASM1: assembly of the tile's modes and the inverse x transform.  KEEP:
+// each mode is assembled once (PLT gradient, potentials), its six pre-phase
+// components kept in shared memory, and the a.nsub sub-lattices emitted from
+// them, each with its own phase; otherwise one sub-lattice (a.shift), the
+// assembly repeated for each group of CG components.
+template <int N, bool PLT, bool KEEP>
+__global__ void __launch_bounds__(KEEP ? FA<N>::t1k : FA<N>::t1, min_blocks(KEEP ? FA<N>::t1k : FA<N>::t1))
+    k_fa_x(FAArgs a) {
   using F = FA<N>;
-  constexpr int P = F::P, CG = F::CG, PP = CG * P, KB = F::Kh / P;
+  constexpr int P = F::P, CG = KEEP ? F::CGK : F::CG, PP = CG * P, KB = F::Kh / P;
   float2 *tw = ff_smem(), *buf = tw + N, *buf2 = buf + (F::nbuf == 2 ? Tile<N, PP, true>::elems : 0);
+  float2 *pv = buf + F::nbuf * Tile<N, PP, true>::elems;  // [6][mode] (KEEP)
   load_tw<N>(tw, a.tw);
+  const int nsub = KEEP ? a.nsub : 1;
 #pragma unroll 1
   for (unsigned u = blockIdx.x; u < unsigned(N * KB); u += gridDim.x) {
     const int j = int(u / KB), kz0 = int(u % KB) * P;
-#pragma unroll 1
-    for (int g0 = 0; g0 < 6; g0 += CG) {
-      // the tile's modes, components g0 .. g0 + CG - 1, PF layout: buf[i][c][p]
+    if constexpr (KEEP) {
+      // each thread later reads back only the entries it wrote here
       for (int t = threadIdx.x; t < N * P; t += blockDim.x) {
         const int i = t / P, p = t - (t / P) * P, kz = kz0 + p;
-        const size_t idx = (size_t(i) * N + j) * F::nk + kz;
         float2 Pm[3], Vm[3];
-        asm_mode<float, PLT>(a.as, i, j, kz, idx, Pm, Vm);
-        float er, ei;
-        lattice_phase<float>(a.as, a.shift, i, j, kz, er, ei);
+        asm_mode<float, PLT>(a.as, i, j, kz, (size_t(i) * N + j) * F::nk + kz, Pm, Vm);
 #pragma unroll
-        for (int c = 0; c < CG; ++c) {
-          const int cc = g0 + c;
-          float2 v = cc < 3 ? Pm[cc] : Vm[cc - 3];
-          if (cc >= 3) {
-            v.x *= a.vscale;
-            v.y *= a.vscale;
-          }
-          buf[i * PP + c * P + p] = make_float2(v.x * er - v.y * ei, v.x * ei + v.y * er);
+        for (int c = 0; c < 3; ++c) {
+          pv[c * (N * P) + t] = Pm[c];
+          pv[(3 + c) * (N * P) + t] = make_float2(Vm[c].x * a.vscale, Vm[c].y * a.vscale);
         }
       }
-      __syncthreads();
-      pencil_fft<N, PP, true, true>(
-          buf, buf2, tw, [&](int q, int n) { return buf[n * PP + q]; },
-          [&](int q, int x, float2 v) {
-            const int c = q / P, p = q - (q / P) * P;
-            a.q[g0 + c][(unsigned(x) * N + j) * F::Kh + kz0 + p] = v;
-          });
-      __syncthreads();  // the next round assembles into buf
+    }
+#pragma unroll 1
+    for (int s = 0; s < nsub; ++s) {
+#pragma unroll 1
+      for (int g0 = 0; g0 < 6; g0 += CG) {
+        // the tile's modes, components g0 .. g0 + CG - 1, PF layout: buf[i][c][p]
+        for (int t = threadIdx.x; t < N * P; t += blockDim.x) {
+          const int i = t / P, p = t - (t / P) * P, kz = kz0 + p;
+          float2 v6[CG];
+          if constexpr (KEEP) {
+#pragma unroll
+            for (int c = 0; c < CG; ++c) v6[c] = pv[(g0 + c) * (N * P) + t];
+          } else {
+            float2 Pm[3], Vm[3];
+            asm_mode<float, PLT>(a.as, i, j, kz, (size_t(i) * N + j) * F::nk + kz, Pm, Vm);
+#pragma unroll
+            for (int c = 0; c < CG; ++c) {
+              const int cc = g0 + c;
+              v6[c] = cc < 3 ? Pm[cc] : make_float2(Vm[cc - 3].x * a.vscale, Vm[cc - 3].y * a.vscale);
+            }
+          }
+          float er, ei;
+          lattice_phase<float>(a.as, a.shift + s, i, j, kz, er, ei);
+#pragma unroll
+          for (int c = 0; c < CG; ++c) {
+            const float2 v = v6[c];
+            buf[i * PP + c * P + p] = make_float2(v.x * er - v.y * ei, v.x * ei + v.y * er);
+          }
+        }
+        __syncthreads();
+        pencil_fft<N, PP, true, true>(
+            buf, buf2, tw, [&](int q, int n) { return buf[n * PP + q]; },
+            [&](int q, int x, float2 v) {
+              const int c = q / P, p = q - (q / P) * P;
+              a.qx[s * 6 + g0 + c][(unsigned(x) * N + j) * F::Kh + kz0 + p] = v;
+            });
+        __syncthreads();  // the next round assembles into buf
+      }
     }
   }
 }

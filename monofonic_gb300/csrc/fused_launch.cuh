@@ -1,7 +1,8 @@
 // Host-side launchers of the fused transforms (fused.cuh), one instantiation
 // per padded length M (the ff_m*.cu translation units compile them in
 // parallel).  ff_launch_m<M> launches one pass with pencil tile `p`: pencils
-// per CTA for the x/y passes (4, 8 or 16), rows per CTA for the z passes.
+// per CTA for the x/y passes (4, 8 or 16); for the z passes 1 or 2 rows per
+// CTA, or 3: the wide shape (one row, many pencils per transform).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -30,13 +31,39 @@ template <int M, int RW, int NIN> struct ZG {
 
 constexpr size_t kFFSmemMax = 227 * 1024;
 
+// the wide z shape (tile 3): one row per group and as many pencils per
+// transform as about 92 registers a thread (704 threads) and the shared
+// memory allow (one CTA per SM), the fewest rounds per row and, among those,
+// the fewest idle pencils.  For the long padded lengths, whose narrow shapes
+// leave only a few warps per SM.
+constexpr size_t zw_smem(int M, int NIN, int G) {
+  const size_t kh = size_t(M / 3), np = size_t(NIN + (NIN & 1));
+  return 32 + size_t(M) * 8 + NIN * kh * 8 + np * size_t(M) * 4 + 2 * size_t(G) * size_t(M + (M >> 4)) * 8;
+}
+constexpr int zw_pick(int M, int NIN, int maxJ) {
+  const int npi = (NIN + (NIN & 1)) / 2;
+  int gmax = 0;
+  for (int g = 1; g <= npi && g * maxJ <= 704 && zw_smem(M, NIN, g) <= kFFSmemMax; ++g) gmax = g;
+  if (gmax == 0) return 0;
+  const int rounds = (npi + gmax - 1) / gmax;
+  return (npi + rounds - 1) / rounds;
+}
+template <int M, int NIN> struct ZGW {
+  static constexpr int G = zw_pick(M, NIN, Fac<M>::maxJ);
+};
+
 template <int M, int RW> constexpr bool ff_z_fits() {
-  return ZR<M, RW, ZG<M, RW, 6>::G, 6>::smem <= kFFSmemMax && ZR<M, RW, ZG<M, RW, 17>::G, 17>::smem <= kFFSmemMax;
+  if constexpr (RW == 3) {
+    return ZGW<M, 6>::G > 0 && ZGW<M, 17>::G > 0;
+  } else {
+    return ZR<M, RW, ZG<M, RW, 6>::G, 6>::smem <= kFFSmemMax && ZR<M, RW, ZG<M, RW, 17>::G, 17>::smem <= kFFSmemMax;
+  }
 }
 
 template <int M> bool ff_valid_m(int op, int p) {
   constexpr int Kh = M / 3;
-  if (op == FF_ZSRC2 || op == FF_ZSRC3) return (p == 1 && ff_z_fits<M, 1>()) || (p == 2 && ff_z_fits<M, 2>());
+  if (op == FF_ZSRC2 || op == FF_ZSRC3)
+    return (p == 1 && ff_z_fits<M, 1>()) || (p == 2 && ff_z_fits<M, 2>()) || (p == 3 && ff_z_fits<M, 3>());
   if (op < 0 || op >= FF_NOPS) return false;
   return (p == 4 || p == 8 || p == 16) && Kh % p == 0 && p * Fac<M>::maxJ <= 1024 &&
          (size_t(M) + 4 * size_t(M) * p) * sizeof(float2) <= kFFSmemMax;
@@ -107,22 +134,27 @@ template <int M, int P> cudaError_t ff_launch_xy(int op, const FArgs &a, cudaStr
   }
 }
 
-template <int M, int RW> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStream_t s) {
-  if constexpr (!ff_z_fits<M, RW>()) {
+// z tile p: 1 and 2 rows per group (two tile buffers), 3 the wide shape
+template <int M, int P> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStream_t s) {
+  if constexpr (!ff_z_fits<M, P>()) {
     return cudaErrorInvalidConfiguration;
   } else {
+    constexpr int RW = P == 3 ? 1 : P;
+    constexpr bool W = P == 3;
     const size_t groups = size_t(M) * M / RW;
     if (op == FF_ZSRC2) {
-      constexpr int G = ZG<M, RW, 6>::G;
-      using Z = ZR<M, RW, G, 6>;
+      constexpr int G = W ? ZGW<M, 6>::G : ZG<M, RW, 6>::G;
+      using Z = ZR<M, RW, G, 6, W>;
+      static_assert(Z::smem <= kFFSmemMax, "z tile exceeds shared memory");
       if (a.mode)
-        MFX_FF_PERSISTENT((k_ff_zsrc2<M, RW, G, 1>), Z::threads, Z::smem, groups, s, a);
+        MFX_FF_PERSISTENT((k_ff_zsrc2<M, RW, G, 1, W>), Z::threads, Z::smem, groups, s, a);
       else
-        MFX_FF_PERSISTENT((k_ff_zsrc2<M, RW, G, 0>), Z::threads, Z::smem, groups, s, a);
+        MFX_FF_PERSISTENT((k_ff_zsrc2<M, RW, G, 0, W>), Z::threads, Z::smem, groups, s, a);
     } else {
-      constexpr int G = ZG<M, RW, 17>::G;
-      using Z = ZR<M, RW, G, 17>;
-      MFX_FF_PERSISTENT((k_ff_zsrc3<M, RW, G>), Z::threads, Z::smem, groups, s, a);
+      constexpr int G = W ? ZGW<M, 17>::G : ZG<M, RW, 17>::G;
+      using Z = ZR<M, RW, G, 17, W>;
+      static_assert(Z::smem <= kFFSmemMax, "z tile exceeds shared memory");
+      MFX_FF_PERSISTENT((k_ff_zsrc3<M, RW, G, W>), Z::threads, Z::smem, groups, s, a);
     }
     return cudaGetLastError();
   }
@@ -130,7 +162,8 @@ template <int M, int RW> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStr
 
 template <int M> cudaError_t ff_launch_m(int op, int p, const FArgs &a, cudaStream_t s) {
   if (!ff_valid_m<M>(op, p)) return cudaErrorInvalidConfiguration;
-  if (op == FF_ZSRC2 || op == FF_ZSRC3) return p == 1 ? ff_launch_z<M, 1>(op, a, s) : ff_launch_z<M, 2>(op, a, s);
+  if (op == FF_ZSRC2 || op == FF_ZSRC3)
+    return p == 1 ? ff_launch_z<M, 1>(op, a, s) : (p == 2 ? ff_launch_z<M, 2>(op, a, s) : ff_launch_z<M, 3>(op, a, s));
   switch (p) {
     case 4: return ff_launch_xy<M, 4>(op, a, s);
     case 8: return ff_launch_xy<M, 8>(op, a, s);
@@ -147,10 +180,20 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
   if constexpr (F::s1 > kFFSmemMax || F::s2 > kFFSmemMax || F::s3 > kFFSmemMax || F::t1 > 1024) {
     return cudaErrorInvalidConfiguration;
   } else {
+    constexpr size_t units1 = size_t(N) * (F::Kh / F::P);
     switch (op) {
       case FA_X:
-        if (plt) MFX_FF_PERSISTENT((k_fa_x<N, true>), F::t1, F::s1, size_t(N) * (F::Kh / F::P), s, a);
-        else MFX_FF_PERSISTENT((k_fa_x<N, false>), F::t1, F::s1, size_t(N) * (F::Kh / F::P), s, a);
+        if (a.nsub > 1) {
+          if constexpr (F::keep) {
+            if (plt) MFX_FF_PERSISTENT((k_fa_x<N, true, true>), F::t1k, F::s1k, units1, s, a);
+            else MFX_FF_PERSISTENT((k_fa_x<N, false, true>), F::t1k, F::s1k, units1, s, a);
+          } else {
+            return cudaErrorInvalidValue;
+          }
+        } else {
+          if (plt) MFX_FF_PERSISTENT((k_fa_x<N, true, false>), F::t1, F::s1, units1, s, a);
+          else MFX_FF_PERSISTENT((k_fa_x<N, false, false>), F::t1, F::s1, units1, s, a);
+        }
         break;
       case FA_Y:
         MFX_FF_PERSISTENT((k_fa_y<N>), F::t2, F::s2, size_t(N) * (F::Kh / F::P2) * 6, s, a);
@@ -170,6 +213,7 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
 #define MFX_FF_DECL(M)                                                            \
   cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s);     \
   cudaError_t fa_launch_##M(int op, bool plt, const FAArgs &a, cudaStream_t s); \
+  bool fa_keep_##M();                                                           \
   bool ff_valid_##M(int op, int p);
 MFX_FF_LENGTHS(MFX_FF_DECL)
 #undef MFX_FF_DECL
@@ -179,6 +223,7 @@ MFX_FF_LENGTHS(MFX_FF_DECL)
   cudaError_t fa_launch_##M(int op, bool plt, const FAArgs &a, cudaStream_t s) {                               \
     return fa_launch_m<M>(op, plt, a, s);                                                                      \
   }                                                                                                            \
+  bool fa_keep_##M() { return FA<2 * M / 3>::keep; }                                                          \
   bool ff_valid_##M(int op, int p) { return ff_valid_m<M>(op, p); }
 
 inline bool ff_length_supported(int M) {
@@ -200,6 +245,15 @@ inline int ff_maxj(int M) {
 inline bool ff_valid(int M, int op, int p) {
 #define MFX_FF_CASE(L) \
   if (M == L) return ff_valid_##L(op, p);
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return false;
+}
+
+// whether ASM1 emits several sub-lattices from one assembly at this length
+inline bool fa_keep(int M) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return fa_keep_##L();
   MFX_FF_LENGTHS(MFX_FF_CASE)
 #undef MFX_FF_CASE
   return false;

@@ -285,7 +285,7 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     monkeypatch.setenv("MFX_FUSED", "1")
     j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
     pxy, pz = j.autotune()
-    assert pxy in (4, 8, 16) and pz in (1, 2)
+    assert pxy in (4, 8, 16) and pz in (1, 2, 3)
     j.run()
     fused = [j.field(f) for f in fids]
     pf = j.particles()
@@ -305,6 +305,27 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     assert np.array_equal(pf[2], pr[2])
 
 
+@pytest.mark.parametrize("n,lattice,order,plt", [(64, 2, 3, True), (96, 1, 2, False), (48, 2, 2, False)])
+def test_fused_assembly_once_for_all_sublattices(mfxlib, engine, n, lattice, order, plt, monkeypatch):
+    """Fused assembly: each mode assembled once and all sub-lattices emitted
+    from it gives the particles of the per-sub-lattice assembly."""
+    tab = engine.plt_table(lattice) if plt else None
+    c = Case(mfxlib, n, 300.0, 24.0, order, 99, lattice=lattice, plt=tab)
+    monkeypatch.setenv("MFX_FUSED", "1")
+    out = []
+    for keep in ("1", "0"):
+        monkeypatch.setenv("MFX_FA_KEEP", keep)
+        j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
+        j.run()
+        out.append(j.particles())
+        j.close()
+    delta = c.L / (c.n * 2 ** (lattice / 3.0))
+    assert np.all(np.isfinite(out[0][0])) and np.all(np.isfinite(out[0][1]))
+    assert np.sqrt(np.mean(((out[0][0] - out[1][0]) / delta) ** 2)) < 1e-7
+    assert rel_l2(out[0][1].astype(np.float64), out[1][1].astype(np.float64)) < 1e-6
+    assert np.array_equal(out[0][2], out[1][2])
+
+
 @pytest.mark.parametrize("n,lattice", [(64, 2), (48, 2)])
 def test_fused_rerun_is_identical(mfxlib, engine, n, lattice, monkeypatch):
     """A second run of the same job (the particle stage reuses the padded
@@ -315,7 +336,7 @@ def test_fused_rerun_is_identical(mfxlib, engine, n, lattice, monkeypatch):
     fids = [mfxlib.FIELD_PHI2, mfxlib.FIELD_PHI3, mfxlib.FIELD_A3Y]
     first = None
     for pxy in (4, 8, 16):
-        for pz in (1, 2):
+        for pz in (1, 2, 3):
             j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
             try:
                 j.set_tiles(pxy, pz)
