@@ -263,8 +263,51 @@ def run_ours(args):
         e2e_t.append(time.perf_counter() - t1)
     barrier()
     e2e_ms, e2e_val = replica_throughput(float(np.mean(e2e_t)) * 1e3, npart, device="cuda")
-    e2e = {"value": e2e_val, "unit": "particles/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+    e2e_serial = {"value": e2e_val, "unit": "particles/s", "ms_per_step": e2e_ms,
+                  "mode": "one step at a time: upload, run, download, next step"}
+    e2e = dict(e2e_serial)
+    # pipelined output: with two particle sets (mfx_job_set_output_ring) a step
+    # computes while the previous step's particles download (the host link,
+    # ~190 GB/s, then bounds the step rather than adding to it).  Every step
+    # still uploads its inputs and downloads all its particles into its own
+    # page-locked host buffers (two sets, alternating); no L2 flush is needed
+    # between steps: each step's inputs come from the host and its HBM traffic
+    # (~17 GB at 256^3) is far above the 129 MB L2.
+    ring = False
+    if 2 * d2h <= (40 << 30):  # two host sets of one step's particles, page-locked
+        try:
+            job.set_output_ring(True)
+            ring = True
+        except RuntimeError:
+            ring = False
+    if ring:
+        host = [(pinned(npart * 3 * 8), pinned(npart * 3 * (8 if vel64 else 4)), pinned(npart * 8)) for _ in range(2)]
+        sets = [tuple(x[1] for x in st) for st in host]  # numpy views; `host` keeps the tensors alive
+
+        def step(k):
+            job.upload(hs, ha, hp)
+            job.run(wait=False)
+            p, v, i = sets[k % 2]
+            job.fetch_particles_range_async(0, npart, p.ctypes.data, v.ctypes.data, i.ctypes.data)
+
+        for k in range(2):
+            step(k)
+        job.wait()
+        job.wait_fetch()
+        barrier()
+        t1 = time.perf_counter()
+        for k in range(args.steps):
+            step(k)
+        job.wait()
+        job.wait_fetch()
+        barrier()
+        e2e_ms, e2e_val = replica_throughput((time.perf_counter() - t1) * 1e3 / args.steps, npart, device="cuda")
+        e2e = {"value": e2e_val, "unit": "particles/s", "ms_per_step": e2e_ms,
+               "mode": "pipelined: step k+1 computes while step k's particles download (output ring)"}
+        job.set_output_ring(False)
+    e2e.update({"h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)})
+    if ring:
+        e2e["serial"] = e2e_serial
 
     out = None
     if rank == 0:

@@ -136,6 +136,27 @@ int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void
    that each order's displacement and velocity can be read on its own (the
    per-order error statement of the FP32 form).  Not capturable in a graph. */
 int mfx_job_assemble(mfx_job *job, int orders_mask);
+/* Pipelined output (no counterpart in the reference, whose output plugins
+   write a realisation after it is generated): on = 1 gives the job two
+   particle sets of its own, outside the arena (2 x the particle bytes,
+   charged to the engine budget; MFX_EADMIT / MFX_ENOMEM when they do not
+   fit), and runs alternate between them, so that a run computes while the
+   particles of the previous run are still being copied to the host by
+   mfx_job_fetch_particles_range_async.  A run's assembly waits only for the
+   downloads from the set it writes.  on = 0 returns to the arena's particle
+   arrays.  Either way the particles of earlier runs are no longer fetchable.
+   MFX_ESTATE for a captured job (and capture refuses a job with the ring). */
+int mfx_job_set_output_ring(mfx_job *job, int on);
+/* Enqueues the download of particles [first, first + count) of the job's
+   last run into host buffers (page-locked for the copies to overlap) behind
+   the job's enqueued work, and returns.  Call it before the next
+   mfx_job_run.  The buffers are filled when mfx_job_wait_fetch returns.
+   Without the output ring the next run waits for the download before it
+   starts (its fields overwrite the particles); mfx_job_assemble always waits
+   for it. */
+int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count, void *pos, void *vel, void *ids);
+/* Waits for the job's asynchronous downloads. */
+int mfx_job_wait_fetch(mfx_job *job);
 /* Device pointers of the particle arrays (valid until the next run/destroy). */
 int mfx_job_particles_device(mfx_job *job, const void **pos, const void **vel, const void **ids,
                              size_t *num_particles);

@@ -139,6 +139,14 @@ struct mfx_job {
   size_t rsize = 8;
   cudaStream_t stream = nullptr;
   cudaStream_t xfer[4] = {};  // particle downloads, split across copy streams
+  // pipelined output (mfx_job_set_output_ring): two particle sets outside the
+  // arena; a run writes set ring_next while the downloads of the other set's
+  // particles (enqueued on xfer[0] by the asynchronous fetch) may still run
+  char *ring = nullptr;
+  size_t ring_set_bytes = 0;
+  int ring_next = 0;
+  cudaEvent_t ring_free[2] = {};  // the last download from set s is done
+  cudaEvent_t fetched = nullptr;  // the last asynchronous download is done
   cudaEvent_t ev[6] = {};
   bool timed = false;
   // arena
@@ -640,7 +648,7 @@ static int autotune_fused(mfx_job *j) {
   int best_xy = j->ff_pxy;
   float tbest = 1e30f;
   int rc = MFX_OK;
-  for (int p : {16, 8, 4}) {
+  for (int p : {32, 16, 8, 4}) {
     if (!ff::ff_valid(M, ff::FF_XFWD, p)) continue;
     const float t = timed([&] {
       // the Hessian passes of phi1 and one forward x/y pair
@@ -836,6 +844,17 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
   return MFX_OK;
 }
 
+// points the particle arrays at ring set s (pos | vel | ids)
+static void ring_point(mfx_job *j, int s) {
+  const size_t np = j->npart;
+  char *a = j->ring + size_t(s) * j->ring_set_bytes;
+  j->pos = a;
+  a += align_up(np * 3 * (j->d.pos64 ? 8 : 4));
+  j->vel = a;
+  a += align_up(np * 3 * (j->d.vel64 ? 8 : 4));
+  j->ids = a;
+}
+
 template <typename R> static int run_pipeline(mfx_job *j) {
   const int order = j->d.lpt_order;
   const size_t mreal = size_t(j->M) * j->M * (j->M + 2);
@@ -844,6 +863,13 @@ template <typename R> static int run_pipeline(mfx_job *j) {
   j->fft_execs = 0;
   j->prof_recs.clear();
   j->ev_next = 0;
+  // an asynchronous download of the last run's particles may still read them:
+  // in the arena they lie in the region this run's fields overwrite, so the
+  // run waits for it; in the ring only this run's assembly waits, for the
+  // download from the set it writes
+  if (j->fetched && !j->ring) CU(cudaStreamWaitEvent(j->stream, j->fetched, 0));
+  const int rset = j->ring_next;
+  if (j->ring) ring_point(j, rset);
   if (j->timed) CU(cudaEventRecord(j->ev[0], j->stream));
   TRY(launch_noise<R>(j, 2, j->nf[0]));
   if (j->timed) CU(cudaEventRecord(j->ev[1], j->stream));
@@ -910,8 +936,10 @@ template <typename R> static int run_pipeline(mfx_job *j) {
   }
   }  // cuFFT path
   if (j->timed) CU(cudaEventRecord(j->ev[3], j->stream));
+  if (j->ring) CU(cudaStreamWaitEvent(j->stream, j->ring_free[rset], 0));
   if (j->d.want_particles) TRY(assemble_stage<R>(j, 7));
   if (j->timed) CU(cudaEventRecord(j->ev[4], j->stream));
+  if (j->ring) j->ring_next = rset ^ 1;
   j->has_run = true;
   j->noise_only = false;
   return MFX_OK;
@@ -964,11 +992,21 @@ static void free_job(mfx_job *j) {
   for (auto &e : j->ev_pool)
     if (e) cudaEventDestroy(e);
   for (auto &x : j->xfer)
-    if (x) cudaStreamDestroy(x);
+    if (x) {
+      cudaStreamSynchronize(x);
+      cudaStreamDestroy(x);
+    }
+  if (j->ring) {
+    cudaFreeAsync(j->ring, j->stream);
+    cudaStreamSynchronize(j->stream);
+  }
+  for (auto &e : j->ring_free)
+    if (e) cudaEventDestroy(e);
+  if (j->fetched) cudaEventDestroy(j->fetched);
   if (j->stream) cudaStreamDestroy(j->stream);
   if (j->eng) {
     std::lock_guard<std::mutex> lk(j->eng->mu);
-    j->eng->in_use -= std::min(j->eng->in_use, j->arena_bytes);
+    j->eng->in_use -= std::min(j->eng->in_use, j->arena_bytes + 2 * j->ring_set_bytes);
   }
   delete j;
 }
@@ -1354,6 +1392,7 @@ int mfx_job_assemble(mfx_job *job, int orders_mask) {
   CU(cudaSetDevice(job->eng->device));
   job->ev_next = 0;
   job->prof_recs.clear();
+  if (job->fetched) CU(cudaStreamWaitEvent(job->stream, job->fetched, 0));  // downloads of these particles
   TRY(job->fp64 ? assemble_stage<double>(job, orders_mask) : assemble_stage<float>(job, orders_mask));
   CU(cudaStreamSynchronize(job->stream));
   return MFX_OK;
@@ -1392,6 +1431,7 @@ int mfx_job_capture(mfx_job *job) {
   if (!job) return set_error(MFX_EINVAL, "null job");
   CU(cudaSetDevice(job->eng->device));
   if (job->gexec) return MFX_OK;
+  if (job->ring) return set_error(MFX_ESTATE, "a job with an output ring cannot be captured");
   cudaGraph_t g = nullptr;
   TRY(capture_pipeline(job, &g));
   cudaError_t e = cudaGraphInstantiate(&job->gexec, g, 0);
@@ -1514,6 +1554,100 @@ int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
                       {ids, static_cast<char *>(job->ids) + is * first, is * count}};
   return download(job, xs, 3);
+  GUARD_END
+}
+
+int mfx_job_set_output_ring(mfx_job *job, int on) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
+  if (job->gexec) return set_error(MFX_ESTATE, "job already captured into a graph");
+  CU(cudaSetDevice(job->eng->device));
+  if (!on == !job->ring) return MFX_OK;
+  for (auto &x : job->xfer)
+    if (x) CU(cudaStreamSynchronize(x));
+  CU(cudaStreamSynchronize(job->stream));
+  mfx_engine *eng = job->eng;
+  if (!on) {
+    CU(cudaFreeAsync(job->ring, job->stream));
+    CU(cudaStreamSynchronize(job->stream));
+    job->ring = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(eng->mu);
+      eng->in_use -= std::min(eng->in_use, 2 * job->ring_set_bytes);
+    }
+    job->ring_set_bytes = 0;
+    // back to the arena's particle arrays (the last run's particles are gone)
+    job->has_run = false;
+    char *a = job->region;
+    job->pos = a;
+    a += align_up(job->npart * 3 * (job->d.pos64 ? 8 : 4));
+    job->vel = a;
+    a += align_up(job->npart * 3 * (job->d.vel64 ? 8 : 4));
+    job->ids = a;
+    return MFX_OK;
+  }
+  const size_t np = job->npart;
+  const size_t set = align_up(np * 3 * (job->d.pos64 ? 8 : 4)) + align_up(np * 3 * (job->d.vel64 ? 8 : 4)) +
+                     align_up(np * (job->d.id64 ? 8 : 4));
+  {
+    std::lock_guard<std::mutex> lk(eng->mu);
+    if (eng->in_use + 2 * set > eng->budget)
+      return set_error(MFX_EADMIT, "output ring needs %zu bytes, engine budget has %zu free", 2 * set,
+                       eng->budget - std::min(eng->budget, eng->in_use));
+    eng->in_use += 2 * set;
+  }
+  char *r = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&r), 2 * set, job->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(job->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    std::lock_guard<std::mutex> lk(eng->mu);
+    eng->in_use -= std::min(eng->in_use, 2 * set);
+    return set_error(MFX_ENOMEM, "output ring of %zu bytes: %s", 2 * set, cudaGetErrorString(e));
+  }
+  for (auto &ev : job->ring_free)
+    if (!ev) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  job->ring = r;
+  job->ring_set_bytes = set;
+  job->ring_next = 0;
+  job->has_run = false;
+  ring_point(job, 0);
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count, void *pos, void *vel, void *ids) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
+  if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has not produced particles");
+  if (first > job->npart || count > job->npart - first)
+    return set_error(MFX_EINVAL, "range [%zu, %zu) outside the %zu particles", first, first + count, job->npart);
+  CU(cudaSetDevice(job->eng->device));
+  if (!job->xfer[0]) CU(cudaStreamCreateWithFlags(&job->xfer[0], cudaStreamNonBlocking));
+  if (!job->fetched) CU(cudaEventCreateWithFlags(&job->fetched, cudaEventDisableTiming));
+  cudaStream_t x = job->xfer[0];
+  // after the job's work enqueued so far (the run whose particles these are)
+  CU(cudaEventRecord(job->fetched, job->stream));
+  CU(cudaStreamWaitEvent(x, job->fetched, 0));
+  const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
+  const Xfer xs[3] = {{pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
+                      {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
+                      {ids, static_cast<char *>(job->ids) + is * first, is * count}};
+  for (const Xfer &q : xs)
+    if (q.dst && q.bytes) CU(cudaMemcpyAsync(q.dst, q.src, q.bytes, cudaMemcpyDefault, x));
+  CU(cudaEventRecord(job->fetched, x));
+  if (job->ring) CU(cudaEventRecord(job->ring_free[job->ring_next ^ 1], x));
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_wait_fetch(mfx_job *job) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (job->xfer[0]) CU(cudaStreamSynchronize(job->xfer[0]));
+  return MFX_OK;
   GUARD_END
 }
 

@@ -310,6 +310,49 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
 }
 #endif
 
+#if defined(__CUDACC__)
+// One step of the in-place, multi-item form: NT threads each hold up to
+// ceil(PP J / NT) butterflies, read all of them (ld), meet at a barrier and
+// write them (st); pencil index fastest (the x/y tile layout).
+template <int L, int R, int NS, bool INV, int PP, int NT, class Ld, class St>
+__device__ __forceinline__ void mi_step(const float2 *tw, const Ld &ld, const St &st) {
+  using S = Step<L, R, NS, INV>;
+  constexpr int NI = PP * S::J, I = (NI + NT - 1) / NT;
+  float2 v[I][R];
+#pragma unroll
+  for (int it = 0; it < I; ++it) {
+    const int t = int(threadIdx.x) + it * NT;
+    if (t < NI) S::gather(t / PP, [&](int n) { return ld(t % PP, n); }, tw, v[it]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < I; ++it) {
+    const int t = int(threadIdx.x) + it * NT;
+    if (t < NI) S::scatter(t / PP, [&](int n, float2 x) { st(t % PP, n, x); }, v[it]);
+  }
+}
+
+// PP pencils of length L in place in buf (Tile<L, PP, true>), NT threads (fewer
+// than PP * maxJ: the tiles too wide for one butterfly per thread).  ld(q, n)
+// may read buf and st(q, k, v) may write it; the caller synchronises before
+// reading what st wrote.  One barrier per step and one between steps.
+template <int L, int PP, bool INV, int NT, class Ld, class St>
+__device__ __forceinline__ void pencil_fft_mi(float2 *buf, const float2 *tw, const Ld &ld, const St &st) {
+  using F = Fac<L>;
+  using T = Tile<L, PP, true>;
+  auto lb = [&](int q, int n) { return buf[T::at(q, n)]; };
+  auto sb = [&](int q, int n, float2 x) { buf[T::at(q, n)] = x; };
+  mi_step<L, F::R1, 1, INV, PP, NT>(tw, ld, sb);
+  __syncthreads();
+  if constexpr (F::steps == 3) {
+    mi_step<L, F::R2, F::R1, INV, PP, NT>(tw, lb, sb);
+    __syncthreads();
+  }
+  constexpr int RL = F::steps == 3 ? F::R3 : F::R2;
+  mi_step<L, RL, L / RL, INV, PP, NT>(tw, lb, st);
+}
+#endif
+
 // ---------------------------------------------------------------------------
 // index maps
 // ---------------------------------------------------------------------------
@@ -467,10 +510,37 @@ __device__ __forceinline__ void stage_rows(float2 *stage, const float2 *src, uns
   }
 }
 
+// x/y tile of P pencils.  Lean form, for tiles whose P * maxJ butterflies
+// exceed 1024 threads: a third as many threads, each holding up to three
+// butterflies of a step (registers for them: the register file is shared out
+// in whole warps per scheduler), and one tile buffer (in-place transforms)
+// beside the staging.
 template <int M, int P, int ROWS> struct XY {
-  static constexpr int threads = P * Fac<M>::maxJ;
-  static constexpr int minb = min_blocks(threads);
-  static constexpr size_t smem = size_t(M + 2 * Tile<M, P, true>::elems + 2 * ROWS * P) * sizeof(float2);
+  static constexpr bool lean = P * Fac<M>::maxJ > 1024;
+  static constexpr int threads = lean ? (P * Fac<M>::maxJ / 3) / 32 * 32 : P * Fac<M>::maxJ;
+  static constexpr int minb = lean ? 1 : min_blocks(threads);
+  static constexpr int nbuf = lean ? 1 : 2;
+  static constexpr size_t smem = size_t(M + nbuf * Tile<M, P, true>::elems + 2 * ROWS * P) * sizeof(float2);
+};
+
+// the transform of an x/y tile: pencil_fft, or pencil_fft_mi in the lean form
+// (buf2 == buf there)
+template <int M, int P, bool INV, class Ld, class St>
+__device__ __forceinline__ void xy_fft(float2 *buf, float2 *buf2, const float2 *tw, const Ld &ld, const St &st) {
+  if constexpr (XY<M, P, M>::lean)
+    pencil_fft_mi<M, P, INV, XY<M, P, M>::threads>(buf, tw, ld, st);
+  else
+    pencil_fft<M, P, true, INV>(buf, buf2, tw, ld, st);
+}
+// the tile buffers and the staging area of an x/y kernel's shared memory
+template <int M, int P> struct XYMem {
+  float2 *tw, *buf, *buf2, *stage;
+  __device__ __forceinline__ XYMem(float2 *base) {
+    tw = base;
+    buf = tw + M;
+    buf2 = XY<M, P, M>::lean ? buf : buf + Tile<M, P, true>::elems;
+    stage = buf + XY<M, P, M>::nbuf * Tile<M, P, true>::elems;
+  }
 };
 
 // The persistent unit loop: fetch(u, stage) issues unit u's copies,
@@ -500,7 +570,8 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::t
     k_ff_y3(FArgs a) {
   using D = Dims<M>;
   constexpr int ROWS = D::N, KB = D::Kh / P;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems, *stage = buf2 + Tile<M, P, true>::elems;
+  const XYMem<M, P> sm(ff_smem());
+  float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
   xy_units(
       unsigned(D::N * KB), ROWS * P, stage,
@@ -513,7 +584,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::t
 #pragma unroll 1
         for (int o = 0; o < 3; ++o) {
           float2 *out = a.dst[o] + (i * M * D::Kh + kz0);
-          pencil_fft<M, P, true, true>(
+          xy_fft<M, P, true>(
               buf, buf2, tw,
               [&](int q, int n) -> float2 {
                 const int j = unpad_index(n, D::N);
@@ -541,7 +612,8 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::t
     k_ff_x_inv(FArgs a) {
   using D = Dims<M>;
   constexpr int ROWS = D::N, KB = D::Kh / P;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems, *stage = buf2 + Tile<M, P, true>::elems;
+  const XYMem<M, P> sm(ff_smem());
+  float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
   const unsigned nsrc = a.mode ? unsigned(a.ncomp) : 3u;
   xy_units(
@@ -559,7 +631,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::t
         for (int k = 0; k < ncs; ++k) {
           const int c = a.mode ? int(s) : (s == 0 ? 2 * k : (s == 1 ? (k == 0 ? 3 : 5) : 1));
           float2 *out = a.dst[c] + off;
-          pencil_fft<M, P, true, true>(
+          xy_fft<M, P, true>(
               buf, buf2, tw,
               [&](int q, int n) -> float2 {
                 const int i = unpad_index(n, D::N);
@@ -584,7 +656,8 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::t
 template <int M, int P> __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_x_fwd(FArgs a) {
   using D = Dims<M>;
   constexpr int ROWS = M, KB = D::Kh / P;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + Tile<M, P, true>::elems, *stage = buf2 + Tile<M, P, true>::elems;
+  const XYMem<M, P> sm(ff_smem());
+  float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
   const unsigned nc = unsigned(a.ncomp);
   xy_units(
@@ -596,7 +669,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, M>::threads, 
       [&](unsigned u, const float2 *st) {
         const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
         float2 *dst = a.dst[c] + (yy * D::Kh + kz0);
-        pencil_fft<M, P, true, false>(
+        xy_fft<M, P, false>(
             buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
             [&](int q, int k, float2 v) {
               const int i = unpad_index(k, D::N);
@@ -617,7 +690,8 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
   using D = Dims<M>;
   using T = Tile<M, P, true>;
   constexpr int ROWS = M, KB = D::Kh / P;
-  float2 *tw = ff_smem(), *buf = tw + M, *buf2 = buf + T::elems, *stage = buf2 + T::elems;
+  const XYMem<M, P> sm(ff_smem());
+  float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
   const unsigned nc = unsigned(a.ncomp);
   xy_units(
@@ -632,7 +706,7 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
         if constexpr (MODE == 0) {
           const float kx = float(sidx(int(i), D::N)) * a.kfac;
           float2 *out = dst + i * D::N * D::nk + kz0;
-          pencil_fft<M, P, true, false>(
+          xy_fft<M, P, false>(
               buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
               [&](int q, int k, float2 v) {
                 const int j = unpad_index(k, D::N);
@@ -653,7 +727,7 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
           float2 *out = dst + (i * M * D::Kh + kz0);
           const bool row_kept = int(i) != D::nh;
           float2 *mid = obuf<M>(buf, buf2);
-          pencil_fft<M, P, true, false>(
+          xy_fft<M, P, false>(
               buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
               [&](int q, int k, float2 v) {
                 const int j = unpad_index(k, D::N);
@@ -661,7 +735,7 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
                 mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
               });
           __syncthreads();
-          pencil_fft<M, P, true, true>(
+          xy_fft<M, P, true>(
               buf, buf2, tw, [&](int q, int n) { return mid[T::at(q, n)]; },
               [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
         }

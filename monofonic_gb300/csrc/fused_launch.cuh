@@ -1,7 +1,7 @@
 // Host-side launchers of the fused transforms (fused.cuh), one instantiation
 // per padded length M (the ff_m*.cu translation units compile them in
 // parallel).  ff_launch_m<M> launches one pass with pencil tile `p`: pencils
-// per CTA for the x/y passes (4, 8 or 16); for the z passes 1 or 2 rows per
+// per CTA for the x/y passes (4, 8, 16 or 32); for the z passes 1 or 2 rows per
 // CTA, or 3: the wide shape (one row, many pencils per transform).
 #pragma once
 #include <cuda_runtime.h>
@@ -60,13 +60,17 @@ template <int M, int RW> constexpr bool ff_z_fits() {
   }
 }
 
+// an x/y tile of P pencils fits one CTA (threads, shared memory) and the kz range
+template <int M, int P> constexpr bool xy_ok() {
+  return (M / 3) % P == 0 && XY<M, P, M>::threads <= 1024 && XY<M, P, M>::smem <= kFFSmemMax;
+}
+
 template <int M> bool ff_valid_m(int op, int p) {
-  constexpr int Kh = M / 3;
   if (op == FF_ZSRC2 || op == FF_ZSRC3)
     return (p == 1 && ff_z_fits<M, 1>()) || (p == 2 && ff_z_fits<M, 2>()) || (p == 3 && ff_z_fits<M, 3>());
   if (op < 0 || op >= FF_NOPS) return false;
-  return (p == 4 || p == 8 || p == 16) && Kh % p == 0 && p * Fac<M>::maxJ <= 1024 &&
-         (size_t(M) + 4 * size_t(M) * p) * sizeof(float2) <= kFFSmemMax;
+  return (p == 4 && xy_ok<M, 4>()) || (p == 8 && xy_ok<M, 8>()) || (p == 16 && xy_ok<M, 16>()) ||
+         (p == 32 && xy_ok<M, 32>());
 }
 
 // lets a kernel instance use up to 227 KB of dynamic shared memory; the
@@ -104,7 +108,7 @@ template <class K> static unsigned ff_persistent_grid(K kernel, int threads, siz
   } while (0)
 
 template <int M, int P> cudaError_t ff_launch_xy(int op, const FArgs &a, cudaStream_t s) {
-  if constexpr (P * Fac<M>::maxJ > 1024 || (M / 3) % P != 0 || XY<M, P, M>::smem > kFFSmemMax) {
+  if constexpr (!xy_ok<M, P>()) {
     return cudaErrorInvalidConfiguration;
   } else {
     constexpr int N = 2 * M / 3, KB = (M / 3) / P;
@@ -167,7 +171,8 @@ template <int M> cudaError_t ff_launch_m(int op, int p, const FArgs &a, cudaStre
   switch (p) {
     case 4: return ff_launch_xy<M, 4>(op, a, s);
     case 8: return ff_launch_xy<M, 8>(op, a, s);
-    default: return ff_launch_xy<M, 16>(op, a, s);
+    case 16: return ff_launch_xy<M, 16>(op, a, s);
+    default: return ff_launch_xy<M, 32>(op, a, s);
   }
 }
 

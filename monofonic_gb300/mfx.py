@@ -31,7 +31,8 @@ EXPORTS = [
     "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
     "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
     "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
-    "mfx_cosmology_amp_table", "mfx_run_config",
+    "mfx_cosmology_amp_table", "mfx_run_config", "mfx_job_set_output_ring", "mfx_job_fetch_particles_range_async",
+    "mfx_job_wait_fetch",
 ]
 
 
@@ -117,6 +118,9 @@ def load(build_if_missing: bool = False):
     L.mfx_cosmology_growth.argtypes = [vp, dbl, C.POINTER(dbl)]
     L.mfx_cosmology_amp_table.argtypes = [vp, u32, dbl, vp, sz]
     L.mfx_run_config.argtypes = [vp, C.c_char_p]
+    L.mfx_job_set_output_ring.argtypes = [vp, i32]
+    L.mfx_job_fetch_particles_range_async.argtypes = [vp, sz, sz, vp, vp, vp]
+    L.mfx_job_wait_fetch.argtypes = [vp]
     _lib = L
     return L
 
@@ -368,6 +372,19 @@ class Job:
         L.mfx_job_fetch_particles_range.argtypes = [C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p, C.c_void_p,
                                                     C.c_void_p]
         check(L.mfx_job_fetch_particles_range(self._h, first, count, pos, vel, ids))
+
+    def set_output_ring(self, on: bool = True):
+        """Pipelined output: two particle sets outside the arena, so that a run
+        computes while the previous run's particles are still downloading."""
+        check(load().mfx_job_set_output_ring(self._h, 1 if on else 0))
+
+    def fetch_particles_range_async(self, first: int, count: int, pos, vel, ids):
+        """Enqueues the download of particles [first, first + count) of the last
+        run to page-locked host addresses and returns; wait_fetch() completes it."""
+        check(load().mfx_job_fetch_particles_range_async(self._h, first, count, pos, vel, ids))
+
+    def wait_fetch(self):
+        check(load().mfx_job_wait_fetch(self._h))
 
     def particles_range(self, first: int, count: int):
         """Particles [first, first + count) as numpy arrays."""

@@ -59,3 +59,40 @@ def test_ensemble_members_match_standalone_runs(mfxlib, engine):
     ref = run_alone(mfxlib, engine, specs[2])
     assert np.array_equal(again[0], ref[0])
     b.close()
+
+
+@pytest.mark.parametrize("ring", [True, False])
+def test_pipelined_downloads_match_runs_one_at_a_time(mfxlib, engine, ring):
+    """Asynchronous downloads, with the output ring (runs alternate between two
+    particle sets and compute while the previous run's particles download) and
+    without it (the next run waits): three runs of one job, three seeds through
+    mfx_job_upload, each run enqueued right after the previous run's download,
+    give each seed's particles of a run made alone."""
+    import torch
+    specs = [spec(mfxlib, 48, 150.0, 24.0, 3, s, lattice=1, precision=mfxlib.FP32C) for s in (31, 32, 33)]
+    refs = [run_alone(mfxlib, engine, sp) for sp in specs]
+    sp0 = specs[0]
+    j = mfxlib.Job(engine, 48, 150.0, 3, sp0["seed_table"], sp0["amp_table"], sp0["coef"], lattice=1,
+                   precision=mfxlib.FP32C, lunit=sp0["lunit"], vunit=sp0["vunit"])
+    if ring:
+        j.set_output_ring(True)
+    npart = j.num_particles
+    bufs = []
+    for _ in specs:
+        bufs.append((torch.empty((npart, 3), dtype=torch.float64 if j.pos64 else torch.float32, pin_memory=True),
+                     torch.empty((npart, 3), dtype=torch.float64 if j.vel64 else torch.float32, pin_memory=True),
+                     torch.empty(npart, dtype=torch.int64 if j.id64 else torch.int32, pin_memory=True)))
+    for sp, (p, v, i) in zip(specs, bufs):
+        j.upload(sp["seed_table"], sp["amp_table"])
+        j.run(wait=False)
+        j.fetch_particles_range_async(0, npart, p.data_ptr(), v.data_ptr(), i.data_ptr())
+    j.wait()
+    j.wait_fetch()
+    for ref, (p, v, i) in zip(refs, bufs):
+        assert np.array_equal(p.numpy(), ref[0])
+        assert np.array_equal(v.numpy(), ref[1])
+        assert np.array_equal(i.numpy().view(ref[2].dtype), ref[2])
+    # the synchronous fetch reads the last run's set
+    last = j.particles()
+    assert np.array_equal(last[0], refs[-1][0])
+    j.close()
