@@ -184,7 +184,9 @@ int mfx_job_destroy(mfx_job *job);
 
 /* Sets the pencil-tile shape of the fused transforms by hand (the choice
    mfx_job_autotune makes by timing): pencils per CTA of the x/y passes
-   (4, 8 or 16) and the z passes' shape: 1 or 2 rows per CTA, or 3 for one
+   (4, 8, 16 or 32; tiles wider than 1024 butterflies run in the lean form:
+   a third as many threads, in-place transforms) and the z passes' shape:
+   1 or 2 rows per CTA, or 3 for one
    row per CTA and as many pencils per transform as one CTA per SM holds
    (the wide shape of the long padded lengths), for both z passes (2LPT and
    3LPT sources).  MFX_EINVAL for a shape the padded length does not admit,

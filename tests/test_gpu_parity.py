@@ -285,7 +285,7 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     monkeypatch.setenv("MFX_FUSED", "1")
     j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
     pxy, pz = j.autotune()
-    assert pxy in (4, 8, 16) and pz in (1, 2, 3)
+    assert pxy in (4, 8, 16, 32) and pz in (1, 2, 3)
     j.run()
     fused = [j.field(f) for f in fids]
     pf = j.particles()
@@ -303,6 +303,29 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     assert np.sqrt(np.mean(((pf[0] - pr[0]) / delta) ** 2)) < 1e-6
     assert rel_l2(pf[1].astype(np.float64), pr[1].astype(np.float64)) < 5e-6
     assert np.array_equal(pf[2], pr[2])
+
+
+@pytest.mark.parametrize("n,lean,plain", [(192, 32, 8), (384, 16, 8)])
+def test_lean_xy_tiles_match_plain_tiles(mfxlib, engine, n, lean, plain, monkeypatch):
+    """x/y tiles too wide for one butterfly per thread (lean form: a third as
+    many threads, in-place transforms) give the fields and particles of the
+    plain tiles to rounding."""
+    monkeypatch.setenv("MFX_FUSED", "1")
+    c = Case(mfxlib, n, 300.0, 24.0, 3, 5, lattice=1, plt=engine.plt_table(1))
+    fids = [mfxlib.FIELD_PHI2, mfxlib.FIELD_PHI3, mfxlib.FIELD_A3X, mfxlib.FIELD_A3Z]
+    out = []
+    for p in (lean, plain):
+        j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
+        j.set_tiles(p, 1)
+        j.run()
+        out.append(([j.field(f) for f in fids], j.particles()))
+        j.close()
+    # FP32 rounding of the same sums (the A3 components carry the most cancellation)
+    for f, a, b in zip(fids, out[0][0], out[1][0]):
+        assert np.all(np.isfinite(a)) and rel_l2(a, b) < 5e-6, (f, rel_l2(a, b))
+    delta = c.L / (c.n * 2 ** (1 / 3.0))
+    assert np.sqrt(np.mean(((out[0][1][0] - out[1][1][0]) / delta) ** 2)) < 1e-7
+    assert rel_l2(out[0][1][1], out[1][1][1]) < 1e-6
 
 
 @pytest.mark.parametrize("n,lattice,order,plt", [(64, 2, 3, True), (96, 1, 2, False), (48, 2, 2, False)])
@@ -335,7 +358,7 @@ def test_fused_rerun_is_identical(mfxlib, engine, n, lattice, monkeypatch):
     c = Case(mfxlib, n, 300.0, 24.0, 3, 4242, lattice=lattice, plt=engine.plt_table(lattice))
     fids = [mfxlib.FIELD_PHI2, mfxlib.FIELD_PHI3, mfxlib.FIELD_A3Y]
     first = None
-    for pxy in (4, 8, 16):
+    for pxy in (4, 8, 16, 32):
         for pz in (1, 2, 3):
             j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
             try:
