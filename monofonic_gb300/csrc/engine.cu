@@ -728,6 +728,12 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   const char *env = getenv("MFX_FA_KEEP");
   const bool keep = !(env && env[0] == '0');
   const int nsub = (keep && ns > 1 && ff::fa_keep(j->M) && j->group >= ns) ? ns : 1;
+  // ASM1 in halves (tiles of 8 pencils) from N = 384 up, where the x pass's
+  // 32-byte row pieces of the 4-pencil tiles lie megabytes apart (768^3 FCC:
+  // 57 -> 44 ms; 256^3 BCC: 0.63 -> 0.93 ms, so not there); MFX_FA_HALVES
+  // = 0 / 1 in the environment forces it off / on (for comparisons)
+  const char *envh = getenv("MFX_FA_HALVES");
+  const bool halves = nsub > 1 && ff::fa_halves(j->M) && (envh ? envh[0] == '1' : N >= 384);
   const bool plt = as.plt != nullptr;
   ff::FAArgs fa{};
   fa.as = as;
@@ -744,6 +750,7 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   fa.vscale = vscale;
   fa.vunscale = 1.0 / double(vscale);
   fa.vunscale_f = float(fa.vunscale);
+  fa.halves = halves ? 1 : 0;
   auto pass = [&](int op, const char *name, double bytes) -> int {
     KBEGIN(j);
     const cudaError_t e = ff::fa_launch(j->M, op, plt, fa, j->stream);

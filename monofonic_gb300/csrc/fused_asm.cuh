@@ -29,6 +29,7 @@ struct FAArgs {
   float2 *q[6];           // component fields [N][N][N/2] of sub-lattice `shift` (ASM2 in place, ASM3 input)
   float2 *qx[24];         // ASM1 output: component c of sub-lattice shift + s at qx[6 s + c], s < nsub
   int nsub;               // sub-lattices ASM1 emits from one assembly of each mode (1 unless FA::keep)
+  int halves;             // ASM1 in halves (tiles of 8 pencils; FA::halves), with nsub > 1
   const float2 *tw;       // W_N^t, t < N
   int *status;            // set when a bounded wait ran out
   int shift;              // sub-lattice
@@ -73,6 +74,14 @@ template <int N> struct FA {
   static constexpr bool keep = s1k_of<CGK> <= kKeepMax;
   static constexpr int t1k = CGK * P * maxJ;
   static constexpr size_t s1k = s1k_of<CGK>;
+  // ASM1 in halves (x8): tiles of 8 pencils (64-byte row pieces instead of 32),
+  // each mode assembled twice — once for the three displacement components,
+  // once for the three velocity components, each half kept in shared memory —
+  // and every component transformed in place (one tile buffer)
+  static constexpr int P8 = 8;
+  static constexpr int t1h = 384;
+  static constexpr size_t s1h = size_t(N + N * P8 + 3 * N * P8) * sizeof(float2);
+  static constexpr bool halves = Kh % P8 == 0 && s1h <= 227 * 1024;
   static constexpr size_t s2 = size_t(N + nbuf * Tile<N, P2, true>::elems + 2 * N * P2) * sizeof(float2);
   static constexpr size_t head = 32;
   static constexpr size_t s3 = head + size_t(N) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
@@ -145,6 +154,54 @@ __global__ void __launch_bounds__(KEEP ? FA<N>::t1k : FA<N>::t1, min_blocks(KEEP
               a.qx[s * 6 + g0 + c][(unsigned(x) * N + j) * F::Kh + kz0 + p] = v;
             });
         __syncthreads();  // the next round assembles into buf
+      }
+    }
+  }
+}
+
+// ASM1 in halves: as the KEEP form, with tiles of 8 pencils and the six
+// components in two halves of three (the displacement, then the velocity
+// components), each half from its own assembly of the tile's modes; every
+// (sub-lattice, component) pencil set is transformed in place.
+template <int N, bool PLT>
+__global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
+  using F = FA<N>;
+  constexpr int P = F::P8, KB = F::Kh / P, NT = F::t1h;
+  using T = Tile<N, P, true>;
+  float2 *tw = ff_smem(), *buf = tw + N, *pv = buf + T::elems;  // pv [3][mode]
+  load_tw<N>(tw, a.tw);
+#pragma unroll 1
+  for (unsigned u = blockIdx.x; u < unsigned(N * KB); u += gridDim.x) {
+    const int j = int(u / KB), kz0 = int(u % KB) * P;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      // each thread later reads back only the entries it wrote here
+      for (int t = threadIdx.x; t < N * P; t += NT) {
+        const int i = t / P, p = t - (t / P) * P, kz = kz0 + p;
+        float2 Pm[3], Vm[3];
+        asm_mode<float, PLT>(a.as, i, j, kz, (size_t(i) * N + j) * F::nk + kz, Pm, Vm);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          pv[c * (N * P) + t] = h == 0 ? Pm[c] : make_float2(Vm[c].x * a.vscale, Vm[c].y * a.vscale);
+      }
+#pragma unroll 1
+      for (int s = 0; s < a.nsub; ++s) {
+#pragma unroll 1
+        for (int c = 0; c < 3; ++c) {
+          // the previous transform's last step has read buf before its barrier
+          for (int t = threadIdx.x; t < N * P; t += NT) {
+            const int i = t / P, p = t - (t / P) * P;
+            float er, ei;
+            lattice_phase<float>(a.as, a.shift + s, i, j, kz0 + p, er, ei);
+            const float2 v = pv[c * (N * P) + t];
+            buf[T::at(p, i)] = make_float2(v.x * er - v.y * ei, v.x * ei + v.y * er);
+          }
+          __syncthreads();
+          float2 *dst = a.qx[s * 6 + 3 * h + c] + (unsigned(j) * F::Kh + kz0);
+          pencil_fft_mi<N, P, true, NT>(
+              buf, tw, [&](int q, int n) { return buf[T::at(q, n)]; },
+              [&](int q, int x, float2 v) { dst[unsigned(x) * N * F::Kh + q] = v; });
+        }
       }
     }
   }

@@ -188,7 +188,14 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
     constexpr size_t units1 = size_t(N) * (F::Kh / F::P);
     switch (op) {
       case FA_X:
-        if (a.nsub > 1) {
+        if (a.nsub > 1 && a.halves) {
+          if constexpr (F::halves) {
+            if (plt) MFX_FF_PERSISTENT((k_fa_x_halves<N, true>), F::t1h, F::s1h, size_t(N) * (F::Kh / F::P8), s, a);
+            else MFX_FF_PERSISTENT((k_fa_x_halves<N, false>), F::t1h, F::s1h, size_t(N) * (F::Kh / F::P8), s, a);
+          } else {
+            return cudaErrorInvalidValue;
+          }
+        } else if (a.nsub > 1) {
           if constexpr (F::keep) {
             if (plt) MFX_FF_PERSISTENT((k_fa_x<N, true, true>), F::t1k, F::s1k, units1, s, a);
             else MFX_FF_PERSISTENT((k_fa_x<N, false, true>), F::t1k, F::s1k, units1, s, a);
@@ -219,6 +226,7 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
   cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s);     \
   cudaError_t fa_launch_##M(int op, bool plt, const FAArgs &a, cudaStream_t s); \
   bool fa_keep_##M();                                                           \
+  bool fa_halves_##M();                                                         \
   bool ff_valid_##M(int op, int p);
 MFX_FF_LENGTHS(MFX_FF_DECL)
 #undef MFX_FF_DECL
@@ -229,6 +237,7 @@ MFX_FF_LENGTHS(MFX_FF_DECL)
     return fa_launch_m<M>(op, plt, a, s);                                                                      \
   }                                                                                                            \
   bool fa_keep_##M() { return FA<2 * M / 3>::keep; }                                                          \
+  bool fa_halves_##M() { return FA<2 * M / 3>::halves; }                                                      \
   bool ff_valid_##M(int op, int p) { return ff_valid_m<M>(op, p); }
 
 inline bool ff_length_supported(int M) {
@@ -250,6 +259,15 @@ inline int ff_maxj(int M) {
 inline bool ff_valid(int M, int op, int p) {
 #define MFX_FF_CASE(L) \
   if (M == L) return ff_valid_##L(op, p);
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return false;
+}
+
+// whether ASM1 in halves (tiles of 8 pencils) is built for this length
+inline bool fa_halves(int M) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return fa_halves_##L();
   MFX_FF_LENGTHS(MFX_FF_CASE)
 #undef MFX_FF_CASE
   return false;

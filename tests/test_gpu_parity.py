@@ -331,22 +331,27 @@ def test_lean_xy_tiles_match_plain_tiles(mfxlib, engine, n, lean, plain, monkeyp
 @pytest.mark.parametrize("n,lattice,order,plt", [(64, 2, 3, True), (96, 1, 2, False), (48, 2, 2, False)])
 def test_fused_assembly_once_for_all_sublattices(mfxlib, engine, n, lattice, order, plt, monkeypatch):
     """Fused assembly: each mode assembled once and all sub-lattices emitted
-    from it gives the particles of the per-sub-lattice assembly."""
+    from it (tiles of 4 pencils, or of 8 in halves) gives the particles of the
+    per-sub-lattice assembly."""
     tab = engine.plt_table(lattice) if plt else None
     c = Case(mfxlib, n, 300.0, 24.0, order, 99, lattice=lattice, plt=tab)
     monkeypatch.setenv("MFX_FUSED", "1")
     out = []
-    for keep in ("1", "0"):
+    # all sub-lattices from one assembly (tiles of 4), the same in halves
+    # (tiles of 8, each half assembled on its own), one sub-lattice at a time
+    for keep, halves in (("1", "0"), ("1", "1"), ("0", "0")):
         monkeypatch.setenv("MFX_FA_KEEP", keep)
+        monkeypatch.setenv("MFX_FA_HALVES", halves)
         j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
         j.run()
         out.append(j.particles())
         j.close()
     delta = c.L / (c.n * 2 ** (lattice / 3.0))
-    assert np.all(np.isfinite(out[0][0])) and np.all(np.isfinite(out[0][1]))
-    assert np.sqrt(np.mean(((out[0][0] - out[1][0]) / delta) ** 2)) < 1e-7
-    assert rel_l2(out[0][1].astype(np.float64), out[1][1].astype(np.float64)) < 1e-6
-    assert np.array_equal(out[0][2], out[1][2])
+    for o in out[1:]:
+        assert np.all(np.isfinite(o[0])) and np.all(np.isfinite(o[1]))
+        assert np.sqrt(np.mean(((out[0][0] - o[0]) / delta) ** 2)) < 1e-7
+        assert rel_l2(out[0][1].astype(np.float64), o[1].astype(np.float64)) < 1e-6
+        assert np.array_equal(out[0][2], o[2])
 
 
 @pytest.mark.parametrize("n,lattice", [(64, 2), (48, 2)])
