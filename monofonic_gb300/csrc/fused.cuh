@@ -313,8 +313,8 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
 #if defined(__CUDACC__)
 // One step of the in-place, multi-item form: NT threads each hold up to
 // ceil(PP J / NT) butterflies, read all of them (ld), meet at a barrier and
-// write them (st); pencil index fastest (the x/y tile layout).
-template <int L, int R, int NS, bool INV, int PP, int NT, class Ld, class St>
+// write them (st); task order as split<PP, J, PF>.
+template <int L, int R, int NS, bool INV, int PP, bool PF, int NT, class Ld, class St>
 __device__ __forceinline__ void mi_step(const float2 *tw, const Ld &ld, const St &st) {
   using S = Step<L, R, NS, INV>;
   constexpr int NI = PP * S::J, I = (NI + NT - 1) / NT;
@@ -322,34 +322,43 @@ __device__ __forceinline__ void mi_step(const float2 *tw, const Ld &ld, const St
 #pragma unroll
   for (int it = 0; it < I; ++it) {
     const int t = int(threadIdx.x) + it * NT;
-    if (t < NI) S::gather(t / PP, [&](int n) { return ld(t % PP, n); }, tw, v[it]);
+    if (t < NI) {
+      int q, j;
+      split<PP, S::J, PF>(t, q, j);
+      S::gather(j, [&](int n) { return ld(q, n); }, tw, v[it]);
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < I; ++it) {
     const int t = int(threadIdx.x) + it * NT;
-    if (t < NI) S::scatter(t / PP, [&](int n, float2 x) { st(t % PP, n, x); }, v[it]);
+    if (t < NI) {
+      int q, j;
+      split<PP, S::J, PF>(t, q, j);
+      S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v[it]);
+    }
   }
 }
 
-// PP pencils of length L in place in buf (Tile<L, PP, true>), NT threads (fewer
-// than PP * maxJ: the tiles too wide for one butterfly per thread).  ld(q, n)
-// may read buf and st(q, k, v) may write it; the caller synchronises before
-// reading what st wrote.  One barrier per step and one between steps.
-template <int L, int PP, bool INV, int NT, class Ld, class St>
+// PP pencils of length L in place in buf (Tile<L, PP, PF>), NT threads (for
+// the x/y tiles fewer than PP * maxJ: the tiles too wide for one butterfly
+// per thread).  ld(q, n) may read buf and st(q, k, v) may write it; the
+// caller synchronises before reading what st wrote.  One barrier per step and
+// one between steps.
+template <int L, int PP, bool PF, bool INV, int NT, class Ld, class St>
 __device__ __forceinline__ void pencil_fft_mi(float2 *buf, const float2 *tw, const Ld &ld, const St &st) {
   using F = Fac<L>;
-  using T = Tile<L, PP, true>;
+  using T = Tile<L, PP, PF>;
   auto lb = [&](int q, int n) { return buf[T::at(q, n)]; };
   auto sb = [&](int q, int n, float2 x) { buf[T::at(q, n)] = x; };
-  mi_step<L, F::R1, 1, INV, PP, NT>(tw, ld, sb);
+  mi_step<L, F::R1, 1, INV, PP, PF, NT>(tw, ld, sb);
   __syncthreads();
   if constexpr (F::steps == 3) {
-    mi_step<L, F::R2, F::R1, INV, PP, NT>(tw, lb, sb);
+    mi_step<L, F::R2, F::R1, INV, PP, PF, NT>(tw, lb, sb);
     __syncthreads();
   }
   constexpr int RL = F::steps == 3 ? F::R3 : F::R2;
-  mi_step<L, RL, L / RL, INV, PP, NT>(tw, lb, st);
+  mi_step<L, RL, L / RL, INV, PP, PF, NT>(tw, lb, st);
 }
 #endif
 
@@ -528,7 +537,7 @@ template <int M, int P, int ROWS> struct XY {
 template <int M, int P, bool INV, class Ld, class St>
 __device__ __forceinline__ void xy_fft(float2 *buf, float2 *buf2, const float2 *tw, const Ld &ld, const St &st) {
   if constexpr (XY<M, P, M>::lean)
-    pencil_fft_mi<M, P, INV, XY<M, P, M>::threads>(buf, tw, ld, st);
+    pencil_fft_mi<M, P, true, INV, XY<M, P, M>::threads>(buf, tw, ld, st);
   else
     pencil_fft<M, P, true, INV>(buf, buf2, tw, ld, st);
 }

@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
           }
           __syncthreads();
           float2 *dst = a.qx[s * 6 + 3 * h + c] + (unsigned(j) * F::Kh + kz0);
-          pencil_fft_mi<N, P, true, NT>(
+          pencil_fft_mi<N, P, true, true, NT>(
               buf, tw, [&](int q, int n) { return buf[T::at(q, n)]; },
               [&](int q, int x, float2 v) { dst[unsigned(x) * N * F::Kh + q] = v; });
         }
