@@ -186,10 +186,11 @@ int mfx_job_destroy(mfx_job *job);
    mfx_job_autotune makes by timing): pencils per CTA of the x/y passes
    (4, 8, 16 or 32; tiles wider than 1024 butterflies run in the lean form:
    a third as many threads, in-place transforms) and the z passes' shape:
-   1 or 2 rows per CTA, or 3 for one
-   row per CTA and as many pencils per transform as one CTA per SM holds
-   (the wide shape of the long padded lengths), for both z passes (2LPT and
-   3LPT sources).  MFX_EINVAL for a shape the padded length does not admit,
+   1 or 2 rows per CTA, 3 for one row per CTA and as many pencils per
+   transform as one CTA per SM holds (the wide shape of the long padded
+   lengths), or 4 for one row per CTA of three warps, each pencil transformed
+   by one warp (padded lengths up to 576), for both z passes (2LPT and 3LPT
+   sources).  MFX_EINVAL for a shape the padded length does not admit,
    MFX_ESTATE for a job without the fused transforms. */
 int mfx_job_set_tiles(mfx_job *job, int pencils_xy, int rows_z);
 /* Autotuner of the FP32 form's fused transforms: times every admissible

@@ -670,7 +670,7 @@ static int autotune_fused(mfx_job *j) {
   for (int op : {ff::FF_ZSRC2, ff::FF_ZSRC3}) {
     if (op == ff::FF_ZSRC3 && j->d.lpt_order < 3) continue;
     tbest = 1e30f;
-    for (int p : {1, 2, 3}) {
+    for (int p : {1, 2, 3, 4}) {
       if (rc != MFX_OK || !ff::ff_valid(M, op, p)) continue;
       const float t = timed([&] {
         ff::FArgs z = ff_args(j);

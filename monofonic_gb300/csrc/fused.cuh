@@ -966,15 +966,16 @@ __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
   }
 }
 
+// the sources of one z element from its pair slots hp[c * stride] (slot c:
+// fields 2c, 2c + 1), formed in place
 // ZSRC2: phi1 Hessians (src[0..5], C-space) -> 2LPT source (dst[0]) and, with
 // mode 1, the five first-pair products of convolve3 (dst[1..5]).
-template <int M, int RW, int G, int MODE, bool WIDE>
-__global__ void __launch_bounds__(ZR<M, RW, G, 6, WIDE>::threads, ZR<M, RW, G, 6, WIDE>::minb) k_ff_zsrc2(FArgs a) {
-  z_rows<M, RW, G, 6, MODE ? 6 : 1>(a, [&](float2 *hp) {
+template <int MODE> struct Src2 {
+  __device__ __forceinline__ void operator()(float2 *hp, int stride) const {
     float v[6], s[6];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float2 x = hp[c * M];
+      const float2 x = hp[c * stride];
       v[2 * c] = x.x;
       v[2 * c + 1] = x.y;
     }
@@ -982,31 +983,199 @@ __global__ void __launch_bounds__(ZR<M, RW, G, 6, WIDE>::threads, ZR<M, RW, G, 6
     if (MODE) {
       pair_products(v, s + 1);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) hp[c * M] = make_float2(s[2 * c], s[2 * c + 1]);
+      for (int c = 0; c < 3; ++c) hp[c * stride] = make_float2(s[2 * c], s[2 * c + 1]);
     } else {
       hp[0].x = s[0];
     }
-  });
-}
-
+  }
+};
 // ZSRC3: phi1 Hessians src[0..5], phi2 Hessians src[6..11] and the truncated
 // pair products src[12..16] (C-space) -> phi3 source (dst[0]) and A3 (dst[1..3]).
 // The outputs may alias inputs: a row's spectra are staged before any of its
 // outputs is written.
-template <int M, int RW, int G, bool WIDE>
-__global__ void __launch_bounds__(ZR<M, RW, G, 17, WIDE>::threads, ZR<M, RW, G, 17, WIDE>::minb) k_ff_zsrc3(FArgs a) {
-  z_rows<M, RW, G, 17, 4>(a, [&](float2 *hp) {
+struct Src3 {
+  __device__ __forceinline__ void operator()(float2 *hp, int stride) const {
     float f[18], s[4];
 #pragma unroll
     for (int c = 0; c < 9; ++c) {
-      const float2 x = hp[c * M];
+      const float2 x = hp[c * stride];
       f[2 * c] = x.x;
       f[2 * c + 1] = x.y;
     }
     src_phi3(f, f + 6, f + 12, s);
     hp[0] = make_float2(s[0], s[1]);
-    hp[M] = make_float2(s[2], s[3]);
-  });
+    hp[stride] = make_float2(s[2], s[3]);
+  }
+};
+
+template <int M, int RW, int G, int MODE, bool WIDE>
+__global__ void __launch_bounds__(ZR<M, RW, G, 6, WIDE>::threads, ZR<M, RW, G, 6, WIDE>::minb) k_ff_zsrc2(FArgs a) {
+  z_rows<M, RW, G, 6, MODE ? 6 : 1>(a, [&](float2 *hp) { Src2<MODE>()(hp, M); });
+}
+
+template <int M, int RW, int G, bool WIDE>
+__global__ void __launch_bounds__(ZR<M, RW, G, 17, WIDE>::threads, ZR<M, RW, G, 17, WIDE>::minb) k_ff_zsrc3(FArgs a) {
+  z_rows<M, RW, G, 17, 4>(a, [&](float2 *hp) { Src3()(hp, M); });
+}
+
+// ---------------------------------------------------------------------------
+// Warp z passes (z tile 4): one row per group, three warps per CTA, each
+// complex pencil transformed by one warp in place in its own padded slot of
+// the row scratch with __syncwarp between the steps: three CTA barriers per
+// row (staged inputs in, inverse transforms done, sources formed) instead of
+// two per transform.  For lengths whose steps have at most 96 butterflies
+// (three per lane).
+// ---------------------------------------------------------------------------
+template <int L> struct WP {
+  static constexpr int padL = L + (L >> 4);
+  MFX_HD static int at(int n) { return n + (n >> 4); }
+};
+
+template <int L, int R, int NS, bool INV, class Ld, class St>
+__device__ __forceinline__ void warp_step(const float2 *tw, int lane, const Ld &ld, const St &st) {
+  using S = Step<L, R, NS, INV>;
+  constexpr int I = (S::J + 31) / 32;
+  float2 v[I][R];
+#pragma unroll
+  for (int it = 0; it < I; ++it) {
+    const int j = lane + 32 * it;
+    if (j < S::J) S::gather(j, ld, tw, v[it]);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int it = 0; it < I; ++it) {
+    const int j = lane + 32 * it;
+    if (j < S::J) S::scatter(j, st, v[it]);
+  }
+  __syncwarp();
+}
+
+// one pencil of length L through one warp, in place in p (WP layout): ld(n)
+// gives input n (it may read p); output k lands in p[WP<L>::at(k)]
+template <int L, bool INV, class Ld>
+__device__ __forceinline__ void warp_fft(float2 *p, const float2 *tw, const Ld &ld) {
+  using F = Fac<L>;
+  const int lane = int(threadIdx.x) & 31;
+  auto lp = [&](int n) { return p[WP<L>::at(n)]; };
+  auto sp = [&](int n, float2 x) { p[WP<L>::at(n)] = x; };
+  warp_step<L, F::R1, 1, INV>(tw, lane, ld, sp);
+  if constexpr (F::steps == 3) warp_step<L, F::R2, F::R1, INV>(tw, lane, lp, sp);
+  constexpr int RL = F::steps == 3 ? F::R3 : F::R2;
+  warp_step<L, RL, L / RL, INV>(tw, lane, lp, sp);
+}
+
+template <int M, int NIN> struct ZW {
+  using D = Dims<M>;
+  static constexpr int NPI = (NIN + (NIN & 1)) / 2;  // complex pencils of the inverse transforms
+  static constexpr int warps = 3;                     // each takes NPI / 3 pencils (3 or 1)
+  static_assert(NPI % warps == 0, "whole pencils per warp");
+  static constexpr int threads = 32 * warps;
+  static constexpr int padL = WP<M>::padL;
+  static constexpr size_t head = 32;
+  static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(NIN * D::Kh) * sizeof(float2) +
+                                 size_t(NPI * padL) * sizeof(float2);
+  // CTAs per SM by shared memory and by about 128 registers a thread (a lane
+  // holds up to three butterflies of a step)
+  static constexpr int by_smem = int(233472 / (smem + 1024));
+  static constexpr int by_regs = 65536 / (threads * 128) < 1 ? 1 : 65536 / (threads * 128);
+  static constexpr int minb = by_regs < by_smem ? by_regs : (by_smem < 1 ? 1 : by_smem);
+  static constexpr bool ok = Fac<M>::maxJ <= 96;
+};
+
+template <int M, int NIN, int NOUT, class Src>
+__device__ __forceinline__ void z_rows_w(const FArgs &a, const Src &sources) {
+  using Z = ZW<M, NIN>;
+  using D = Dims<M>;
+  constexpr int NPO = (NOUT + 1) / 2, padL = Z::padL;
+  char *base = reinterpret_cast<char *>(ff_smem());
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base);
+  volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
+  float2 *tw = reinterpret_cast<float2 *>(base + Z::head);
+  float2 *stage = tw + M;           // [c][Kh]
+  float2 *h = stage + NIN * D::Kh;  // pencil p at h + p * padL (WP layout)
+  const size_t ngroups = size_t(M) * M;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    *flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  load_tw<M>(tw, a.tw);  // includes a barrier
+  const int warp = int(threadIdx.x) >> 5, lane = int(threadIdx.x) & 31;
+  size_t g = blockIdx.x;
+  if (threadIdx.x == 0 && g < ngroups) z_fetch<M, 1, NIN>(a, g, stage, bar);
+#pragma unroll 1
+  for (uint32_t it = 0; g < ngroups; ++it, g += gridDim.x) {
+    const size_t gn = g + gridDim.x;
+    if (threadIdx.x == 0 && !mbar_wait_bounded(bar, it & 1)) *flag = 1;
+    __syncthreads();
+    if (*flag) {
+      // the copies did not land: report, let them finish (bounded), leave
+      if (threadIdx.x == 0) {
+        if (a.status) atomicExch(a.status, 1);
+        mbar_wait_bounded(bar, it & 1);
+      }
+      return;
+    }
+#pragma unroll 1
+    for (int pc = warp; pc < Z::NPI; pc += Z::warps) {
+      // inverse transform of pencil pc: fields (2 pc, 2 pc + 1) as A + iB
+      const int c0 = 2 * pc, c1 = c0 + 1;
+      warp_fft<M, true>(h + pc * padL, tw, [&](int n) -> float2 {
+        int m;
+        bool conj;
+        if (n < D::Kh) {
+          m = n;
+          conj = false;
+        } else if (n > M - D::Kh) {
+          m = M - n;
+          conj = true;
+        } else {
+          return make_float2(0.f, 0.f);
+        }
+        float2 va = stage[c0 * D::Kh + m];
+        float2 vb = c1 < NIN ? stage[c1 * D::Kh + m] : make_float2(0.f, 0.f);
+        if (m == 0) {
+          va.y = 0.f;
+          vb.y = 0.f;
+        }
+        return conj ? pack_pair_conj(va, vb) : pack_pair(va, vb);
+      });
+    }
+    __syncthreads();  // the stage is free; every field of the row is in h
+    if (threadIdx.x == 0 && gn < ngroups) z_fetch<M, 1, NIN>(a, gn, stage, bar);
+    for (int n = threadIdx.x; n < M; n += blockDim.x) sources(h + WP<M>::at(n), padL);
+    __syncthreads();
+#pragma unroll 1
+    for (int pc = warp; pc < NPO; pc += Z::warps) {
+      // forward transform of sources (2 pc, 2 pc + 1) and their kz < Kh spectra
+      float2 *hp = h + pc * padL;
+      const bool odd_last = (NOUT & 1) && pc == NPO - 1;
+      warp_fft<M, false>(hp, tw, [&](int n) -> float2 {
+        float2 v = hp[WP<M>::at(n)];
+        if (odd_last) v.y = 0.f;
+        return v;
+      });
+      const int f0 = 2 * pc, f1 = f0 + 1;
+      for (int k = lane; k < D::Kh; k += 32) {
+        const float2 z = hp[WP<M>::at(k)], zm = hp[WP<M>::at(k == 0 ? 0 : M - k)];
+        float2 sa, sb;
+        unpack_pair(z, zm, sa, sb);
+        a.dst[f0][g * D::Kh + k] = sa;
+        if (f1 < NOUT) a.dst[f1][g * D::Kh + k] = sb;
+      }
+    }
+    // h is rewritten after the barrier at the top of the next row
+  }
+}
+
+template <int M, int MODE>
+__global__ void __launch_bounds__(ZW<M, 6>::threads, ZW<M, 6>::minb) k_ff_zsrc2w(FArgs a) {
+  z_rows_w<M, 6, MODE ? 6 : 1>(a, Src2<MODE>());
+}
+
+template <int M>
+__global__ void __launch_bounds__(ZW<M, 17>::threads, ZW<M, 17>::minb) k_ff_zsrc3w(FArgs a) {
+  z_rows_w<M, 17, 4>(a, Src3());
 }
 #endif
 

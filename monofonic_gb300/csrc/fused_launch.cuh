@@ -2,7 +2,8 @@
 // per padded length M (the ff_m*.cu translation units compile them in
 // parallel).  ff_launch_m<M> launches one pass with pencil tile `p`: pencils
 // per CTA for the x/y passes (4, 8, 16 or 32); for the z passes 1 or 2 rows per
-// CTA, or 3: the wide shape (one row, many pencils per transform).
+// CTA, 3: the wide shape (one row, many pencils per transform), 4: the warp
+// passes (one row, one warp per pencil).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -53,7 +54,9 @@ template <int M, int NIN> struct ZGW {
 };
 
 template <int M, int RW> constexpr bool ff_z_fits() {
-  if constexpr (RW == 3) {
+  if constexpr (RW == 4) {
+    return ZW<M, 17>::ok && ZW<M, 17>::smem <= kFFSmemMax && ZW<M, 6>::smem <= kFFSmemMax;
+  } else if constexpr (RW == 3) {
     return ZGW<M, 6>::G > 0 && ZGW<M, 17>::G > 0;
   } else {
     return ZR<M, RW, ZG<M, RW, 6>::G, 6>::smem <= kFFSmemMax && ZR<M, RW, ZG<M, RW, 17>::G, 17>::smem <= kFFSmemMax;
@@ -67,7 +70,8 @@ template <int M, int P> constexpr bool xy_ok() {
 
 template <int M> bool ff_valid_m(int op, int p) {
   if (op == FF_ZSRC2 || op == FF_ZSRC3)
-    return (p == 1 && ff_z_fits<M, 1>()) || (p == 2 && ff_z_fits<M, 2>()) || (p == 3 && ff_z_fits<M, 3>());
+    return (p == 1 && ff_z_fits<M, 1>()) || (p == 2 && ff_z_fits<M, 2>()) || (p == 3 && ff_z_fits<M, 3>()) ||
+           (p == 4 && ff_z_fits<M, 4>());
   if (op < 0 || op >= FF_NOPS) return false;
   return (p == 4 && xy_ok<M, 4>()) || (p == 8 && xy_ok<M, 8>()) || (p == 16 && xy_ok<M, 16>()) ||
          (p == 32 && xy_ok<M, 32>());
@@ -138,10 +142,24 @@ template <int M, int P> cudaError_t ff_launch_xy(int op, const FArgs &a, cudaStr
   }
 }
 
-// z tile p: 1 and 2 rows per group (two tile buffers), 3 the wide shape
+// z tile p: 1 and 2 rows per group (two tile buffers), 3 the wide shape, 4
+// the warp passes
 template <int M, int P> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStream_t s) {
   if constexpr (!ff_z_fits<M, P>()) {
     return cudaErrorInvalidConfiguration;
+  } else if constexpr (P == 4) {
+    const size_t groups = size_t(M) * M;
+    if (op == FF_ZSRC2) {
+      using Z = ZW<M, 6>;
+      if (a.mode)
+        MFX_FF_PERSISTENT((k_ff_zsrc2w<M, 1>), Z::threads, Z::smem, groups, s, a);
+      else
+        MFX_FF_PERSISTENT((k_ff_zsrc2w<M, 0>), Z::threads, Z::smem, groups, s, a);
+    } else {
+      using Z = ZW<M, 17>;
+      MFX_FF_PERSISTENT((k_ff_zsrc3w<M>), Z::threads, Z::smem, groups, s, a);
+    }
+    return cudaGetLastError();
   } else {
     constexpr int RW = P == 3 ? 1 : P;
     constexpr bool W = P == 3;
@@ -166,8 +184,14 @@ template <int M, int P> cudaError_t ff_launch_z(int op, const FArgs &a, cudaStre
 
 template <int M> cudaError_t ff_launch_m(int op, int p, const FArgs &a, cudaStream_t s) {
   if (!ff_valid_m<M>(op, p)) return cudaErrorInvalidConfiguration;
-  if (op == FF_ZSRC2 || op == FF_ZSRC3)
-    return p == 1 ? ff_launch_z<M, 1>(op, a, s) : (p == 2 ? ff_launch_z<M, 2>(op, a, s) : ff_launch_z<M, 3>(op, a, s));
+  if (op == FF_ZSRC2 || op == FF_ZSRC3) {
+    switch (p) {
+      case 1: return ff_launch_z<M, 1>(op, a, s);
+      case 2: return ff_launch_z<M, 2>(op, a, s);
+      case 3: return ff_launch_z<M, 3>(op, a, s);
+      default: return ff_launch_z<M, 4>(op, a, s);
+    }
+  }
   switch (p) {
     case 4: return ff_launch_xy<M, 4>(op, a, s);
     case 8: return ff_launch_xy<M, 8>(op, a, s);

@@ -285,7 +285,7 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     monkeypatch.setenv("MFX_FUSED", "1")
     j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
     pxy, pz = j.autotune()
-    assert pxy in (4, 8, 16, 32) and pz in (1, 2, 3)
+    assert pxy in (4, 8, 16, 32) and pz in (1, 2, 3, 4)
     j.run()
     fused = [j.field(f) for f in fids]
     pf = j.particles()
@@ -364,7 +364,7 @@ def test_fused_rerun_is_identical(mfxlib, engine, n, lattice, monkeypatch):
     fids = [mfxlib.FIELD_PHI2, mfxlib.FIELD_PHI3, mfxlib.FIELD_A3Y]
     first = None
     for pxy in (4, 8, 16, 32):
-        for pz in (1, 2, 3):
+        for pz in (1, 2, 3, 4):
             j = c.job(mfxlib, engine, precision=mfxlib.FP32C)
             try:
                 j.set_tiles(pxy, pz)
