@@ -392,17 +392,24 @@ struct Acc32 {
     add(q);
     lo += e2;
   }
+  // the same for a coefficient C in {1, -1, 2}, whose product with p is exact
+  template <int C> MFX_HD void add_prod(float a, float b) {
+    static_assert(C == 1 || C == -1 || C == 2, "exact coefficients only");
+    const float p = a * b, e = fmaf(a, b, -p);
+    add(float(C) * p);
+    lo += float(C) * e;
+  }
   MFX_HD float value() const { return hi + lo; }
 };
 
 // 2LPT source (ic_generator.cc:530-534) from the six phi1 Hessians
 MFX_HD float src_phi2(const float *h) {
   Acc32 S;
-  S.add_prod(1.f, h[0], h[1] + h[2]);
-  S.add_prod(1.f, h[1], h[2]);
-  S.add_prod(-1.f, h[3], h[3]);
-  S.add_prod(-1.f, h[4], h[4]);
-  S.add_prod(-1.f, h[5], h[5]);
+  S.add_prod<1>(h[0], h[1] + h[2]);
+  S.add_prod<1>(h[1], h[2]);
+  S.add_prod<-1>(h[3], h[3]);
+  S.add_prod<-1>(h[4], h[4]);
+  S.add_prod<-1>(h[5], h[5]);
   return S.value();
 }
 
@@ -411,11 +418,11 @@ MFX_HD float src_phi2(const float *h) {
 MFX_HD void src_phi3(const float *p, const float *q, const float *T, float *s) {
   const float c57 = -5.0f / 7.0f, c107 = 10.0f / 7.0f;
   Acc32 S;
-  S.add_prod(1.f, T[0], p[2]);
-  S.add_prod(2.f, T[1], p[5]);
-  S.add_prod(-1.f, T[2], p[0]);
-  S.add_prod(-1.f, T[3], p[1]);
-  S.add_prod(-1.f, T[4], p[2]);
+  S.add_prod<1>(T[0], p[2]);
+  S.add_prod<2>(T[1], p[5]);
+  S.add_prod<-1>(T[2], p[0]);
+  S.add_prod<-1>(T[3], p[1]);
+  S.add_prod<-1>(T[4], p[2]);
   S.add_prod(c57, p[0], q[1] + q[2]);
   S.add_prod(c57, p[1], q[2] + q[0]);
   S.add_prod(c57, p[2], q[0] + q[1]);
@@ -427,10 +434,10 @@ MFX_HD void src_phi3(const float *p, const float *q, const float *T, float *s) {
   for (int d = 0; d < 3; ++d) {
     const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
     Acc32 A;
-    A.add_prod(1.f, q[hslot(d, d1)], p[hslot(d, d2)]);
-    A.add_prod(-1.f, q[hslot(d, d2)], p[hslot(d, d1)]);
-    A.add_prod(1.f, p[hslot(d1, d2)], q[hslot(d1, d1)] - q[hslot(d2, d2)]);
-    A.add_prod(-1.f, q[hslot(d1, d2)], p[hslot(d1, d1)] - p[hslot(d2, d2)]);
+    A.add_prod<1>(q[hslot(d, d1)], p[hslot(d, d2)]);
+    A.add_prod<-1>(q[hslot(d, d2)], p[hslot(d, d1)]);
+    A.add_prod<1>(p[hslot(d1, d2)], q[hslot(d1, d1)] - q[hslot(d2, d2)]);
+    A.add_prod<-1>(q[hslot(d1, d2)], p[hslot(d1, d1)] - p[hslot(d2, d2)]);
     s[1 + d] = A.value();
   }
 }
