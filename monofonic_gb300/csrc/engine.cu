@@ -809,6 +809,7 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
   a.in_scale1 = 1.0 / j->scale1;
   a.in_scale2 = 1.0 / j->scale2;
   a.in_scale3 = 1.0 / j->scale3;
+  asm_float_coefficients(a);
   if (j->fused) return assemble_fused(j, a);
   const size_t total = size_t(N) * N * j->nk;
   for (int s0 = 0; s0 < j->ns; s0 += j->group) {

@@ -230,6 +230,29 @@ __global__ void __launch_bounds__(FA<N>::t2, min_blocks(FA<N>::t2)) k_fa_y(FAArg
       });
 }
 
+// float -> double by moving the bit fields (exact, the same value the FP64
+// conversion gives): keeps the conversions of the read-out off the FP64 pipe,
+// which is narrow on this part and also carries the q + Psi additions
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  uint32_t ed;
+  if (e == 0xffu) {
+    ed = 0x7ffu;  // inf / nan (the payload moves along)
+  } else if (e != 0u) {
+    ed = e + (1023u - 127u);
+  } else if (m != 0u) {
+    // subnormal float: normalise (a normal double)
+    const int lz = __clz(int(m)) - 8;  // shift bringing the leading one to bit 23
+    m = (m << lz) & 0x7fffffu;
+    ed = uint32_t(1023 - 126 - lz);
+  } else {
+    ed = 0u;  // +-0
+  }
+  const uint64_t d = (uint64_t(u & 0x80000000u) << 32) | (uint64_t(ed) << 52) | (uint64_t(m) << 29);
+  return __longlong_as_double(static_cast<long long>(d));
+}
+
 // ASM3: inverse z transforms (c2r, component pairs (0,1), (2,3), (4,5)) and the
 // particles of RW rows at a time
 template <int N>
@@ -313,9 +336,9 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const float2 a0 = hw[z0 + c], a1 = hw[N + z0 + c], a2 = hw[2 * N + z0 + c];
-        pv[3 * c + 0] = qx + double(a0.x);
-        pv[3 * c + 1] = qy + double(a0.y);
-        pv[3 * c + 2] = a.qtab[2 * N + z0 + c] + double(a1.x);
+        pv[3 * c + 0] = qx + f2d_exact(a0.x);
+        pv[3 * c + 1] = qy + f2d_exact(a0.y);
+        pv[3 * c + 2] = a.qtab[2 * N + z0 + c] + f2d_exact(a1.x);
         vv[3 * c + 0] = a1.y;
         vv[3 * c + 1] = a2.x;
         vv[3 * c + 2] = a2.y;

@@ -422,7 +422,26 @@ struct AsmArgs {
   double g1, g2, g3, g3c, vfac1, vfac2, vfac3;
   double pfac, vfac;    // lunit/L * 1/sqrt(N^3),  vunit/L * 1/sqrt(N^3)
   double in_scale1, in_scale2, in_scale3;  // undo per-field scaling
+  // the FP32 form's coefficients, rounded from the FP64 ones once on the host
+  // (a float kernel that re-derived them per mode would keep the slow FP64
+  // pipe busy): kfac, g_n * in_scale_n (n = 1, 2, 3), g3c * in_scale3,
+  // vfac1..3, pfac, vfac
+  float fkfac, fs1, fs2, fs3, fsa, fv1, fv2, fv3, fpfac, fvfac;
 };
+
+// the float coefficients of an AsmArgs from its FP64 ones
+inline void asm_float_coefficients(AsmArgs &a) {
+  a.fkfac = float(a.kfac);
+  a.fs1 = float(a.g1 * a.in_scale1);
+  a.fs2 = float(a.g2 * a.in_scale2);
+  a.fs3 = float(a.g3 * a.in_scale3);
+  a.fsa = float(a.g3c * a.in_scale3);
+  a.fv1 = float(a.vfac1);
+  a.fv2 = float(a.vfac2);
+  a.fv3 = float(a.vfac3);
+  a.fpfac = float(a.pfac);
+  a.fvfac = float(a.vfac);
+}
 
 // get_cic_kspace (grid_fft.hh:347-373) on a 64 x 64 x 33 real table
 __device__ __forceinline__ double plt_cic(const double *T, double x, double y, double z) {
@@ -497,7 +516,7 @@ __device__ __forceinline__ void plt_grad_f32(const float4 *T, int i, int j, int 
 template <typename R>
 __device__ __forceinline__ void plt_grad(const AsmArgs &a, int i, int j, int k, int N, R G[3], R &vcorr) {
   if constexpr (sizeof(R) == 4) {
-    plt_grad_f32(a.plt4, i, j, k, N, float(a.kfac), G, vcorr);
+    plt_grad_f32(a.plt4, i, j, k, N, a.fkfac, G, vcorr);
   } else {
     const double x = double(i) * a.mapratio, y = double(j) * a.mapratio, z = double(k) * a.mapratio;
     const double twopi = 2.0 * 3.141592653589793;
@@ -538,9 +557,16 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
   // Gp: gradient applied to the displacement, Gv: gradient times vfac_corr
   // applied to the velocity
   R Gp[3], Gv[3];
+  // the coefficients in R (the FP32 form's were rounded on the host)
+  constexpr bool F32 = sizeof(R) == 4;
+  const R c_kf = F32 ? R(a.fkfac) : R(a.kfac);
+  const R c_s1 = F32 ? R(a.fs1) : R(a.g1 * a.in_scale1), c_s2 = F32 ? R(a.fs2) : R(a.g2 * a.in_scale2);
+  const R c_s3 = F32 ? R(a.fs3) : R(a.g3 * a.in_scale3), c_sa = F32 ? R(a.fsa) : R(a.g3c * a.in_scale3);
+  const R c_v1 = F32 ? R(a.fv1) : R(a.vfac1), c_v2 = F32 ? R(a.fv2) : R(a.vfac2), c_v3 = F32 ? R(a.fv3) : R(a.vfac3);
+  const R c_pf = F32 ? R(a.fpfac) : R(a.pfac), c_vf = F32 ? R(a.fvfac) : R(a.vfac);
   if (!PLT) {
     // op::fourier_gradient (operators.hh:46-56): Nyquist index zeroed, exactly odd in k
-    const R kf = R(a.kfac);
+    const R kf = c_kf;
     Gp[0] = (i != nh) ? R(signed_idx(i, N)) * kf : R(0);
     Gp[1] = (j != nh) ? R(signed_idx(j, N)) * kf : R(0);
     Gp[2] = (k != nh) ? R(k) * kf : R(0);
@@ -575,25 +601,25 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
   // phi_tot and its velocity weighting (ic_generator.cc:939-958, 994-1010)
   const C *p1 = reinterpret_cast<const C *>(a.phi[0]);
   C f1 = p1[idx];
-  R ps_re = R(a.g1 * a.in_scale1) * f1.x, ps_im = R(a.g1 * a.in_scale1) * f1.y;
-  R vs_re = R(a.vfac1) * ps_re, vs_im = R(a.vfac1) * ps_im;
+  R ps_re = c_s1 * f1.x, ps_im = c_s1 * f1.y;
+  R vs_re = c_v1 * ps_re, vs_im = c_v1 * ps_im;
   C Ad[3] = {mkc<R>(0, 0), mkc<R>(0, 0), mkc<R>(0, 0)};
   if (a.order > 1) {
     const C f2 = reinterpret_cast<const C *>(a.phi[1])[idx];
-    const R s2 = R(a.g2 * a.in_scale2);
+    const R s2 = c_s2;
     ps_re += s2 * f2.x;
     ps_im += s2 * f2.y;
-    vs_re += R(a.vfac2) * (s2 * f2.x);
-    vs_im += R(a.vfac2) * (s2 * f2.y);
+    vs_re += c_v2 * (s2 * f2.x);
+    vs_im += c_v2 * (s2 * f2.y);
   }
   if (a.order > 2) {
     const C f3 = reinterpret_cast<const C *>(a.phi[2])[idx];
-    const R s3 = R(a.g3 * a.in_scale3);
+    const R s3 = c_s3;
     ps_re += s3 * f3.x;
     ps_im += s3 * f3.y;
-    vs_re += R(a.vfac3) * (s3 * f3.x);
-    vs_im += R(a.vfac3) * (s3 * f3.y);
-    const R sa = R(a.g3c * a.in_scale3);
+    vs_re += c_v3 * (s3 * f3.x);
+    vs_im += c_v3 * (s3 * f3.y);
+    const R sa = c_sa;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const C v = reinterpret_cast<const C *>(a.A3[d])[idx];
@@ -610,10 +636,10 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
     if (a.order > 2) {
       tre += Gp[d1] * Ad[d2].x - Gp[d2] * Ad[d1].x;
       tim += Gp[d1] * Ad[d2].y - Gp[d2] * Ad[d1].y;
-      vre += R(a.vfac3) * (Gv[d1] * Ad[d2].x - Gv[d2] * Ad[d1].x);
-      vim += R(a.vfac3) * (Gv[d1] * Ad[d2].y - Gv[d2] * Ad[d1].y);
+      vre += c_v3 * (Gv[d1] * Ad[d2].x - Gv[d2] * Ad[d1].x);
+      vim += c_v3 * (Gv[d1] * Ad[d2].y - Gv[d2] * Ad[d1].y);
     }
-    const R pf = R(a.pfac), vf = R(a.vfac);
+    const R pf = c_pf, vf = c_vf;
     P[d] = dc ? mkc<R>(0, 0) : mkc<R>(-tim * pf, tre * pf);
     V[d] = dc ? mkc<R>(0, 0) : mkc<R>(-vim * vf, vre * vf);
   }
