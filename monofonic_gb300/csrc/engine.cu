@@ -120,6 +120,7 @@ struct mfx_engine {
   // N -> (pencils per CTA of the x/y passes, rows per CTA of the z passes)
   struct FFTiles {
     int pxy, pz, pz2;
+    int pk[6];
   };
   std::map<int, FFTiles> ff_tuned;  // per grid size: x/y tile, ZSRC3 and ZSRC2 shapes
 };
@@ -130,7 +131,11 @@ struct mfx_job {
   int N = 0, M = 0, nh = 0, nk = 0, mk = 0, ns = 0, group = 0;
   bool fp64 = true;
   bool fused = false;          // padded convolutions through fused.cuh
-  int ff_pxy = 8, ff_pz = 1, ff_pz2 = 1;  // pencils per CTA (x/y passes), ZSRC3 / ZSRC2 shapes (1, 2 rows; 3 wide)
+  int ff_pxy = 8, ff_pz = 1, ff_pz2 = 1;  // pencils per CTA (x/y passes), ZSRC3 / ZSRC2 shapes (1, 2 rows; 3 wide; 4 warp)
+  // x/y tile per pass kind (Y3, X6, XF, YF unpad, YF truncate, XI), tuned
+  // one by one; 0: ff_pxy
+  int ff_pk[6] = {};
+  int xy_tile(int kind) const { return ff_pk[kind] ? ff_pk[kind] : ff_pxy; }
   void *ffB[3] = {};           // B-space [N][M][N/2] complex
   void *ffC[17] = {};          // C-space [M][M][N/2] complex
   float2 *ff_tw = nullptr;     // W_M^t, t < M
@@ -503,6 +508,10 @@ static ff::FArgs ff_args(mfx_job *j) {
   return a;
 }
 
+// x/y pass kinds with a tile of their own (mfx_job::ff_pk)
+enum XYKind { K_Y3 = 0, K_X6 = 1, K_XF = 2, K_YF = 3, K_YT = 4, K_XI = 5 };
+static const char *const kXYNames[6] = {"ff_y3", "ff_x6", "ff_x_fwd", "ff_y_fwd", "ff_y_trunc", "ff_x_inv"};
+
 static int ff_run(mfx_job *j, int op, int p, const ff::FArgs &a, const char *name, double bytes) {
   KBEGIN(j);
   const cudaError_t e = ff::ff_launch(j->M, op, p, a, j->stream);
@@ -521,13 +530,13 @@ static int ff_hessians(mfx_job *j, const void *phi, void *const *C) {
   for (int o = 0; o < 3; ++o) y.dst[o] = static_cast<float2 *>(j->ffB[o]);
   y.ncomp = 3;
   y.fac = float(std::pow(1.5, 1.5) / std::sqrt(M3));
-  TRY(ff_run(j, ff::FF_Y3, j->ff_pxy, y, "ff_y3", double(N) * N * Kh * 8 + 3 * bB));
+  TRY(ff_run(j, ff::FF_Y3, j->xy_tile(K_Y3), y, "ff_y3", double(N) * N * Kh * 8 + 3 * bB));
   ff::FArgs x = ff_args(j);
   for (int o = 0; o < 3; ++o) x.src[o] = static_cast<const float2 *>(j->ffB[o]);
   for (int c = 0; c < 6; ++c) x.dst[c] = static_cast<float2 *>(C[c]);
   x.ncomp = 6;
   x.mode = 0;
-  TRY(ff_run(j, ff::FF_XINV, j->ff_pxy, x, "ff_x6", 3 * bB + 6 * bC));
+  TRY(ff_run(j, ff::FF_XINV, j->xy_tile(K_X6), x, "ff_x6", 3 * bB + 6 * bC));
   return MFX_OK;
 }
 
@@ -543,7 +552,7 @@ static int ff_finish(mfx_job *j, void *D, void *out, int mode) {
   x.src[0] = static_cast<const float2 *>(D);
   x.dst[0] = static_cast<float2 *>(j->ffB[0]);
   x.ncomp = 1;
-  TRY(ff_run(j, ff::FF_XFWD, j->ff_pxy, x, "ff_x_fwd", bC + bB));
+  TRY(ff_run(j, ff::FF_XFWD, j->xy_tile(K_XF), x, "ff_x_fwd", bC + bB));
   ff::FArgs y = ff_args(j);
   y.src[0] = static_cast<const float2 *>(j->ffB[0]);
   y.ncomp = 1;
@@ -551,17 +560,17 @@ static int ff_finish(mfx_job *j, void *D, void *out, int mode) {
   if (mode == 0) {
     y.dst[0] = static_cast<float2 *>(out);
     y.fac = float(1.0 / std::sqrt(M3) / rfac_u);
-    TRY(ff_run(j, ff::FF_YFWD, j->ff_pxy, y, "ff_y_fwd", bB + double(j->n_field_bytes)));
+    TRY(ff_run(j, ff::FF_YFWD, j->xy_tile(K_YF), y, "ff_y_fwd", bB + double(j->n_field_bytes)));
   } else {
     y.dst[0] = static_cast<float2 *>(j->ffB[0]);  // each CTA owns its tile: in place
     y.fac = float((1.0 / std::sqrt(M3) / rfac_u) * rfac_p / std::sqrt(M3));
-    TRY(ff_run(j, ff::FF_YFWD, j->ff_pxy, y, "ff_y_trunc", 2 * bB));
+    TRY(ff_run(j, ff::FF_YFWD, j->xy_tile(K_YT), y, "ff_y_trunc", 2 * bB));
     ff::FArgs xi = ff_args(j);
     xi.src[0] = static_cast<const float2 *>(j->ffB[0]);
     xi.dst[0] = static_cast<float2 *>(out);
     xi.ncomp = 1;
     xi.mode = 1;
-    TRY(ff_run(j, ff::FF_XINV, j->ff_pxy, xi, "ff_x_inv", bB + bC));
+    TRY(ff_run(j, ff::FF_XINV, j->xy_tile(K_XI), xi, "ff_x_inv", bB + bC));
   }
   return MFX_OK;
 }
@@ -623,6 +632,7 @@ static void tune_fused(mfx_job *j) {
     j->ff_pxy = it->second.pxy;
     j->ff_pz = it->second.pz;
     j->ff_pz2 = it->second.pz2;
+    for (int k = 0; k < 6; ++k) j->ff_pk[k] = it->second.pk[k];
   }
 }
 
@@ -648,22 +658,56 @@ static int autotune_fused(mfx_job *j) {
   int best_xy = j->ff_pxy;
   float tbest = 1e30f;
   int rc = MFX_OK;
+  // every x/y tile on the phi1 Hessian passes and one forward x/y pair of each
+  // kind, each launch timed on its own (the job's profiling events); each pass
+  // kind keeps its fastest tile, ff_pxy the fastest over all of them
+  float tk[6], tsum_best = 1e30f;
+  int pk[6] = {};
+  for (int k = 0; k < 6; ++k) tk[k] = 1e30f;
   for (int p : {32, 16, 8, 4}) {
-    if (!ff::ff_valid(M, ff::FF_XFWD, p)) continue;
-    const float t = timed([&] {
-      // the Hessian passes of phi1 and one forward x/y pair
-      const int save = j->ff_pxy;
-      j->ff_pxy = p;
+    if (rc != MFX_OK || !ff::ff_valid(M, ff::FF_XFWD, p)) continue;
+    const int save = j->ff_pxy;
+    int savek[6];
+    for (int k = 0; k < 6; ++k) {
+      savek[k] = j->ff_pk[k];
+      j->ff_pk[k] = 0;
+    }
+    j->ff_pxy = p;
+    float tp[6] = {0, 0, 0, 0, 0, 0};
+    for (int rep = 0; rep < 2 && rc == MFX_OK; ++rep) {  // warm, then timed
+      j->prof = true;
+      j->prof_recs.clear();
+      j->ev_next = 0;
       if (rc == MFX_OK) rc = ff_hessians(j, j->nf[0], &j->ffC[0]);
       if (rc == MFX_OK) rc = ff_finish(j, j->ffC[0], j->ffC[6], 1);
-      j->ff_pxy = save;
-    });
+      if (rc == MFX_OK) rc = ff_finish(j, j->ffC[0], j->nf[1], 0);
+      if (rc == MFX_OK && cudaStreamSynchronize(j->stream) != cudaSuccess) rc = set_error(MFX_ECUDA, "autotune sync");
+      if (rep == 1 && rc == MFX_OK)
+        for (const auto &r : j->prof_recs) {
+          float e = 0;
+          cudaEventElapsedTime(&e, r.a, r.b);
+          for (int k = 0; k < 6; ++k)
+            if (std::strcmp(r.name, kXYNames[k]) == 0) tp[k] += e;
+        }
+    }
+    j->prof_recs.clear();
+    j->ff_pxy = save;
+    for (int k = 0; k < 6; ++k) j->ff_pk[k] = savek[k];
     if (rc != MFX_OK) break;
-    if (t < tbest) {
-      tbest = t;
+    float tsum = 0;
+    for (int k = 0; k < 6; ++k) {
+      tsum += tp[k];
+      if (tp[k] < tk[k]) {
+        tk[k] = tp[k];
+        pk[k] = p;
+      }
+    }
+    if (tsum < tsum_best) {
+      tsum_best = tsum;
       best_xy = p;
     }
   }
+  j->prof = false;
   // the z passes, each shape timed on the job's own fields: ZSRC2 always,
   // ZSRC3 for 3LPT jobs
   int best_z2 = j->ff_pz2, best_z3 = j->ff_pz;
@@ -700,10 +744,11 @@ static int autotune_fused(mfx_job *j) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(MFX_ECUDA, "autotune: %s", cudaGetErrorString(e));
   j->ff_pxy = best_xy;
+  for (int k = 0; k < 6; ++k) j->ff_pk[k] = pk[k];
   j->ff_pz = best_z3;
   j->ff_pz2 = best_z2;
   std::lock_guard<std::mutex> lk(j->eng->mu);
-  j->eng->ff_tuned[N] = {best_xy, best_z3, best_z2};
+  j->eng->ff_tuned[N] = {best_xy, best_z3, best_z2, {pk[0], pk[1], pk[2], pk[3], pk[4], pk[5]}};
   return MFX_OK;
 }
 
@@ -1417,6 +1462,7 @@ int mfx_job_set_tiles(mfx_job *job, int pencils_xy, int rows_z) {
     return set_error(MFX_EINVAL, "z tile of %d rows not admissible for M = %d", rows_z, job->M);
   if (job->gexec) return set_error(MFX_ESTATE, "job already captured into a graph");
   job->ff_pxy = pencils_xy;
+  for (int k = 0; k < 6; ++k) job->ff_pk[k] = 0;
   job->ff_pz = rows_z;
   job->ff_pz2 = rows_z;
   return MFX_OK;
