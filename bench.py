@@ -521,6 +521,17 @@ def run_serving(args):
                           lunit=r["boxlen"], vunit=r["boxlen"] / np.sqrt(1.0 / (1.0 + r["zstart"])),
                           pos64=True, vel64=False, id64=True))
     parts = [(1 << s["lattice"]) * s["ngrid"] ** 3 for s in specs]
+    # the autotuner picks the fused transforms' tiles once per size class at
+    # start-up (the engine keeps them for the jobs the server creates)
+    tuned = {}
+    for s in sorted(specs, key=lambda s: -s["order"]):
+        if s["ngrid"] in tuned or s["order"] < 2:
+            continue
+        j = mfx.Job(eng, s["ngrid"], s["boxlen"], s["order"], s["seed_table"], s["amp_table"], s["coef"],
+                    lattice=s["lattice"], precision=mfx.FP32C, plt_table=s["plt_table"], lunit=s["lunit"],
+                    vunit=s["vunit"], pos64=True, vel64=False, id64=True)
+        tuned[s["ngrid"]] = list(j.autotune())
+        j.close()
     srv = mfx.Server(eng, max_inflight=args.inflight)
     # warm the plan pool and the memory pool with one pass over the size classes
     warm = {}
@@ -594,7 +605,8 @@ def run_serving(args):
         "data": "synthetic (NGenIC white noise, seeds 1..%d; mix from default_rng(7))" % len(specs),
         "config": {"workload": "serve: %d requests, N in {64..384}, order 1-3, SC/BCC/FCC (+PLT), FP32-compensated"
                    % len(specs), "arrival_rate_jobs_per_s": rate, "load_vs_saturated": args.load,
-                   "max_inflight": args.inflight, "particles": sum(parts)},
+                   "max_inflight": args.inflight, "particles": sum(parts),
+                   "tiles_per_size": {str(k): v for k, v in tuned.items()}},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "max": float(np.max(lat))},
         "saturated": {"value": sat_tput, "unit": "particles/s", "span_s": sat_span,
