@@ -540,13 +540,14 @@ template <int M, int P, int ROWS> struct XY {
 };
 
 // the transform of an x/y tile: pencil_fft, or pencil_fft_mi in the lean form
-// (buf2 == buf there)
-template <int M, int P, bool INV, class Ld, class St>
+// (buf2 == buf there).  LDB as for pencil_fft: false where ld reads the stage
+// and the tile's earlier transforms are all of this kind
+template <int M, int P, bool INV, bool LDB = true, class Ld, class St>
 __device__ __forceinline__ void xy_fft(float2 *buf, float2 *buf2, const float2 *tw, const Ld &ld, const St &st) {
   if constexpr (XY<M, P, M>::lean)
     pencil_fft_mi<M, P, true, INV, XY<M, P, M>::threads>(buf, tw, ld, st);
   else
-    pencil_fft<M, P, true, INV>(buf, buf2, tw, ld, st);
+    pencil_fft<M, P, true, INV, LDB>(buf, buf2, tw, ld, st);
 }
 // the tile buffers and the staging area of an x/y kernel's shared memory
 template <int M, int P> struct XYMem {
@@ -600,7 +601,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::t
 #pragma unroll 1
         for (int o = 0; o < 3; ++o) {
           float2 *out = a.dst[o] + (i * M * D::Kh + kz0);
-          xy_fft<M, P, true>(
+          xy_fft<M, P, true, false>(
               buf, buf2, tw,
               [&](int q, int n) -> float2 {
                 const int j = unpad_index(n, D::N);
@@ -647,7 +648,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::t
         for (int k = 0; k < ncs; ++k) {
           const int c = a.mode ? int(s) : (s == 0 ? 2 * k : (s == 1 ? (k == 0 ? 3 : 5) : 1));
           float2 *out = a.dst[c] + off;
-          xy_fft<M, P, true>(
+          xy_fft<M, P, true, false>(
               buf, buf2, tw,
               [&](int q, int n) -> float2 {
                 const int i = unpad_index(n, D::N);
@@ -685,7 +686,7 @@ template <int M, int P> __global__ void __launch_bounds__(XY<M, P, M>::threads, 
       [&](unsigned u, const float2 *st) {
         const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
         float2 *dst = a.dst[c] + (yy * D::Kh + kz0);
-        xy_fft<M, P, false>(
+        xy_fft<M, P, false, false>(
             buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
             [&](int q, int k, float2 v) {
               const int i = unpad_index(k, D::N);
@@ -722,7 +723,7 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
         if constexpr (MODE == 0) {
           const float kx = float(sidx(int(i), D::N)) * a.kfac;
           float2 *out = dst + i * D::N * D::nk + kz0;
-          xy_fft<M, P, false>(
+          xy_fft<M, P, false, false>(
               buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
               [&](int q, int k, float2 v) {
                 const int j = unpad_index(k, D::N);
@@ -743,7 +744,7 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
           float2 *out = dst + (i * M * D::Kh + kz0);
           const bool row_kept = int(i) != D::nh;
           float2 *mid = obuf<M>(buf, buf2);
-          xy_fft<M, P, false>(
+          xy_fft<M, P, false, false>(
               buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
               [&](int q, int k, float2 v) {
                 const int j = unpad_index(k, D::N);
