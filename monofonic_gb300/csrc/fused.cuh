@@ -514,7 +514,6 @@ template <int CHUNK> __device__ __forceinline__ void cp_async(void *dst, const v
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // stages ROWS rows of P complex (row r at src + r * stride) as stage[r * P + q]
 template <int P, int ROWS, int CHUNK>
@@ -561,7 +560,11 @@ template <int M, int P> struct XYMem {
 };
 
 // The persistent unit loop: fetch(u, stage) issues unit u's copies,
-// work(u, stage) transforms it.
+// work(u, stage) transforms it.  One barrier per unit: after it every
+// thread's copies of unit u have landed and every thread has finished unit
+// u - 1, whose stage the copies of the next unit then overwrite while unit u
+// is transformed.
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 template <class Fetch, class Work>
 __device__ __forceinline__ void xy_units(unsigned units, unsigned stage_elems, float2 *stage0, const Fetch &fetch,
                                          const Work &work) {
@@ -572,12 +575,11 @@ __device__ __forceinline__ void xy_units(unsigned units, unsigned stage_elems, f
   for (unsigned it = 0; u < units; ++it, u += gridDim.x) {
     float2 *cur = stage0 + (it & 1) * stage_elems, *nxt = stage0 + ((it & 1) ^ 1) * stage_elems;
     const unsigned un = u + gridDim.x;
+    cp_async_wait_all();
+    __syncthreads();
     if (un < units) fetch(un, nxt);
     cp_async_commit();
-    cp_async_wait_prev();
-    __syncthreads();
     work(u, cur);
-    __syncthreads();  // the stage just read is the next fetch's target
   }
 }
 
@@ -921,7 +923,9 @@ __device__ __forceinline__ void z_forward(const FArgs &a, size_t r0, const float
       a.dst[f0 % NOUT][(r0 + f0 / NOUT) * D::Kh + k] = sa;
       if (f1 < NR) a.dst[f1 % NOUT][(r0 + f1 / NOUT) * D::Kh + k] = sb;
     }
-    __syncthreads();
+    // the next round's transform writes ob; after the last round the barrier
+    // at the top of the next row group stands before any write to it
+    if (g0 + G < NPO) __syncthreads();
   }
 }
 
