@@ -262,11 +262,13 @@ template <int L, int R, int NS, bool INV> struct Step {
 // memory.  LDB = false: ld reads neither buffer and nothing but an earlier
 // call of the same shape reads buf, which then needs no barrier before the
 // first step's writes when that call's last step read buf2 (three steps).
+// B1 = false: no barrier there at all (the caller has one between any earlier
+// reader of buf and this call).
 template <int L> __device__ __forceinline__ float2 *obuf(float2 *buf, float2 *buf2) {
   return Fac<L>::steps == 3 ? buf : buf2;
 }
 
-template <int L, int PP, bool PF, bool INV, bool LDB = true, class Ld, class St>
+template <int L, int PP, bool PF, bool INV, bool LDB = true, bool B1 = true, class Ld, class St>
 __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const float2 *tw, const Ld &ld, const St &st) {
   using F = Fac<L>;
   using T = Tile<L, PP, PF>;
@@ -279,7 +281,7 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
     const bool act = t < PP * S::J;
     if (act) S::gather(j, [&](int n) { return ld(q, n); }, tw, v);
     // ld may read buf; an earlier call's last step may still read it
-    if constexpr (LDB || F::steps != 3) __syncthreads();
+    if constexpr (B1 && (LDB || F::steps != 3)) __syncthreads();
     if (act) S::scatter(j, [&](int n, float2 x) { buf[T::at(q, n)] = x; }, v);
     __syncthreads();
   }

@@ -297,7 +297,8 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
       }
       return;
     }
-    pencil_fft<N, G, false, true>(
+    // buf was last read by the previous group's transform, before the barrier above
+    pencil_fft<N, G, false, true, false, false>(
         buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int w = q / 3, c0 = 2 * (q - w * 3);
@@ -367,7 +368,7 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
         }
       }
     }
-    __syncthreads();  // h2 is rewritten by the next group
+    // h2 is rewritten by the next group's transform, after the barrier at its top
   }
 }
 
