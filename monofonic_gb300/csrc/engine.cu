@@ -772,13 +772,15 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   // MFX_FA_KEEP=0 in the environment assembles per sub-lattice (for comparisons)
   const char *env = getenv("MFX_FA_KEEP");
   const bool keep = !(env && env[0] == '0');
-  const int nsub = (keep && ns > 1 && ff::fa_keep(j->M) && j->group >= ns) ? ns : 1;
+  const int nsub = (keep && ns > 1 && ff::fa_all(j->M) && j->group >= ns) ? ns : 1;
   // ASM1 in halves (tiles of 8 pencils) from N = 384 up, where the x pass's
   // 32-byte row pieces of the 4-pencil tiles lie megabytes apart (768^3 FCC:
-  // 57 -> 44 ms; 256^3 BCC: 0.63 -> 0.93 ms, so not there); MFX_FA_HALVES
-  // = 0 / 1 in the environment forces it off / on (for comparisons)
+  // 57 -> 44 ms; 256^3 BCC: 0.63 -> 0.93 ms, so not there), and wherever the
+  // 4-pencil form does not fit; MFX_FA_HALVES = 0 / 1 in the environment
+  // forces it off / on where both fit (for comparisons)
   const char *envh = getenv("MFX_FA_HALVES");
-  const bool halves = nsub > 1 && ff::fa_halves(j->M) && (envh ? envh[0] == '1' : N >= 384);
+  const bool halves = nsub > 1 && ff::fa_halves(j->M) &&
+                      (!ff::fa_keep(j->M) || (envh ? envh[0] == '1' : N >= 384));
   const bool plt = as.plt != nullptr;
   ff::FAArgs fa{};
   fa.as = as;
@@ -1122,7 +1124,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     // the fused assembly emits all sub-lattices from one assembly of each mode
     // when their components are held together: worth the extra memory while
     // the engine budget has it
-    if (j->fused && d->want_particles && L.group < j->ns && ff::fa_keep(j->M)) {
+    if (j->fused && d->want_particles && L.group < j->ns && ff::fa_all(j->M)) {
       const Layout La = plan_layout(d, work, true);
       if (eng->in_use + La.total <= eng->budget) L = La;
     }

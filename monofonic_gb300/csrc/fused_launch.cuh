@@ -250,6 +250,7 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
   cudaError_t ff_launch_##M(int op, int p, const FArgs &a, cudaStream_t s);     \
   cudaError_t fa_launch_##M(int op, bool plt, const FAArgs &a, cudaStream_t s); \
   bool fa_keep_##M();                                                           \
+  bool fa_all_##M();                                                            \
   bool fa_halves_##M();                                                         \
   bool ff_valid_##M(int op, int p);
 MFX_FF_LENGTHS(MFX_FF_DECL)
@@ -261,6 +262,7 @@ MFX_FF_LENGTHS(MFX_FF_DECL)
     return fa_launch_m<M>(op, plt, a, s);                                                                      \
   }                                                                                                            \
   bool fa_keep_##M() { return FA<2 * M / 3>::keep; }                                                          \
+  bool fa_all_##M() { return FA<2 * M / 3>::keep || FA<2 * M / 3>::halves; }                                  \
   bool fa_halves_##M() { return FA<2 * M / 3>::halves; }                                                      \
   bool ff_valid_##M(int op, int p) { return ff_valid_m<M>(op, p); }
 
@@ -297,7 +299,17 @@ inline bool fa_halves(int M) {
   return false;
 }
 
-// whether ASM1 emits several sub-lattices from one assembly at this length
+// whether ASM1 emits several sub-lattices from one assembly of each mode at
+// this length, in either form (4-pencil tiles or halves)
+inline bool fa_all(int M) {
+#define MFX_FF_CASE(L) \
+  if (M == L) return fa_all_##L();
+  MFX_FF_LENGTHS(MFX_FF_CASE)
+#undef MFX_FF_CASE
+  return false;
+}
+
+// whether ASM1 with 4-pencil tiles emits several sub-lattices at this length
 inline bool fa_keep(int M) {
 #define MFX_FF_CASE(L) \
   if (M == L) return fa_keep_##L();

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "ranlxd.cuh"
 
 namespace mfx {
@@ -467,14 +469,21 @@ __device__ __forceinline__ double plt_cic(const double *T, double x, double y, d
 // split exactly in integers (ix = floor(64 i / N), dx = (64 i mod N)/N), the
 // direction of the interpolation point's k equals that of the mode's signed
 // index vector, and the four tables are read as one float4 per CIC corner.
-__device__ __forceinline__ void plt_grad_f32(const float4 *T, int i, int j, int k, int N, float kfac, float G[3],
+// the FP32 form's PLT tables read from global memory (through the read-only path)
+struct PltGlobal {
+  const float4 *T;
+  __device__ __forceinline__ float4 operator()(int p, int q, int r) const { return __ldg(&T[(p * 64 + q) * 33 + r]); }
+};
+
+// e(p, q, r): entry (p, q, r) of the 64 x 64 x 33 float4 table
+template <class TA>
+__device__ __forceinline__ void plt_grad_f32(const TA &e, int i, int j, int k, int N, float kfac, float G[3],
                                              float &vcorr) {
   const int ix = (64 * i) / N, iy = (64 * j) / N, iz = (64 * k) / N;
   const float invN = 1.0f / float(N);
   const float dx = float((64 * i) % N) * invN, dy = float((64 * j) % N) * invN, dz = float((64 * k) % N) * invN;
   const float tx = 1.0f - dx, ty = 1.0f - dy, tz = 1.0f - dz;
   const int ix1 = (ix + 1) & 63, iy1 = (iy + 1) & 63, iz1 = min(iz + 1, 32);
-  auto e = [T](int p, int q, int r) { return __ldg(&T[(p * 64 + q) * 33 + r]); };
   const float w[8] = {tx * ty * tz, tx * ty * dz, tx * dy * tz, tx * dy * dz,
                       dx * ty * tz, dx * ty * dz, dx * dy * tz, dx * dy * dz};
   const float4 c[8] = {e(ix, iy, iz), e(ix, iy, iz1), e(ix, iy1, iz), e(ix, iy1, iz1),
@@ -516,7 +525,7 @@ __device__ __forceinline__ void plt_grad_f32(const float4 *T, int i, int j, int 
 template <typename R>
 __device__ __forceinline__ void plt_grad(const AsmArgs &a, int i, int j, int k, int N, R G[3], R &vcorr) {
   if constexpr (sizeof(R) == 4) {
-    plt_grad_f32(a.plt4, i, j, k, N, a.fkfac, G, vcorr);
+    plt_grad_f32(PltGlobal{a.plt4}, i, j, k, N, a.fkfac, G, vcorr);
   } else {
     const double x = double(i) * a.mapratio, y = double(j) * a.mapratio, z = double(k) * a.mapratio;
     const double twopi = 2.0 * 3.141592653589793;
@@ -549,9 +558,12 @@ __device__ __forceinline__ void plt_grad(const AsmArgs &a, int i, int j, int k, 
 
 // One k-space mode of the displacement (P) and velocity (V) components before
 // the sub-lattice phase (ic_generator.cc:929-1053): idx = (i N + j)(N/2+1) + k.
-template <typename R, bool PLT>
+// TAB: the FP32 form's PLT table accessor for the mode's own gradient (the
+// kz = 0 mirror still reads the tables in global memory); void: global memory.
+template <typename R, bool PLT, class TAB = void>
 __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, size_t idx,
-                                         typename Cplx<R>::T P[3], typename Cplx<R>::T V[3]) {
+                                         typename Cplx<R>::T P[3], typename Cplx<R>::T V[3],
+                                         const TAB *tab = nullptr) {
   using C = typename Cplx<R>::T;
   const int N = a.N, nh = N >> 1;
   // Gp: gradient applied to the displacement, Gv: gradient times vfac_corr
@@ -574,7 +586,10 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
     for (int d = 0; d < 3; ++d) Gv[d] = Gp[d];
   } else {
     R G[3], vc;
-    plt_grad<R>(a, i, j, k, N, G, vc);
+    if constexpr (!std::is_void<TAB>::value && sizeof(R) == 4)
+      plt_grad_f32(*tab, i, j, k, N, a.fkfac, G, vc);
+    else
+      plt_grad<R>(a, i, j, k, N, G, vc);
     if (k == 0) {
       // On the kz = 0 plane the c2r sees both k and -k.  The interpolated PLT
       // gradient is not exactly odd where the CIC stencil touches the table's

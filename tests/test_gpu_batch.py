@@ -96,3 +96,25 @@ def test_pipelined_downloads_match_runs_one_at_a_time(mfxlib, engine, ring):
     last = j.particles()
     assert np.array_equal(last[0], refs[-1][0])
     j.close()
+
+
+def test_output_ring_state_errors(mfxlib, engine):
+    """The output ring and graph capture exclude each other; asynchronous
+    downloads need particles of a run."""
+    sp = spec(mfxlib, 32, 100.0, 24.0, 2, 5, lattice=1, precision=mfxlib.FP32C)
+    j = mfxlib.Job(engine, 32, 100.0, 2, sp["seed_table"], sp["amp_table"], sp["coef"], lattice=1,
+                   precision=mfxlib.FP32C, lunit=sp["lunit"], vunit=sp["vunit"])
+    buf = np.zeros(j.num_particles * 3, dtype=np.float64)
+    with pytest.raises(RuntimeError):
+        j.fetch_particles_range_async(0, 1, buf.ctypes.data, None, None)  # no run yet
+    j.set_output_ring(True)
+    with pytest.raises(RuntimeError):
+        j.capture()
+    j.set_output_ring(False)
+    j.capture()
+    with pytest.raises(RuntimeError):
+        j.set_output_ring(True)
+    j.run()
+    ref = run_alone(mfxlib, engine, sp)
+    assert np.array_equal(j.particles()[0], ref[0])
+    j.close()
