@@ -66,7 +66,7 @@ template <int N, int P> struct PltSlice {
 template <int N> struct FA {
   static constexpr int maxJ = Fac<N>::maxJ;
   static constexpr int P = 4;
-  static constexpr int P2 = (8 * maxJ <= 256) ? 8 : 4;
+  static constexpr int P2 = (8 * maxJ <= 768) ? 8 : 4;
   static constexpr int CG = (6 * P * maxJ <= 512) ? 6 : ((3 * P * maxJ <= 1024) ? 3 : 2);
   static constexpr int RW = (256 / (3 * maxJ)) >= 8 ? 8 : ((256 / (3 * maxJ)) >= 4 ? 4 : ((256 / (3 * maxJ)) >= 2 ? 2 : 1));
   static constexpr int Kh = N / 2, nk = N / 2 + 1;
