@@ -66,7 +66,13 @@ template <int N, int P> struct PltSlice {
 template <int N> struct FA {
   static constexpr int maxJ = Fac<N>::maxJ;
   static constexpr int P = 4;
-  static constexpr int P2 = (8 * maxJ <= 768) ? 8 : 4;
+  // ASM2 pencils: the widest tile (64- or 128-byte row pieces) whose threads
+  // and shared memory fit one CTA
+  static constexpr size_t s2_of(int p2, int nb) { return size_t(N + nb * N * p2 + 2 * N * p2) * 8; }
+  static constexpr int P2 = ((N / 2) % 16 == 0 && 16 * maxJ <= 1024 &&
+                             s2_of(16, Fac<N>::steps == 3 ? 2 : 1) <= 227 * 1024)
+                                ? 16
+                                : ((8 * maxJ <= 768) ? 8 : 4);
   static constexpr int CG = (6 * P * maxJ <= 512) ? 6 : ((3 * P * maxJ <= 1024) ? 3 : 2);
   static constexpr int RW = (256 / (3 * maxJ)) >= 8 ? 8 : ((256 / (3 * maxJ)) >= 4 ? 4 : ((256 / (3 * maxJ)) >= 2 ? 2 : 1));
   static constexpr int Kh = N / 2, nk = N / 2 + 1;
@@ -98,6 +104,9 @@ template <int N> struct FA {
                                 size_t(PltSlice<N, P8>::elems) * sizeof(float4);
   static constexpr bool halves = Kh % P8 == 0 && s1h <= 227 * 1024;
   static constexpr size_t s2 = size_t(N + nbuf * Tile<N, P2, true>::elems + 2 * N * P2) * sizeof(float2);
+  // CTAs per SM the registers are sized for: no more than shared memory allows
+  static constexpr int minb2 = min_blocks(t2) < int(233472 / (s2 + 1024)) ? min_blocks(t2)
+                               : (int(233472 / (s2 + 1024)) < 1 ? 1 : int(233472 / (s2 + 1024)));
   static constexpr size_t head = 32;
   static constexpr size_t s3 = head + size_t(N) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
                                size_t(RW * 3 * N) * sizeof(float2) + size_t(2 * Tile<N, 3 * RW, false>::elems) * sizeof(float2);
@@ -251,7 +260,7 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
 
 // ASM2: inverse y transforms of the six components, in place
 template <int N>
-__global__ void __launch_bounds__(FA<N>::t2, min_blocks(FA<N>::t2)) k_fa_y(FAArgs a) {
+__global__ void __launch_bounds__(FA<N>::t2, FA<N>::minb2) k_fa_y(FAArgs a) {
   using F = FA<N>;
   constexpr int P = F::P2, KB = F::Kh / P;
   float2 *tw = ff_smem(), *buf = tw + N, *buf2 = buf + (F::nbuf == 2 ? Tile<N, P, true>::elems : 0),
