@@ -819,10 +819,13 @@ template <int M, int RW, int G, int NIN, bool WIDE = false> struct ZR {
   static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(RW * srow) * sizeof(float2) +
                                  size_t(RW) * nin_pad * M * sizeof(float) +
                                  size_t(2 * Tile<M, G, false>::elems) * sizeof(float2);
-  // CTAs per SM: by registers (64 each) and by shared memory (228 KB per SM)
+  // CTAs per SM: by shared memory (228 KB per SM) and by at least 56
+  // registers a thread (no spills for the 2LPT pass at 384 with five CTAs),
+  // at most five (small CTAs of the short lengths keep their registers)
   static constexpr int by_smem = int(233472 / (smem + 1024));
-  static constexpr int minb =
-      WIDE ? 1 : (min_blocks(threads) < by_smem ? min_blocks(threads) : (by_smem < 1 ? 1 : by_smem));
+  static constexpr int by_regs0 = 65536 / (threads * 56) < 1 ? 1 : 65536 / (threads * 56);
+  static constexpr int by_regs = by_regs0 < 5 ? by_regs0 : 5;
+  static constexpr int minb = WIDE ? 1 : (by_regs < by_smem ? by_regs : (by_smem < 1 ? 1 : by_smem));
 };
 
 // issues the bulk copies of row group g (RW rows x NIN spectra) into stage
