@@ -163,7 +163,6 @@ struct mfx_job {
   double *amp = nullptr;
   double *plt = nullptr;
   float4 *plt4 = nullptr;  // FP32 form: the PLT tables interleaved per mode
-  std::vector<float4> plt4_host;
   double2 *phase = nullptr;
   float2 *phase32 = nullptr;  // the phase tables rounded to float (FP32 form)
   double *qtab = nullptr;  // [shift][axis][N] unperturbed coordinates times lunit
@@ -1011,13 +1010,13 @@ static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
     CU(cudaMemcpyAsync(j->plt, d->plt_table, size_t(MFX_PLT_TABLE_DOUBLES) * 8, cudaMemcpyHostToDevice,
                        j->stream));
     if (!j->fp64) {
-      // interleave (D_r, D_theta, D_phi, alpha^-1) per mode for the FP32 form
+      // interleave (D_r, D_theta, D_phi, alpha^-1) per mode for the FP32 form,
+      // on the device from the tables just uploaded: no copy from pageable
+      // host memory (which synchronises the host and can queue behind the
+      // particle downloads of a pipelined run on the copy engine)
       const size_t nm = size_t(MFX_PLT_TABLE_DOUBLES) / 4;
-      j->plt4_host.resize(nm);
-      for (size_t q = 0; q < nm; ++q)
-        j->plt4_host[q] = make_float4(float(d->plt_table[q]), float(d->plt_table[nm + q]),
-                                      float(d->plt_table[2 * nm + q]), float(d->plt_table[3 * nm + q]));
-      CU(cudaMemcpyAsync(j->plt4, j->plt4_host.data(), nm * sizeof(float4), cudaMemcpyHostToDevice, j->stream));
+      k_plt_to_f4<<<int((nm + 255) / 256), 256, 0, j->stream>>>(j->plt, j->plt4, nm);
+      CU(cudaGetLastError());
     }
   }
   return MFX_OK;
@@ -1683,14 +1682,16 @@ int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count
   CU(cudaSetDevice(job->eng->device));
   if (!job->xfer[0]) CU(cudaStreamCreateWithFlags(&job->xfer[0], cudaStreamNonBlocking));
   if (!job->fetched) CU(cudaEventCreateWithFlags(&job->fetched, cudaEventDisableTiming));
-  cudaStream_t x = job->xfer[0];
   // after the job's work enqueued so far (the run whose particles these are)
   CU(cudaEventRecord(job->fetched, job->stream));
-  CU(cudaStreamWaitEvent(x, job->fetched, 0));
+  CU(cudaStreamWaitEvent(job->xfer[0], job->fetched, 0));
   const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
   const Xfer xs[3] = {{pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
                       {ids, static_cast<char *>(job->ids) + is * first, is * count}};
+  // one copy stream: the host link is full with one (193 GB/s on GB300), and
+  // several streams' copies beside a running job made the step times vary
+  cudaStream_t x = job->xfer[0];
   for (const Xfer &q : xs)
     if (q.dst && q.bytes) CU(cudaMemcpyAsync(q.dst, q.src, q.bytes, cudaMemcpyDefault, x));
   CU(cudaEventRecord(job->fetched, x));

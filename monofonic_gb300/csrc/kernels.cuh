@@ -469,6 +469,13 @@ __device__ __forceinline__ double plt_cic(const double *T, double x, double y, d
 // split exactly in integers (ix = floor(64 i / N), dx = (64 i mod N)/N), the
 // direction of the interpolation point's k equals that of the mode's signed
 // index vector, and the four tables are read as one float4 per CIC corner.
+// the FP32 form's PLT tables interleaved per mode, (D_r, D_theta, D_phi,
+// alpha^-1) rounded to float, from the four FP64 tables of nm entries each
+static __global__ void k_plt_to_f4(const double *T, float4 *out, size_t nm) {
+  for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; q < nm; q += size_t(gridDim.x) * blockDim.x)
+    out[q] = make_float4(float(T[q]), float(T[nm + q]), float(T[2 * nm + q]), float(T[3 * nm + q]));
+}
+
 // the FP32 form's PLT tables read from global memory (through the read-only path)
 struct PltGlobal {
   const float4 *T;
