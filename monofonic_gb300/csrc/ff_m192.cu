@@ -1,12 +1,9 @@
-// Fused-transform kernels for padded length(s) 24 48 96 144 (see fused_launch.cuh);
+// Fused-transform kernels for padded length(s) 192 (see fused_launch.cuh);
 // one translation unit per size group so that they compile in parallel.
 #include "fused_launch.cuh"
 
 namespace mfx {
 namespace ff {
-MFX_FF_DEFINE(24)
-MFX_FF_DEFINE(48)
-MFX_FF_DEFINE(96)
-MFX_FF_DEFINE(144)
+MFX_FF_DEFINE(192)
 }  // namespace ff
 }  // namespace mfx
