@@ -238,10 +238,12 @@ def test_3lpt_plt_fp64_32(mfxlib, engine, oracle, lattice):
 # ---------------------------------------------------------------------------
 # FP32-compensated form
 # ---------------------------------------------------------------------------
-def test_fp32c_error_in_interparticle_spacing(mfxlib, engine, oracle):
-    lattice = 1
+@pytest.mark.parametrize("lattice,fixing,L", [(1, False, 300.0), (2, True, 1000.0 * 64 / 768)])
+def test_fp32c_error_in_interparticle_spacing(mfxlib, engine, oracle, lattice, fixing, L):
+    """FP32 form (fused transforms and assembly) against the FP64 oracle: the
+    256^3 BCC and the amplitude-fixed 768^3 FCC configurations' physics at 64^3."""
     tab = engine.plt_table(lattice)
-    c = Case(mfxlib, 64, 300.0, 24.0, 3, 4242, lattice=lattice, plt=tab)
+    c = Case(mfxlib, 64, L, 24.0, 3, 4242, lattice=lattice, fixing=fixing, plt=tab)
     j = c.job(mfxlib, engine, precision=mfxlib.FP32C, pos64=True, vel64=False)
     j.run()
     res = c.oracle(oracle)
