@@ -124,7 +124,9 @@ int mfx_job_run(mfx_job *job);
 int mfx_job_wait(mfx_job *job, int timeout_ms);
 /* Copies the particle container (particle_container.hh:29-188 layout:
    interleaved xyz) into caller buffers; each pointer may be host or device
-   memory or NULL to skip. */
+   memory or NULL to skip.  Ids for a host buffer are not copied: they are a
+   closed form of the particle index (particle_generator.hh:229-248), written
+   by host threads while the positions and velocities cross the host link. */
 int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids);
 /* Copies particles [first, first + count) only, for output plugins that write
    a large container in chunks (the reference's plugins write the whole

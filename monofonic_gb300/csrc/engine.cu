@@ -28,6 +28,8 @@
 #include <stdexcept>
 #include <time.h>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../include/mfx.h"
@@ -172,6 +174,7 @@ struct mfx_job {
   void *mslot[18] = {};
   void *asmbuf[24] = {};
   void *pos = nullptr, *vel = nullptr, *ids = nullptr;
+  std::vector<std::thread> id_fill;  // host threads writing the ids of an asynchronous fetch
   void *work = nullptr;
   size_t work_bytes = 0;
   Plan m_r2c, m_c2r, n_c2r;
@@ -1022,8 +1025,71 @@ static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
   return MFX_OK;
 }
 
+// Particle ids are a closed form of the particle's index, the lattice
+// generator's rule (particle_generator.hh:229-248): particle p = shift * N^3 +
+// cell carries id_offset * ns * N^3 + ns * cell + shift, the value the read-out
+// kernels write on the device.  A fetch writes them into the caller's array
+// with host threads beside the copies instead of moving 8 (or 4) more bytes per
+// particle over the host link, which bounds a realisation end to end.
+struct IdRule {
+  uint64_t base, ns, n3;
+  bool id64;
+};
+static IdRule id_rule(const mfx_job *j) {
+  const uint64_t n3 = uint64_t(j->d.ngrid) * j->d.ngrid * j->d.ngrid, ns = uint64_t(j->ns);
+  return {j->d.id_offset * ns * n3, ns, n3, j->d.id64 != 0};
+}
+template <class T>
+static void write_ids(T *o, uint64_t p0, uint64_t p1, const IdRule &r) {
+  while (p0 < p1) {  // one run of cells per sub-lattice shift
+    const uint64_t s = p0 / r.n3, c0 = p0 % r.n3, c1 = std::min<uint64_t>(r.n3, c0 + (p1 - p0));
+    const uint64_t b = r.base + s;
+    for (uint64_t c = c0; c < c1; ++c) o[c - c0] = T(b + r.ns * c);
+    o += c1 - c0;
+    p0 += c1 - c0;
+  }
+}
+static void write_ids(const IdRule &r, uint64_t p0, uint64_t p1, void *dst) {  // dst holds particle p0
+  if (r.id64) write_ids(static_cast<uint64_t *>(dst), p0, p1, r);
+  else write_ids(static_cast<uint32_t *>(dst), p0, p1, r);
+}
+// starts host threads writing the ids of particles [first, first + count) into
+// dst; join_id_fill waits for them
+static void start_id_fill(mfx_job *j, size_t first, size_t count, void *dst) {
+  if (!dst || !count) return;
+  const IdRule r = id_rule(j);
+  const size_t hw = std::max(2u, std::thread::hardware_concurrency());
+  const size_t nt = std::max<size_t>(1, std::min<size_t>({size_t(8), hw / 2, count >> 21}));
+  const size_t per = (count + nt - 1) / nt, es = r.id64 ? 8 : 4;
+  for (size_t t = 0; t < nt; ++t) {
+    const size_t a = first + t * per, b = std::min(first + count, a + per);
+    if (a >= b) break;
+    void *o = static_cast<char *>(dst) + es * (a - first);
+    try {
+      j->id_fill.emplace_back([r, a, b, o] { write_ids(r, a, b, o); });
+    } catch (const std::system_error &) {
+      write_ids(r, a, b, o);  // no thread to be had: this share is written here
+    }
+  }
+}
+// true when host threads can write p (pageable, page-locked or managed memory);
+// ids for a device destination are copied from the device's array instead
+static bool host_writable(const void *p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return at.type != cudaMemoryTypeDevice;
+}
+static void join_id_fill(mfx_job *j) {
+  for (auto &t : j->id_fill) t.join();
+  j->id_fill.clear();
+}
+
 static void free_job(mfx_job *j) {
   if (!j) return;
+  join_id_fill(j);
   if (j->stream) cudaStreamSynchronize(j->stream);
   if (j->gexec) cudaGraphExecDestroy(j->gexec);
   if (j->graph) cudaGraphDestroy(j->graph);
@@ -1589,10 +1655,15 @@ int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids) {
   if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has not produced particles");
   CU(cudaSetDevice(job->eng->device));
   const size_t np = job->npart;
+  const bool host_ids = ids && host_writable(ids);
   const Xfer xs[3] = {{pos, job->pos, np * 3 * (job->d.pos64 ? 8 : 4)},
                       {vel, job->vel, np * 3 * (job->d.vel64 ? 8 : 4)},
-                      {ids, job->ids, np * (job->d.id64 ? 8 : 4)}};
-  return download(job, xs, 3);
+                      {host_ids ? nullptr : ids, job->ids, np * (job->d.id64 ? 8 : 4)}};
+  join_id_fill(job);
+  if (host_ids) start_id_fill(job, 0, np, ids);
+  const int rc = download(job, xs, 3);
+  join_id_fill(job);
+  return rc;
   GUARD_END
 }
 
@@ -1605,10 +1676,15 @@ int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void
     return set_error(MFX_EINVAL, "range [%zu, %zu) outside the %zu particles", first, first + count, job->npart);
   CU(cudaSetDevice(job->eng->device));
   const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
+  const bool host_ids = ids && host_writable(ids);
   const Xfer xs[3] = {{pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
-                      {ids, static_cast<char *>(job->ids) + is * first, is * count}};
-  return download(job, xs, 3);
+                      {host_ids ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
+  join_id_fill(job);
+  if (host_ids) start_id_fill(job, first, count, ids);
+  const int rc = download(job, xs, 3);
+  join_id_fill(job);
+  return rc;
   GUARD_END
 }
 
@@ -1686,9 +1762,12 @@ int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count
   CU(cudaEventRecord(job->fetched, job->stream));
   CU(cudaStreamWaitEvent(job->xfer[0], job->fetched, 0));
   const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
+  const bool host_ids = ids && host_writable(ids);
   const Xfer xs[3] = {{pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
-                      {ids, static_cast<char *>(job->ids) + is * first, is * count}};
+                      {host_ids ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
+  join_id_fill(job);  // an earlier fetch's ids (long done when fetches are a step apart)
+  if (host_ids) start_id_fill(job, first, count, ids);
   // one copy stream: the host link is full with one (193 GB/s on GB300), and
   // several streams' copies beside a running job made the step times vary
   cudaStream_t x = job->xfer[0];
@@ -1703,6 +1782,7 @@ int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count
 int mfx_job_wait_fetch(mfx_job *job) {
   GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
+  join_id_fill(job);
   if (job->xfer[0]) CU(cudaStreamSynchronize(job->xfer[0]));
   return MFX_OK;
   GUARD_END

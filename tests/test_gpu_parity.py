@@ -386,6 +386,38 @@ def test_fused_rerun_is_identical(mfxlib, engine, n, lattice, monkeypatch):
                 assert rel_l2(x, y) < 1e-6
 
 
+@pytest.mark.parametrize("lattice,id64", [(2, True), (1, False)])
+def test_fetched_ids_follow_the_lattice_rule(mfxlib, engine, lattice, id64):
+    """A fetch writes the ids of host destinations with host threads (a closed
+    form of the particle index, particle_generator.hh:229-248) and copies those
+    of device destinations from the device's array: both agree with the rule
+    for an id offset, for ranges across sub-lattice boundaries and for the
+    asynchronous fetch."""
+    import torch
+    n, off = 32, 5
+    c = Case(mfxlib, n, 300.0, 24.0, 1, 4242, lattice=lattice)
+    j = c.job(mfxlib, engine, precision=mfxlib.FP32C, id64=id64, id_offset=off)
+    j.run()
+    npart, n3 = j.num_particles, n ** 3
+    ns = npart // n3
+    p = np.arange(npart, dtype=np.uint64)
+    want = np.uint64(off * ns * n3) + np.uint64(ns) * (p % np.uint64(n3)) + p // np.uint64(n3)
+    want = want if id64 else want.astype(np.uint32)
+    assert np.array_equal(j.particles()[2], want)
+    first = n3 - 1000
+    count = min(2 * n3 + 37, npart - first)  # across one (BCC) or two (FCC) sub-lattice boundaries
+    assert np.array_equal(j.particles_range(first, count)[2], want[first:first + count])
+    tdt = torch.int64 if id64 else torch.int32
+    dev = torch.zeros(count, dtype=tdt, device="cuda")
+    j.fetch_particles_range_into(first, count, None, None, dev.data_ptr())
+    assert np.array_equal(dev.cpu().numpy().view(want.dtype), want[first:first + count])
+    pinned = torch.zeros(count, dtype=tdt, pin_memory=True)
+    j.fetch_particles_range_async(first, count, None, None, pinned.data_ptr())
+    j.wait_fetch()
+    assert np.array_equal(pinned.numpy().view(want.dtype), want[first:first + count])
+    j.close()
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
 def test_assemble_per_order_is_linear(mfxlib, engine, precision):
     """mfx_job_assemble: the displacements and velocities of the orders taken
