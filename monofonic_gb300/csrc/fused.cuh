@@ -381,27 +381,25 @@ MFX_HD int hslot(int x, int y) {
   return lo == 0 ? (hi == 1 ? 3 : 4) : 5;
 }
 
-// compensated accumulation (Ogita-Rump-Oishi TwoSum / FMA TwoProduct)
+// Kahan accumulation (Kahan 1965, "Further remarks on reducing truncation
+// errors") of the sources' products, with the running compensation c folded
+// into each product by one FMA: y = a*b - c rounded once, t = s + y,
+// c = (t - s) - y.  Four operations a term (TwoProduct + TwoSum take about
+// ten); the sum's error stays within about 2u of the sum of |terms|.
 struct Acc32 {
-  float hi = 0.f, lo = 0.f;
-  MFX_HD void add(float v) {
-    const float s = hi + v, bp = s - hi;
-    lo += (hi - (s - bp)) + (v - bp);
-    hi = s;
+  float s = 0.f, c = 0.f;
+  MFX_HD void step(float y) {
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
   }
-  MFX_HD void add_prod(float c, float a, float b) {
-    const float p = a * b, e = fmaf(a, b, -p), q = c * p, e2 = fmaf(c, p, -q) + c * e;
-    add(q);
-    lo += e2;
-  }
-  // the same for a coefficient C in {1, -1, 2}, whose product with p is exact
+  MFX_HD void add_prod(float k, float a, float b) { step(fmaf(k * a, b, -c)); }
+  // a coefficient C in {1, -1, 2}, whose product with a is exact
   template <int C> MFX_HD void add_prod(float a, float b) {
     static_assert(C == 1 || C == -1 || C == 2, "exact coefficients only");
-    const float p = a * b, e = fmaf(a, b, -p);
-    add(float(C) * p);
-    lo += float(C) * e;
+    step(fmaf(float(C) * a, b, -c));
   }
-  MFX_HD float value() const { return hi + lo; }
+  MFX_HD float value() const { return s - c; }
 };
 
 // 2LPT source (ic_generator.cc:530-534) from the six phi1 Hessians
