@@ -268,7 +268,9 @@ template <int L> __device__ __forceinline__ float2 *obuf(float2 *buf, float2 *bu
   return Fac<L>::steps == 3 ? buf : buf2;
 }
 
-template <int L, int PP, bool PF, bool INV, bool LDB = true, bool B1 = true, class Ld, class St>
+// SL: a barrier between the last step's gathers and its scatters, so that st
+// may write the buffer the last step reads (buf for two steps, buf2 for three)
+template <int L, int PP, bool PF, bool INV, bool LDB = true, bool B1 = true, bool SL = false, class Ld, class St>
 __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const float2 *tw, const Ld &ld, const St &st) {
   using F = Fac<L>;
   using T = Tile<L, PP, PF>;
@@ -304,7 +306,12 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
     float2 v[RL];
     int q, j;
     split<PP, S::J, PF>(t, q, j);
-    if (t < PP * S::J) {
+    if constexpr (SL) {
+      const bool act = t < PP * S::J;
+      if (act) S::gather(j, [&](int n) { return src[T::at(q, n)]; }, tw, v);
+      __syncthreads();
+      if (act) S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v);
+    } else if (t < PP * S::J) {
       S::gather(j, [&](int n) { return src[T::at(q, n)]; }, tw, v);
       S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v);
     }

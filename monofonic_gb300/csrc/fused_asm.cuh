@@ -108,8 +108,15 @@ template <int N> struct FA {
   static constexpr int minb2 = min_blocks(t2) < int(233472 / (s2 + 1024)) ? min_blocks(t2)
                                : (int(233472 / (s2 + 1024)) < 1 ? 1 : int(233472 / (s2 + 1024)));
   static constexpr size_t head = 32;
+  // ASM3: the components land in the tile buffer the transform's last step
+  // reads (in place) or has finished with, so no buffer of their own
   static constexpr size_t s3 = head + size_t(N) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
-                               size_t(RW * 3 * N) * sizeof(float2) + size_t(2 * Tile<N, 3 * RW, false>::elems) * sizeof(float2);
+                               size_t(nbuf * Tile<N, 3 * RW, false>::elems) * sizeof(float2);
+  // CTAs per SM the ASM3 registers are sized for (about 104 a thread), no more
+  // than shared memory allows
+  static constexpr int minb3_r = 65536 / (t3 * 104) < 1 ? 1 : 65536 / (t3 * 104);
+  static constexpr int minb3_s = int(233472 / (s3 + 1024)) < 1 ? 1 : int(233472 / (s3 + 1024));
+  static constexpr int minb3 = minb3_r < minb3_s ? minb3_r : minb3_s;
 };
 
 // stages the slice of tile (j, kz0) with nt threads (the caller synchronises)
@@ -307,17 +314,20 @@ __device__ __forceinline__ double f2d_exact(float f) {
 // ASM3: inverse z transforms (c2r, component pairs (0,1), (2,3), (4,5)) and the
 // particles of RW rows at a time
 template <int N>
-__global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
+__global__ void __launch_bounds__(FA<N>::t3, FA<N>::minb3) k_fa_z(FAArgs a) {
   using F = FA<N>;
   constexpr int RW = F::RW, Kh = F::Kh, G = 3 * RW;
   char *base = reinterpret_cast<char *>(ff_smem());
   uint64_t *bar = reinterpret_cast<uint64_t *>(base);
   volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
   float2 *tw = reinterpret_cast<float2 *>(base + F::head);
-  float2 *stage = tw + N;            // [w][c][Kh]
-  float2 *h2 = stage + RW * 6 * Kh;  // [w][pair][z]
-  float2 *buf = h2 + RW * 3 * N;
-  float2 *buf2 = buf + Tile<N, G, false>::elems;
+  float2 *stage = tw + N;                        // [w][c][Kh]
+  float2 *buf = stage + RW * 6 * Kh;
+  float2 *buf2 = F::nbuf == 2 ? buf + Tile<N, G, false>::elems : nullptr;
+  // [w][pair][z]: written by the transform's last step into buf, which that
+  // step reads in place with two steps (a barrier between its reads and
+  // writes) and has finished with after the middle step with three
+  float2 *h2 = buf;
   const size_t ngroups = size_t(N) * N / RW;
   constexpr uint32_t rowbytes = uint32_t(Kh) * sizeof(float2);
   auto fetch = [&](size_t g) {
@@ -348,8 +358,8 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
       }
       return;
     }
-    // buf was last read by the previous group's transform, before the barrier above
-    pencil_fft<N, G, false, true, false, false>(
+    // buf (h2) was last read by the previous group's read-out, before the barrier above
+    pencil_fft<N, G, false, true, false, false, Fac<N>::steps == 2>(
         buf, buf2, tw,
         [&](int q, int n) -> float2 {
           const int w = q / 3, c0 = 2 * (q - w * 3);
@@ -375,18 +385,20 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
         [&](int q, int z, float2 v) { h2[q * N + z] = v; });
     __syncthreads();  // the stage is free, the components are in h2
     if (threadIdx.x == 0 && gn < ngroups) fetch(gn);
-    for (int t = threadIdx.x; t < RW * (N / 4); t += blockDim.x) {
-      const int w = t / (N / 4), z0 = 4 * (t - w * (N / 4));
+    // two particles per thread (registers for three CTAs per SM); every store
+    // a 16- or 8-byte vector store
+    for (int t = threadIdx.x; t < RW * (N / 2); t += blockDim.x) {
+      const int w = t / (N / 2), z0 = 2 * (t - w * (N / 2));
       const size_t row = g * RW + w, cell = row * N + z0;
       const int x = int(row / N), y = int(row - size_t(x) * N);
       const float2 *hw = h2 + w * 3 * N;
       // q + Psi in FP64; the velocities stay in float unless stored in FP64
       // (FP64 arithmetic and conversions are slow on this part)
-      double pv[12];
-      float vv[12];
+      double pv[6];
+      float vv[6];
       const double qx = a.qtab[x], qy = a.qtab[N + y];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
+      for (int c = 0; c < 2; ++c) {
         const float2 a0 = hw[z0 + c], a1 = hw[N + z0 + c], a2 = hw[2 * N + z0 + c];
         pv[3 * c + 0] = qx + f2d_exact(a0.x);
         pv[3 * c + 1] = qy + f2d_exact(a0.y);
@@ -395,28 +407,26 @@ __global__ void __launch_bounds__(FA<N>::t3, 2) k_fa_z(FAArgs a) {
         vv[3 * c + 1] = a2.x;
         vv[3 * c + 2] = a2.y;
       }
-      if (a.pos64) store12(reinterpret_cast<double *>(a.pos) + 3 * (pbase + cell), pv);
-      else store12(reinterpret_cast<float *>(a.pos) + 3 * (pbase + cell), pv);
+      if (a.pos64) store6(reinterpret_cast<double *>(a.pos) + 3 * (pbase + cell), pv);
+      else store6(reinterpret_cast<float *>(a.pos) + 3 * (pbase + cell), pv);
       if (a.vel64) {
-        double vd[12];
+        double vd[6];
 #pragma unroll
-        for (int c = 0; c < 12; ++c) vd[c] = double(vv[c]) * a.vunscale;
-        store12(reinterpret_cast<double *>(a.vel) + 3 * (pbase + cell), vd);
+        for (int c = 0; c < 6; ++c) vd[c] = double(vv[c]) * a.vunscale;
+        store6(reinterpret_cast<double *>(a.vel) + 3 * (pbase + cell), vd);
       } else {
 #pragma unroll
-        for (int c = 0; c < 12; ++c) vv[c] *= a.vunscale_f;
-        store12(reinterpret_cast<float *>(a.vel) + 3 * (pbase + cell), vv);
+        for (int c = 0; c < 6; ++c) vv[c] *= a.vunscale_f;
+        store6(reinterpret_cast<float *>(a.vel) + 3 * (pbase + cell), vv);
       }
       if (a.ids) {
         const uint64_t st = uint64_t(a.nshift_total), id0 = a.id_offset + st * cell + uint64_t(a.shift);
-        if (a.id64) {
-          ulonglong2 *o = reinterpret_cast<ulonglong2 *>(reinterpret_cast<uint64_t *>(a.ids) + pbase + cell);
-          o[0] = make_ulonglong2(id0, id0 + st);
-          o[1] = make_ulonglong2(id0 + 2 * st, id0 + 3 * st);
-        } else {
-          *reinterpret_cast<uint4 *>(reinterpret_cast<uint32_t *>(a.ids) + pbase + cell) =
-              make_uint4(uint32_t(id0), uint32_t(id0 + st), uint32_t(id0 + 2 * st), uint32_t(id0 + 3 * st));
-        }
+        if (a.id64)
+          *reinterpret_cast<ulonglong2 *>(reinterpret_cast<uint64_t *>(a.ids) + pbase + cell) =
+              make_ulonglong2(id0, id0 + st);
+        else
+          *reinterpret_cast<uint2 *>(reinterpret_cast<uint32_t *>(a.ids) + pbase + cell) =
+              make_uint2(uint32_t(id0), uint32_t(id0 + st));
       }
     }
     // h2 is rewritten by the next group's transform, after the barrier at its top

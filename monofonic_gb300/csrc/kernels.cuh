@@ -759,6 +759,21 @@ __device__ __forceinline__ void store12(float *o, const double *v) {
         make_float4(float(v[4 * q]), float(v[4 * q + 1]), float(v[4 * q + 2]), float(v[4 * q + 3]));
 }
 
+// 6 consecutive outputs (2 particles x xyz, the first at an even index): 16-byte
+// stores for double, 8-byte ones for float
+__device__ __forceinline__ void store6(double *o, const double *v) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) reinterpret_cast<double2 *>(o)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+}
+__device__ __forceinline__ void store6(float *o, const float *v) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) reinterpret_cast<float2 *>(o)[q] = make_float2(v[2 * q], v[2 * q + 1]);
+}
+__device__ __forceinline__ void store6(float *o, const double *v) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) reinterpret_cast<float2 *>(o)[q] = make_float2(float(v[2 * q]), float(v[2 * q + 1]));
+}
+
 // One thread per 4 consecutive cells along k (N is a multiple of 4): every
 // store is a 16-byte vector store and a warp writes one contiguous run.
 template <typename R, typename PosT, typename VelT>
