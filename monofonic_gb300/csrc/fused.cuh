@@ -1096,10 +1096,10 @@ template <int M, int NIN> struct ZW {
   static constexpr size_t head = 32;
   static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(NIN * D::Kh) * sizeof(float2) +
                                  size_t(NPI * padL) * sizeof(float2);
-  // CTAs per SM by shared memory and by about 128 registers a thread (a lane
-  // holds up to three butterflies of a step)
+  // CTAs per SM by shared memory and by about 168 registers a thread (a lane
+  // holds up to three butterflies of a step; 128 spilled in the 2LPT pass)
   static constexpr int by_smem = int(233472 / (smem + 1024));
-  static constexpr int by_regs = 65536 / (threads * 128) < 1 ? 1 : 65536 / (threads * 128);
+  static constexpr int by_regs = 65536 / (threads * 168) < 1 ? 1 : 65536 / (threads * 168);
   static constexpr int minb = by_regs < by_smem ? by_regs : (by_smem < 1 ? 1 : by_smem);
   static constexpr bool ok = Fac<M>::maxJ <= 96;
 };
