@@ -90,6 +90,18 @@ def replica_throughput(local_ms, local_particles, device="cpu"):
     return float(t.item()), float(n.item()) / (float(t.item()) * 1e-3)
 
 
+_CLOCK_DIR = None
+
+
+def clock_csv(name):
+    """Path for an nvidia-smi sample file, in a per-process temporary directory."""
+    global _CLOCK_DIR
+    if _CLOCK_DIR is None:
+        import tempfile
+        _CLOCK_DIR = tempfile.mkdtemp(prefix="mfx_bench_clocks_")
+    return os.path.join(_CLOCK_DIR, name)
+
+
 class Clocks:
     """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
 
@@ -206,7 +218,7 @@ def run_ours(args):
         job.run()
     job.set_profiling(True)
     barrier()
-    clocks = Clocks(local, str(ROOT / "gpurun_out" / ("clocks_rank%d.csv" % rank))) if rank == 0 else None
+    clocks = Clocks(local, clock_csv("clocks_rank%d.csv" % rank)) if rank == 0 else None
     dev_ms, prof_tot = [], {}
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -421,7 +433,7 @@ def run_ensemble(args):
         dist.init_process_group("nccl")
         dist.barrier()
     torch.cuda.synchronize()
-    clocks = Clocks(local, str(ROOT / "gpurun_out" / "clocks_ensemble.csv")) if rank == 0 else None
+    clocks = Clocks(local, clock_csv("clocks_ensemble.csv")) if rank == 0 else None
     ms = []
     for _ in range(args.steps):
         l2_flush(flush)
@@ -576,7 +588,7 @@ def run_serving(args):
             tk[q] = srv.submit(s)
 
     th = threading.Thread(target=producer)
-    clocks = Clocks(0, str(ROOT / "gpurun_out" / "clocks_serving.csv"))
+    clocks = Clocks(0, clock_csv("clocks_serving.csv"))
     th.start()
     th.join()
     lat = []
@@ -736,7 +748,6 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end pass and the report")
     ap.add_argument("--tiles", default="", help="fused-transform tiles 'PXY,PZ' instead of the autotuner's")
     args = ap.parse_args()
-    (ROOT / "gpurun_out").mkdir(exist_ok=True)
     if args.impl == "reference":
         out = run_reference(args)
         if out:

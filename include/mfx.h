@@ -252,10 +252,16 @@ int mfx_server_destroy(mfx_server *s);
    code that owns all of HBM through its own pool, or one running under a
    device-memory cap).  It allocates nothing; the device copy of the seed table
    lives in a fixed 4 MiB __device__ array, so ngrid is limited to
-   MFX_NOALLOC_MAX_NGRID and larger sizes are rejected with MFX_EINVAL.  The
-   first call on a device resolves that array's address (make it before any
-   stream capture).  Calls share the array: calls that overlap on the GPU race,
-   so order them on one stream.  `stream` is a cudaStream_t or NULL. */
+   MFX_NOALLOC_MAX_NGRID and larger sizes are rejected with MFX_EINVAL.  That
+   array and the call's kernels become resident on a device when
+   mfx_engine_create runs there (also under CUDA's lazy module loading), so
+   create the engine before reserving the rest of HBM and before any stream
+   capture; they stay resident until the process exits.  Calls share the
+   array: calls that overlap on the GPU race, so order them on one stream.
+   The seed table is read by a copy ordered on `stream`: a page-locked
+   seed_table must stay unchanged until the work on `stream` has finished
+   (pageable memory is staged before the call returns).  The call leaves the
+   caller's current device unchanged.  `stream` is a cudaStream_t or NULL. */
 #define MFX_NOALLOC_MAX_NGRID 1024
 int mfx_noise_fill_noalloc(mfx_engine *eng, uint32_t ngrid, double boxlen, const uint32_t *seed_table, int raw,
                            int fixing, int inversion, int precision, void *out_device, void *stream);

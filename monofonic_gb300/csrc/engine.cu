@@ -1429,6 +1429,7 @@ int mfx_engine_create(const mfx_engine_opts *opts, mfx_engine **out) {
     return set_error(MFX_ECUDA, "no CUDA device available");
   if (dev < 0 || dev >= count) return set_error(MFX_EINVAL, "device %d out of range", dev);
   CU(cudaSetDevice(dev));
+  TRY(noalloc_prepare(dev));
   size_t free_b = 0, total_b = 0;
   CU(cudaMemGetInfo(&free_b, &total_b));
   auto *e = new mfx_engine();

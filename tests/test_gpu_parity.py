@@ -81,6 +81,13 @@ def test_device_ranlux_stream_bit_exact(engine, oracle, seed):
     assert np.array_equal(got, oracle.ranlxd1_words(seed, 3000))
 
 
+def test_device_ranlux_matches_gsl_known_answer(engine):
+    """GSL's published ranlxd1 value (rng/test.c: seed 1, 10000th draw of
+    gsl_rng_get = 1998227290, i.e. the top 32 bits of the 48-bit word)."""
+    w = int(engine.ranlxd1_words(1, 10000)[-1])
+    assert w >> 16 == 1998227290
+
+
 def test_device_ranlux_on_seed_table_entries(mfxlib, engine, oracle):
     t = mfxlib.ngenic_seed_table(12345, 32)
     for s in t[[0, 5, 100, 1023]]:
