@@ -1,23 +1,29 @@
 """Benchmark of the LPT initial-condition hot path on GB300.
 
-Default workload (one GPU): 3LPT + PLT on a BCC lattice, 256^3 grid,
-2 x 256^3 particles, box 300 Mpc/h, z_start = 24, NGenIC seed 4242, E&H
-transfer function (Omega_m 0.3, Omega_b 0.045, h 0.7, sigma_8 0.81,
-n_s 0.965), FP32-compensated form.  One step = one full pass of the hot path
-(white noise -> phi1/phi2/phi3/A3 -> displacements/velocities -> particles).
+Default workload (one GPU): 3LPT + PLT on an FCC lattice, 768^3 grid (padded
+convolutions at 1152^3), 4 x 768^3 = 1.81e9 particles, box 1000 Mpc/h,
+z_start = 24, amplitude-fixed NGenIC white noise (seed 1), E&H transfer
+function (Omega_m 0.3, Omega_b 0.045, h 0.7, sigma_8 0.81, n_s 0.965),
+FP32-compensated form.  One step = one full pass of the hot path (white noise
+-> phi1/phi2/phi3/A3 -> displacements/velocities -> particles).  ``--workload
+bcc256`` runs the 3LPT + PLT BCC 256^3 configuration instead.
 
   value  particles/s with all inputs resident in HBM (device time, CUDA events
          on the engine's stream, L2 flushed between steps)
   e2e    the same through the C ABI with host buffers: every step uploads the
          seed / amplitude / PLT tables from pinned host memory and copies the
-         particles (f64 positions, f32 velocities, u64 IDs) back to pinned
-         host memory
-  fp64_form  the plain FP64 form of the same workload, for the FP32/FP64 ratio
+         particles (f64 positions, f32 velocities) back to pinned host memory
+         (ids written on the host)
+  fp64_form  the plain FP64 form of the same workload, for the FP32/FP64 ratio,
+         with its FFT throughput against GB300's FP64 rate
   roofline   the dominant own kernel against the measured HBM copy bandwidth
 
-``--impl reference`` times the CPU restatement of the reference path (the
-reference itself cannot be built: it needs FFTW3, GSL and HDF5) on a bounded
-sample of the same workload with all host cores.
+``--impl reference`` times the C++/OpenMP restatement of the reference's CPU
+path (oracle/lpt_omp.cc: the reference's loop structure and its 99 padded
+FFTs per 3LPT run, with an own FFT instead of FFTW; the reference itself
+cannot be built: it needs FFTW3, GSL and HDF5) with all host cores, on a
+bounded sample of the same workload's physics (a smaller grid, throughput
+per particle).
 
 Multi-GPU (torchrun): independent replicas, one realisation per rank (seed +
 rank), no data-path collective; value = all ranks' particles / max time.
@@ -50,6 +56,14 @@ WORKLOADS = {
     "bcc128": (128, 150.0, 24.0, 3, 1, True, 4242, False),
 }
 LATNAME = {0: "sc", 1: "bcc", 2: "fcc"}
+# grid of the CPU restatement's timed sample: once in our own line's
+# cpu_baseline, and per step in the reference arm (bounded so that the whole
+# --steps/--warmup run stays within a few minutes)
+CPU_SAMPLE = {"fcc768": 384, "fcc512": 256, "fcc384": 384, "bcc256": 256, "bcc128": 128, "sc64": 64}
+REF_SAMPLE = {"fcc768": 192, "fcc512": 192, "fcc384": 192, "bcc256": 256, "bcc128": 128, "sc64": 64}
+# GB300 FP64 (non-tensor) arithmetic rate, NVIDIA's published figure (FLOP/s):
+# the ceiling of the plain FP64 form's cuFFT transforms
+FP64_PEAK_SPEC = 1.25e12
 
 
 def describe(name, prec):
@@ -649,12 +663,21 @@ def fp64_and_error(args, eng, inp, plt_tab, out):
         j.run()
         if prec == mfx.FP64:
             ms = []
+            j.set_profiling(True)
+            fft = {}
             for _ in range(max(1, min(args.steps, 3))):
                 torch.cuda.synchronize()
                 j.run()
                 ms.append(sum(j.stage_times()))
+                for k, (kms, kby, kcnt) in j.kernel_profile().items():
+                    if k.startswith("cufft"):
+                        a = fft.setdefault(k, [0.0, 0.0])
+                        a[0] += kms
+                        a[1] += kby
+            j.set_profiling(False)
             res["fp64_form"] = {"value": j.num_particles / (np.mean(ms) * 1e-3), "unit": "particles/s",
                                 "ms_per_step": float(np.mean(ms)), "steps": len(ms)}
+            res["fp64_form"]["fft_rate"] = fp64_fft_rate(fft, inp["n"], len(ms), float(np.mean(ms)))
         # compared particles: all of them up to 64M (16M per order), else the first ones
         count = min(j.num_particles, 1 << 26)
         count_o = min(j.num_particles, 1 << 24)
@@ -679,56 +702,103 @@ def fp64_and_error(args, eng, inp, plt_tab, out):
     return res
 
 
-def oracle_sample(n_sample, name, threads_note):
-    """Times the oracle (CPU restatement, numpy + multi-threaded pocketfft) on the
-    workload's physics at grid n_sample; returns particles/s."""
-    from oracle import cosmo as ocosmo, lpt, plt as oplt
+def fp64_fft_rate(fft, n, steps, ms_step):
+    """FLOP rate of the plain FP64 form's cuFFT transforms: 2.5 L log2 L per
+    real transform of L points (the usual split-radix count), transforms
+    counted from the bytes each execution moves (2 x the padded field)."""
+    m = 3 * n // 2
+    out = {}
+    flops = ms = 0.0
+    for k, (kms, kby) in fft.items():
+        length = m if k.endswith("_M") else n
+        field = (length + 2) * length * length * 8.0
+        count = kby / (2.0 * field) / steps
+        f = count * 2.5 * length ** 3 * np.log2(float(length) ** 3)
+        out[k] = {"transforms_per_step": count, "ms_per_step": kms / steps,
+                  "gflops": f / (kms / steps * 1e-3) / 1e9 if kms else None}
+        flops += f
+        ms += kms / steps
+    rate = flops / (ms * 1e-3) if ms else None
+    return {"kernels": out, "fft_ms_per_step": ms, "share_of_step": ms / ms_step if ms_step else None,
+            "fft_tflops": rate / 1e12 if rate else None, "fp64_peak_tflops": FP64_PEAK_SPEC / 1e12,
+            "frac_of_fp64_peak": rate / FP64_PEAK_SPEC if rate else None,
+            "peak_source": "GB300 FP64 published rate (spec figure, not measured)"}
+
+
+def cpu_restatement(n_sample, name, plt_tab=None, seed_offset=0):
+    """One pass of the C++/OpenMP restatement of the reference path
+    (oracle/lpt_omp.cc) on the workload's physics at grid n_sample (box scaled
+    with the grid so the modes sampled keep their spacing); inputs from the
+    oracle's own cosmology.  Returns (particles/s, seconds, stage seconds)."""
+    from oracle import cosmo as ocosmo, lpt
     n, L, z, order, lat, plt, seed, fix = WORKLOADS[name]
+    Ls = L * n_sample / n
     c = ocosmo.Cosmology()
     a = 1.0 / (1.0 + z)
-    dplus, vfac = c.growth(a), c.vfact(a)
-    seeds = lpt.ngenic_seed_table(seed, n_sample)
-    grad = None
-    tab_s = 0.0
-    if plt:
-        t0 = time.perf_counter()
-        tab = oplt.plt_tables(lat)
-        tab_s = time.perf_counter() - t0
-        grad = oplt.PLTGradient(n_sample, L, tab)
+    kf = 2 * np.pi / Ls
+    q = np.arange(3 * (n_sample // 2) ** 2 + 1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        k = kf * np.sqrt(q)
+        amp = np.where(q > 0, c.amplitude(k) / (k * k), 0.0)
+    coef = lpt.lpt_coefficients(c.growth(a), c.vfact(a), order)
+    seeds = lpt.ngenic_seed_table(seed + seed_offset, n_sample)
     t0 = time.perf_counter()
-    res = lpt.run_lpt(n_sample, L, seeds, c.amplitude, order, dplus, vfac, lattice=lat, lunit=L,
-                      vunit=L / np.sqrt(a), fixing=fix, grad=grad)
+    res = lpt.run_lpt_omp(n_sample, Ls, seeds, amp, order, coef, lattice=lat, lunit=Ls, vunit=Ls / np.sqrt(a),
+                          fixing=fix, plt_table=plt_tab if plt else None)
     dt = time.perf_counter() - t0
-    npart = (1 << lat) * n_sample ** 3
-    return npart / dt, dt, tab_s, res
+    return (1 << lat) * n_sample ** 3 / dt, dt, [float(x) for x in res["times"]]
+
+
+def oracle_plt_tables(name):
+    """PLT tables of the workload's lattice from the oracle (numpy, CPU), or None."""
+    n, L, z, order, lat, plt, seed, fix = WORKLOADS[name]
+    if not plt:
+        return None, 0.0
+    from oracle import plt as oplt
+    t0 = time.perf_counter()
+    tab = oplt.plt_tables(lat)
+    return tab, time.perf_counter() - t0
+
+
+def cpu_sample_text(n_sample, name, dt, stages, tab_s, threads):
+    n, order = WORKLOADS[name][0], WORKLOADS[name][3]
+    return ("one full hot-path pass (noise -> %dLPT potentials -> particles, FP64) at %d^3 of the %d^3 workload "
+            "(%.1f s; stages noise/phi1/phi2/phi3/A3/particles %s s), throughput per particle extrapolated to "
+            "%d^3; PLT table build (%.1f s) excluded as on the GPU; C++/OpenMP CPU restatement of the reference "
+            "loops (oracle/lpt_omp.cc, %d threads; own FFT, not FFTW)"
+            % (order, n_sample, n, dt, "/".join("%.2f" % x for x in stages), n, tab_s, threads))
 
 
 def run_reference(args):
+    """The reference arm: the C++/OpenMP restatement of the reference's CPU
+    path, each step one pass on a bounded sample of the workload."""
     rank, world, local = dist_env()
     if rank != 0:
         return None
     from oracle import lpt
     lpt.build_lib()
-    n_sample = 128 if WORKLOADS[args.workload][0] >= 128 else WORKLOADS[args.workload][0]
-    vals, dts = [], []
-    tab_s = 0.0
+    lpt.build_omp_lib()
+    threads = int(lpt.omp_lib().mfxo_omp_threads())
+    n_sample = REF_SAMPLE[args.workload]
+    tab, tab_s = oracle_plt_tables(args.workload)
+    vals, dts, stages = [], [], None
     for s in range(args.warmup + args.steps):
-        v, dt, ts, _ = oracle_sample(n_sample, args.workload, "")
-        tab_s = max(tab_s, ts)
+        v, dt, st = cpu_restatement(n_sample, args.workload, tab, seed_offset=s)
         if s >= args.warmup:
             vals.append(v)
             dts.append(dt)
-    v = float(np.mean(vals))
-    cores = os.cpu_count()
-    sample = ("full hot path (noise -> 3LPT potentials -> particles, FP64) at %d^3 of the %d^3 workload, "
-              "PLT table build (%.1f s) excluded; CPU restatement (numpy + pocketfft, %d threads for FFTs): "
-              "the reference needs FFTW3/GSL/HDF5, absent on this image" % (n_sample, WORKLOADS[args.workload][0], tab_s, cores))
+            stages = st
+    total = sum(dts)
+    npart = (1 << WORKLOADS[args.workload][4]) * n_sample ** 3
+    v = npart * len(dts) / total
+    sample = cpu_sample_text(n_sample, args.workload, float(np.mean(dts)), stages, tab_s, threads)
+    cfg = describe(args.workload, args.precision)
+    cfg["timed_sample_grid"] = n_sample
     return {"metric": metric_name(args.workload, args.precision), "impl": "reference",
             "value": v, "unit": "particles/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(dts)) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (NGenIC white noise, seeded)",
-            "config": describe(args.workload, args.precision),
-            "cpu_baseline": {"value": v, "unit": "particles/s", "cores": cores, "kind": "port", "sample": sample},
+            "dtype": "f64", "data": "synthetic (NGenIC white noise, seeded)", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "particles/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -738,7 +808,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bcc256", choices=sorted(WORKLOADS) + ["ensemble64", "serve"])
+    ap.add_argument("--workload", default="fcc768", choices=sorted(WORKLOADS) + ["ensemble64", "serve"])
     ap.add_argument("--requests", type=int, default=48, help="serve: number of requests")
     ap.add_argument("--load", type=float, default=0.8, help="serve: arrival rate / saturated job rate")
     ap.add_argument("--inflight", type=int, default=8, help="serve: max jobs in flight")
@@ -772,11 +842,14 @@ def main():
         if not args.no_cpu_baseline and world == 1:
             from oracle import lpt
             lpt.build_lib()
-            n_sample = 128 if inp["n"] >= 128 else inp["n"]
-            v, dt, ts, _ = oracle_sample(n_sample, args.workload, "")
-            out["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": os.cpu_count(), "kind": "port",
-                                   "sample": "one full hot-path pass at %d^3 of the %d^3 workload (%.1f s), PLT table build excluded; "
-                                             "CPU restatement in numpy + multi-threaded pocketfft" % (n_sample, inp["n"], dt)}
+            lpt.build_omp_lib()
+            threads = int(lpt.omp_lib().mfxo_omp_threads())
+            n_sample = CPU_SAMPLE[args.workload]
+            tab, tab_s = oracle_plt_tables(args.workload)
+            v, dt, st = cpu_restatement(n_sample, args.workload, tab)
+            out["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": threads, "kind": "port",
+                                   "sample": cpu_sample_text(n_sample, args.workload, dt, st, tab_s, threads)}
+            out["config"]["cpu_baseline_timed_grid"] = n_sample
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

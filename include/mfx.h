@@ -100,7 +100,11 @@ size_t mfx_last_error(char *buf, size_t len);
 const char *mfx_version(void);
 
 /* ---- engine -------------------------------------------------------------- */
-/* Replaces the process-wide FFTW/OpenMP set-up of main.cc:156-182. */
+/* Replaces the process-wide FFTW/OpenMP set-up of main.cc:156-182.
+   Jobs, batches and servers made on an engine keep it alive: destroying the
+   engine while some remain only marks it closing, and the last of them to be
+   destroyed releases it (the engine must not be used after
+   mfx_engine_destroy either way). */
 int mfx_engine_create(const mfx_engine_opts *opts, mfx_engine **out);
 int mfx_engine_destroy(mfx_engine *eng);
 /* Device bytes a job with this descriptor needs (arena + FFT work area). */

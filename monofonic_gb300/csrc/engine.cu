@@ -115,6 +115,10 @@ struct mfx_engine {
   size_t budget = 0;
   std::mutex mu;
   size_t in_use = 0;
+  // jobs and servers alive on this engine; mfx_engine_destroy with some still
+  // alive only marks the engine closing, and the last of them releases it
+  int holders = 0;
+  bool closing = false;
   // cuFFT plans returned by finished jobs, reused by later jobs of the same
   // size class (plan creation is the slowest part of admitting a job)
   std::vector<Plan> plan_pool;
@@ -356,6 +360,26 @@ static int acquire_plan(mfx_engine *eng, Plan &p, int n, bool fp64, bool r2c, in
   p.fp64 = fp64;
   p.r2c = r2c;
   return MFX_OK;
+}
+
+// The engine outlives the jobs and servers made on it: each holds a reference.
+static void engine_retain(mfx_engine *eng) {
+  std::lock_guard<std::mutex> lk(eng->mu);
+  ++eng->holders;
+}
+
+static void engine_free(mfx_engine *eng) {
+  for (auto &p : eng->plan_pool) destroy_plan(p);
+  delete eng;
+}
+
+static void engine_release(mfx_engine *eng) {
+  bool last = false;
+  {
+    std::lock_guard<std::mutex> lk(eng->mu);
+    last = --eng->holders == 0 && eng->closing;
+  }
+  if (last) engine_free(eng);
 }
 
 static void release_plan(mfx_engine *eng, Plan &p) {
@@ -1124,11 +1148,13 @@ static void free_job(mfx_job *j) {
     if (e) cudaEventDestroy(e);
   if (j->fetched) cudaEventDestroy(j->fetched);
   if (j->stream) cudaStreamDestroy(j->stream);
-  if (j->eng) {
-    std::lock_guard<std::mutex> lk(j->eng->mu);
-    j->eng->in_use -= std::min(j->eng->in_use, j->arena_bytes + 2 * j->ring_set_bytes);
+  mfx_engine *eng = j->eng;
+  if (eng) {
+    std::lock_guard<std::mutex> lk(eng->mu);
+    eng->in_use -= std::min(eng->in_use, j->arena_bytes + 2 * j->ring_set_bytes);
   }
   delete j;
+  if (eng) engine_release(eng);
 }
 
 static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
@@ -1136,6 +1162,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   CU(cudaSetDevice(eng->device));
   auto *j = new mfx_job();
   j->eng = eng;
+  engine_retain(eng);
   j->d = *d;
   j->N = d->ngrid;
   j->M = 3 * j->N / 2;
@@ -1449,8 +1476,12 @@ int mfx_engine_create(const mfx_engine_opts *opts, mfx_engine **out) {
 
 int mfx_engine_destroy(mfx_engine *eng) {
   if (!eng) return MFX_OK;
-  for (auto &p : eng->plan_pool) destroy_plan(p);
-  delete eng;
+  {
+    std::lock_guard<std::mutex> lk(eng->mu);
+    eng->closing = true;
+    if (eng->holders > 0) return MFX_OK;  // the last job or server releases it
+  }
+  engine_free(eng);
   return MFX_OK;
 }
 
@@ -2128,6 +2159,7 @@ int mfx_server_create(mfx_engine *eng, int max_inflight, mfx_server **out) {
   if (!eng || !out || max_inflight < 1) return set_error(MFX_EINVAL, "bad arguments");
   auto *s = new mfx_server();
   s->eng = eng;
+  engine_retain(eng);
   s->max_inflight = max_inflight;
   s->worker = std::thread(server_loop, s);
   *out = s;
@@ -2236,7 +2268,9 @@ int mfx_server_destroy(mfx_server *s) {
     if (kv.second->job) free_job(kv.second->job);
     if (kv.second->done) cudaEventDestroy(kv.second->done);
   }
+  mfx_engine *eng = s->eng;
   delete s;
+  engine_release(eng);
   return MFX_OK;
 }
 

@@ -51,7 +51,70 @@ def build_lib() -> pathlib.Path:
     return out
 
 
+def build_omp_lib() -> pathlib.Path:
+    """Compile the C++/OpenMP restatement (oracle/lpt_omp.cc, with the NGenIC
+    fill of oracle/ranlux.c) into oracle/_build/liblpt_omp.so (if stale)."""
+    srcs = [_HERE / "lpt_omp.cc", _HERE / "ranlux.c"]
+    out = _BUILD / "liblpt_omp.so"
+    _BUILD.mkdir(exist_ok=True)
+    if not out.exists() or any(out.stat().st_mtime < s.stat().st_mtime for s in srcs):
+        import subprocess
+        obj = _BUILD / ("ranlux_omp.o.tmp%d" % os.getpid())
+        tmp = out.with_suffix(".so.tmp%d" % os.getpid())
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-c", str(srcs[1]), "-o", str(obj)])
+        subprocess.check_call(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", str(tmp),
+                               str(srcs[0]), str(obj), "-lm"])
+        os.replace(tmp, out)
+        obj.unlink()
+    return out
+
+
 _lib = None
+_omp = None
+
+
+def omp_lib():
+    """The C++/OpenMP restatement (CPU baseline of the hot path)."""
+    global _omp
+    if _omp is None:
+        L = ctypes.CDLL(str(build_omp_lib()))
+        L.mfxo_omp_fft1.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.mfxo_omp_fft3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.mfxo_omp_lpt.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        _omp = L
+    return _omp
+
+
+def run_lpt_omp(n, L, seed_table, amp_table, order, coef, lattice=0, lunit=1.0, vunit=1.0, fixing=False,
+                inversion=False, plt_table=None, want_fields=False):
+    """The C++/OpenMP restatement of the whole path (oracle/lpt_omp.cc).
+    amp_table[q] = amplitude(kf sqrt q) / (kf^2 q); coef as lpt_coefficients.
+    Returns dict(pos, vel, ids, times[, phi, phi2, phi3, A3])."""
+    ns = 1 << lattice
+    npart = ns * n ** 3
+    pos = np.empty((npart, 3))
+    vel = np.empty((npart, 3))
+    ids = np.empty(npart, dtype=np.uint64)
+    times = np.zeros(6)
+    nk = n // 2 + 1
+    fields = np.zeros((6, n, n, nk), dtype=np.complex128) if want_fields else None
+    seeds = np.ascontiguousarray(seed_table, dtype=np.uint32)
+    amp = np.ascontiguousarray(amp_table, dtype=np.float64)
+    cf = np.array([coef["g1"], coef["g2"], coef["g3"], coef["g3c"], coef["vfac1"], coef["vfac2"], coef["vfac3"]])
+    tab = None if plt_table is None else np.ascontiguousarray(plt_table, dtype=np.float64)
+    rc = omp_lib().mfxo_omp_lpt(n, L, order, lattice, int(fixing), int(inversion), seeds.ctypes.data, amp.ctypes.data,
+                                len(amp), None if tab is None else tab.ctypes.data, cf.ctypes.data, lunit, vunit,
+                                pos.ctypes.data, vel.ctypes.data, ids.ctypes.data,
+                                None if fields is None else fields.ctypes.data, times.ctypes.data)
+    if rc != 0:
+        raise ValueError("mfxo_omp_lpt rejected the arguments")
+    out = dict(pos=pos, vel=vel, ids=ids, times=times)
+    if want_fields:
+        out.update(phi=fields[0], phi2=fields[1], phi3=fields[2], A3=[fields[3], fields[4], fields[5]])
+    return out
 
 
 def lib():

@@ -483,6 +483,20 @@ def test_invalid_descriptors_are_errors_not_faults(mfxlib, engine):
         mfxlib.Job(engine, 16, 100.0, 2, c.seeds, c.amp[:10], c.coef)
 
 
+def test_job_outliving_its_engine_is_released_cleanly(mfxlib):
+    """Destroying an engine while a job on it is alive only marks it closing:
+    the job stays usable and its destruction releases the engine."""
+    eng = mfxlib.Engine(0)
+    c = Case(mfxlib, 16, 100.0, 49.0, 2, 1)
+    j = c.job(mfxlib, eng)
+    j.run()
+    eng.close()
+    pos, vel, ids = j.particles()
+    assert np.all(np.isfinite(pos)) and np.all(np.isfinite(vel))
+    j.run()
+    j.close()
+
+
 def test_wait_timeout_is_bounded(mfxlib, engine):
     c = Case(mfxlib, 64, 100.0, 49.0, 3, 1)
     j = c.job(mfxlib, engine)
