@@ -142,17 +142,49 @@ int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void
    that each order's displacement and velocity can be read on its own (the
    per-order error statement of the FP32 form).  Not capturable in a graph. */
 int mfx_job_assemble(mfx_job *job, int orders_mask);
+/* Baryon + CDM runs (ic_generator.cc:706-1064 with [setup] DoBaryons):
+   both species share the LPT potentials of one mfx_job_run and differ in the
+   assembly.  mfx_job_set_species selects the species the next run or
+   mfx_job_assemble produces: its lattice (the baryons' secondary lattice is
+   shifted by particle_generator.hh:56-63), its particle IDoffset
+   (ic_generator.cc:738-739), the linear relative-velocity term
+   -vfac1 C A_theta_bc(k) w grad / k^2 added to the velocities before
+   vfac_corr (ic_generator.cc:1016-1020; amp_tbc = get_amplitude_theta_bc per
+   |k|^2 index like amp_table, NULL for none) and the particle masses
+   (1 + C delta_bc(x)) * mass_factor / (n_s N^3) with delta_bc(k) =
+   w A_delta_bc(k) (ic_generator.cc:749-780, particle_generator.hh:369-427;
+   amp_dbc = get_amplitude_delta_bc per |k|^2 index, NULL for unperturbed
+   masses); c_species is the C factor of ic_generator.cc:718-726 and
+   mass_factor = Omega_species * output_plugin::mass_unit.  want_masses = 0
+   skips the masses.  NULL restores the single species of the descriptor. */
+typedef struct {
+  int secondary_lattice;
+  uint64_t id_offset;
+  double c_species;
+  double mass_factor;
+  const double *amp_dbc;
+  const double *amp_tbc;
+  size_t amp_len; /* length of amp_dbc / amp_tbc, >= 3*(N/2)^2 + 1 */
+  int want_masses;
+} mfx_species_desc;
+int mfx_job_set_species(mfx_job *job, const mfx_species_desc *species);
+/* Masses of particles [first, first + count) of the last run or assembly with
+   masses (double when the job's positions are double, else float;
+   particle_container.hh:44-74), into host or device memory. */
+int mfx_job_fetch_masses(mfx_job *job, size_t first, size_t count, void *out);
 /* Pipelined output (no counterpart in the reference, whose output plugins
-   write a realisation after it is generated): on = 1 gives the job two
-   particle sets of its own, outside the arena (2 x the particle bytes,
-   charged to the engine budget; MFX_EADMIT / MFX_ENOMEM when they do not
-   fit), and runs alternate between them, so that a run computes while the
-   particles of the previous run are still being copied to the host by
-   mfx_job_fetch_particles_range_async.  A run's assembly waits only for the
-   downloads from the set it writes.  on = 0 returns to the arena's particle
-   arrays.  Either way the particles of earlier runs are no longer fetchable.
-   MFX_ESTATE for a captured job (and capture refuses a job with the ring). */
-int mfx_job_set_output_ring(mfx_job *job, int on);
+   write a realisation after it is generated): `sets` = 1 or 2 gives the job
+   that many particle sets of its own, outside the arena (charged to the
+   engine budget; MFX_EADMIT / MFX_ENOMEM when they do not fit), and runs take
+   them in turn, so that a run computes while the particles of earlier runs
+   are still being copied to the host by mfx_job_fetch_particles_range_async.
+   A run's assembly waits only for the downloads from the set it writes: with
+   two sets the whole next run overlaps a download, with one set (the choice
+   when two do not fit beside the fields) everything before its assembly does.
+   sets = 0 returns to the arena's particle arrays.  Either way the particles
+   of earlier runs are no longer fetchable.  MFX_ESTATE for a captured job
+   (and capture refuses a job with the ring). */
+int mfx_job_set_output_ring(mfx_job *job, int sets);
 /* Enqueues the download of particles [first, first + count) of the job's
    last run into host buffers (page-locked for the copies to overlap) behind
    the job's enqueued work, and returns.  Call it before the next
@@ -232,13 +264,17 @@ int mfx_batch_destroy(mfx_batch *b);
 
 /* Serving: a request loop with admission by HBM footprint (no counterpart in
    the reference, which runs one job per process, main.cc:73-289).  Submitted
-   jobs (their tables are copied) wait in a FIFO queue; an admission thread
-   admits the head as soon as fewer than max_inflight jobs run and its arena
-   fits the engine's HBM budget, and runs it on its own stream, so jobs that
-   arrive while others are on the GPU overlap with them.  Results stay
-   resident until mfx_server_release; mfx_server_job gives the finished job
-   (fetch particles / fields through the mfx_job_* calls).
-   mfx_server_ticket_times: submit -> admit and submit -> done (ms). */
+   jobs (their tables are copied) wait in a queue; an admission thread admits
+   the oldest queued job that fits -- fewer than max_inflight jobs running and
+   its arena within the engine's HBM budget -- so a later job that fits may
+   start while a larger head waits, until the head has waited longer than the
+   bypass age limit (default 100 ms; mfx_server_set_policy), after which only
+   the head is admitted.  Two setup threads create admitted jobs and enqueue
+   them on their own streams, so jobs that arrive while others are on the GPU
+   overlap with them.  Results stay resident until mfx_server_release;
+   mfx_server_job gives the finished job (fetch particles / fields through the
+   mfx_job_* calls).  mfx_server_ticket_times: submit -> admit and
+   submit -> done (ms). */
 typedef struct mfx_server mfx_server;
 int mfx_server_create(mfx_engine *eng, int max_inflight, mfx_server **out);
 int mfx_server_submit(mfx_server *s, const mfx_job_desc *desc, uint64_t *ticket);
@@ -247,6 +283,9 @@ int mfx_server_ticket_times(mfx_server *s, uint64_t ticket, double *queued_ms, d
 int mfx_server_job(mfx_server *s, uint64_t ticket, mfx_job **job);
 int mfx_server_release(mfx_server *s, uint64_t ticket);
 int mfx_server_destroy(mfx_server *s);
+/* bypass = 0: strict first-in first-out admission; otherwise a later job may
+   pass a head that has waited at most bypass_age_ms. */
+int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms);
 
 /* Allocation-free white-noise fill (no counterpart in the reference): writes
    the NGenIC noise of RNG_plugin::Fill_Grid -- raw (raw = 1) or normalised /

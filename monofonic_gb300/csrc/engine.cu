@@ -150,11 +150,14 @@ struct mfx_job {
   size_t rsize = 8;
   cudaStream_t stream = nullptr;
   cudaStream_t xfer[4] = {};  // particle downloads, split across copy streams
-  // pipelined output (mfx_job_set_output_ring): two particle sets outside the
-  // arena; a run writes set ring_next while the downloads of the other set's
-  // particles (enqueued on xfer[0] by the asynchronous fetch) may still run
+  // pipelined output (mfx_job_set_output_ring): one or two particle sets
+  // outside the arena; a run writes set ring_next while the downloads of the
+  // earlier runs' particles (enqueued on xfer[0] by the asynchronous fetch)
+  // may still run -- with two sets the whole run overlaps them, with one set
+  // everything before the run's assembly does
   char *ring = nullptr;
   size_t ring_set_bytes = 0;
+  int ring_sets = 0;
   int ring_next = 0;
   cudaEvent_t ring_free[2] = {};  // the last download from set s is done
   cudaEvent_t fetched = nullptr;  // the last asynchronous download is done
@@ -190,6 +193,18 @@ struct mfx_job {
   bool has_run = false, noise_only = false;
   size_t npart = 0;
   double scale1 = 1, scale2 = 1, scale3 = 1;  // per-field scales of the FP32 form
+  // baryon + CDM species of the next assembly (mfx_job_set_species)
+  std::vector<double> amp_host;    // the amplitude table, for the species' ratio tables
+  uint64_t base_id_offset = 0;     // the descriptor's IDoffset
+  double lat_off[3] = {0, 0, 0};   // secondary-lattice shift (particle_generator.hh:56-63)
+  double c_species = 0, mass_factor = 0;
+  bool want_masses = false, has_masses = false;
+  char *sp_mem = nullptr;          // one allocation: tables, mass field, masses, FFT work
+  size_t sp_bytes = 0, sp_len = 0;
+  double *qvbc = nullptr, *rho_ratio = nullptr;
+  float *qvbc32 = nullptr;
+  void *rho = nullptr, *mass = nullptr, *rho_work = nullptr;
+  Plan rho_c2r;
   // per-launch profiling (events on the job stream + algorithmic bytes)
   struct ProfRec {
     const char *name;
@@ -848,6 +863,44 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   return MFX_OK;
 }
 
+// Particle masses of the job's species (mfx_job_set_species), per sub-lattice:
+// the delta_bc field from phi1 with the sub-lattice phase, its c2r and the
+// read-out (ic_generator.cc:749-780, particle_generator.hh:369-427)
+template <typename R> static int mass_stage(mfx_job *j) {
+  const int N = j->N, nsm = num_sm();
+  const double N3 = double(N) * N * N;
+  MassArgs m{};
+  m.phi1 = j->nf[0];
+  m.ratio = j->rho_ratio;
+  m.ratio_len = j->rho_ratio ? j->sp_len : 0;
+  m.phase = j->phase;
+  m.field = j->rho;
+  m.mass = j->mass;
+  m.N = N;
+  m.nshift_total = j->ns;
+  m.c_species = j->c_species;
+  m.norm = 1.0 / std::sqrt(N3);
+  m.scale = j->mass_factor / (double(j->ns) * N3);
+  const size_t total = size_t(N) * N * j->nk;
+  for (int s = 0; s < j->ns; ++s) {
+    m.shift = s;
+    KBEGIN(j);
+    k_mass_field<R><<<grid_for(total, 256, nsm), 256, 0, j->stream>>>(m);
+    KEND(j, "mass_field", 2.0 * j->n_field_bytes);
+    kbegin(j);
+    if (j->fp64) CF(cufftExecZ2D(j->rho_c2r.h, (cufftDoubleComplex *)j->rho, (cufftDoubleReal *)j->rho));
+    else CF(cufftExecC2R(j->rho_c2r.h, (cufftComplex *)j->rho, (cufftReal *)j->rho));
+    j->fft_execs++;
+    kend_prof(j, "cufft_c2r_mass", 2.0 * j->n_field_bytes);
+    KBEGIN(j);
+    if (j->d.pos64) k_masses<R, double><<<grid_for(size_t(N3), 256, nsm), 256, 0, j->stream>>>(m);
+    else k_masses<R, float><<<grid_for(size_t(N3), 256, nsm), 256, 0, j->stream>>>(m);
+    KEND(j, "masses", N3 * (double(j->rsize) + (j->d.pos64 ? 8.0 : 4.0)));
+  }
+  j->has_masses = true;
+  return MFX_OK;
+}
+
 template <typename R> static int assemble_stage(mfx_job *j, int mask) {
   const int order = j->d.lpt_order;
   const int nsm = num_sm();
@@ -883,7 +936,15 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
   a.in_scale2 = 1.0 / j->scale2;
   a.in_scale3 = 1.0 / j->scale3;
   asm_float_coefficients(a);
-  if (j->fused) return assemble_fused(j, a);
+  if (j->qvbc && (mask & 1)) {
+    a.qvbc = j->qvbc;
+    a.qvbc32 = j->qvbc32;
+    a.qvbc_len = j->sp_len;
+  }
+  if (j->fused) {
+    TRY(assemble_fused(j, a));
+    return j->want_masses ? mass_stage<R>(j) : MFX_OK;
+  }
   const size_t total = size_t(N) * N * j->nk;
   for (int s0 = 0; s0 < j->ns; s0 += j->group) {
     const int g = std::min(j->group, j->ns - s0);
@@ -907,9 +968,9 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
       p.pos64 = j->d.pos64;
       p.vel64 = j->d.vel64;
       p.id64 = j->d.id64;
-      p.sx = kShifts[j->d.lattice][s0 + s][0];
-      p.sy = kShifts[j->d.lattice][s0 + s][1];
-      p.sz = kShifts[j->d.lattice][s0 + s][2];
+      p.sx = kShifts[j->d.lattice][s0 + s][0] + j->lat_off[0];
+      p.sy = kShifts[j->d.lattice][s0 + s][1] + j->lat_off[1];
+      p.sz = kShifts[j->d.lattice][s0 + s][2] + j->lat_off[2];
       p.lunit = j->d.lunit;
       p.qtab = j->qtab + size_t(s0 + s) * 3 * N;
       p.id_offset = j->d.id_offset * uint64_t(j->ns) * uint64_t(N3);
@@ -922,7 +983,7 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
       KEND(j, "particles", N3 * (6.0 * j->rsize + 3.0 * (p.pos64 ? 8 : 4) + 3.0 * (p.vel64 ? 8 : 4) + (p.id64 ? 8 : 4)));
     }
   }
-  return MFX_OK;
+  return j->want_masses ? mass_stage<R>(j) : MFX_OK;
 }
 
 // points the particle arrays at ring set s (pos | vel | ids)
@@ -1020,7 +1081,7 @@ template <typename R> static int run_pipeline(mfx_job *j) {
   if (j->ring) CU(cudaStreamWaitEvent(j->stream, j->ring_free[rset], 0));
   if (j->d.want_particles) TRY(assemble_stage<R>(j, 7));
   if (j->timed) CU(cudaEventRecord(j->ev[4], j->stream));
-  if (j->ring) j->ring_next = rset ^ 1;
+  if (j->ring) j->ring_next = (rset + 1) % j->ring_sets;
   j->has_run = true;
   j->noise_only = false;
   return MFX_OK;
@@ -1031,6 +1092,7 @@ template <typename R> static int run_pipeline(mfx_job *j) {
 // ---------------------------------------------------------------------------
 static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
   const int N = j->N;
+  j->amp_host.assign(d->amp_table, d->amp_table + d->amp_table_len);
   CU(cudaMemcpyAsync(j->seeds, d->seed_table, size_t(N) * N * 4, cudaMemcpyHostToDevice, j->stream));
   CU(cudaMemcpyAsync(j->amp, d->amp_table, d->amp_table_len * 8, cudaMemcpyHostToDevice, j->stream));
   if (d->plt) {
@@ -1147,14 +1209,56 @@ static void free_job(mfx_job *j) {
   for (auto &e : j->ring_free)
     if (e) cudaEventDestroy(e);
   if (j->fetched) cudaEventDestroy(j->fetched);
+  if (j->sp_mem) {
+    cudaFreeAsync(j->sp_mem, j->stream);
+    cudaStreamSynchronize(j->stream);
+  }
+  if (j->eng) release_plan(j->eng, j->rho_c2r);
+  else destroy_plan(j->rho_c2r);
   if (j->stream) cudaStreamDestroy(j->stream);
   mfx_engine *eng = j->eng;
   if (eng) {
     std::lock_guard<std::mutex> lk(eng->mu);
-    eng->in_use -= std::min(eng->in_use, j->arena_bytes + 2 * j->ring_set_bytes);
+    eng->in_use -= std::min(eng->in_use, j->arena_bytes + size_t(j->ring_sets) * j->ring_set_bytes + j->sp_bytes);
   }
   delete j;
   if (eng) engine_release(eng);
+}
+
+// phase tables exp(i s_a k_a dx) per sub-lattice and axis (grid_fft.hh:836-839)
+// and the unperturbed lattice coordinates (m + s)/N * lunit, the reference's
+// get_unit_r_shifted(...)[axis] * lunit (grid_fft.hh:240-250,
+// particle_generator.hh:529-531); s includes the species' secondary-lattice
+// shift (particle_generator.hh:388-395)
+static int upload_shift_tables(mfx_job *j) {
+  const int N = j->N;
+  const mfx_job_desc *d = &j->d;
+  std::vector<double2> ph(size_t(j->ns) * 3 * N);
+  const double kfac = 2.0 * M_PI / d->boxlen, dx = d->boxlen / N;
+  for (int s = 0; s < j->ns; ++s)
+    for (int ax = 0; ax < 3; ++ax)
+      for (int m = 0; m < N; ++m) {
+        const double km = (double(m) - double(m > N / 2) * N) * kfac;
+        const double th = (kShifts[d->lattice][s][ax] + j->lat_off[ax]) * km * dx;
+        ph[(size_t(s) * 3 + ax) * N + m] = make_double2(std::cos(th), std::sin(th));
+      }
+  std::vector<double> qt(size_t(j->ns) * 3 * N);
+  for (int s = 0; s < j->ns; ++s)
+    for (int ax = 0; ax < 3; ++ax)
+      for (int m = 0; m < N; ++m)
+        qt[(size_t(s) * 3 + ax) * N + m] =
+            (double(m) + (kShifts[d->lattice][s][ax] + j->lat_off[ax])) / double(N) * d->lunit;
+  std::vector<float2> ph32(ph.size());
+  for (size_t q = 0; q < ph.size(); ++q) ph32[q] = make_float2(float(ph[q].x), float(ph[q].y));
+  if (cudaMemcpyAsync(j->phase, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, j->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(j->phase32, ph32.data(), ph32.size() * sizeof(float2), cudaMemcpyHostToDevice, j->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(j->qtab, qt.data(), qt.size() * sizeof(double), cudaMemcpyHostToDevice, j->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(j->stream) != cudaSuccess)
+    return set_error(MFX_ECUDA, "phase table upload failed");
+  return MFX_OK;
 }
 
 static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
@@ -1164,6 +1268,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   j->eng = eng;
   engine_retain(eng);
   j->d = *d;
+  j->base_id_offset = d->id_offset;
   j->N = d->ngrid;
   j->M = 3 * j->N / 2;
   j->nh = j->N / 2;
@@ -1325,38 +1430,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
   for (Plan *pl : {&j->m_r2c, &j->m_c2r, &j->n_c2r})
     if (pl->valid && cufftSetStream(pl->h, j->stream) != CUFFT_SUCCESS)
       return fail(set_error(MFX_ECUDA, "cufftSetStream failed"));
-  // phase tables exp(i s_a k_a dx) per sub-lattice and axis (grid_fft.hh:836-839)
-  {
-    const int N = j->N;
-    std::vector<double2> ph(size_t(j->ns) * 3 * N);
-    const double kfac = 2.0 * M_PI / d->boxlen, dx = d->boxlen / N;
-    for (int s = 0; s < j->ns; ++s)
-      for (int ax = 0; ax < 3; ++ax)
-        for (int m = 0; m < N; ++m) {
-          const double km = (double(m) - double(m > N / 2) * N) * kfac;
-          const double th = kShifts[d->lattice][s][ax] * km * dx;
-          ph[(size_t(s) * 3 + ax) * N + m] = make_double2(std::cos(th), std::sin(th));
-        }
-    // unperturbed lattice coordinates (m + s)/N * lunit, the reference's
-    // get_unit_r_shifted(...)[axis] * lunit (grid_fft.hh:240-250,
-    // particle_generator.hh:529-531)
-    std::vector<double> qt(size_t(j->ns) * 3 * N);
-    for (int s = 0; s < j->ns; ++s)
-      for (int ax = 0; ax < 3; ++ax)
-        for (int m = 0; m < N; ++m)
-          qt[(size_t(s) * 3 + ax) * N + m] = (double(m) + kShifts[d->lattice][s][ax]) / double(N) * d->lunit;
-    std::vector<float2> ph32(ph.size());
-    for (size_t q = 0; q < ph.size(); ++q) ph32[q] = make_float2(float(ph[q].x), float(ph[q].y));
-    if (cudaMemcpyAsync(j->phase, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, j->stream) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(j->phase32, ph32.data(), ph32.size() * sizeof(float2), cudaMemcpyHostToDevice, j->stream) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(j->qtab, qt.data(), qt.size() * sizeof(double), cudaMemcpyHostToDevice, j->stream) !=
-            cudaSuccess)
-      return fail(set_error(MFX_ECUDA, "phase table upload failed"));
-    if (cudaStreamSynchronize(j->stream) != cudaSuccess)
-      return fail(set_error(MFX_ECUDA, "phase table upload failed"));
-  }
+  if ((rc = upload_shift_tables(j)) != MFX_OK) return fail(rc);
   if ((rc = upload_tables(j, d)) != MFX_OK) return fail(rc);
   if (cudaStreamSynchronize(j->stream) != cudaSuccess) return fail(set_error(MFX_ECUDA, "table upload failed"));
   *out = j;
@@ -1551,6 +1625,141 @@ int mfx_job_assemble(mfx_job *job, int orders_mask) {
   GUARD_END
 }
 
+// drops the species' allocation and plan (the job's stream is idle)
+static void release_species(mfx_job *job) {
+  if (job->sp_mem) {
+    cudaFreeAsync(job->sp_mem, job->stream);
+    cudaStreamSynchronize(job->stream);
+    std::lock_guard<std::mutex> lk(job->eng->mu);
+    job->eng->in_use -= std::min(job->eng->in_use, job->sp_bytes);
+  }
+  release_plan(job->eng, job->rho_c2r);
+  job->sp_mem = nullptr;
+  job->sp_bytes = job->sp_len = 0;
+  job->qvbc = job->rho_ratio = nullptr;
+  job->qvbc32 = nullptr;
+  job->rho = job->mass = job->rho_work = nullptr;
+  job->want_masses = job->has_masses = false;
+  job->c_species = job->mass_factor = 0.0;
+  for (double &o : job->lat_off) o = 0.0;
+  job->d.id_offset = job->base_id_offset;
+}
+
+int mfx_job_set_species(mfx_job *job, const mfx_species_desc *sp) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
+  if (job->gexec) return set_error(MFX_ESTATE, "job already captured into a graph");
+  const size_t len = 3 * size_t(job->nh) * job->nh + 1;
+  if (sp && (sp->amp_dbc || sp->amp_tbc) && sp->amp_len < len)
+    return set_error(MFX_EINVAL, "species tables need %zu entries (got %zu)", len, sp->amp_len);
+  if (sp && !(std::isfinite(sp->c_species) && std::isfinite(sp->mass_factor)))
+    return set_error(MFX_EINVAL, "species factors must be finite");
+  CU(cudaSetDevice(job->eng->device));
+  for (auto &x : job->xfer)
+    if (x) CU(cudaStreamSynchronize(x));
+  CU(cudaStreamSynchronize(job->stream));
+  release_species(job);
+  if (sp) {
+    static const double kSecond[3][3] = {{0.5, 0.5, 0.5}, {0.5, 0.5, 0.0}, {0.5, 0.5, 0.5}};
+    for (int ax = 0; ax < 3; ++ax) job->lat_off[ax] = sp->secondary_lattice ? kSecond[job->d.lattice][ax] : 0.0;
+    job->d.id_offset = sp->id_offset;
+    job->c_species = sp->c_species;
+    job->mass_factor = sp->mass_factor;
+    job->want_masses = sp->want_masses != 0;
+    const int N = job->N;
+    const bool vbc = sp->amp_tbc != nullptr, dbc = job->want_masses && sp->amp_dbc != nullptr;
+    const size_t rs = job->fp64 ? 8 : 4;
+    size_t off_q = 0, off_q32 = 0, off_r = 0, off_rho = 0, off_m = 0, off_w = 0, tot = 0;
+    auto take = [&](size_t &off, size_t bytes) {
+      off = tot;
+      tot += align_up(bytes);
+    };
+    if (vbc) {
+      take(off_q, len * 8);
+      take(off_q32, len * 4);
+    }
+    if (dbc) take(off_r, len * 8);
+    if (job->want_masses) {
+      TRY(acquire_plan(job->eng, job->rho_c2r, N, job->fp64, false));
+      take(off_rho, size_t(N) * N * (N + 2) * rs);
+      take(off_m, job->npart * (job->d.pos64 ? 8 : 4));
+      take(off_w, std::max<size_t>(job->rho_c2r.work, 256));
+    }
+    if (tot) {
+      {
+        std::lock_guard<std::mutex> lk(job->eng->mu);
+        if (job->eng->in_use + tot > job->eng->budget) {
+          release_plan(job->eng, job->rho_c2r);
+          return set_error(MFX_EADMIT, "species buffers need %zu bytes beyond the engine budget", tot);
+        }
+        job->eng->in_use += tot;
+      }
+      cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&job->sp_mem), tot, job->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(job->stream);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        job->sp_mem = nullptr;
+        std::lock_guard<std::mutex> lk(job->eng->mu);
+        job->eng->in_use -= std::min(job->eng->in_use, tot);
+        release_plan(job->eng, job->rho_c2r);
+        return set_error(MFX_ENOMEM, "species buffers of %zu bytes: %s", tot, cudaGetErrorString(e));
+      }
+      job->sp_bytes = tot;
+    }
+    job->sp_len = len;
+    // host tables: with w = -phi1 / A(n) (phi1 = -A(n) w, A the amplitude table)
+    const double kf = 2.0 * M_PI / job->d.boxlen, g1 = job->d.g1;
+    const std::vector<double> &A = job->amp_host;
+    if (vbc) {
+      // velocity weight of phi1 times 1 + C A_theta_bc / (A k^2 g1)
+      std::vector<double> q(len, 0.0);
+      std::vector<float> q32(len, 0.f);
+      for (size_t n = 1; n < len; ++n)
+        if (n < A.size() && A[n] != 0.0 && g1 != 0.0)
+          q[n] = sp->c_species * sp->amp_tbc[n] / (A[n] * kf * kf * double(n) * g1);
+      for (size_t n = 0; n < len; ++n) q32[n] = float(q[n]);
+      job->qvbc = reinterpret_cast<double *>(job->sp_mem + off_q);
+      job->qvbc32 = reinterpret_cast<float *>(job->sp_mem + off_q32);
+      CU(cudaMemcpyAsync(job->qvbc, q.data(), len * 8, cudaMemcpyHostToDevice, job->stream));
+      CU(cudaMemcpyAsync(job->qvbc32, q32.data(), len * 4, cudaMemcpyHostToDevice, job->stream));
+    }
+    if (dbc) {
+      // delta_bc(k) = w A_delta_bc = -(phi1 field / scale1) A_delta_bc / A
+      std::vector<double> r(len, 0.0);
+      for (size_t n = 1; n < len; ++n)
+        if (n < A.size() && A[n] != 0.0) r[n] = -sp->amp_dbc[n] / (A[n] * job->scale1);
+      job->rho_ratio = reinterpret_cast<double *>(job->sp_mem + off_r);
+      CU(cudaMemcpyAsync(job->rho_ratio, r.data(), len * 8, cudaMemcpyHostToDevice, job->stream));
+    }
+    if (job->want_masses) {
+      job->rho = job->sp_mem + off_rho;
+      job->mass = job->sp_mem + off_m;
+      job->rho_work = job->sp_mem + off_w;
+      CF(cufftSetWorkArea(job->rho_c2r.h, job->rho_work));
+      CF(cufftSetStream(job->rho_c2r.h, job->stream));
+    }
+    CU(cudaStreamSynchronize(job->stream));
+  }
+  TRY(upload_shift_tables(job));
+  return MFX_OK;
+  GUARD_END
+}
+
+int mfx_job_fetch_masses(mfx_job *job, size_t first, size_t count, void *out) {
+  GUARD_BEGIN
+  if (!job || !out) return set_error(MFX_EINVAL, "null argument");
+  if (!job->has_masses || !job->mass) return set_error(MFX_ESTATE, "no masses: set a species with masses and run");
+  if (first > job->npart || count > job->npart - first)
+    return set_error(MFX_EINVAL, "range [%zu, %zu) outside the %zu particles", first, first + count, job->npart);
+  CU(cudaSetDevice(job->eng->device));
+  CU(cudaStreamSynchronize(job->stream));
+  const size_t es = job->d.pos64 ? 8 : 4;
+  CU(cudaMemcpy(out, static_cast<char *>(job->mass) + es * first, es * count, cudaMemcpyDefault));
+  return MFX_OK;
+  GUARD_END
+}
+
 int mfx_job_set_tiles(mfx_job *job, int pencils_xy, int rows_z) {
   GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
@@ -1726,20 +1935,22 @@ int mfx_job_set_output_ring(mfx_job *job, int on) {
   if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
   if (job->gexec) return set_error(MFX_ESTATE, "job already captured into a graph");
   CU(cudaSetDevice(job->eng->device));
-  if (!on == !job->ring) return MFX_OK;
+  if (on < 0 || on > 2) return set_error(MFX_EINVAL, "output sets must be 0, 1 or 2 (got %d)", on);
+  if (on == job->ring_sets) return MFX_OK;
   for (auto &x : job->xfer)
     if (x) CU(cudaStreamSynchronize(x));
   CU(cudaStreamSynchronize(job->stream));
   mfx_engine *eng = job->eng;
-  if (!on) {
+  if (job->ring) {
     CU(cudaFreeAsync(job->ring, job->stream));
     CU(cudaStreamSynchronize(job->stream));
     job->ring = nullptr;
     {
       std::lock_guard<std::mutex> lk(eng->mu);
-      eng->in_use -= std::min(eng->in_use, 2 * job->ring_set_bytes);
+      eng->in_use -= std::min(eng->in_use, size_t(job->ring_sets) * job->ring_set_bytes);
     }
     job->ring_set_bytes = 0;
+    job->ring_sets = 0;
     // back to the arena's particle arrays (the last run's particles are gone)
     job->has_run = false;
     char *a = job->region;
@@ -1748,31 +1959,33 @@ int mfx_job_set_output_ring(mfx_job *job, int on) {
     job->vel = a;
     a += align_up(job->npart * 3 * (job->d.vel64 ? 8 : 4));
     job->ids = a;
-    return MFX_OK;
   }
+  if (!on) return MFX_OK;
   const size_t np = job->npart;
   const size_t set = align_up(np * 3 * (job->d.pos64 ? 8 : 4)) + align_up(np * 3 * (job->d.vel64 ? 8 : 4)) +
                      align_up(np * (job->d.id64 ? 8 : 4));
+  const size_t total = size_t(on) * set;
   {
     std::lock_guard<std::mutex> lk(eng->mu);
-    if (eng->in_use + 2 * set > eng->budget)
-      return set_error(MFX_EADMIT, "output ring needs %zu bytes, engine budget has %zu free", 2 * set,
+    if (eng->in_use + total > eng->budget)
+      return set_error(MFX_EADMIT, "output ring needs %zu bytes, engine budget has %zu free", total,
                        eng->budget - std::min(eng->budget, eng->in_use));
-    eng->in_use += 2 * set;
+    eng->in_use += total;
   }
   char *r = nullptr;
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&r), 2 * set, job->stream);
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&r), total, job->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(job->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     std::lock_guard<std::mutex> lk(eng->mu);
-    eng->in_use -= std::min(eng->in_use, 2 * set);
-    return set_error(MFX_ENOMEM, "output ring of %zu bytes: %s", 2 * set, cudaGetErrorString(e));
+    eng->in_use -= std::min(eng->in_use, total);
+    return set_error(MFX_ENOMEM, "output ring of %zu bytes: %s", total, cudaGetErrorString(e));
   }
   for (auto &ev : job->ring_free)
     if (!ev) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   job->ring = r;
   job->ring_set_bytes = set;
+  job->ring_sets = on;
   job->ring_next = 0;
   job->has_run = false;
   ring_point(job, 0);
@@ -1806,7 +2019,8 @@ int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count
   for (const Xfer &q : xs)
     if (q.dst && q.bytes) CU(cudaMemcpyAsync(q.dst, q.src, q.bytes, cudaMemcpyDefault, x));
   CU(cudaEventRecord(job->fetched, x));
-  if (job->ring) CU(cudaEventRecord(job->ring_free[job->ring_next ^ 1], x));
+  // the set the last run wrote
+  if (job->ring) CU(cudaEventRecord(job->ring_free[(job->ring_next + job->ring_sets - 1) % job->ring_sets], x));
   return MFX_OK;
   GUARD_END
 }
@@ -2047,13 +2261,20 @@ int mfx_debug_ranlxd1_words(mfx_engine *eng, unsigned long seed, size_t count, u
 // Serving: a request loop with admission by HBM footprint.
 //
 // Requests are copied at submission and queued.  An admission thread admits
-// the queue head as soon as an in-flight slot is free and the job's arena fits
-// the engine's HBM budget (strict FIFO, so large jobs are not starved), runs it
-// on its own stream and keeps its fields and particles resident on the device
-// until the client fetches and releases it.  Admitted jobs overlap on the GPU;
-// arenas come from the stream-ordered pool and FFT plans from the plan pool,
-// so admission and retirement never synchronise the device.  A job's results
-// do not depend on what else runs: every job has its own arena and plans.
+// a queued job as soon as an in-flight slot is free and the job's arena fits
+// the engine's HBM budget: the oldest job that fits, scanning from the head
+// (a later job may pass a head that does not fit yet), unless the head has
+// waited longer than the bypass age limit, after which only the head may be
+// admitted, so that large jobs are not starved.  Admitted jobs are set up --
+// arena, tables, launches -- by a small pool of setup threads, so that setting
+// up one job never holds back the admission of the next; the footprints of
+// admitted jobs are reserved against the budget until their arenas exist.
+// Each job runs on its own stream and keeps its fields and particles resident
+// on the device until the client fetches and releases it.  Admitted jobs
+// overlap on the GPU; arenas come from the stream-ordered pool and FFT plans
+// from the plan pool, so admission and retirement never synchronise the
+// device.  A job's results do not depend on what else runs: every job has its
+// own arena and plans.
 // ---------------------------------------------------------------------------
 #include <chrono>
 #include <condition_variable>
@@ -2072,29 +2293,51 @@ struct Ticket {
   std::vector<double> amp, plt;
   size_t footprint = 0;
   clk::time_point t_submit, t_admit, t_done;
-  int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+  int state = 0;  // 0 queued, 4 admitted (being set up), 1 running, 2 done, 3 failed
   int rc = MFX_OK;
   std::string err;
   mfx_job *job = nullptr;
   cudaEvent_t done = nullptr;
 };
+constexpr int kSetupThreads = 2;
 }  // namespace
 
 struct mfx_server {
   mfx_engine *eng = nullptr;
   int max_inflight = 8;
+  bool bypass = true;
+  double bypass_age_ms = 100.0;
   std::mutex mu;
   std::condition_variable cv;
-  std::deque<Ticket *> queue;
+  std::deque<Ticket *> queue;     // waiting for admission
+  std::deque<Ticket *> setup_q;   // admitted, waiting for a setup thread
   std::map<uint64_t, std::unique_ptr<Ticket>> tickets;
   std::thread worker;
+  std::vector<std::thread> setup;
   bool stop = false;
   uint64_t next_id = 1;
-  int inflight = 0;
+  int inflight = 0;     // admitted and not yet finished (setting up or running)
+  size_t reserved = 0;  // footprints of admitted jobs whose arenas do not exist yet
 };
 
 static double ms_between(clk::time_point a, clk::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+// Index of the queued job to admit next, or -1 (s->mu held).
+static int pick_admission(mfx_server *s, clk::time_point now) {
+  if (s->queue.empty()) return -1;
+  size_t in_use;
+  {
+    std::lock_guard<std::mutex> ek(s->eng->mu);
+    in_use = s->eng->in_use;
+  }
+  const bool head_may_be_passed = s->bypass && ms_between(s->queue.front()->t_submit, now) <= s->bypass_age_ms;
+  for (size_t q = 0; q < s->queue.size(); ++q) {
+    if (q > 0 && !head_may_be_passed) break;
+    if (in_use + s->reserved + s->queue[q]->footprint <= s->eng->budget) return int(q);
+  }
+  return -1;
 }
 
 static void server_loop(mfx_server *s) {
@@ -2116,39 +2359,56 @@ static void server_loop(mfx_server *s) {
       --s->inflight;
       s->cv.notify_all();
     }
-    // admit from the queue head while a slot and the HBM budget allow
-    while (!s->queue.empty() && s->inflight < s->max_inflight) {
-      Ticket *t = s->queue.front();
-      bool fits;
-      {
-        std::lock_guard<std::mutex> ek(s->eng->mu);
-        fits = s->eng->in_use + t->footprint <= s->eng->budget;
-      }
-      if (!fits) break;  // wait for running jobs to finish and results to be released
-      s->queue.pop_front();
-      lk.unlock();
-      mfx_job *j = nullptr;
-      int rc = create_job(s->eng, &t->d, &j);
-      std::string err = rc == MFX_OK ? "" : g_last_error;
-      if (rc == MFX_OK) rc = j->fp64 ? run_pipeline<double>(j) : run_pipeline<float>(j);
-      if (rc == MFX_OK && cudaEventRecord(t->done, j->stream) != cudaSuccess) rc = MFX_ECUDA;
-      if (rc != MFX_OK && err.empty()) err = g_last_error;
-      lk.lock();
-      t->t_admit = clk::now();
-      if (rc != MFX_OK) {
-        if (j) free_job(j);
-        t->state = 3;
-        t->rc = rc;
-        t->err = err;
-        t->t_done = t->t_admit;
-        s->cv.notify_all();
-        continue;
-      }
-      t->job = j;
-      t->state = 1;
+    // admit while a slot and the HBM budget allow; the setup threads take it from here
+    while (s->inflight < s->max_inflight) {
+      const auto now = clk::now();
+      const int q = pick_admission(s, now);
+      if (q < 0) break;  // wait for running jobs to finish and results to be released
+      Ticket *t = s->queue[size_t(q)];
+      s->queue.erase(s->queue.begin() + q);
+      t->t_admit = now;
+      t->state = 4;
+      s->reserved += t->footprint;
       ++s->inflight;
+      s->setup_q.push_back(t);
+      s->cv.notify_all();
     }
     s->cv.wait_for(lk, std::chrono::microseconds(s->inflight > 0 ? 50 : 2000));
+  }
+}
+
+static void setup_loop(mfx_server *s) {
+  cudaSetDevice(s->eng->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (true) {
+    s->cv.wait(lk, [s] { return s->stop || !s->setup_q.empty(); });
+    if (s->stop) return;
+    Ticket *t = s->setup_q.front();
+    s->setup_q.pop_front();
+    lk.unlock();
+    mfx_job *j = nullptr;
+    int rc = create_job(s->eng, &t->d, &j);
+    std::string err = rc == MFX_OK ? "" : g_last_error;
+    if (rc == MFX_OK) rc = j->fp64 ? run_pipeline<double>(j) : run_pipeline<float>(j);
+    if (rc == MFX_OK && cudaEventRecord(t->done, j->stream) != cudaSuccess) rc = MFX_ECUDA;
+    if (rc != MFX_OK && err.empty()) err = g_last_error;
+    if (rc != MFX_OK && j) {
+      free_job(j);
+      j = nullptr;
+    }
+    lk.lock();
+    s->reserved -= std::min(s->reserved, t->footprint);
+    if (rc != MFX_OK) {
+      t->state = 3;
+      t->rc = rc;
+      t->err = err;
+      t->t_done = clk::now();
+      --s->inflight;
+    } else {
+      t->job = j;
+      t->state = 1;
+    }
+    s->cv.notify_all();
   }
 }
 
@@ -2162,9 +2422,19 @@ int mfx_server_create(mfx_engine *eng, int max_inflight, mfx_server **out) {
   engine_retain(eng);
   s->max_inflight = max_inflight;
   s->worker = std::thread(server_loop, s);
+  for (int q = 0; q < kSetupThreads; ++q) s->setup.emplace_back(setup_loop, s);
   *out = s;
   return MFX_OK;
   GUARD_END
+}
+
+int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms) {
+  if (!s || bypass_age_ms < 0) return set_error(MFX_EINVAL, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->bypass = bypass != 0;
+  s->bypass_age_ms = bypass_age_ms;
+  s->cv.notify_all();
+  return MFX_OK;
 }
 
 int mfx_server_submit(mfx_server *s, const mfx_job_desc *desc, uint64_t *ticket) {
@@ -2264,6 +2534,8 @@ int mfx_server_destroy(mfx_server *s) {
     s->cv.notify_all();
   }
   if (s->worker.joinable()) s->worker.join();
+  for (auto &th : s->setup)
+    if (th.joinable()) th.join();
   for (auto &kv : s->tickets) {
     if (kv.second->job) free_job(kv.second->job);
     if (kv.second->done) cudaEventDestroy(kv.second->done);

@@ -429,6 +429,12 @@ struct AsmArgs {
   // pipe busy): kfac, g_n * in_scale_n (n = 1, 2, 3), g3c * in_scale3,
   // vfac1..3, pfac, vfac
   float fkfac, fs1, fs2, fs3, fsa, fv1, fv2, fv3, fpfac, fvfac;
+  // baryon + CDM runs: the linear relative-velocity term of a species
+  // (ic_generator.cc:1016-1020) as a factor 1 + qvbc[n] on phi1's velocity
+  // weight, n = |k|^2 / kf^2 (null: no term)
+  const double *qvbc;
+  const float *qvbc32;
+  size_t qvbc_len;
 };
 
 // the float coefficients of an AsmArgs from its FP64 ones
@@ -625,6 +631,15 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
   C f1 = p1[idx];
   R ps_re = c_s1 * f1.x, ps_im = c_s1 * f1.y;
   R vs_re = c_v1 * ps_re, vs_im = c_v1 * ps_im;
+  if (a.qvbc) {
+    // -vfac1 C A_theta_bc w grad / k^2 with w = -phi1 / A(k): phi1's velocity
+    // weight times 1 + C A_theta_bc / (A k^2 g1)
+    const int si = signed_idx(i, N), sj = signed_idx(j, N);
+    const size_t n = size_t(si * si + sj * sj + k * k);
+    const R q = n < a.qvbc_len ? (F32 ? R(a.qvbc32[n]) : R(a.qvbc[n])) : R(0);
+    vs_re += q * vs_re;
+    vs_im += q * vs_im;
+  }
   C Ad[3] = {mkc<R>(0, 0), mkc<R>(0, 0), mkc<R>(0, 0)};
   if (a.order > 1) {
     const C f2 = reinterpret_cast<const C *>(a.phi[1])[idx];
@@ -711,6 +726,62 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
             mkc<R>(V[d].x * er - V[d].y * ei, V[d].x * ei + V[d].y * er);
       }
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (5b) particle masses of a baryon + CDM species (ic_generator.cc:749-780,
+//      particle_generator.hh:369-427): delta_bc(k) = w A_delta_bc(k) =
+//      ratio[n] * phi1 (ratio = -A_delta_bc / A per |k|^2 index n, with the
+//      field's scale folded in), times the sub-lattice phase; after the c2r,
+//      mass = (1 + C delta_bc(x) / sqrt(N^3)) * mass_factor / (n_s N^3)
+// ---------------------------------------------------------------------------
+struct MassArgs {
+  const void *phi1;      // N-grid k-space
+  const double *ratio;   // per |k|^2 index
+  size_t ratio_len;
+  const double2 *phase;  // [ns][3][N]
+  void *field;           // N-grid, in-place c2r layout
+  void *mass;            // particle masses (double or float)
+  int N, shift, nshift_total;
+  double c_species, norm, scale;  // norm = 1/sqrt(N^3), scale = mass_factor / (n_s N^3)
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_mass_field(MassArgs a) {
+  using C = typename Cplx<R>::T;
+  const int N = a.N, nk = N / 2 + 1;
+  const size_t total = size_t(N) * N * nk;
+  const C *p1 = reinterpret_cast<const C *>(a.phi1);
+  C *out = reinterpret_cast<C *>(a.field);
+  const double2 *ph = a.phase + size_t(a.shift) * 3 * N;
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int k = int(idx % nk);
+    const size_t t = idx / nk;
+    const int j = int(t % N), i = int(t / N);
+    const int si = signed_idx(i, N), sj = signed_idx(j, N);
+    const size_t n = size_t(si * si + sj * sj + k * k);
+    const double r = (n > 0 && n < a.ratio_len) ? a.ratio[n] : 0.0;
+    const double2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
+    const double exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
+    const double er = exy_re * ez.x - exy_im * ez.y, ei = exy_re * ez.y + exy_im * ez.x;
+    const C f = p1[idx];
+    const double vr = r * double(f.x), vi = r * double(f.y);
+    out[idx] = mkc<R>(R(vr * er - vi * ei), R(vr * ei + vi * er));
+  }
+}
+
+template <typename R, typename M>
+__global__ void __launch_bounds__(256) k_masses(MassArgs a) {
+  const int N = a.N;
+  const size_t n3 = size_t(N) * N * N;
+  const R *f = reinterpret_cast<const R *>(a.field);
+  M *mass = reinterpret_cast<M *>(a.mass) + size_t(a.shift) * n3;
+  for (size_t c = size_t(blockIdx.x) * blockDim.x + threadIdx.x; c < n3; c += size_t(gridDim.x) * blockDim.x) {
+    const size_t row = c / size_t(N), k = c - row * size_t(N);
+    const double rho = double(f[row * size_t(N + 2) + k]) * a.norm;
+    mass[c] = M(((1.0 + a.c_species * rho) * a.scale));
   }
 }
 

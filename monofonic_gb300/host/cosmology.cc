@@ -475,6 +475,19 @@ double calculator::get_amplitude(double k, tf_type type) const {
   return std::pow(k, 0.5 * m_n_s_) * transfer_function_->compute(k, type) * m_sqrtpnorm_;
 }
 
+double calculator::get_amplitude_delta_bc(double k, bool withvbc) const {
+  const double dratio = Dplus_target_ / Dplus_start_;
+  const double dbc = transfer_function_->compute(k, delta_bc) +
+                     (withvbc ? 2.0 * transfer_function_->compute(k, theta_bc) * (std::sqrt(dratio) - 1.0) : 0.0);
+  return std::pow(k, 0.5 * m_n_s_) * dbc * (m_sqrtpnorm_ * Dplus_target_);
+}
+
+double calculator::get_amplitude_theta_bc(double k, bool withvbc) const {
+  const double dratio = Dplus_target_ / Dplus_start_;
+  const double tbc = transfer_function_->compute(k, theta_bc) * std::sqrt(dratio);
+  return withvbc ? std::pow(k, 0.5 * m_n_s_) * tbc * (m_sqrtpnorm_ * Dplus_target_) : 0.0;
+}
+
 // sigma_8 of the unnormalised spectrum (cosmology_calculator.hh:441-455,
 // 472-485): 4 pi int k^2 W^2(8k) k^n_s T^2 dk over [kmin, kmax], integrated
 // in ln k to a relative accuracy far below the reference's 1e-10 target.

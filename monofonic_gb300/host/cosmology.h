@@ -95,6 +95,11 @@ class calculator {
   double get_vfact(double a) const { return f_of_a_(a) * a * H_of_a(a) / cosmo_param_["h"]; }
   double get_vfact_start() const { return vfac_start_; }
   double get_amplitude(double k, tf_type type) const;
+  // back-scaled delta_bc and relative-velocity theta_bc amplitudes of a baryon
+  // + CDM run (cosmology_calculator.hh:434-450); zero for transfer functions
+  // without separate baryon and CDM transfers (E&H)
+  double get_amplitude_delta_bc(double k, bool withvbc) const;
+  double get_amplitude_theta_bc(double k, bool withvbc) const;
   double compute_sigma8() const;
 
   cosmo_parameters cosmo_param_;

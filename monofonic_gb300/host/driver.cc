@@ -3,8 +3,8 @@
 // output-plugin interface it writes through (output_plugin.hh:33-133).
 //
 // Config keys are the reference's ([setup] GridRes, BoxLength, zstart,
-// LPTorder, ParticleLoad, DoFixing, DoInversion; [random] generator, seed;
-// [cosmology] ...; [output] format, filename).  Two reference compile-time
+// LPTorder, ParticleLoad, DoFixing, DoInversion, DoBaryons, DoBaryonVrel;
+// [random] generator, seed; [cosmology] ...; [output] format, filename).  Two reference compile-time
 // switches become run-time keys: [setup] DoPLT (CMakeLists.txt:111, ENABLE_PLT)
 // and [execution] Precision = double | float (CMakeLists.txt:82-93,
 // CODE_PRECISION; "float" selects the FP32-compensated form).
@@ -31,8 +31,8 @@ enum class cosmo_species { dm, baryon, neutrino };
 
 // particle::container (particle_container.hh:29-188): interleaved xyz
 struct particle_container {
-  std::vector<float> positions32_, velocities32_;
-  std::vector<double> positions64_, velocities64_;
+  std::vector<float> positions32_, velocities32_, mass32_;
+  std::vector<double> positions64_, velocities64_, mass64_;
   std::vector<uint32_t> ids32_;
   std::vector<uint64_t> ids64_;
   size_t get_local_num_particles() const { return std::max(ids32_.size(), ids64_.size()); }
@@ -73,10 +73,15 @@ class binary_output_plugin : public output_plugin {
     b64reals_ = cf.get_value_safe<bool>("output", "UseDoublePrecision", true);
     b64ids_ = cf.get_value_safe<bool>("output", "UseLongids", true);
   }
-  void write_particle_data(const particle_container &pc, const cosmo_species &, double Omega) override {
-    FILE *f = std::fopen(fname_.c_str(), "wb");
-    if (!f) throw std::runtime_error("cannot open output file '" + fname_ + "'");
-    const char magic[8] = {'M', 'F', 'X', 'I', 'C', '0', '0', '1'};
+  // one file per species: the dark matter (or CDM) particles in `filename`,
+  // the baryons of a two-species run in `filename.baryon`; files of
+  // particles with individual masses carry them after the ids (format 002)
+  void write_particle_data(const particle_container &pc, const cosmo_species &s, double Omega) override {
+    const std::string fn = s == cosmo_species::baryon ? fname_ + ".baryon" : fname_;
+    FILE *f = std::fopen(fn.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot open output file '" + fn + "'");
+    const bool masses = !pc.mass64_.empty() || !pc.mass32_.empty();
+    const char magic[8] = {'M', 'F', 'X', 'I', 'C', '0', '0', masses ? '2' : '1'};
     const uint64_t np = pc.get_local_num_particles();
     const uint32_t rs = b64reals_ ? 8 : 4, is = b64ids_ ? 8 : 4;
     const double hdr[3] = {lunit_, Omega, cc_.cosmo_param_["h"]};
@@ -91,8 +96,12 @@ class binary_output_plugin : public output_plugin {
     }
     if (b64ids_) ok = ok && std::fwrite(pc.ids64_.data(), 8, np, f) == np;
     else ok = ok && std::fwrite(pc.ids32_.data(), 4, np, f) == np;
+    if (masses) {
+      if (b64reals_) ok = ok && std::fwrite(pc.mass64_.data(), 8, np, f) == np;
+      else ok = ok && std::fwrite(pc.mass32_.data(), 4, np, f) == np;
+    }
     std::fclose(f);
-    if (!ok) throw std::runtime_error("short write to '" + fname_ + "'");
+    if (!ok) throw std::runtime_error("short write to '" + fn + "'");
   }
   bool has_64bit_reals() const override { return b64reals_; }
   bool has_64bit_ids() const override { return b64ids_; }
@@ -212,8 +221,45 @@ int run_config(mfx_engine *eng, const std::string &text) {
     pc.ids32_.resize(np);
     ip = pc.ids32_.data();
   }
-  if ((rc = mfx_job_fetch_particles(cl.job, pp, vp, ip)) != MFX_OK) return rc;
-  out->write_particle_data(pc, cosmo_species::dm, cc.cosmo_param_["Omega_m"]);
+  const bool baryons = cf.get_value_safe<bool>("setup", "DoBaryons", false);
+  if (!baryons) {
+    if ((rc = mfx_job_fetch_particles(cl.job, pp, vp, ip)) != MFX_OK) return rc;
+    out->write_particle_data(pc, cosmo_species::dm, cc.cosmo_param_["Omega_m"]);
+    return MFX_OK;
+  }
+  // baryon + CDM: both species from the potentials of the run above
+  // (ic_generator.cc:151-166, 706-780, 1016-1020), masses per particle
+  const bool vrel = cf.get_value_safe<bool>("setup", "DoBaryonVrel", false);
+  const double Om = cc.cosmo_param_["Omega_m"], Ob = cc.cosmo_param_["Omega_b"];
+  const double fb = Ob / Om;
+  std::vector<double> dbc(alen, 0.0), tbc(alen, 0.0);
+  for (size_t n = 1; n < alen; ++n) {
+    const double k = 2.0 * M_PI / boxlen * std::sqrt(double(n));
+    dbc[n] = cc.get_amplitude_delta_bc(k, vrel);
+    tbc[n] = cc.get_amplitude_theta_bc(k, vrel);
+  }
+  if (d.pos64) pc.mass64_.resize(np);
+  else pc.mass32_.resize(np);
+  void *mp = d.pos64 ? static_cast<void *>(pc.mass64_.data()) : static_cast<void *>(pc.mass32_.data());
+  const double munit = 1.0;  // the binary plugin's mass unit (masses in units of the critical density x box volume)
+  for (const cosmo_species sp : {cosmo_species::dm, cosmo_species::baryon}) {
+    const bool bar = sp == cosmo_species::baryon;
+    const double omega = bar ? Ob : Om - Ob;
+    mfx_species_desc s{};
+    s.secondary_lattice = bar;
+    s.id_offset = bar ? 1 : 0;
+    s.c_species = bar ? 1.0 - fb : -fb;
+    s.mass_factor = omega * munit;
+    s.amp_dbc = dbc.data();
+    s.amp_tbc = vrel ? tbc.data() : nullptr;
+    s.amp_len = alen;
+    s.want_masses = 1;
+    if ((rc = mfx_job_set_species(cl.job, &s)) != MFX_OK) return rc;
+    if ((rc = mfx_job_assemble(cl.job, 7)) != MFX_OK) return rc;
+    if ((rc = mfx_job_fetch_particles(cl.job, pp, vp, ip)) != MFX_OK) return rc;
+    if ((rc = mfx_job_fetch_masses(cl.job, 0, np, mp)) != MFX_OK) return rc;
+    out->write_particle_data(pc, sp, omega);
+  }
   return MFX_OK;
 }
 

@@ -28,7 +28,7 @@ EXPORTS = [
     "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
     "mfx_job_destroy", "mfx_job_autotune", "mfx_job_capture", "mfx_batch_create", "mfx_batch_run", "mfx_batch_wait",
     "mfx_batch_job", "mfx_batch_destroy", "mfx_server_create", "mfx_server_submit", "mfx_server_wait",
-    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
+    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_server_set_policy", "mfx_job_set_species", "mfx_job_fetch_masses", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
     "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
     "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
     "mfx_cosmology_amp_table", "mfx_run_config", "mfx_job_set_output_ring", "mfx_job_fetch_particles_range_async",
@@ -58,6 +58,12 @@ class JobDesc(C.Structure):
         ("pos64", C.c_int), ("vel64", C.c_int), ("id64", C.c_int), ("id_offset", C.c_uint64),
         ("want_particles", C.c_int),
     ]
+
+
+class SpeciesDesc(C.Structure):
+    _fields_ = [("secondary_lattice", C.c_int), ("id_offset", C.c_uint64), ("c_species", C.c_double),
+                ("mass_factor", C.c_double), ("amp_dbc", C.c_void_p), ("amp_tbc", C.c_void_p),
+                ("amp_len", C.c_size_t), ("want_masses", C.c_int)]
 
 
 _lib = None
@@ -373,10 +379,38 @@ class Job:
                                                     C.c_void_p]
         check(L.mfx_job_fetch_particles_range(self._h, first, count, pos, vel, ids))
 
-    def set_output_ring(self, on: bool = True):
-        """Pipelined output: two particle sets outside the arena, so that a run
-        computes while the previous run's particles are still downloading."""
-        check(load().mfx_job_set_output_ring(self._h, 1 if on else 0))
+    def set_output_ring(self, on=True):
+        """Pipelined output: particle sets outside the arena, so that a run
+        computes while the previous run's particles are still downloading.
+        on: True = two sets, False = none, or the number of sets (0, 1, 2)."""
+        sets = (2 if on else 0) if isinstance(on, bool) else int(on)
+        check(load().mfx_job_set_output_ring(self._h, sets))
+
+    def set_species(self, secondary=False, id_offset=0, c_species=0.0, mass_factor=0.0, amp_dbc=None,
+                    amp_tbc=None, want_masses=True, reset=False):
+        """Species of the next assembly of a baryon + CDM run (mfx_job_set_species);
+        reset=True restores the descriptor's single species."""
+        L = load()
+        L.mfx_job_set_species.argtypes = [C.c_void_p, C.c_void_p]
+        if reset:
+            check(L.mfx_job_set_species(self._h, None))
+            return
+        dbc = None if amp_dbc is None else np.ascontiguousarray(amp_dbc, dtype=np.float64)
+        tbc = None if amp_tbc is None else np.ascontiguousarray(amp_tbc, dtype=np.float64)
+        ln = len(dbc) if dbc is not None else (len(tbc) if tbc is not None else 0)
+        sd = SpeciesDesc(int(secondary), int(id_offset), float(c_species), float(mass_factor),
+                         dbc.ctypes.data if dbc is not None else None, tbc.ctypes.data if tbc is not None else None,
+                         ln, int(want_masses))
+        check(L.mfx_job_set_species(self._h, C.byref(sd)))
+
+    def masses(self, first: int = 0, count=None) -> np.ndarray:
+        """Particle masses of the last assembly with masses."""
+        L = load()
+        L.mfx_job_fetch_masses.argtypes = [C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p]
+        count = self.num_particles - first if count is None else count
+        out = np.zeros(count, dtype=np.float64 if self.pos64 else np.float32)
+        check(L.mfx_job_fetch_masses(self._h, first, count, out.ctypes.data))
+        return out
 
     def fetch_particles_range_async(self, first: int, count: int, pos, vel, ids):
         """Enqueues the download of particles [first, first + count) of the last
@@ -564,6 +598,13 @@ class Server:
 
     def wait(self, ticket: int, timeout_ms: int = -1):
         check(load().mfx_server_wait(self._h, ticket, timeout_ms))
+
+    def set_policy(self, bypass: bool = True, bypass_age_ms: float = 100.0):
+        """Admission order: a later job that fits may pass a head that has
+        waited at most bypass_age_ms (bypass), or strict first-in first-out."""
+        L = load()
+        L.mfx_server_set_policy.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        check(L.mfx_server_set_policy(self._h, int(bypass), float(bypass_age_ms)))
 
     def times(self, ticket: int):
         q, l = C.c_double(), C.c_double()

@@ -493,6 +493,101 @@ def particles(fields, coef, grad, lattice, n, L, lunit, vunit, order, id_offset=
     return pos, vel, ids
 
 
+# particle_generator.hh:56-63: the secondary lattice of a second species
+SECOND_LATTICE_SHIFT = {0: (0.5, 0.5, 0.5), 1: (0.5, 0.5, 0.0), 2: (0.5, 0.5, 0.5)}
+
+
+def amp_of_index(table, n, L):
+    """A per-mode array from a table indexed by |k|^2 / kf^2 = i^2 + j^2 + k^2
+    over signed mode indices (zero beyond the table)."""
+    i = _signed(n, n)
+    kk = np.arange(n // 2 + 1, dtype=np.float64)
+    q = (i[:, None, None] ** 2 + i[None, :, None] ** 2 + kk[None, None, :] ** 2).astype(np.int64)
+    t = np.asarray(table, dtype=np.float64)
+    out = np.zeros(q.shape)
+    ok = q < len(t)
+    out[ok] = t[q[ok]]
+    return out
+
+
+def species_particles(fields, noise, coef, grad, lattice, n, L, lunit, vunit, order, c_species,
+                      mass_factor, amp_dbc=None, amp_tbc=None, secondary=False, id_offset=0):
+    """One species of a baryon + CDM run (ic_generator.cc:706-1064): positions
+    from the shared LPT displacement on the species' lattice (the secondary
+    lattice for baryons, shifted by SECOND_LATTICE_SHIFT before the read-out,
+    particle_generator.hh:388-395, 510-517), velocities with the linear
+    relative-velocity term -vfac1 C A_theta_bc(k) w grad_d / k^2 added before
+    vfac_corr (ic_generator.cc:1016-1020), masses (1 + C delta_bc(x)) *
+    mass_factor / (n_s N^3) with delta_bc(k) = w A_delta_bc(k)
+    (ic_generator.cc:749-780, particle_generator.hh:369-427), ids with the
+    species' IDoffset.  amp_dbc / amp_tbc: get_amplitude_delta_bc /
+    get_amplitude_theta_bc per |k|^2 index (None: zero).
+    Returns pos, vel, ids, masses."""
+    phi, phi2, phi3, A3 = fields
+    shifts = LATTICE_SHIFTS[lattice]
+    ns = len(shifts)
+    n3 = n ** 3
+    kx, ky, kz = kvec(n, L)
+    k2 = kx * kx + ky * ky + kz * kz
+    sec = SECOND_LATTICE_SHIFT[lattice] if secondary else (0.0, 0.0, 0.0)
+
+    def read_out(f, d=None, q_unit=None):
+        out = np.zeros(ns * n3)
+        for ish, s in enumerate(shifts):
+            if ish == 0 and secondary:
+                f = shift_field(f, sec, n, L)
+            if ish > 0:
+                prev = shifts[ish - 1]
+                f = shift_field(f, (s[0] - prev[0], s[1] - prev[1], s[2] - prev[2]), n, L)
+            vals = f.reshape(-1)
+            if d is not None:
+                idx = np.arange(n, dtype=np.float64)
+                shape = [1, 1, 1]
+                shape[d] = n
+                qd = ((idx + s[d] + sec[d]) / float(n)).reshape(shape)
+                vals = (qd * q_unit + f).reshape(-1)
+            out[ish * n3:(ish + 1) * n3] = vals
+        return out
+
+    pos = np.zeros((ns * n3, 3))
+    vel = np.zeros((ns * n3, 3))
+    for d in range(3):
+        pos[:, d] = read_out(fft_c2r(assemble_displacement(d, fields, coef, grad, lunit, L, order), n), d, lunit)
+    tbc = amp_of_index(amp_tbc, n, L) if amp_tbc is not None else None
+    for d in range(3):
+        dp, dpp = (d + 1) % 3, (d + 2) % 3
+        pv = coef["vfac1"] * phi
+        if order > 1:
+            pv = pv + coef["vfac2"] * phi2
+        if order > 2:
+            pv = pv + coef["vfac3"] * phi3
+        tmp = _times_i(grad.gradient(d), pv)
+        if order > 2:
+            tmp = tmp + coef["vfac3"] * (_times_i(grad.gradient(dp), A3[dpp]) - _times_i(grad.gradient(dpp), A3[dp]))
+        if tbc is not None:
+            with np.errstate(divide="ignore", invalid="ignore"):
+                term = coef["vfac1"] * c_species * tbc * noise * 1j * grad.gradient(d) / k2
+            term[0, 0, 0] = 0.0
+            tmp = tmp - term
+        tmp = tmp * grad.vfac_corr()
+        tmp = tmp * (vunit / L)
+        tmp[0, 0, 0] = 0.0
+        vel[:, d] = read_out(fft_c2r(tmp, n))
+    masses = np.full(ns * n3, mass_factor / (ns * n3))
+    if amp_dbc is not None:
+        rho = noise * amp_of_index(amp_dbc, n, L)
+        rho[0, 0, 0] = 0.0
+        r = fft_c2r(rho, n)
+        r = (1.0 + c_species * r) * mass_factor
+        masses = read_out(r) / (ns * n3)
+    cell = np.arange(n3, dtype=np.uint64)
+    ids = np.zeros(ns * n3, dtype=np.uint64)
+    off = np.uint64(id_offset * ns * n3)
+    for il in range(ns):
+        ids[il * n3:(il + 1) * n3] = off + np.uint64(ns) * cell + np.uint64(il)
+    return pos, vel, ids, masses
+
+
 def run_lpt(n, L, seed_table, amplitude, order, dplus, vfac, lattice=0, lunit=1.0, vunit=1.0,
             fixing=False, inversion=False, grad=None, want_particles=True):
     """The whole hot path, ic_generator.cc:288-1064, for one species (dm, no baryons)."""

@@ -61,13 +61,14 @@ def test_ensemble_members_match_standalone_runs(mfxlib, engine):
     b.close()
 
 
-@pytest.mark.parametrize("ring", [True, False])
+@pytest.mark.parametrize("ring", [2, 1, 0])
 def test_pipelined_downloads_match_runs_one_at_a_time(mfxlib, engine, ring):
-    """Asynchronous downloads, with the output ring (runs alternate between two
-    particle sets and compute while the previous run's particles download) and
-    without it (the next run waits): three runs of one job, three seeds through
-    mfx_job_upload, each run enqueued right after the previous run's download,
-    give each seed's particles of a run made alone."""
+    """Asynchronous downloads, with the output ring of two particle sets (runs
+    alternate between them and compute while the previous run's particles
+    download), of one set (a run's assembly waits for the previous download)
+    and without it (the next run waits): three runs of one job, three seeds
+    through mfx_job_upload, each run enqueued right after the previous run's
+    download, give each seed's particles of a run made alone."""
     import torch
     specs = [spec(mfxlib, 48, 150.0, 24.0, 3, s, lattice=1, precision=mfxlib.FP32C) for s in (31, 32, 33)]
     refs = [run_alone(mfxlib, engine, sp) for sp in specs]
@@ -75,7 +76,7 @@ def test_pipelined_downloads_match_runs_one_at_a_time(mfxlib, engine, ring):
     j = mfxlib.Job(engine, 48, 150.0, 3, sp0["seed_table"], sp0["amp_table"], sp0["coef"], lattice=1,
                    precision=mfxlib.FP32C, lunit=sp0["lunit"], vunit=sp0["vunit"])
     if ring:
-        j.set_output_ring(True)
+        j.set_output_ring(ring)
     npart = j.num_particles
     bufs = []
     for _ in specs:

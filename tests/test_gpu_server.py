@@ -39,6 +39,13 @@ def alone(mfx, engine, sp):
 
 def test_server_results_same_alone_and_in_the_mix(mfxlib, engine):
     specs = mixed_specs(mfxlib, engine, 10)
+    # two larger jobs in the mix: 3LPT + PLT FCC at 128^3 and 2LPT BCC at 192^3, FP32 form
+    for n, lat, order in ((128, 2, 3), (192, 1, 2)):
+        sp = spec(mfxlib, n, 300.0 * n / 256, 24.0, order, 500 + n, lattice=lat, precision=mfxlib.FP32C)
+        if lat not in _PLT:
+            _PLT[lat] = engine.plt_table(lat)
+        sp["plt_table"] = _PLT[lat]
+        specs.insert(3 + len(specs) % 4, sp)
     srv = mfxlib.Server(engine, max_inflight=4)
     tickets = [srv.submit(sp) for sp in specs]
     for t in tickets:
@@ -92,3 +99,83 @@ def test_server_wait_timeout_is_an_error_not_a_hang(mfxlib, engine):
     with pytest.raises(mfxlib.MfxError):
         srv.release(t)
     srv.close()
+
+
+def _footprint(mfx, engine, sp):
+    import ctypes
+    j = mfx.Job(engine, sp["ngrid"], sp["boxlen"], sp["order"], sp["seed_table"], sp["amp_table"], sp["coef"],
+                want_particles=True)
+    fp = ctypes.c_size_t()
+    mfx.check(mfx.load().mfx_job_footprint(engine.handle, ctypes.byref(j.desc), ctypes.byref(fp)))
+    j.close()
+    return fp.value
+
+
+@pytest.mark.parametrize("bypass", [True, False])
+def test_server_bounded_bypass_of_a_head_that_does_not_fit(mfxlib, bypass):
+    """A budget for one large job and a little more: while the first large job's
+    results are held, a second large job cannot be admitted.  With bypass, the
+    small jobs queued behind it start and finish anyway; with strict
+    first-in first-out admission they wait behind it.  Releasing the first
+    large job lets the rest through, in both policies."""
+    big = [spec(mfxlib, 64, 100.0, 24.0, 3, 300 + q) for q in range(2)]
+    small = [spec(mfxlib, 16, 25.0, 24.0, 1, 400 + q) for q in range(2)]
+    probe = mfxlib.Engine(0)
+    fb, fs = _footprint(mfxlib, probe, big[0]), _footprint(mfxlib, probe, small[0])
+    probe.close()
+    eng = mfxlib.Engine(0, hbm_budget_bytes=int(fb * 1.5) + 4 * fs)
+    srv = mfxlib.Server(eng, max_inflight=4)
+    srv.set_policy(bypass=bypass, bypass_age_ms=60000.0)
+    t_big0 = srv.submit(big[0])
+    srv.wait(t_big0, 60000)
+    t_big1 = srv.submit(big[1])
+    t_small = [srv.submit(sp) for sp in small]
+    if bypass:
+        for t in t_small:
+            srv.wait(t, 60000)
+    else:
+        with pytest.raises(mfxlib.MfxError) as e:
+            srv.wait(t_small[0], 500)
+        assert e.value.code == mfxlib.MFX_ETIMEOUT
+    with pytest.raises(mfxlib.MfxError):
+        srv.wait(t_big1, 200)  # the head still does not fit
+    srv.release(t_big0)
+    srv.wait(t_big1, 60000)
+    for t in t_small:
+        srv.wait(t, 60000)
+    ref = alone(mfxlib, eng, small[1])
+    got = srv.job(t_small[1]).particles()
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    for t in [t_big1] + t_small:
+        srv.release(t)
+    srv.close()
+    eng.close()
+
+
+def test_server_age_limit_stops_bypassing_an_old_head(mfxlib):
+    """With an age limit of zero the head is never passed: a small job that
+    would fit waits behind a large head that does not."""
+    big = [spec(mfxlib, 64, 100.0, 24.0, 3, 310 + q) for q in range(2)]
+    small = spec(mfxlib, 16, 25.0, 24.0, 1, 410)
+    probe = mfxlib.Engine(0)
+    fb, fs = _footprint(mfxlib, probe, big[0]), _footprint(mfxlib, probe, small)
+    probe.close()
+    eng = mfxlib.Engine(0, hbm_budget_bytes=int(fb * 1.5) + 4 * fs)
+    srv = mfxlib.Server(eng, max_inflight=4)
+    srv.set_policy(bypass=True, bypass_age_ms=0.0)
+    t0 = srv.submit(big[0])
+    srv.wait(t0, 60000)
+    t1 = srv.submit(big[1])
+    import time
+    time.sleep(0.01)  # the head is now older than the limit
+    ts = srv.submit(small)
+    with pytest.raises(mfxlib.MfxError):
+        srv.wait(ts, 500)
+    srv.release(t0)
+    srv.wait(t1, 60000)
+    srv.wait(ts, 60000)
+    srv.release(t1)
+    srv.release(ts)
+    srv.close()
+    eng.close()
