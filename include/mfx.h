@@ -172,6 +172,22 @@ int mfx_job_set_species(mfx_job *job, const mfx_species_desc *species);
    masses (double when the job's positions are double, else float;
    particle_container.hh:44-74), into host or device memory. */
 int mfx_job_fetch_masses(mfx_job *job, size_t first, size_t count, void *out);
+/* Semiclassical (PPT) Eulerian fields of a species (ic_generator.cc:783-901,
+   output_type::field_eulerian): from the potentials of the last mfx_job_run,
+   the wave function psi = sqrt(1 + C delta_bc) exp(i (phi [+ phi2]) /
+   (hbar D+)) with hbar = 1.01 max|grad phi| / (pi D+), one free drift step and
+   (2LPT and above) a second kick, then the density contrast
+   delta = |psi|^2 - 1 and the velocities v_d = D+ vfac / L * vunit *
+   hbar Im(conj(psi) d_d psi) / |psi|^2 -- the fields the reference hands to
+   output_plugin::write_grid_data (density, vx, vy, vz).  Computed in FP64
+   for either arithmetic form, through complex FFTs on the device.
+   c_species and amp_dbc (get_amplitude_delta_bc per |k|^2 index, NULL for
+   none) as in mfx_species_desc; D+ = -g1 and vfac = vfac1 of the job.  Each
+   output is N^3 doubles, x slowest (host or device memory, NULL to skip);
+   *hbar (optional) receives hbar.  Device scratch of about 56 N^3 bytes is
+   allocated for the call and freed before it returns. */
+int mfx_job_ppt_fields(mfx_job *job, double c_species, const double *amp_dbc, size_t amp_len, double *delta,
+                       double *vx, double *vy, double *vz, double *hbar);
 /* Pipelined output (no counterpart in the reference, whose output plugins
    write a realisation after it is generated): `sets` = 1 or 2 gives the job
    that many particle sets of its own, outside the arena (charged to the

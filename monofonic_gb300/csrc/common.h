@@ -3,6 +3,7 @@
 #include <string>
 
 struct mfx_engine;
+struct mfx_job;
 
 namespace mfx {
 // Records `fmt` as the calling thread's last error and returns `code`.
@@ -14,4 +15,19 @@ int engine_device(const mfx_engine *eng);
 // its fixed scratch array and kernels become resident at engine creation
 // instead of at that entry point's first call.
 int noalloc_prepare(int dev);
+
+// What the Eulerian (PPT) field pass needs of a finished job: its device,
+// stream and k-space potentials (phi1, phi2: N x N x (N/2+1) complex of double
+// or float, stored as scale x the unscaled potential), the growth
+// coefficients, the amplitude table (host copy) and the velocity unit.
+struct JobFields {
+  int device, N, order;
+  bool fp64, has_potentials;
+  void *stream;  // cudaStream_t
+  const void *phi1, *phi2;
+  double scale1, scale2, g1, g2, vfac1, boxlen, vunit;
+  const double *amp;
+  size_t amp_len;
+};
+int job_fields(const mfx_job *job, JobFields *out);
 }  // namespace mfx

@@ -228,6 +228,28 @@ struct mfx_job {
 
 int mfx::engine_device(const mfx_engine *eng) { return eng ? eng->device : 0; }
 
+int mfx::job_fields(const mfx_job *j, JobFields *o) {
+  if (!j || !o) return set_error(MFX_EINVAL, "null argument");
+  o->device = j->eng->device;
+  o->N = j->N;
+  o->order = j->d.lpt_order;
+  o->fp64 = j->fp64;
+  o->has_potentials = j->has_run && !j->noise_only;
+  o->stream = j->stream;
+  o->phi1 = j->nf[0];
+  o->phi2 = j->d.lpt_order > 1 ? j->nf[1] : nullptr;
+  o->scale1 = j->scale1;
+  o->scale2 = j->scale2;
+  o->g1 = j->d.g1;
+  o->g2 = j->d.g2;
+  o->vfac1 = j->d.vfac1;
+  o->boxlen = j->d.boxlen;
+  o->vunit = j->d.vunit;
+  o->amp = j->amp_host.data();
+  o->amp_len = j->amp_host.size();
+  return MFX_OK;
+}
+
 // ---------------------------------------------------------------------------
 // sizes
 // ---------------------------------------------------------------------------

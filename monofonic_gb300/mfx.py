@@ -28,7 +28,7 @@ EXPORTS = [
     "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
     "mfx_job_destroy", "mfx_job_autotune", "mfx_job_capture", "mfx_batch_create", "mfx_batch_run", "mfx_batch_wait",
     "mfx_batch_job", "mfx_batch_destroy", "mfx_server_create", "mfx_server_submit", "mfx_server_wait",
-    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_server_set_policy", "mfx_job_set_species", "mfx_job_fetch_masses", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
+    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_server_set_policy", "mfx_job_set_species", "mfx_job_fetch_masses", "mfx_job_ppt_fields", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
     "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
     "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
     "mfx_cosmology_amp_table", "mfx_run_config", "mfx_job_set_output_ring", "mfx_job_fetch_particles_range_async",
@@ -402,6 +402,21 @@ class Job:
                          dbc.ctypes.data if dbc is not None else None, tbc.ctypes.data if tbc is not None else None,
                          ln, int(want_masses))
         check(L.mfx_job_set_species(self._h, C.byref(sd)))
+
+    def ppt_fields(self, c_species=0.0, amp_dbc=None):
+        """Semiclassical (PPT) Eulerian density contrast and velocities of the
+        last run's potentials (mfx_job_ppt_fields): (delta, (vx, vy, vz), hbar),
+        each field N x N x N."""
+        L = load()
+        L.mfx_job_ppt_fields.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+        n = self.n
+        dbc = None if amp_dbc is None else np.ascontiguousarray(amp_dbc, dtype=np.float64)
+        out = [np.zeros((n, n, n)) for _ in range(4)]
+        hb = C.c_double()
+        check(L.mfx_job_ppt_fields(self._h, float(c_species), dbc.ctypes.data if dbc is not None else None,
+                                   len(dbc) if dbc is not None else 0, *[o.ctypes.data for o in out], C.byref(hb)))
+        return out[0], tuple(out[1:]), hb.value
 
     def masses(self, first: int = 0, count=None) -> np.ndarray:
         """Particle masses of the last assembly with masses."""

@@ -588,6 +588,50 @@ def species_particles(fields, noise, coef, grad, lattice, n, L, lunit, vunit, or
     return pos, vel, ids, masses
 
 
+def ppt_fields(phi_s, phi2_s, noise, order, n, L, dplus, vfac, vunit, c_species=0.0, amp_dbc=None):
+    """Semiclassical (PPT) Eulerian density and velocity fields of one species,
+    ic_generator.cc:783-901: rho = sqrt(1 + C delta_bc(x)); hbar from the
+    largest nearest-neighbour step of the real-space phi (the x loop stops one
+    short of the last plane, ic_generator.cc:813-829) as maxdphi / pi / D+ x
+    1.01; psi = rho exp(i (phi [+ phi2]) / (hbar D+)); one drift step
+    exp(-i hbar k^2 D+ / 2) in k-space; for 2LPT and above a second kick
+    exp(i phi2 / (hbar D+)); delta = |psi|^2 - 1 and
+    v_d = vunit' Re[(conj(psi) d_d psi - psi conj(d_d psi)) / (2i / hbar)] / (1 + delta)
+    with vunit' = D+ vfac / L * vunit.  phi_s, phi2_s: the growth-scaled
+    potentials (k-space).  Returns delta, (vx, vy, vz), hbar."""
+    phir = fft_c2r(phi_s, n)
+    rho = np.ones((n, n, n))
+    if amp_dbc is not None:
+        d = noise * amp_of_index(amp_dbc, n, L)
+        d[0, 0, 0] = 0.0
+        rho = np.sqrt(1.0 + c_species * fft_c2r(d, n))
+    dx = np.abs(np.roll(phir, -1, axis=0) - phir)[:n - 1]
+    dy = np.abs(np.roll(phir, -1, axis=1) - phir)[:n - 1]
+    dz = np.abs(np.roll(phir, -1, axis=2) - phir)[:n - 1]
+    maxdphi = max(dx.max(), dy.max(), dz.max())
+    hbar = maxdphi / np.pi / dplus * 1.01
+    if order == 1:
+        psi = rho * np.exp(1j / hbar * (phir / dplus))
+    else:
+        phi2r = fft_c2r(phi2_s, n)
+        psi = rho * np.exp(1j / hbar * (phir + phi2r) / dplus)
+    kfac = 2.0 * np.pi / L
+    k1 = _signed(n, n) * kfac
+    kx, ky, kz = k1[:, None, None], k1[None, :, None], k1[None, None, :]
+    k2 = kx * kx + ky * ky + kz * kz
+    psi = np.fft.ifftn(np.fft.fftn(psi) * np.exp(-0.5j * hbar * k2 * dplus))
+    if order >= 2:
+        psi = psi * np.exp(1j / hbar * phi2r / dplus)
+    delta = psi.real ** 2 + psi.imag ** 2 - 1.0
+    vu = dplus * vfac / L * vunit
+    vel = []
+    fk = np.fft.fftn(psi)
+    for kd in (kx, ky, kz):
+        g = np.fft.ifftn(fk * (1j * kd))
+        vel.append(vu * np.real((np.conj(psi) * g - psi * np.conj(g)) / (2.0j / hbar)) / (1.0 + delta))
+    return delta, vel, hbar
+
+
 def run_lpt(n, L, seed_table, amplitude, order, dplus, vfac, lattice=0, lunit=1.0, vunit=1.0,
             fixing=False, inversion=False, grad=None, want_particles=True):
     """The whole hot path, ic_generator.cc:288-1064, for one species (dm, no baryons)."""
