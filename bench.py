@@ -104,6 +104,14 @@ def replica_throughput(local_ms, local_particles, device="cpu"):
     return float(t.item()), float(n.item()) / (float(t.item()) * 1e-3)
 
 
+_T0 = time.perf_counter()
+
+
+def progress(msg):
+    """Phase markers with elapsed seconds, on stderr (the JSON line is stdout)."""
+    print("[bench %7.1f s] %s" % (time.perf_counter() - _T0, msg), file=sys.stderr, flush=True)
+
+
 _CLOCK_DIR = None
 
 
@@ -228,8 +236,10 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    progress("job created, tiles %s; warm-up" % (tiles,))
     for _ in range(args.warmup):
         job.run()
+    progress("timed device steps")
     job.set_profiling(True)
     barrier()
     clocks = Clocks(local, clock_csv("clocks_rank%d.csv" % rank)) if rank == 0 else None
@@ -276,6 +286,7 @@ def run_ours(args):
             job.fetch_particles_range_into(first, min(chunk, npart - first), pb.ctypes.data, vb.ctypes.data,
                                            ib.ctypes.data)
 
+    progress("end to end, one step at a time")
     job.upload(hs, ha, hp)
     job.run()
     fetch_all()
@@ -315,6 +326,7 @@ def run_ours(args):
             break
         except RuntimeError:
             continue
+    progress("end to end, pipelined with %d device set(s)" % ring)
     if ring:
         nh = 2 if ring == 2 else 1
         host = [(pinned(npart * 3 * 8), pinned(npart * 3 * (8 if vel64 else 4)), pinned(npart * 8)) for _ in range(nh)]
@@ -831,6 +843,7 @@ def run_reference(args):
     vals, dts, stages = [], [], None
     for s in range(args.warmup + args.steps):
         v, dt, st = cpu_restatement(n_sample, args.workload, tab, seed_offset=s)
+        progress("reference step %d: %.1f s" % (s, dt))
         if s >= args.warmup:
             vals.append(v)
             dts.append(dt)
@@ -888,6 +901,7 @@ def main():
             print(json.dumps(out))
     elif rank == 0:
         if not args.no_fp64 and args.precision == "fp32c":
+            progress("plain FP64 form and the error statement")
             out.update(fp64_and_error(args, eng, inp, plt_tab, out))
         if not args.no_cpu_baseline and world == 1:
             from oracle import lpt
@@ -895,6 +909,7 @@ def main():
             lpt.build_omp_lib()
             threads = int(lpt.omp_lib().mfxo_omp_threads())
             n_sample = CPU_SAMPLE[args.workload]
+            progress("CPU baseline at %d^3 (%d threads)" % (n_sample, threads))
             tab, tab_s = oracle_plt_tables(args.workload)
             v, dt, st = cpu_restatement(n_sample, args.workload, tab)
             out["cpu_baseline"] = {"value": v, "unit": "particles/s", "cores": threads, "kind": "port",

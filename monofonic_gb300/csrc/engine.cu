@@ -2308,6 +2308,10 @@ int mfx_debug_ranlxd1_words(mfx_engine *eng, unsigned long seed, size_t count, u
 namespace {
 using clk = std::chrono::steady_clock;
 
+// the life of a request; a ticket is finished (results readable or an error
+// recorded) exactly when its state is kDone or kFailed
+enum TicketState { kQueued = 0, kSetup = 1, kRunning = 2, kDone = 3, kFailed = 4 };
+
 struct Ticket {
   uint64_t id = 0;
   mfx_job_desc d{};
@@ -2315,7 +2319,7 @@ struct Ticket {
   std::vector<double> amp, plt;
   size_t footprint = 0;
   clk::time_point t_submit, t_admit, t_done;
-  int state = 0;  // 0 queued, 4 admitted (being set up), 1 running, 2 done, 3 failed
+  int state = 0;  // TicketState
   int rc = MFX_OK;
   std::string err;
   mfx_job *job = nullptr;
@@ -2369,11 +2373,11 @@ static void server_loop(mfx_server *s) {
     // retire finished jobs (their results stay resident)
     for (auto &kv : s->tickets) {
       Ticket *t = kv.second.get();
-      if (t->state != 1) continue;
+      if (t->state != kRunning) continue;
       const cudaError_t q = cudaEventQuery(t->done);
       if (q == cudaErrorNotReady) continue;
       t->t_done = clk::now();
-      t->state = (q == cudaSuccess) ? 2 : 3;
+      t->state = (q == cudaSuccess) ? kDone : kFailed;
       if (q != cudaSuccess) {
         t->rc = MFX_ECUDA;
         t->err = cudaGetErrorString(q);
@@ -2389,7 +2393,7 @@ static void server_loop(mfx_server *s) {
       Ticket *t = s->queue[size_t(q)];
       s->queue.erase(s->queue.begin() + q);
       t->t_admit = now;
-      t->state = 4;
+      t->state = kSetup;
       s->reserved += t->footprint;
       ++s->inflight;
       s->setup_q.push_back(t);
@@ -2421,14 +2425,14 @@ static void setup_loop(mfx_server *s) {
     lk.lock();
     s->reserved -= std::min(s->reserved, t->footprint);
     if (rc != MFX_OK) {
-      t->state = 3;
+      t->state = kFailed;
       t->rc = rc;
       t->err = err;
       t->t_done = clk::now();
       --s->inflight;
     } else {
       t->job = j;
-      t->state = 1;
+      t->state = kRunning;
     }
     s->cv.notify_all();
   }
@@ -2495,11 +2499,11 @@ int mfx_server_wait(mfx_server *s, uint64_t ticket, int timeout_ms) {
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
   Ticket *t = it->second.get();
-  auto pred = [t] { return t->state >= 2; };
+  auto pred = [t] { return t->state >= kDone; };
   if (timeout_ms < 0) s->cv.wait(lk, pred);
   else if (!s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
     return set_error(MFX_ETIMEOUT, "ticket %llu not finished after %d ms", (unsigned long long)ticket, timeout_ms);
-  if (t->state == 3) return set_error(t->rc, "ticket %llu failed: %s", (unsigned long long)ticket, t->err.c_str());
+  if (t->state == kFailed) return set_error(t->rc, "ticket %llu failed: %s", (unsigned long long)ticket, t->err.c_str());
   return MFX_OK;
   GUARD_END
 }
@@ -2510,7 +2514,7 @@ int mfx_server_ticket_times(mfx_server *s, uint64_t ticket, double *queued_ms, d
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket");
   Ticket *t = it->second.get();
-  if (t->state < 2) return set_error(MFX_ESTATE, "ticket not finished");
+  if (t->state < kDone) return set_error(MFX_ESTATE, "ticket not finished");
   if (queued_ms) *queued_ms = ms_between(t->t_submit, t->t_admit);
   if (latency_ms) *latency_ms = ms_between(t->t_submit, t->t_done);
   return MFX_OK;
@@ -2521,7 +2525,7 @@ int mfx_server_job(mfx_server *s, uint64_t ticket, mfx_job **job) {
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket");
-  if (it->second->state != 2) return set_error(MFX_ESTATE, "ticket not finished");
+  if (it->second->state != kDone) return set_error(MFX_ESTATE, "ticket not finished");
   *job = it->second->job;
   return MFX_OK;
 }
@@ -2534,7 +2538,7 @@ int mfx_server_release(mfx_server *s, uint64_t ticket) {
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->tickets.find(ticket);
     if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket");
-    if (it->second->state < 2) return set_error(MFX_ESTATE, "ticket still queued or running");
+    if (it->second->state < kDone) return set_error(MFX_ESTATE, "ticket still queued, being set up or running");
     t = std::move(it->second);
     s->tickets.erase(it);
   }

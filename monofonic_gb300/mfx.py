@@ -264,11 +264,13 @@ class Engine:
 
 
 def lpt_coefficients(dplus: float, vfac: float, order: int) -> dict:
-    """ic_generator.cc:252-269"""
+    """ic_generator.cc:252-269, evaluated in the reference's order (left to
+    right, D+ * D+ * D+ rather than a power), so that the coefficients equal
+    the reference's bit for bit"""
     return dict(g1=-dplus,
                 g2=(-3.0 / 7.0 * dplus * dplus) if order > 1 else 0.0,
-                g3=(1.0 / 3.0 * dplus ** 3) if order > 2 else 0.0,
-                g3c=(1.0 / 7.0 * dplus ** 3) if order > 2 else 0.0,
+                g3=(1.0 / 3.0 * dplus * dplus * dplus) if order > 2 else 0.0,
+                g3c=(1.0 / 7.0 * dplus * dplus * dplus) if order > 2 else 0.0,
                 vfac1=vfac, vfac2=2 * vfac, vfac3=3 * vfac)
 
 
