@@ -270,6 +270,16 @@ def run_ours(args):
         return {"profiling_run": True, "workload": args.workload, "value": value, "ms_per_step": ms_step,
                 "kernels": kern, "clocks": clk, "fused_tiles": list(tiles) if tiles else None}, None, inp, plt_tab
     # ---- e2e through the C ABI with host buffers ----
+    # the FP32 form keeps float displacements on the device and forms q + Psi
+    # in FP64 on the host (mfx_job_set_host_positions: the same doubles), so a
+    # particle crosses the host link in 12 + 12 bytes instead of 24 + 12
+    host_pos = False
+    if prec == mfx.FP32C:
+        try:
+            job.set_host_positions(True)
+            host_pos = True
+        except RuntimeError:
+            host_pos = False
     # particles come back in chunks of at most 128M (a bounded pinned buffer),
     # the way an output plugin drains them
     chunk = min(npart, 1 << 27)
@@ -279,7 +289,7 @@ def run_ours(args):
     h2d = hs.nbytes + ha.nbytes + (hp.nbytes if hp is not None else 0)
     # positions and velocities cross the host link; the ids (a closed form of the
     # particle index) are written into the host buffer by the fetch's host threads
-    d2h = npart * (3 * 8 + 3 * (8 if vel64 else 4))
+    d2h = npart * (3 * (4 if host_pos else 8) + 3 * (8 if vel64 else 4))
 
     def fetch_all():
         for first in range(0, npart, chunk):
@@ -315,9 +325,11 @@ def run_ours(args):
     # one reused: a step's download starts after the previous one has ended);
     # no L2 flush is needed between steps: each step's inputs come from the
     # host and its HBM traffic (17 GB at 256^3) is far above the 129 MB L2.
-    host_set = d2h + npart * 8
+    host_set = npart * (3 * 8 + 3 * (8 if vel64 else 4) + 8)  # f64 positions, velocities, ids
     ring = 0
-    for sets, host_sets in ((2, 2), (1, 1)):
+    # with host-side positions one host set serves both device sets: a fetch
+    # joins the previous fetch's host threads before it enqueues its copies
+    for sets, host_sets in ((2, 1 if host_pos else 2), (1, 1)):
         if host_sets * host_set > (100 << 30):
             continue
         try:
@@ -328,7 +340,7 @@ def run_ours(args):
             continue
     progress("end to end, pipelined with %d device set(s)" % ring)
     if ring:
-        nh = 2 if ring == 2 else 1
+        nh = host_sets
         host = [(pinned(npart * 3 * 8), pinned(npart * 3 * (8 if vel64 else 4)), pinned(npart * 8)) for _ in range(nh)]
         sets = [tuple(x[1] for x in st) for st in host]  # numpy views; `host` keeps the tensors alive
 
@@ -357,7 +369,9 @@ def run_ours(args):
                         "(output ring of one set; its assembly waits for the download)")}
         job.set_output_ring(0)
     e2e.update({"h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "ids": "written into the host buffers by the fetch (host threads, beside the copies)"})
+                "ids": "written into the host buffers by the fetch (host threads, beside the copies)",
+                "positions": ("float displacements copied, q + Psi formed in FP64 by the fetch's host threads"
+                              if host_pos else "FP64 positions copied")})
     if ring:
         e2e["serial"] = e2e_serial
 

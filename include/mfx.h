@@ -201,6 +201,20 @@ int mfx_job_ppt_fields(mfx_job *job, double c_species, const double *amp_dbc, si
    of earlier runs are no longer fetchable.  MFX_ESTATE for a captured job
    (and capture refuses a job with the ring). */
 int mfx_job_set_output_ring(mfx_job *job, int sets);
+/* Host-side positions (FP32 form, fused route, 64-bit positions; no
+   counterpart in the reference): the read-out keeps each particle's float
+   displacement Psi on the device instead of q + Psi in FP64, and every fetch
+   into host memory copies the 12 displacement bytes instead of 24 position
+   bytes and forms q + Psi in FP64 with host threads from the lattice
+   coordinates -- the same doubles the device would store (the FP32 form's Psi
+   is a float, and both sides add it to the same q in FP64).  With the ids
+   also written on the host, a particle crosses the host link in 24 bytes
+   (f32 velocities) instead of 44.  Positions and ids then reach host memory
+   only (MFX_ESTATE for device destinations), and mfx_job_particles_device
+   returns the displacements as the position array.  Set it before
+   mfx_job_set_output_ring; a job that has run is re-assembled in the new
+   form.  on = 0 returns to device-side positions. */
+int mfx_job_set_host_positions(mfx_job *job, int on);
 /* Enqueues the download of particles [first, first + count) of the job's
    last run into host buffers (page-locked for the copies to overlap) behind
    the job's enqueued work, and returns.  Call it before the next

@@ -181,7 +181,14 @@ struct mfx_job {
   void *mslot[18] = {};
   void *asmbuf[24] = {};
   void *pos = nullptr, *vel = nullptr, *ids = nullptr;
-  std::vector<std::thread> id_fill;  // host threads writing the ids of an asynchronous fetch
+  std::vector<std::thread> id_fill;  // host threads writing the ids / positions of a fetch
+  // host-side positions (mfx_job_set_host_positions): the device keeps float
+  // displacements, a fetch copies them to page-locked staging and host threads
+  // form q + Psi in FP64 from the lattice coordinates qhost ([shift][axis][N])
+  bool host_q = false;
+  float *psi_host = nullptr;
+  std::vector<double> qhost;
+  cudaEvent_t psi_ev[16] = {};
   void *work = nullptr;
   size_t work_bytes = 0;
   Plan m_r2c, m_c2r, n_c2r;
@@ -826,7 +833,8 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   const double qf = double(N) * N * (N / 2) * 8;  // one component field
   const double nfb = double(j->n_field_bytes);
   const double N3 = double(N) * N * N;
-  const double pb = N3 * (3.0 * (j->d.pos64 ? 8 : 4) + 3.0 * (j->d.vel64 ? 8 : 4) + (j->d.id64 ? 8 : 4));
+  const double pb = j->host_q ? N3 * (12.0 + 3.0 * (j->d.vel64 ? 8 : 4))
+                               : N3 * (3.0 * (j->d.pos64 ? 8 : 4) + 3.0 * (j->d.vel64 ? 8 : 4) + (j->d.id64 ? 8 : 4));
   // velocity / displacement magnitude ratio of the assembly: vfac * vunit / lunit
   const double vfmax = std::max({std::fabs(as.vfac1), std::fabs(as.vfac2), std::fabs(as.vfac3)});
   const double ratio = (vfmax > 0 && as.pfac != 0) ? vfmax * std::fabs(as.vfac / as.pfac) : 1.0;
@@ -851,7 +859,8 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   fa.status = j->dstatus;
   fa.pos = j->pos;
   fa.vel = j->vel;
-  fa.ids = j->ids;
+  fa.ids = j->host_q ? nullptr : j->ids;  // host-side positions: the fetch writes the ids
+  fa.pos_disp = j->host_q ? 1 : 0;
   fa.pos64 = j->d.pos64;
   fa.vel64 = j->d.vel64;
   fa.id64 = j->d.id64;
@@ -1013,10 +1022,10 @@ static void ring_point(mfx_job *j, int s) {
   const size_t np = j->npart;
   char *a = j->ring + size_t(s) * j->ring_set_bytes;
   j->pos = a;
-  a += align_up(np * 3 * (j->d.pos64 ? 8 : 4));
+  a += align_up(np * 3 * (j->host_q ? 4 : (j->d.pos64 ? 8 : 4)));
   j->vel = a;
   a += align_up(np * 3 * (j->d.vel64 ? 8 : 4));
-  j->ids = a;
+  j->ids = j->host_q ? nullptr : a;
 }
 
 template <typename R> static int run_pipeline(mfx_job *j) {
@@ -1190,6 +1199,59 @@ static bool host_writable(const void *p) {
   }
   return at.type != cudaMemoryTypeDevice;
 }
+// q + Psi in FP64 for particles [p0, p1) from the float displacements in the
+// staging buffer (indexed by particle), the device's read-out sum
+// (fused_asm.cuh k_fa_z) done on the host: the same doubles
+static void write_positions(const mfx_job *j, size_t p0, size_t p1, double *dst) {  // dst holds particle p0
+  const size_t N = size_t(j->N), n3 = N * N * N;
+  const float *psi = j->psi_host;
+  size_t p = p0;
+  while (p < p1) {
+    const size_t s = p / n3, c = p - s * n3, x = c / (N * N), y = (c / N) % N;
+    const double *q = j->qhost.data() + s * 3 * N;
+    const double qx = q[x], qy = q[N + y];
+    const size_t zend = std::min(p1 - p, N - c % N);  // to the end of this row
+    for (size_t t = 0, z = c % N; t < zend; ++t, ++z, ++p) {
+      double *o = dst + 3 * (p - p0);
+      const float *f = psi + 3 * p;
+      o[0] = qx + double(f[0]);
+      o[1] = qy + double(f[1]);
+      o[2] = q[2 * N + z] + double(f[2]);
+    }
+  }
+}
+
+// The float displacements of particles [first, first + count) to the staging
+// buffer on stream x, in chunks each followed by an event, and host threads
+// that wait for their chunk and write q + Psi into dst (joined by join_id_fill).
+static int start_pos_fill(mfx_job *j, size_t first, size_t count, void *dst, cudaStream_t x) {
+  if (!j->psi_host) {
+    CU(cudaHostAlloc(reinterpret_cast<void **>(&j->psi_host), j->npart * 3 * sizeof(float), cudaHostAllocDefault));
+  }
+  const size_t hw = std::max(2u, std::thread::hardware_concurrency());
+  const size_t nt = std::max<size_t>(1, std::min<size_t>({size_t(16), hw, (count >> 18) + 1}));
+  const size_t per = (count + nt - 1) / nt;
+  const float *src = static_cast<const float *>(j->pos);
+  for (size_t t = 0; t < nt; ++t) {
+    const size_t a = first + t * per, b = std::min(first + count, a + per);
+    if (a >= b) break;
+    if (!j->psi_ev[t]) CU(cudaEventCreateWithFlags(&j->psi_ev[t], cudaEventDisableTiming));
+    CU(cudaMemcpyAsync(j->psi_host + 3 * a, src + 3 * a, (b - a) * 3 * sizeof(float), cudaMemcpyDeviceToHost, x));
+    CU(cudaEventRecord(j->psi_ev[t], x));
+    cudaEvent_t ev = j->psi_ev[t];
+    double *o = static_cast<double *>(dst) + 3 * (a - first);
+    auto work = [j, ev, a, b, o] {
+      if (cudaEventSynchronize(ev) == cudaSuccess) write_positions(j, a, b, o);
+    };
+    try {
+      j->id_fill.emplace_back(work);
+    } catch (const std::system_error &) {
+      work();
+    }
+  }
+  return MFX_OK;
+}
+
 static void join_id_fill(mfx_job *j) {
   for (auto &t : j->id_fill) t.join();
   j->id_fill.clear();
@@ -1235,6 +1297,9 @@ static void free_job(mfx_job *j) {
     cudaFreeAsync(j->sp_mem, j->stream);
     cudaStreamSynchronize(j->stream);
   }
+  if (j->psi_host) cudaFreeHost(j->psi_host);
+  for (auto &e : j->psi_ev)
+    if (e) cudaEventDestroy(e);
   if (j->eng) release_plan(j->eng, j->rho_c2r);
   else destroy_plan(j->rho_c2r);
   if (j->stream) cudaStreamDestroy(j->stream);
@@ -1272,6 +1337,7 @@ static int upload_shift_tables(mfx_job *j) {
             (double(m) + (kShifts[d->lattice][s][ax] + j->lat_off[ax])) / double(N) * d->lunit;
   std::vector<float2> ph32(ph.size());
   for (size_t q = 0; q < ph.size(); ++q) ph32[q] = make_float2(float(ph[q].x), float(ph[q].y));
+  j->qhost = qt;
   if (cudaMemcpyAsync(j->phase, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, j->stream) !=
           cudaSuccess ||
       cudaMemcpyAsync(j->phase32, ph32.data(), ph32.size() * sizeof(float2), cudaMemcpyHostToDevice, j->stream) !=
@@ -1916,17 +1982,7 @@ int mfx_job_fetch_particles(mfx_job *job, void *pos, void *vel, void *ids) {
   if (!job) return set_error(MFX_EINVAL, "null job");
   if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
   if (!job->has_run || job->noise_only) return set_error(MFX_ESTATE, "job has not produced particles");
-  CU(cudaSetDevice(job->eng->device));
-  const size_t np = job->npart;
-  const bool host_ids = ids && host_writable(ids);
-  const Xfer xs[3] = {{pos, job->pos, np * 3 * (job->d.pos64 ? 8 : 4)},
-                      {vel, job->vel, np * 3 * (job->d.vel64 ? 8 : 4)},
-                      {host_ids ? nullptr : ids, job->ids, np * (job->d.id64 ? 8 : 4)}};
-  join_id_fill(job);
-  if (host_ids) start_id_fill(job, 0, np, ids);
-  const int rc = download(job, xs, 3);
-  join_id_fill(job);
-  return rc;
+  return mfx_job_fetch_particles_range(job, 0, job->npart, pos, vel, ids);
   GUARD_END
 }
 
@@ -1940,14 +1996,51 @@ int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void
   CU(cudaSetDevice(job->eng->device));
   const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
   const bool host_ids = ids && host_writable(ids);
-  const Xfer xs[3] = {{pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
+  if (job->host_q && ((pos && !host_writable(pos)) || (ids && !host_ids)))
+    return set_error(MFX_ESTATE, "a job with host-side positions fetches positions and ids into host memory only");
+  const Xfer xs[3] = {{job->host_q ? nullptr : pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
                       {host_ids ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
   join_id_fill(job);
   if (host_ids) start_id_fill(job, first, count, ids);
+  if (job->host_q && pos) {
+    if (!job->xfer[0]) CU(cudaStreamCreateWithFlags(&job->xfer[0], cudaStreamNonBlocking));
+    if (!job->fetched) CU(cudaEventCreateWithFlags(&job->fetched, cudaEventDisableTiming));
+    CU(cudaEventRecord(job->fetched, job->stream));
+    CU(cudaStreamWaitEvent(job->xfer[0], job->fetched, 0));
+    const int prc = start_pos_fill(job, first, count, pos, job->xfer[0]);
+    if (prc != MFX_OK) {
+      join_id_fill(job);
+      return prc;
+    }
+  }
   const int rc = download(job, xs, 3);
   join_id_fill(job);
   return rc;
+  GUARD_END
+}
+
+int mfx_job_set_host_positions(mfx_job *job, int on) {
+  GUARD_BEGIN
+  if (!job) return set_error(MFX_EINVAL, "null job");
+  if (!job->d.want_particles) return set_error(MFX_ESTATE, "job was created without particles");
+  if (on && !(job->fused && !job->fp64 && job->d.pos64))
+    return set_error(MFX_ESTATE, "host-side positions need the FP32 form's fused route and 64-bit positions");
+  if (job->ring) return set_error(MFX_ESTATE, "set host-side positions before the output ring");
+  if (job->gexec) return set_error(MFX_ESTATE, "job already captured into a graph");
+  if (!on == !job->host_q) return MFX_OK;
+  CU(cudaSetDevice(job->eng->device));
+  join_id_fill(job);
+  for (auto &x : job->xfer)
+    if (x) CU(cudaStreamSynchronize(x));
+  CU(cudaStreamSynchronize(job->stream));
+  job->host_q = on != 0;
+  // the particles of the last run, in the new form
+  if (job->has_run && !job->noise_only) {
+    TRY(assemble_stage<float>(job, 7));
+    CU(cudaStreamSynchronize(job->stream));
+  }
+  return MFX_OK;
   GUARD_END
 }
 
@@ -1984,8 +2077,9 @@ int mfx_job_set_output_ring(mfx_job *job, int on) {
   }
   if (!on) return MFX_OK;
   const size_t np = job->npart;
-  const size_t set = align_up(np * 3 * (job->d.pos64 ? 8 : 4)) + align_up(np * 3 * (job->d.vel64 ? 8 : 4)) +
-                     align_up(np * (job->d.id64 ? 8 : 4));
+  // host-side positions: float displacements and no ids on the device
+  const size_t set = align_up(np * 3 * (job->host_q ? 4 : (job->d.pos64 ? 8 : 4))) +
+                     align_up(np * 3 * (job->d.vel64 ? 8 : 4)) + (job->host_q ? 0 : align_up(np * (job->d.id64 ? 8 : 4)));
   const size_t total = size_t(on) * set;
   {
     std::lock_guard<std::mutex> lk(eng->mu);
@@ -2030,11 +2124,14 @@ int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count
   CU(cudaStreamWaitEvent(job->xfer[0], job->fetched, 0));
   const size_t ps = job->d.pos64 ? 8 : 4, vs = job->d.vel64 ? 8 : 4, is = job->d.id64 ? 8 : 4;
   const bool host_ids = ids && host_writable(ids);
-  const Xfer xs[3] = {{pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
+  if (job->host_q && ((pos && !host_writable(pos)) || (ids && !host_ids)))
+    return set_error(MFX_ESTATE, "a job with host-side positions fetches positions and ids into host memory only");
+  const Xfer xs[3] = {{job->host_q ? nullptr : pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
                       {host_ids ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
-  join_id_fill(job);  // an earlier fetch's ids (long done when fetches are a step apart)
+  join_id_fill(job);  // an earlier fetch's host threads (long done when fetches are a step apart)
   if (host_ids) start_id_fill(job, first, count, ids);
+  if (job->host_q && pos) TRY(start_pos_fill(job, first, count, pos, job->xfer[0]));
   // one copy stream: the host link is full with one (193 GB/s on GB300), and
   // several streams' copies beside a running job made the step times vary
   cudaStream_t x = job->xfer[0];

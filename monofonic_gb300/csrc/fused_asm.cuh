@@ -36,6 +36,10 @@ struct FAArgs {
   // particle output (particle_generator.hh:212-253, 499-543, 597-639)
   void *pos, *vel, *ids;
   int pos64, vel64, id64, nshift_total;
+  // 1: the positions array receives the float displacements Psi (3 floats a
+  // particle) instead of q + Psi; the fetch forms q + Psi in FP64 on the host
+  // (mfx_job_set_host_positions), the same doubles the device would store
+  int pos_disp;
   const double *qtab;     // [3][N] unperturbed coordinates of this sub-lattice
   uint64_t id_offset;
   // The velocity components are carried times vscale and multiplied by
@@ -394,21 +398,31 @@ __global__ void __launch_bounds__(FA<N>::t3, FA<N>::minb3) k_fa_z(FAArgs a) {
       const float2 *hw = h2 + w * 3 * N;
       // q + Psi in FP64; the velocities stay in float unless stored in FP64
       // (FP64 arithmetic and conversions are slow on this part)
-      double pv[6];
-      float vv[6];
-      const double qx = a.qtab[x], qy = a.qtab[N + y];
+      float pf[6], vv[6];
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         const float2 a0 = hw[z0 + c], a1 = hw[N + z0 + c], a2 = hw[2 * N + z0 + c];
-        pv[3 * c + 0] = qx + f2d_exact(a0.x);
-        pv[3 * c + 1] = qy + f2d_exact(a0.y);
-        pv[3 * c + 2] = a.qtab[2 * N + z0 + c] + f2d_exact(a1.x);
+        pf[3 * c + 0] = a0.x;
+        pf[3 * c + 1] = a0.y;
+        pf[3 * c + 2] = a1.x;
         vv[3 * c + 0] = a1.y;
         vv[3 * c + 1] = a2.x;
         vv[3 * c + 2] = a2.y;
       }
-      if (a.pos64) store6(reinterpret_cast<double *>(a.pos) + 3 * (pbase + cell), pv);
-      else store6(reinterpret_cast<float *>(a.pos) + 3 * (pbase + cell), pv);
+      if (a.pos_disp) {
+        store6(reinterpret_cast<float *>(a.pos) + 3 * (pbase + cell), pf);
+      } else {
+        double pv[6];
+        const double qx = a.qtab[x], qy = a.qtab[N + y];
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          pv[3 * c + 0] = qx + f2d_exact(pf[3 * c + 0]);
+          pv[3 * c + 1] = qy + f2d_exact(pf[3 * c + 1]);
+          pv[3 * c + 2] = a.qtab[2 * N + z0 + c] + f2d_exact(pf[3 * c + 2]);
+        }
+        if (a.pos64) store6(reinterpret_cast<double *>(a.pos) + 3 * (pbase + cell), pv);
+        else store6(reinterpret_cast<float *>(a.pos) + 3 * (pbase + cell), pv);
+      }
       if (a.vel64) {
         double vd[6];
 #pragma unroll

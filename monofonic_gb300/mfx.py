@@ -28,7 +28,7 @@ EXPORTS = [
     "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
     "mfx_job_destroy", "mfx_job_autotune", "mfx_job_capture", "mfx_batch_create", "mfx_batch_run", "mfx_batch_wait",
     "mfx_batch_job", "mfx_batch_destroy", "mfx_server_create", "mfx_server_submit", "mfx_server_wait",
-    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_server_set_policy", "mfx_job_set_species", "mfx_job_fetch_masses", "mfx_job_ppt_fields", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
+    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_server_set_policy", "mfx_job_set_species", "mfx_job_fetch_masses", "mfx_job_ppt_fields", "mfx_job_set_host_positions", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
     "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
     "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
     "mfx_cosmology_amp_table", "mfx_run_config", "mfx_job_set_output_ring", "mfx_job_fetch_particles_range_async",
@@ -387,6 +387,13 @@ class Job:
         on: True = two sets, False = none, or the number of sets (0, 1, 2)."""
         sets = (2 if on else 0) if isinstance(on, bool) else int(on)
         check(load().mfx_job_set_output_ring(self._h, sets))
+
+    def set_host_positions(self, on: bool = True):
+        """Positions leave the device as float displacements; fetches into host
+        memory form q + Psi in FP64 on the host (mfx_job_set_host_positions)."""
+        L = load()
+        L.mfx_job_set_host_positions.argtypes = [C.c_void_p, C.c_int]
+        check(L.mfx_job_set_host_positions(self._h, int(on)))
 
     def set_species(self, secondary=False, id_offset=0, c_species=0.0, mass_factor=0.0, amp_dbc=None,
                     amp_tbc=None, want_masses=True, reset=False):

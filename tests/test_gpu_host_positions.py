@@ -1,0 +1,100 @@
+"""Host-side positions (mfx_job_set_host_positions): the FP32 form keeps float
+displacements on the device and the fetch forms q + Psi in FP64 on the host.
+The particles must equal those of device-side positions bit for bit -- through
+the synchronous fetch, ranges across sub-lattice boundaries, and the
+asynchronous fetch with output rings of one and two sets over several runs."""
+import numpy as np
+import pytest
+
+from test_gpu_batch import run_alone, spec
+
+pytestmark = pytest.mark.gpu
+
+
+def _job(mfx, engine, sp, **kw):
+    return mfx.Job(engine, sp["ngrid"], sp["boxlen"], sp["order"], sp["seed_table"], sp["amp_table"], sp["coef"],
+                   lattice=sp["lattice"], precision=sp["precision"], plt_table=sp.get("plt_table"),
+                   lunit=sp["lunit"], vunit=sp["vunit"], pos64=True, vel64=False, id64=True, **kw)
+
+
+@pytest.mark.parametrize("lattice,plt", [(1, True), (2, False)])
+def test_host_positions_equal_device_positions(mfxlib, engine, lattice, plt):
+    sp = spec(mfxlib, 48, 150.0, 24.0, 3, 21, lattice=lattice, precision=mfxlib.FP32C)
+    if plt:
+        sp["plt_table"] = engine.plt_table(lattice)
+    j = _job(mfxlib, engine, sp)
+    j.run()
+    ref = j.particles()
+    j.set_host_positions(True)  # re-assembles the last run in the new form
+    got = j.particles()
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    n3 = 48 ** 3
+    first, count = n3 - 777, min(n3 + 1555, j.num_particles - (n3 - 777))
+    rng = j.particles_range(first, count)
+    for a, b in zip(rng, ref):
+        assert np.array_equal(a, b[first:first + count])
+    j.run()
+    for a, b in zip(j.particles(), ref):
+        assert np.array_equal(a, b)
+    j.set_host_positions(False)
+    for a, b in zip(j.particles(), ref):
+        assert np.array_equal(a, b)
+    j.close()
+
+
+@pytest.mark.parametrize("ring", [0, 1, 2])
+def test_host_positions_pipelined(mfxlib, engine, ring):
+    """Three runs, three seeds, each fetched asynchronously right after its run
+    is enqueued: every seed's particles equal a run made alone."""
+    import torch
+    specs = [spec(mfxlib, 48, 150.0, 24.0, 3, s, lattice=1, precision=mfxlib.FP32C) for s in (41, 42, 43)]
+    for sp in specs:
+        sp["plt_table"] = None
+    refs = []
+    for sp in specs:
+        j = _job(mfxlib, engine, sp)
+        j.run()
+        refs.append(j.particles())
+        j.close()
+    sp0 = specs[0]
+    j = _job(mfxlib, engine, sp0)
+    j.set_host_positions(True)
+    if ring:
+        j.set_output_ring(ring)
+    npart = j.num_particles
+    bufs = [(torch.empty((npart, 3), dtype=torch.float64, pin_memory=True),
+             torch.empty((npart, 3), dtype=torch.float32, pin_memory=True),
+             torch.empty(npart, dtype=torch.int64, pin_memory=True)) for _ in specs]
+    for sp, (p, v, i) in zip(specs, bufs):
+        j.upload(sp["seed_table"], sp["amp_table"])
+        j.run(wait=False)
+        j.fetch_particles_range_async(0, npart, p.data_ptr(), v.data_ptr(), i.data_ptr())
+    j.wait()
+    j.wait_fetch()
+    for ref, (p, v, i) in zip(refs, bufs):
+        assert np.array_equal(p.numpy(), ref[0])
+        assert np.array_equal(v.numpy(), ref[1])
+        assert np.array_equal(i.numpy().view(np.uint64), ref[2])
+    j.close()
+
+
+def test_host_positions_errors(mfxlib, engine):
+    import torch
+    sp = spec(mfxlib, 32, 100.0, 24.0, 2, 5, lattice=0)  # plain FP64 form
+    j = _job(mfxlib, engine, sp)
+    with pytest.raises(mfxlib.MfxError):
+        j.set_host_positions(True)
+    j.close()
+    sp = spec(mfxlib, 32, 100.0, 24.0, 2, 5, lattice=0, precision=mfxlib.FP32C)
+    j = _job(mfxlib, engine, sp)
+    j.set_output_ring(1)
+    with pytest.raises(mfxlib.MfxError):
+        j.set_host_positions(True)  # after the ring
+    j.set_output_ring(0)
+    j.set_host_positions(True)
+    j.run()
+    dev = torch.zeros((j.num_particles, 3), dtype=torch.float64, device="cuda")
+    with pytest.raises(RuntimeError):
+        j.fetch_particles_range_into(0, j.num_particles, dev.data_ptr(), None, None)
+    j.close()
