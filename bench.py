@@ -274,7 +274,7 @@ def run_ours(args):
     # in FP64 on the host (mfx_job_set_host_positions: the same doubles), so a
     # particle crosses the host link in 12 + 12 bytes instead of 24 + 12
     host_pos = False
-    if prec == mfx.FP32C:
+    if prec == mfx.FP32C and args.host_positions:
         try:
             job.set_host_positions(True)
             host_pos = True
@@ -327,9 +327,10 @@ def run_ours(args):
     # host and its HBM traffic (17 GB at 256^3) is far above the 129 MB L2.
     host_set = npart * (3 * 8 + 3 * (8 if vel64 else 4) + 8)  # f64 positions, velocities, ids
     ring = 0
-    # with host-side positions one host set serves both device sets: a fetch
-    # joins the previous fetch's host threads before it enqueues its copies
-    for sets, host_sets in ((2, 1 if host_pos else 2), (1, 1)):
+    # one page-locked host set serves one or two device sets: a step's copies
+    # go on the copy stream after the previous step's, and a fetch joins the
+    # previous fetch's host threads before it starts its own
+    for sets, host_sets in ((2, 1), (1, 1)):
         if host_sets * host_set > (100 << 30):
             continue
         try:
@@ -893,6 +894,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="profiling runs: skip the end-to-end pass and the report")
+    ap.add_argument("--host-positions", action="store_true",
+                    help="end to end: float displacements cross the link, q + Psi formed on the host")
     ap.add_argument("--tiles", default="", help="fused-transform tiles 'PXY,PZ' instead of the autotuner's")
     args = ap.parse_args()
     if args.impl == "reference":

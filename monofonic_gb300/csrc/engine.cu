@@ -187,6 +187,10 @@ struct mfx_job {
   // form q + Psi in FP64 from the lattice coordinates qhost ([shift][axis][N])
   bool host_q = false;
   float *psi_host = nullptr;
+  // the fused read-out writes no device ids (every host destination gets them
+  // from host threads); a device destination gets them from k_fill_ids, and
+  // mfx_job_particles_device from this array, filled on request
+  void *ids_dev = nullptr;
   std::vector<double> qhost;
   cudaEvent_t psi_ev[16] = {};
   void *work = nullptr;
@@ -859,7 +863,7 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
   fa.status = j->dstatus;
   fa.pos = j->pos;
   fa.vel = j->vel;
-  fa.ids = j->host_q ? nullptr : j->ids;  // host-side positions: the fetch writes the ids
+  fa.ids = nullptr;  // ids on request (k_fill_ids) or from the fetch's host threads
   fa.pos_disp = j->host_q ? 1 : 0;
   fa.pos64 = j->d.pos64;
   fa.vel64 = j->d.vel64;
@@ -1025,7 +1029,7 @@ static void ring_point(mfx_job *j, int s) {
   a += align_up(np * 3 * (j->host_q ? 4 : (j->d.pos64 ? 8 : 4)));
   j->vel = a;
   a += align_up(np * 3 * (j->d.vel64 ? 8 : 4));
-  j->ids = j->host_q ? nullptr : a;
+  j->ids = (j->host_q || j->fused) ? nullptr : a;  // the fused read-out writes no device ids
 }
 
 template <typename R> static int run_pipeline(mfx_job *j) {
@@ -1252,6 +1256,18 @@ static int start_pos_fill(mfx_job *j, size_t first, size_t count, void *dst, cud
   return MFX_OK;
 }
 
+// ids [first, first + count) of the last run into device memory dst on stream st
+// (ordered after the job's work; the fused read-out writes no ids itself)
+static int fill_ids_device(mfx_job *j, size_t first, size_t count, void *dst, cudaStream_t st) {
+  const IdRule r = id_rule(j);
+  const size_t b = std::min<size_t>((count + 255) / 256, size_t(num_sm()) * 16);
+  const unsigned g = unsigned(std::max<size_t>(b, 1));
+  if (r.id64) k_fill_ids<uint64_t><<<g, 256, 0, st>>>(static_cast<uint64_t *>(dst), first, count, r.base, r.ns, r.n3);
+  else k_fill_ids<uint32_t><<<g, 256, 0, st>>>(static_cast<uint32_t *>(dst), first, count, r.base, r.ns, r.n3);
+  CU(cudaGetLastError());
+  return MFX_OK;
+}
+
 static void join_id_fill(mfx_job *j) {
   for (auto &t : j->id_fill) t.join();
   j->id_fill.clear();
@@ -1298,6 +1314,10 @@ static void free_job(mfx_job *j) {
     cudaStreamSynchronize(j->stream);
   }
   if (j->psi_host) cudaFreeHost(j->psi_host);
+  if (j->ids_dev) {
+    cudaFreeAsync(j->ids_dev, j->stream);
+    cudaStreamSynchronize(j->stream);
+  }
   for (auto &e : j->psi_ev)
     if (e) cudaEventDestroy(e);
   if (j->eng) release_plan(j->eng, j->rho_c2r);
@@ -1500,7 +1520,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     a += align_up(np * 3 * (d->pos64 ? 8 : 4));
     j->vel = a;
     a += align_up(np * 3 * (d->vel64 ? 8 : 4));
-    j->ids = a;
+    j->ids = j->fused ? nullptr : a;  // the fused read-out writes no device ids
     a += align_up(np * (d->id64 ? 8 : 4));
     for (int q = 0; q < 6 * j->group; ++q) {
       j->asmbuf[q] = a;
@@ -1998,11 +2018,13 @@ int mfx_job_fetch_particles_range(mfx_job *job, size_t first, size_t count, void
   const bool host_ids = ids && host_writable(ids);
   if (job->host_q && ((pos && !host_writable(pos)) || (ids && !host_ids)))
     return set_error(MFX_ESTATE, "a job with host-side positions fetches positions and ids into host memory only");
+  const bool kernel_ids = ids && !host_ids && !job->ids;  // no device array: the closed form on the device
   const Xfer xs[3] = {{job->host_q ? nullptr : pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
-                      {host_ids ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
+                      {(host_ids || kernel_ids) ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
   join_id_fill(job);
   if (host_ids) start_id_fill(job, first, count, ids);
+  if (kernel_ids) TRY(fill_ids_device(job, first, count, ids, job->stream));
   if (job->host_q && pos) {
     if (!job->xfer[0]) CU(cudaStreamCreateWithFlags(&job->xfer[0], cudaStreamNonBlocking));
     if (!job->fetched) CU(cudaEventCreateWithFlags(&job->fetched, cudaEventDisableTiming));
@@ -2073,13 +2095,14 @@ int mfx_job_set_output_ring(mfx_job *job, int on) {
     a += align_up(job->npart * 3 * (job->d.pos64 ? 8 : 4));
     job->vel = a;
     a += align_up(job->npart * 3 * (job->d.vel64 ? 8 : 4));
-    job->ids = a;
+    job->ids = job->fused ? nullptr : a;
   }
   if (!on) return MFX_OK;
   const size_t np = job->npart;
-  // host-side positions: float displacements and no ids on the device
+  // host-side positions: float displacements; the fused read-out: no device ids
+  const bool no_ids = job->host_q || job->fused;
   const size_t set = align_up(np * 3 * (job->host_q ? 4 : (job->d.pos64 ? 8 : 4))) +
-                     align_up(np * 3 * (job->d.vel64 ? 8 : 4)) + (job->host_q ? 0 : align_up(np * (job->d.id64 ? 8 : 4)));
+                     align_up(np * 3 * (job->d.vel64 ? 8 : 4)) + (no_ids ? 0 : align_up(np * (job->d.id64 ? 8 : 4)));
   const size_t total = size_t(on) * set;
   {
     std::lock_guard<std::mutex> lk(eng->mu);
@@ -2126,12 +2149,14 @@ int mfx_job_fetch_particles_range_async(mfx_job *job, size_t first, size_t count
   const bool host_ids = ids && host_writable(ids);
   if (job->host_q && ((pos && !host_writable(pos)) || (ids && !host_ids)))
     return set_error(MFX_ESTATE, "a job with host-side positions fetches positions and ids into host memory only");
+  const bool kernel_ids = ids && !host_ids && !job->ids;  // no device array: the closed form on the device
   const Xfer xs[3] = {{job->host_q ? nullptr : pos, static_cast<char *>(job->pos) + 3 * ps * first, 3 * ps * count},
                       {vel, static_cast<char *>(job->vel) + 3 * vs * first, 3 * vs * count},
-                      {host_ids ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
+                      {(host_ids || kernel_ids) ? nullptr : ids, static_cast<char *>(job->ids) + is * first, is * count}};
   join_id_fill(job);  // an earlier fetch's host threads (long done when fetches are a step apart)
   if (host_ids) start_id_fill(job, first, count, ids);
   if (job->host_q && pos) TRY(start_pos_fill(job, first, count, pos, job->xfer[0]));
+  if (kernel_ids) TRY(fill_ids_device(job, first, count, ids, job->xfer[0]));
   // one copy stream: the host link is full with one (193 GB/s on GB300), and
   // several streams' copies beside a running job made the step times vary
   cudaStream_t x = job->xfer[0];
@@ -2154,12 +2179,27 @@ int mfx_job_wait_fetch(mfx_job *job) {
 }
 
 int mfx_job_particles_device(mfx_job *job, const void **pos, const void **vel, const void **ids, size_t *np) {
+  GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
   if (pos) *pos = job->pos;
   if (vel) *vel = job->vel;
-  if (ids) *ids = job->ids;
+  if (ids) {
+    if (job->ids) {
+      *ids = job->ids;
+    } else {
+      // the fused read-out writes no ids: fill them into an array of their own
+      CU(cudaSetDevice(job->eng->device));
+      if (!job->ids_dev) {
+        CU(cudaMallocAsync(&job->ids_dev, job->npart * (job->d.id64 ? 8 : 4), job->stream));
+      }
+      TRY(fill_ids_device(job, 0, job->npart, job->ids_dev, job->stream));
+      CU(cudaStreamSynchronize(job->stream));
+      *ids = job->ids_dev;
+    }
+  }
   if (np) *np = job->npart;
   return MFX_OK;
+  GUARD_END
 }
 
 int mfx_job_fetch_field(mfx_job *job, int field_id, double *out) {

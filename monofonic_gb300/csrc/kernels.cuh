@@ -730,6 +730,20 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// (5a) particle ids [first, first + count) into dst (particle_generator.hh:
+//      229-248): particle p = shift * N^3 + cell carries base + ns * cell + shift
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_fill_ids(T *dst, uint64_t first, uint64_t count, uint64_t base, uint64_t ns,
+                                                  uint64_t n3) {
+  for (uint64_t q = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < count;
+       q += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t p = first + q, s = p / n3;
+    dst[q] = T(base + ns * (p - s * n3) + s);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // (5b) particle masses of a baryon + CDM species (ic_generator.cc:749-780,
 //      particle_generator.hh:369-427): delta_bc(k) = w A_delta_bc(k) =
 //      ratio[n] * phi1 (ratio = -A_delta_bc / A per |k|^2 index n, with the

@@ -1,5 +1,6 @@
 """Host-side positions (mfx_job_set_host_positions): the FP32 form keeps float
-displacements on the device and the fetch forms q + Psi in FP64 on the host.
+displacements on the device and the fetch forms q + Psi in FP64 on the host
+(fused route: grids whose padded length is instantiated, here 64^3 -> 96).
 The particles must equal those of device-side positions bit for bit -- through
 the synchronous fetch, ranges across sub-lattice boundaries, and the
 asynchronous fetch with output rings of one and two sets over several runs."""
@@ -19,7 +20,7 @@ def _job(mfx, engine, sp, **kw):
 
 @pytest.mark.parametrize("lattice,plt", [(1, True), (2, False)])
 def test_host_positions_equal_device_positions(mfxlib, engine, lattice, plt):
-    sp = spec(mfxlib, 48, 150.0, 24.0, 3, 21, lattice=lattice, precision=mfxlib.FP32C)
+    sp = spec(mfxlib, 64, 200.0, 24.0, 3, 21, lattice=lattice, precision=mfxlib.FP32C)
     if plt:
         sp["plt_table"] = engine.plt_table(lattice)
     j = _job(mfxlib, engine, sp)
@@ -29,7 +30,7 @@ def test_host_positions_equal_device_positions(mfxlib, engine, lattice, plt):
     got = j.particles()
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
-    n3 = 48 ** 3
+    n3 = 64 ** 3
     first, count = n3 - 777, min(n3 + 1555, j.num_particles - (n3 - 777))
     rng = j.particles_range(first, count)
     for a, b in zip(rng, ref):
@@ -48,7 +49,7 @@ def test_host_positions_pipelined(mfxlib, engine, ring):
     """Three runs, three seeds, each fetched asynchronously right after its run
     is enqueued: every seed's particles equal a run made alone."""
     import torch
-    specs = [spec(mfxlib, 48, 150.0, 24.0, 3, s, lattice=1, precision=mfxlib.FP32C) for s in (41, 42, 43)]
+    specs = [spec(mfxlib, 64, 200.0, 24.0, 3, s, lattice=1, precision=mfxlib.FP32C) for s in (41, 42, 43)]
     for sp in specs:
         sp["plt_table"] = None
     refs = []
@@ -97,4 +98,26 @@ def test_host_positions_errors(mfxlib, engine):
     dev = torch.zeros((j.num_particles, 3), dtype=torch.float64, device="cuda")
     with pytest.raises(RuntimeError):
         j.fetch_particles_range_into(0, j.num_particles, dev.data_ptr(), None, None)
+    j.close()
+
+
+def test_fused_device_ids_on_request(mfxlib, engine):
+    """The fused read-out writes no device ids: a device destination gets them
+    from the id kernel (the lattice rule), and mfx_job_particles_device fills an
+    array of its own on request."""
+    import ctypes
+    import torch
+    sp = spec(mfxlib, 32, 100.0, 24.0, 2, 7, lattice=2, precision=mfxlib.FP32C)
+    j = _job(mfxlib, engine, sp, id_offset=3)
+    j.run()
+    want = j.particles()[2]
+    dev = torch.zeros(j.num_particles, dtype=torch.int64, device="cuda")
+    j.fetch_particles_range_into(0, j.num_particles, None, None, dev.data_ptr())
+    assert np.array_equal(dev.cpu().numpy().view(np.uint64), want)
+    L = mfxlib.load()
+    pp, vp, ip, n = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_size_t()
+    for _ in range(2):
+        mfxlib.check(L.mfx_job_particles_device(j.handle, ctypes.byref(pp), ctypes.byref(vp), ctypes.byref(ip),
+                                                ctypes.byref(n)))
+        assert ip.value and pp.value and n.value == j.num_particles
     j.close()
