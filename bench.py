@@ -622,6 +622,7 @@ def run_serving(args):
         tuned[s["ngrid"]] = list(j.autotune())
         j.close()
     srv = mfx.Server(eng, max_inflight=args.inflight)
+    srv.set_policy(bypass=True, bypass_age_ms=100.0, size_priority=not args.no_priority)
     # warm the plan pool and the memory pool with one pass over the size classes
     warm = {}
     for s in specs:
@@ -683,8 +684,12 @@ def run_serving(args):
     clk = clocks.stop()
     srv.close()
     target = args.p99_target_ms
-    meets = [pt for pt in sweep if pt["p99_ms"] <= target]
-    best = max(meets, key=lambda pt: pt["throughput"]) if meets else None
+    # the highest offered load up to which every point of the sweep met the target
+    best = None
+    for pt in sorted(sweep, key=lambda pt: pt["load"]):
+        if pt["p99_ms"] > target:
+            break
+        best = pt
     # the plain FP64 form, one job at a time, on a sample of the requests
     serial_s, serial_parts = 0.0, 0
     if not args.no_fp64:
@@ -707,10 +712,12 @@ def run_serving(args):
         "config": {"workload": "serve: %d requests per load point, N in {64..384}, order 1-3, SC/BCC/FCC (+PLT), "
                                "FP32-compensated" % len(specs), "max_inflight": args.inflight,
                    "admission": "oldest job that fits; a head older than 100 ms is not passed",
+                   "stream_priority": "by footprint" if not args.no_priority else "default for every job",
                    "particles_per_point": sum(parts), "tiles_per_size": {str(k): v for k, v in tuned.items()}},
         "p99_target_ms": target,
         "throughput_at_target_vs_batched": best["throughput_vs_batched"] if best else None,
         "load_at_target": best["load"] if best else None,
+        "target_rule": "the highest offered load up to which every load point's p99 met the target",
         "batched": {"value": sat_tput, "unit": "particles/s", "span_s": sat_span,
                     "p50_ms": float(np.percentile(sat_lat, 50)), "p99_ms": float(np.percentile(sat_lat, 99)),
                     "mode": "every request queued at once"},
@@ -889,7 +896,8 @@ def main():
                     default=[0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1], help="serve: offered loads / batched job rate")
     ap.add_argument("--p99-target-ms", type=float, default=100.0, help="serve: stated p99 job latency target")
     ap.add_argument("--fp64-sample", type=int, default=48, help="serve: requests run serially in FP64")
-    ap.add_argument("--inflight", type=int, default=8, help="serve: max jobs in flight")
+    ap.add_argument("--no-priority", action="store_true", help="serve: every job at the default stream priority")
+    ap.add_argument("--inflight", type=int, default=4, help="serve: max jobs in flight")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")

@@ -41,6 +41,10 @@ extern "C" {
 #define MFX_FP32C 1 /* FP32 FFTs/products, compensated 3LPT source sums,
                        FP64 tables and FP64 q+Psi position sum              */
 
+/* white-noise generators (the [random] generator key) */
+#define MFX_NOISE_NGENIC 0
+#define MFX_NOISE_MUSIC1 1
+
 /* fields fetchable with mfx_job_fetch_field (k-space, N x N x (N/2+1) complex) */
 #define MFX_FIELD_NOISE 0 /* white noise as RNG_plugin::Fill_Grid leaves it   */
 #define MFX_FIELD_PHI1 1  /* phi(1), unscaled, ic_generator.cc:509-516         */
@@ -92,6 +96,13 @@ typedef struct {
   int id64;   /* IDs as uint64 (else uint32), output_plugin::has_64bit_ids    */
   uint64_t id_offset; /* lattice_generator IDoffset (particle_generator.hh:232) */
   int want_particles; /* 0: stop after the LPT potentials (fields only)     */
+  /* the [random] generator plugin (random_plugin.cc:62-81): MFX_NOISE_NGENIC
+     reads seed_table; MFX_NOISE_MUSIC1 (random_music.cc, one level: the seed
+     given at the grid's own level, ngrid a power of two) draws the noise on
+     the device from music_seed and music_cubesize and ignores seed_table */
+  int noise_generator;
+  int64_t music_seed;       /* [random] seed[log2 ngrid], > 0              */
+  uint32_t music_cubesize;  /* [random] cubesize, 0 = 32 (random_plugin.hh:24) */
 } mfx_job_desc;
 
 /* ---- errors -------------------------------------------------------------- */
@@ -313,8 +324,11 @@ int mfx_server_ticket_times(mfx_server *s, uint64_t ticket, double *queued_ms, d
 int mfx_server_job(mfx_server *s, uint64_t ticket, mfx_job **job);
 int mfx_server_release(mfx_server *s, uint64_t ticket);
 int mfx_server_destroy(mfx_server *s);
-/* bypass = 0: strict first-in first-out admission; otherwise a later job may
-   pass a head that has waited at most bypass_age_ms. */
+/* bypass bit 0 clear: strict first-in first-out admission; set: a later job
+   may pass a head that has waited at most bypass_age_ms.  Jobs run on CUDA
+   streams whose priority grows with their footprint (one level per factor of
+   four above 64 MB): the largest requests set the latency tail.  bypass bit 1
+   set: every job at the default priority. */
 int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms);
 
 /* Allocation-free white-noise fill (no counterpart in the reference): writes

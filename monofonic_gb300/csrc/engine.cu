@@ -36,6 +36,7 @@
 #include "common.h"
 #include "kernels.cuh"
 #include "fused_launch.cuh"
+#include "music.cuh"
 
 namespace mfx {
 
@@ -196,6 +197,7 @@ struct mfx_job {
   void *work = nullptr;
   size_t work_bytes = 0;
   Plan m_r2c, m_c2r, n_c2r;
+  Plan n_r2c;  // N-grid forward transform of the MUSIC1 cube noise
   // CUDA graph of the whole pipeline (mfx_job_capture)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -283,7 +285,21 @@ static int check_desc(const mfx_job_desc *d) {
   if (d->lpt_order < 1 || d->lpt_order > 3) return set_error(MFX_EINVAL, "lpt_order must be 1, 2 or 3");
   if (d->lattice < 0 || d->lattice > 2) return set_error(MFX_EINVAL, "lattice must be SC, BCC or FCC");
   if (d->precision != MFX_FP64 && d->precision != MFX_FP32C) return set_error(MFX_EINVAL, "bad precision");
-  if (!d->seed_table) return set_error(MFX_EINVAL, "seed_table is required");
+  if (d->noise_generator == MFX_NOISE_NGENIC) {
+    if (!d->seed_table) return set_error(MFX_EINVAL, "seed_table is required");
+  } else if (d->noise_generator == MFX_NOISE_MUSIC1) {
+    // one level at the grid's own resolution: 2^levelmin cells per axis
+    // (random_music.cc:75), cubes that tile it (random_music_wnoise_generator.cc:588-626)
+    if (d->ngrid & (d->ngrid - 1)) return set_error(MFX_EINVAL, "MUSIC1 noise needs ngrid a power of two (got %u)", d->ngrid);
+    if (d->music_seed <= 0) return set_error(MFX_EINVAL, "MUSIC1 noise needs a positive seed");
+    const unsigned cs = d->music_cubesize ? d->music_cubesize : 32u;
+    if (cs < 2 || (d->ngrid >= cs && d->ngrid % cs != 0))
+      return set_error(MFX_EINVAL, "MUSIC1 cubesize %u does not tile ngrid %u", cs, d->ngrid);
+    if (std::min(cs, d->ngrid) > 256u)
+      return set_error(MFX_EINVAL, "MUSIC1 cubes above 256^3 cells (one sequential stream each) are not supported");
+  } else {
+    return set_error(MFX_EINVAL, "unknown noise_generator %d", d->noise_generator);
+  }
   size_t need = 3 * size_t(d->ngrid / 2) * (d->ngrid / 2) + 1;
   if (!d->amp_table || d->amp_table_len < need)
     return set_error(MFX_EINVAL, "amp_table needs at least %zu entries", need);
@@ -297,6 +313,9 @@ static int check_desc(const mfx_job_desc *d) {
 // sends the FP32 form through cuFFT as well (for comparisons).
 static bool fused_supported(const mfx_job_desc *d) {
   if (d->precision != MFX_FP32C || d->lpt_order < 2) return false;
+  // the pruned transforms take phi(1) with empty Nyquist planes (NGenIC's
+  // noise); MUSIC1 noise fills them
+  if (d->noise_generator != MFX_NOISE_NGENIC) return false;
   const char *env = getenv("MFX_FUSED");
   if (env && env[0] == '0') return false;
   const int N = d->ngrid, M = 3 * N / 2;
@@ -454,8 +473,8 @@ static int exec_fft(mfx_job *j, Plan &p, void *buf, bool r2c) {
     else CF(cufftExecC2R(p.h, (cufftComplex *)buf, (cufftReal *)buf));
   }
   j->fft_execs++;
-  const bool m = (&p != &j->n_c2r);
-  kend_prof(j, m ? (r2c ? "cufft_r2c_M" : "cufft_c2r_M") : "cufft_c2r_N",
+  const bool m = (&p != &j->n_c2r) && (&p != &j->n_r2c);
+  kend_prof(j, m ? (r2c ? "cufft_r2c_M" : "cufft_c2r_M") : (r2c ? "cufft_r2c_N" : "cufft_c2r_N"),
             2.0 * double(m ? j->m_field_bytes : j->n_field_bytes) * p.batch);
   return MFX_OK;
 }
@@ -524,6 +543,43 @@ template <typename R> static int launch_noise(mfx_job *j, int mode, void *out) {
   k_noise_phi1<R><<<(cols + 127) / 128, 128, 0, j->stream>>>(a, (typename Cplx<R>::T *)out);
   KEND(j, "noise_phi1", j->n_field_bytes + 4.0 * cols + 8.0 * j->d.amp_table_len);
   return MFX_OK;
+}
+
+// MUSIC1 noise: cube normals into the padded real field, the N-grid forward
+// transform in place, then the k-space pass (music.cuh)
+template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
+  const int N = j->N;
+  music::CubeArgs c;
+  c.seed = reinterpret_cast<const long long *>(j->seeds);
+  c.N = N;
+  const int cs = j->d.music_cubesize ? int(j->d.music_cubesize) : 32;
+  c.cs = N < cs ? N : cs;
+  c.nc = N / c.cs;
+  c.row = 2LL * (N / 2 + 1);
+  const double cells = double(N) * N * N;
+  KBEGIN(j);
+  music::k_music_cubes<R><<<unsigned(c.nc) * c.nc * c.nc, 32, 0, j->stream>>>(c, (R *)out);
+  KEND(j, "music_cubes", cells * sizeof(R));
+  TRY(exec_fft(j, j->n_r2c, out, true));
+  music::KArgs k;
+  k.amp = j->amp;
+  k.amp_len = j->d.amp_table_len;
+  k.N = N;
+  k.mode = mode;
+  k.fixing = j->d.fixing;
+  k.unit = 1.0 / std::sqrt(cells);
+  const double volfac = std::pow(j->d.boxlen / N / 2.0 / M_PI, 1.5);
+  k.norm = (j->d.inversion ? -1.0 : 1.0) / volfac;
+  k.out_scale = j->scale1;
+  const size_t modes = size_t(N) * N * (N / 2 + 1);
+  KBEGIN(j);
+  music::k_music_phi1<R><<<grid_for(modes, 256, num_sm()), 256, 0, j->stream>>>(k, (typename Cplx<R>::T *)out);
+  KEND(j, "music_phi1", 2.0 * j->n_field_bytes + (mode == 2 ? 8.0 * j->d.amp_table_len : 0.0));
+  return MFX_OK;
+}
+
+template <typename R> static int make_noise(mfx_job *j, int mode, void *out) {
+  return j->d.noise_generator == MFX_NOISE_MUSIC1 ? launch_music<R>(j, mode, out) : launch_noise<R>(j, mode, out);
 }
 
 static const int8_t kHa[6] = {0, 1, 2, 0, 0, 1};
@@ -1048,7 +1104,7 @@ template <typename R> static int run_pipeline(mfx_job *j) {
   const int rset = j->ring_next;
   if (j->ring) ring_point(j, rset);
   if (j->timed) CU(cudaEventRecord(j->ev[0], j->stream));
-  TRY(launch_noise<R>(j, 2, j->nf[0]));
+  TRY(make_noise<R>(j, 2, j->nf[0]));
   if (j->timed) CU(cudaEventRecord(j->ev[1], j->stream));
   void **H1 = &j->mslot[0];
   if (j->fused) {
@@ -1128,7 +1184,12 @@ template <typename R> static int run_pipeline(mfx_job *j) {
 static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
   const int N = j->N;
   j->amp_host.assign(d->amp_table, d->amp_table + d->amp_table_len);
-  CU(cudaMemcpyAsync(j->seeds, d->seed_table, size_t(N) * N * 4, cudaMemcpyHostToDevice, j->stream));
+  // the MUSIC1 base seed lives on the device like NGenIC's table, so that a
+  // captured pipeline draws the noise of the seed uploaded last
+  if (d->noise_generator == MFX_NOISE_NGENIC)
+    CU(cudaMemcpyAsync(j->seeds, d->seed_table, size_t(N) * N * 4, cudaMemcpyHostToDevice, j->stream));
+  else
+    CU(cudaMemcpyAsync(j->seeds, &d->music_seed, sizeof(int64_t), cudaMemcpyHostToDevice, j->stream));
   CU(cudaMemcpyAsync(j->amp, d->amp_table, d->amp_table_len * 8, cudaMemcpyHostToDevice, j->stream));
   if (d->plt) {
     CU(cudaMemcpyAsync(j->plt, d->plt_table, size_t(MFX_PLT_TABLE_DOUBLES) * 8, cudaMemcpyHostToDevice,
@@ -1283,10 +1344,12 @@ static void free_job(mfx_job *j) {
     release_plan(j->eng, j->m_r2c);
     release_plan(j->eng, j->m_c2r);
     release_plan(j->eng, j->n_c2r);
+    release_plan(j->eng, j->n_r2c);
   } else {
     destroy_plan(j->m_r2c);
     destroy_plan(j->m_c2r);
     destroy_plan(j->n_c2r);
+    destroy_plan(j->n_r2c);
   }
   // stream-ordered free: never synchronises other jobs' streams
   if (j->arena) {
@@ -1369,7 +1432,8 @@ static int upload_shift_tables(mfx_job *j) {
   return MFX_OK;
 }
 
-static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
+// priority: the CUDA stream priority of the job's stream (0: the default)
+static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int priority = 0) {
   TRY(check_desc(d));
   CU(cudaSetDevice(eng->device));
   auto *j = new mfx_job();
@@ -1399,7 +1463,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     free_job(j);
     return code;
   };
-  if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithPriority(&j->stream, cudaStreamNonBlocking, priority) != cudaSuccess)
     return fail(set_error(MFX_ECUDA, "cudaStreamCreate failed"));
   for (auto &e : j->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(set_error(MFX_ECUDA, "cudaEventCreate failed"));
@@ -1422,6 +1486,10 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
     const long long nfb = (long long)align_up(n_field_bytes(j->N, j->rsize));
     if ((rc = acquire_plan(eng, j->n_c2r, j->N, j->fp64, false, 6, nfb)) != MFX_OK) return fail(rc);
     work = std::max(work, j->n_c2r.work);
+  }
+  if (d->noise_generator == MFX_NOISE_MUSIC1) {
+    if ((rc = acquire_plan(eng, j->n_r2c, j->N, j->fp64, true)) != MFX_OK) return fail(rc);
+    work = std::max(work, j->n_r2c.work);
   }
   Layout L = plan_layout(d, work);
   {
@@ -1534,8 +1602,10 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out) {
       return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
     if (j->n_c2r.valid && cufftSetWorkArea(j->n_c2r.h, j->work) != CUFFT_SUCCESS)
       return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
+    if (j->n_r2c.valid && cufftSetWorkArea(j->n_r2c.h, j->work) != CUFFT_SUCCESS)
+      return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
   }
-  for (Plan *pl : {&j->m_r2c, &j->m_c2r, &j->n_c2r})
+  for (Plan *pl : {&j->m_r2c, &j->m_c2r, &j->n_c2r, &j->n_r2c})
     if (pl->valid && cufftSetStream(pl->h, j->stream) != CUFFT_SUCCESS)
       return fail(set_error(MFX_ECUDA, "cufftSetStream failed"));
   if ((rc = upload_shift_tables(j)) != MFX_OK) return fail(rc);
@@ -1678,6 +1748,7 @@ int mfx_job_footprint(mfx_engine *eng, const mfx_job_desc *desc, size_t *bytes) 
   const bool fused = fused_supported(desc);
   size_t work = (desc->want_particles && !fused) ? 6 * n_field_bytes(desc->ngrid, rs) : 0;
   if (desc->lpt_order >= 2 && !fused) work = std::max(work, size_t(M) * M * (M / 2 + 1) * 2 * rs);
+  if (desc->noise_generator == MFX_NOISE_MUSIC1) work = std::max(work, n_field_bytes(desc->ngrid, rs));
   *bytes = plan_layout(desc, work).total;
   return MFX_OK;
   GUARD_END
@@ -1694,9 +1765,11 @@ int mfx_job_upload(mfx_job *job, const mfx_job_desc *desc) {
   GUARD_BEGIN
   if (!job) return set_error(MFX_EINVAL, "null job");
   TRY(check_desc(desc));
-  if (desc->ngrid != job->d.ngrid || desc->amp_table_len != job->d.amp_table_len || desc->plt != job->d.plt)
+  if (desc->ngrid != job->d.ngrid || desc->amp_table_len != job->d.amp_table_len || desc->plt != job->d.plt ||
+      desc->noise_generator != job->d.noise_generator || desc->music_cubesize != job->d.music_cubesize)
     return set_error(MFX_EINVAL, "upload descriptor does not match the job's sizes");
   job->d.seed_table = desc->seed_table;
+  job->d.music_seed = desc->music_seed;
   job->d.amp_table = desc->amp_table;
   job->d.plt_table = desc->plt_table;
   return upload_tables(job, desc);
@@ -1920,8 +1993,8 @@ int mfx_job_run_noise(mfx_job *job, int raw) {
   if (!job) return set_error(MFX_EINVAL, "null job");
   CU(cudaSetDevice(job->eng->device));
   job->own_launches = 0;
-  int rc = job->fp64 ? launch_noise<double>(job, raw ? 0 : 1, job->nf[0])
-                     : launch_noise<float>(job, raw ? 0 : 1, job->nf[0]);
+  int rc = job->fp64 ? make_noise<double>(job, raw ? 0 : 1, job->nf[0])
+                     : make_noise<float>(job, raw ? 0 : 1, job->nf[0]);
   if (rc == MFX_OK) {
     job->noise_only = true;
     job->has_run = true;
@@ -2470,6 +2543,7 @@ struct mfx_server {
   int max_inflight = 8;
   bool bypass = true;
   double bypass_age_ms = 100.0;
+  bool size_priority = true;  // stream priority grows with the job's footprint
   std::mutex mu;
   std::condition_variable cv;
   std::deque<Ticket *> queue;     // waiting for admission
@@ -2540,6 +2614,18 @@ static void server_loop(mfx_server *s) {
   }
 }
 
+// Larger jobs run on higher-priority streams: the largest requests set the
+// latency tail, and the kernels of the small ones, which wait for them, are
+// short.  One priority level per factor of four in footprint above 64 MB,
+// up to the device's range.
+static int stream_priority_for(size_t footprint) {
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
+  int level = 0;
+  for (size_t f = footprint >> 26; f >= 4; f >>= 2) ++level;  // 64 MB units, x4 per level
+  return std::max(greatest, least - level);
+}
+
 static void setup_loop(mfx_server *s) {
   cudaSetDevice(s->eng->device);
   std::unique_lock<std::mutex> lk(s->mu);
@@ -2550,7 +2636,7 @@ static void setup_loop(mfx_server *s) {
     s->setup_q.pop_front();
     lk.unlock();
     mfx_job *j = nullptr;
-    int rc = create_job(s->eng, &t->d, &j);
+    int rc = create_job(s->eng, &t->d, &j, s->size_priority ? stream_priority_for(t->footprint) : 0);
     std::string err = rc == MFX_OK ? "" : g_last_error;
     if (rc == MFX_OK) rc = j->fp64 ? run_pipeline<double>(j) : run_pipeline<float>(j);
     if (rc == MFX_OK && cudaEventRecord(t->done, j->stream) != cudaSuccess) rc = MFX_ECUDA;
@@ -2596,6 +2682,7 @@ int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms) {
   std::lock_guard<std::mutex> lk(s->mu);
   s->bypass = bypass != 0;
   s->bypass_age_ms = bypass_age_ms;
+  s->size_priority = (bypass & 2) == 0;  // bit 1: every job at the default priority
   s->cv.notify_all();
   return MFX_OK;
 }
@@ -2607,10 +2694,10 @@ int mfx_server_submit(mfx_server *s, const mfx_job_desc *desc, uint64_t *ticket)
   auto t = std::make_unique<Ticket>();
   t->d = *desc;
   const size_t n = desc->ngrid;
-  t->seeds.assign(desc->seed_table, desc->seed_table + n * n);
+  if (desc->noise_generator == MFX_NOISE_NGENIC) t->seeds.assign(desc->seed_table, desc->seed_table + n * n);
   t->amp.assign(desc->amp_table, desc->amp_table + desc->amp_table_len);
   if (desc->plt) t->plt.assign(desc->plt_table, desc->plt_table + MFX_PLT_TABLE_DOUBLES);
-  t->d.seed_table = t->seeds.data();
+  t->d.seed_table = desc->noise_generator == MFX_NOISE_NGENIC ? t->seeds.data() : nullptr;
   t->d.amp_table = t->amp.data();
   t->d.plt_table = desc->plt ? t->plt.data() : nullptr;
   TRY(mfx_job_footprint(s->eng, desc, &t->footprint));

@@ -603,16 +603,18 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
       plt_grad_f32(*tab, i, j, k, N, a.fkfac, G, vc);
     else
       plt_grad<R>(a, i, j, k, N, G, vc);
-    if (k == 0) {
-      // On the kz = 0 plane the c2r sees both k and -k.  The interpolated PLT
-      // gradient is not exactly odd where the CIC stencil touches the table's
-      // Nyquist node (stored once, with +k), so the plane would not be
-      // Hermitian and the real field would depend on the FFT library's pass
-      // order.  Taking the odd part makes the input Hermitian; it equals what
-      // a c2c-then-c2r transform of the unsymmetrised plane yields.
+    if (k == 0 || k == nh) {
+      // On the kz = 0 and kz = N/2 planes the c2r sees both k and -k.  The
+      // interpolated PLT gradient is not exactly odd where the CIC stencil
+      // touches the table's Nyquist node (stored once, with +k), so the plane
+      // would not be Hermitian and the real field would depend on the FFT
+      // library's pass order.  Taking the odd part makes the input Hermitian;
+      // it equals what a c2c-then-c2r transform of the unsymmetrised plane
+      // yields.  (The kz = N/2 plane carries modes only with noise that fills
+      // the Nyquist planes, MUSIC1's.)
       const int im = i ? N - i : 0, jm = j ? N - j : 0;
       R Gm[3], vcm;
-      plt_grad<R>(a, im, jm, 0, N, Gm, vcm);
+      plt_grad<R>(a, im, jm, k, N, Gm, vcm);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         Gp[d] = R(0.5) * (G[d] - Gm[d]);

@@ -1,0 +1,232 @@
+// MUSIC1 white noise on the device (the [random] generator = MUSIC1 plugin,
+// one level: the seed given at the grid's own level).
+//
+//   random_music.cc:92-116            Fill_Grid copies the level's cells into the grid
+//   random_music_wnoise_generator.cc  cubes of cubesize^3 cells, cube
+//     :588-626                        icube = (ic ncubes + jc) ncubes + kc seeded with
+//                                     baseseed + icube, cells ii, jj, kk (kk fastest)
+//                                     drawn in order by gsl_ran_ugaussian_ratio_method
+//                                     on gsl_rng_mt19937
+//   ic_generator.cc:294-383           forward transform (1/sqrt(N^3)), fixing,
+//                                     inversion, 1/volfac
+//   ic_generator.cc:509-516           phi(1) = -w amplitude(k) / k^2, DC zeroed
+//
+// The generators are GSL's, restated from their published algorithms:
+// MT19937 (Matsumoto and Nishimura 1998, with their 2002 seeding: x0 = s,
+// x_i = 1812433253 (x_{i-1} ^ (x_{i-1} >> 30)) + i, seed 0 meaning 4357;
+// uniform = output / 2^32) and Leva's ratio-of-uniforms normal (ACM TOMS 18
+// (1992) 449) with its published bounding constants.
+//
+// One warp draws one cube.  The 624-word state lives in shared memory and the
+// twist runs in four dependency-ordered phases across the lanes.  Each normal
+// of the ratio method consumes a pair of consecutive outputs (u, v) and either
+// accepts it or moves on to the next pair, so the pairs of one state block are
+// tested in parallel (one pair per lane) and the accepted ones are ranked in
+// stream order with a ballot: cell c of the cube gets the c-th accepted pair,
+// exactly as the sequential generator hands them out.  624 outputs are 312
+// whole pairs, so no pair straddles a twist.
+//
+// The mean subtraction of the reference (cube means, then the global mean)
+// shifts every cell by one constant, which only moves the k = 0 mode; the
+// k-space kernel sets that mode to zero, the value the reference's zero-mean
+// field has up to rounding.
+#pragma once
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace mfx {
+namespace music {
+
+constexpr int kMtN = 624, kMtM = 397;
+constexpr uint32_t kMtMatrix = 0x9908b0dfu, kUpper = 0x80000000u, kLower = 0x7fffffffu;
+
+__device__ __forceinline__ uint32_t mt_mix(uint32_t a, uint32_t b, uint32_t c) {
+  const uint32_t y = (a & kUpper) | (b & kLower);
+  return c ^ (y >> 1) ^ ((y & 1u) ? kMtMatrix : 0u);
+}
+
+__device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+
+// Regenerates the 624-word block in place.  Element k of the sequential
+// twist reads x[k], x[k+1] and x[(k+397) mod 624]; the last of these is an
+// old word for k < 227 and a new one (x[k-227]) after that, and x[0] is new
+// for k = 623.  Each phase reads all its inputs before any lane writes.
+__device__ __forceinline__ void mt_twist(uint32_t *x, int lane) {
+  constexpr int P1 = kMtN - kMtM;  // 227
+  uint32_t t[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int k = lane + 32 * r;
+    if (k < P1) t[r] = mt_mix(x[k], x[k + 1], x[k + kMtM]);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int k = lane + 32 * r;
+    if (k < P1) x[k] = t[r];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int k = P1 + lane + 32 * r;
+    if (k < 2 * P1) t[r] = mt_mix(x[k], x[k + 1], x[k - P1]);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int k = P1 + lane + 32 * r;
+    if (k < 2 * P1) x[k] = t[r];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    const int k = 2 * P1 + lane + 32 * r;
+    if (k < kMtN - 1) t[r] = mt_mix(x[k], x[k + 1], x[k - P1]);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    const int k = 2 * P1 + lane + 32 * r;
+    if (k < kMtN - 1) x[k] = t[r];
+  }
+  __syncwarp();
+  if (lane == 0) x[kMtN - 1] = mt_mix(x[kMtN - 1], x[0], x[kMtM - 1]);
+  __syncwarp();
+}
+
+// The ratio method's acceptance of one pair of outputs, in the operation
+// order of the sequential C code (no contraction): u = 1 - U1,
+// v = 1.7156 (U2 - 1/2), x = u - s, y = |v| - t, Q = x^2 + y (a y - b x);
+// accepted when Q < r1, or Q <= r2 and v^2 <= -4 u^2 ln u.  A float estimate
+// of Q (error below 1e-6 here) settles the pairs far from both bounds; the
+// rest take the exact double test.
+__device__ __forceinline__ bool leva_accept(uint32_t w1, uint32_t w2, double &u, double &v) {
+  constexpr double s = 0.449871, t = -0.386595, a = 0.19600, b = 0.25472, r1 = 0.27597, r2 = 0.27846;
+  constexpr double two32 = 1.0 / 4294967296.0;
+  u = __dsub_rn(1.0, double(w1) * two32);
+  v = __dmul_rn(double(w2) * two32 - 0.5, 1.7156);
+  {
+    const float uf = float(u), vf = float(v);
+    const float xf = uf - float(s), yf = fabsf(vf) - float(t);
+    const float qf = xf * xf + yf * (float(a) * yf - float(b) * xf);
+    if (qf < float(r1) - 1e-5f) return true;
+    if (qf > float(r2) + 1e-5f) return false;
+  }
+  const double x = __dsub_rn(u, s), y = __dsub_rn(fabs(v), t);
+  const double q = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, __dsub_rn(__dmul_rn(a, y), __dmul_rn(b, x))));
+  if (q < r1) return true;
+  if (q > r2) return false;
+  return !(__dmul_rn(v, v) > __dmul_rn(__dmul_rn(__dmul_rn(-4.0, u), u), log(u)));
+}
+
+struct CubeArgs {
+  const long long *seed;  // baseseed of the level (device memory)
+  int N;             // grid cells per axis
+  int cs;            // cube edge (N itself when N < cubesize)
+  int nc;            // cubes per axis
+  long long row;     // real elements between consecutive k-rows (2 (N/2 + 1))
+};
+
+// One warp per cube: blockDim.x == 32, gridDim.x == nc^3.  Writes cube cells
+// into the padded real layout of an in-place r2c transform.
+template <typename R> __global__ void __launch_bounds__(32) k_music_cubes(CubeArgs a, R *out) {
+  __shared__ uint32_t x[kMtN];
+  const int lane = threadIdx.x;
+  const long long icube = blockIdx.x;
+  const int nc = a.nc, cs = a.cs;
+  const int ic = int(icube / (nc * nc)), jc = int((icube / nc) % nc), kc = int(icube % nc);
+  if (lane == 0) {
+    // gsl_rng_set(mt19937, baseseed + icube): the seed as an unsigned long,
+    // its low 32 bits used
+    const unsigned long long cseed = static_cast<unsigned long long>(*a.seed + icube);
+    uint32_t s = cseed == 0 ? 4357u : uint32_t(cseed & 0xffffffffull);
+    x[0] = s;
+    for (int k = 1; k < kMtN; ++k) {
+      s = 1812433253u * (s ^ (s >> 30)) + uint32_t(k);
+      x[k] = s;
+    }
+  }
+  __syncwarp();
+  const int total = cs * cs * cs, cs2 = cs * cs;
+  R *base = out + (size_t(ic) * cs * a.N + size_t(jc) * cs) * size_t(a.row) + size_t(kc) * cs;
+  int produced = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  while (produced < total) {
+    mt_twist(x, lane);
+    for (int p0 = 0; p0 < kMtN / 2 && produced < total; p0 += 32) {
+      const int p = p0 + lane;
+      bool acc = false;
+      double u = 1.0, v = 0.0;
+      if (p < kMtN / 2) acc = leva_accept(mt_temper(x[2 * p]), mt_temper(x[2 * p + 1]), u, v);
+      const unsigned m = __ballot_sync(0xffffffffu, acc);
+      const int c = produced + __popc(m & lt);
+      if (acc && c < total) {
+        const int ii = c / cs2, jj = (c / cs) % cs, kk = c % cs;
+        base[(size_t(ii) * a.N + jj) * size_t(a.row) + kk] = R(v / u);
+      }
+      produced += __popc(m);
+    }
+    __syncwarp();
+  }
+}
+
+struct KArgs {
+  const double *amp;  // amp[n] = amplitude(kf sqrt n)/(kf^2 n)
+  size_t amp_len;
+  int N;
+  int mode;           // 0: raw noise, 1: normalised noise, 2: phi(1)
+  int fixing;
+  double unit;        // 1/sqrt(N^3): the forward transform's norm
+  double norm;        // (+-1)/volfac
+  double out_scale;   // extra factor on phi(1) (per-field scaling of the FP32 form)
+};
+
+// k-space pass over the r2c output of the cube noise, in place: the unitary
+// norm, the k = 0 mode set to zero, then (modes 1, 2) fixing, inversion and
+// 1/volfac, and (mode 2) -amplitude(k)/k^2.  Unlike NGenIC's noise the
+// Nyquist planes carry modes.
+template <typename R> __global__ void __launch_bounds__(256) k_music_phi1(KArgs a, typename Cplx<R>::T *f) {
+  const int N = a.N, nk = (N >> 1) + 1;
+  const size_t total = size_t(N) * N * nk;
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int k = int(idx % nk);
+    const size_t col = idx / nk;
+    const int j = int(col % N), i = int(col / N);
+    if ((i | j | k) == 0) {
+      f[idx] = mkc<R>(R(0), R(0));
+      continue;
+    }
+    auto z = f[idx];
+    R re = R(double(z.x) * a.unit), im = R(double(z.y) * a.unit);
+    if (a.mode >= 1) {
+      if (a.fixing) {
+        const R m = sqrt(re * re + im * im);
+        if (m != R(0)) {
+          re /= m;
+          im /= m;
+        }
+      }
+      re *= R(a.norm);
+      im *= R(a.norm);
+      if (a.mode == 2) {
+        const int si = signed_idx(i, N), sj = signed_idx(j, N);
+        const size_t n = size_t(si * si + sj * sj + k * k);
+        const R fa = (n < a.amp_len) ? R(-a.amp[n] * a.out_scale) : R(0);
+        re *= fa;
+        im *= fa;
+      }
+    }
+    f[idx] = mkc<R>(re, im);
+  }
+}
+
+}  // namespace music
+}  // namespace mfx

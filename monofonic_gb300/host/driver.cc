@@ -143,9 +143,32 @@ int run_config(mfx_engine *eng, const std::string &text) {
   else if (load == "bcc") lattice = MFX_LATTICE_BCC;
   else if (load == "fcc") lattice = MFX_LATTICE_FCC;
   else throw std::runtime_error("ParticleLoad '" + load + "' is not supported by this engine (sc, bcc, fcc)");
+  // [random] generator (random_plugin.cc:62-81): NGENIC with its seed, or
+  // MUSIC1 with one seed[level] at the grid's own level (random_music.cc:75,
+  // 160-215); seeds at other levels need MUSIC1's multi-level refinement
   const std::string gen = cf.get_value<std::string>("random", "generator");
-  if (gen != "NGENIC") throw std::runtime_error("random generator '" + gen + "' is not supported (NGENIC)");
-  const long seed = cf.get_value<long>("random", "seed");
+  long seed = 0;
+  int noise_gen = MFX_NOISE_NGENIC;
+  unsigned cubesize = 0;
+  if (gen == "NGENIC") {
+    seed = cf.get_value<long>("random", "seed");
+  } else if (gen == "MUSIC1") {
+    int lmin = 0;
+    while ((1u << lmin) < ngrid) ++lmin;
+    if ((1u << lmin) != ngrid) throw std::runtime_error("MUSIC1 white noise needs GridRes a power of two");
+    for (int l = 0; l < 32; ++l) {
+      const std::string key = "seed[" + std::to_string(l) + "]";
+      if (l != lmin && cf.contains_key("random", key))
+        throw std::runtime_error("MUSIC1 " + key + ": seeds at levels other than log2(GridRes) = " +
+                                 std::to_string(lmin) + " (multi-level refinement) are not supported");
+    }
+    seed = cf.get_value<long>("random", "seed[" + std::to_string(lmin) + "]");
+    if (seed <= 0) throw std::runtime_error("Seed values need to be >0");
+    cubesize = cf.get_value_safe<unsigned>("random", "cubesize", 32);
+    noise_gen = MFX_NOISE_MUSIC1;
+  } else {
+    throw std::runtime_error("random generator '" + gen + "' is not supported (NGENIC, MUSIC1)");
+  }
   const std::string prec = cf.get_value_safe<std::string>("execution", "Precision", "double");
 
   calculator cc(cf);
@@ -156,8 +179,11 @@ int run_config(mfx_engine *eng, const std::string &text) {
   if (!om.count(fmt)) throw std::runtime_error("Output plug-in '" + fmt + "' not found");
   auto out = om[fmt](cf, cc);
 
-  std::vector<uint32_t> seeds(size_t(ngrid) * ngrid);
-  ngenic_seed_table(seed, ngrid, seeds.data());
+  std::vector<uint32_t> seeds;
+  if (noise_gen == MFX_NOISE_NGENIC) {
+    seeds.resize(size_t(ngrid) * ngrid);
+    ngenic_seed_table(seed, ngrid, seeds.data());
+  }
   const size_t alen = 3 * size_t(ngrid / 2) * (ngrid / 2) + 1;
   std::vector<double> amp(alen);
   fill_amp_table(cc, ngrid, boxlen, amp.data(), alen);
@@ -177,7 +203,10 @@ int run_config(mfx_engine *eng, const std::string &text) {
   d.precision = (prec == "float") ? MFX_FP32C : MFX_FP64;
   d.fixing = cf.get_value_safe<bool>("setup", "DoFixing", false);
   d.inversion = cf.get_value_safe<bool>("setup", "DoInversion", false);
-  d.seed_table = seeds.data();
+  d.seed_table = seeds.empty() ? nullptr : seeds.data();
+  d.noise_generator = noise_gen;
+  d.music_seed = noise_gen == MFX_NOISE_MUSIC1 ? seed : 0;
+  d.music_cubesize = cubesize;
   d.amp_table = amp.data();
   d.amp_table_len = alen;
   d.plt_table = do_plt ? plt.data() : nullptr;

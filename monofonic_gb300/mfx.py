@@ -14,6 +14,7 @@ from . import build as _build
 
 MFX_OK, MFX_EINVAL, MFX_ENOMEM, MFX_ECUDA, MFX_ETIMEOUT, MFX_ECANCEL, MFX_ESTATE, MFX_EADMIT = 0, -1, -2, -3, -4, -5, -6, -7
 SC, BCC, FCC = 0, 1, 2
+NOISE_NGENIC, NOISE_MUSIC1 = 0, 1
 FP64, FP32C = 0, 1
 FIELD_NOISE, FIELD_PHI1, FIELD_PHI2, FIELD_PHI3, FIELD_A3X, FIELD_A3Y, FIELD_A3Z = range(7)
 PLT_NGRID = 64
@@ -57,6 +58,7 @@ class JobDesc(C.Structure):
         ("lunit", C.c_double), ("vunit", C.c_double),
         ("pos64", C.c_int), ("vel64", C.c_int), ("id64", C.c_int), ("id_offset", C.c_uint64),
         ("want_particles", C.c_int),
+        ("noise_generator", C.c_int), ("music_seed", C.c_int64), ("music_cubesize", C.c_uint32),
     ]
 
 
@@ -194,8 +196,15 @@ class Cosmology:
 
 
 def ini_text(ngrid, boxlen, zstart, order, seed, lattice="sc", sigma8=0.81, omega_m=0.3, omega_b=0.045,
-             h0=70.0, n_s=0.965, fixing=False, plt=False, precision="double", fmt="binary", filename="ics.bin"):
-    """INI text in monofonIC's config format for the configs this engine serves."""
+             h0=70.0, n_s=0.965, fixing=False, plt=False, precision="double", fmt="binary", filename="ics.bin",
+             generator="NGENIC", cubesize=32):
+    """INI text in monofonIC's config format for the configs this engine serves.
+    generator="MUSIC1" gives the seed at the grid's level, seed[log2 ngrid]."""
+    if generator == "MUSIC1":
+        level = int(ngrid).bit_length() - 1
+        rnd = f"generator = MUSIC1\nseed[{level}] = {seed}\ncubesize = {cubesize}"
+    else:
+        rnd = f"generator = {generator}\nseed = {seed}"
     return f"""[setup]
 GridRes = {ngrid}
 BoxLength = {boxlen}
@@ -215,8 +224,7 @@ transfer = eisenstein
 ZeroRadiation = true
 m_nu1 = 0
 [random]
-generator = NGENIC
-seed = {seed}
+{rnd}
 [execution]
 Precision = {precision}
 [output]
@@ -279,13 +287,18 @@ class Job:
 
     def __init__(self, engine: Engine, ngrid, boxlen, order, seed_table, amp_table, coef, lattice=SC,
                  precision=FP64, plt_table=None, fixing=False, inversion=False, lunit=1.0, vunit=1.0,
-                 pos64=True, vel64=True, id64=True, id_offset=0, want_particles=True):
+                 pos64=True, vel64=True, id64=True, id_offset=0, want_particles=True,
+                 noise_generator=None, music_seed=0, music_cubesize=32):
+        """seed_table: NGenIC's per-column seeds; None with noise_generator=
+        NOISE_MUSIC1, which draws the noise from music_seed and music_cubesize."""
         self.engine = engine
         self.n = ngrid
         self.lattice = lattice
         self.precision = precision
         self.pos64, self.vel64, self.id64 = pos64, vel64, id64
-        self._seed = np.ascontiguousarray(seed_table, dtype=np.uint32)
+        if noise_generator is None:
+            noise_generator = NOISE_NGENIC if seed_table is not None else NOISE_MUSIC1
+        self._seed = None if seed_table is None else np.ascontiguousarray(seed_table, dtype=np.uint32)
         self._amp = np.ascontiguousarray(amp_table, dtype=np.float64)
         self._plt = None if plt_table is None else np.ascontiguousarray(plt_table, dtype=np.float64)
         d = JobDesc()
@@ -293,7 +306,10 @@ class Job:
         d.plt = 1 if plt_table is not None else 0
         d.precision = precision
         d.fixing, d.inversion = int(fixing), int(inversion)
-        d.seed_table = self._seed.ctypes.data
+        d.seed_table = self._seed.ctypes.data if self._seed is not None else None
+        d.noise_generator = noise_generator
+        d.music_seed = music_seed
+        d.music_cubesize = music_cubesize
         d.amp_table = self._amp.ctypes.data
         d.amp_table_len = self._amp.size
         d.plt_table = self._plt.ctypes.data if self._plt is not None else None
@@ -323,9 +339,11 @@ class Job:
     def handle(self):
         return self._h
 
-    def upload(self, seed_table=None, amp_table=None, plt_table=None):
+    def upload(self, seed_table=None, amp_table=None, plt_table=None, music_seed=None):
         if seed_table is not None:
             np.copyto(self._seed, seed_table)
+        if music_seed is not None:
+            self.desc.music_seed = music_seed
         if amp_table is not None:
             np.copyto(self._amp, amp_table)
         if plt_table is not None and self._plt is not None:
@@ -623,12 +641,13 @@ class Server:
     def wait(self, ticket: int, timeout_ms: int = -1):
         check(load().mfx_server_wait(self._h, ticket, timeout_ms))
 
-    def set_policy(self, bypass: bool = True, bypass_age_ms: float = 100.0):
+    def set_policy(self, bypass: bool = True, bypass_age_ms: float = 100.0, size_priority: bool = True):
         """Admission order: a later job that fits may pass a head that has
-        waited at most bypass_age_ms (bypass), or strict first-in first-out."""
+        waited at most bypass_age_ms (bypass), or strict first-in first-out;
+        size_priority: larger jobs on higher-priority streams."""
         L = load()
         L.mfx_server_set_policy.argtypes = [C.c_void_p, C.c_int, C.c_double]
-        check(L.mfx_server_set_policy(self._h, int(bypass), float(bypass_age_ms)))
+        check(L.mfx_server_set_policy(self._h, int(bool(bypass)) | (0 if size_priority else 2), float(bypass_age_ms)))
 
     def times(self, ticket: int):
         q, l = C.c_double(), C.c_double()

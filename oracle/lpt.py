@@ -39,14 +39,17 @@ WORKERS = os.cpu_count() or 1
 # RANLUX / NGenIC (C restatement in oracle/ranlux.c)
 # ----------------------------------------------------------------------------
 def build_lib() -> pathlib.Path:
-    """Compile oracle/ranlux.c into oracle/_build/liboracle_rng.so (if stale)."""
-    src = _HERE / "ranlux.c"
+    """Compile oracle/ranlux.c and oracle/music.c into
+    oracle/_build/liboracle_rng.so (if stale)."""
+    srcs = [_HERE / "ranlux.c", _HERE / "music.c"]
     out = _BUILD / "liboracle_rng.so"
     _BUILD.mkdir(exist_ok=True)
-    if not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+    if not out.exists() or any(out.stat().st_mtime < s.stat().st_mtime for s in srcs):
         import subprocess
         tmp = out.with_suffix(".so.tmp%d" % os.getpid())
-        subprocess.check_call(["gcc", "-O2", "-shared", "-fPIC", "-o", str(tmp), str(src), "-lm"])
+        # no FMA contraction: the ratio method's tests round like plain C on every host
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-o", str(tmp)]
+                              + [str(x) for x in srcs] + ["-lm"])
         os.replace(tmp, out)
     return out
 
@@ -124,7 +127,35 @@ def lib():
         _lib.mfxo_ranlxd1_words.argtypes = [ctypes.c_ulong, ctypes.c_size_t, ctypes.c_void_p]
         _lib.mfxo_ngenic_seed_table.argtypes = [ctypes.c_long, ctypes.c_size_t, ctypes.c_void_p]
         _lib.mfxo_ngenic_fill.argtypes = [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        _lib.mfxo_mt19937_words.argtypes = [ctypes.c_ulong, ctypes.c_size_t, ctypes.c_void_p]
+        _lib.mfxo_leva_normals.argtypes = [ctypes.c_ulong, ctypes.c_size_t, ctypes.c_void_p]
+        _lib.mfxo_music_noise.argtypes = [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_long, ctypes.c_void_p]
     return _lib
+
+
+def mt19937_words(seed: int, count: int) -> np.ndarray:
+    out = np.zeros(count, dtype=np.uint32)
+    lib().mfxo_mt19937_words(seed, count, out.ctypes.data)
+    return out
+
+
+def leva_normals(seed: int, count: int) -> np.ndarray:
+    out = np.zeros(count)
+    lib().mfxo_leva_normals(seed, count, out.ctypes.data)
+    return out
+
+
+def music_noise_real(n: int, seed: int, cubesize: int = 32) -> np.ndarray:
+    """MUSIC1 single-level white noise in real space (oracle/music.c)."""
+    out = np.zeros((n, n, n))
+    lib().mfxo_music_noise(n, cubesize, seed, out.ctypes.data)
+    return out
+
+
+def music_fill(n: int, seed: int, cubesize: int = 32) -> np.ndarray:
+    """RNG_music::Fill_Grid followed by the IC generator's forward transform:
+    the k-space white noise (random_music.cc:92-116, ic_generator.cc:305-383)."""
+    return fft_r2c(music_noise_real(n, seed, cubesize))
 
 
 def ranlxd1_words(seed: int, count: int) -> np.ndarray:
@@ -633,9 +664,12 @@ def ppt_fields(phi_s, phi2_s, noise, order, n, L, dplus, vfac, vunit, c_species=
 
 
 def run_lpt(n, L, seed_table, amplitude, order, dplus, vfac, lattice=0, lunit=1.0, vunit=1.0,
-            fixing=False, inversion=False, grad=None, want_particles=True):
-    """The whole hot path, ic_generator.cc:288-1064, for one species (dm, no baryons)."""
-    w = ngenic_fill(n, seed_table)
+            fixing=False, inversion=False, grad=None, want_particles=True, noise=None):
+    """The whole hot path, ic_generator.cc:288-1064, for one species (dm, no baryons).
+
+    noise: the raw k-space white noise of another generator (music_fill, before
+    normalisation) in place of NGenIC's from seed_table."""
+    w = ngenic_fill(n, seed_table) if noise is None else noise
     w = normalise_noise(w, n, L, fixing, inversion)
     phi = phi1_from_noise(w, n, L, amplitude)
     phi2, phi3, A3 = lpt_potentials(phi, n, L, order)

@@ -211,3 +211,60 @@ def test_config_parser_and_errors(mfxlib):
     txt = mfxlib.ini_text(32, 50.0, 24.0, 3, 3).replace("Omega_m = 0.3", "Omega_m = 0.31 # trailing comment")
     c = mfxlib.Cosmology(txt)
     assert c.get("Omega_m") == 0.31
+
+
+# ---------------------------------------------------------------------------
+# MUSIC1 white noise (oracle/music.c): GSL's mt19937 and ratio-method normals
+# ---------------------------------------------------------------------------
+def test_mt19937_tenthousandth_output_is_the_cpp_standards(oracle):
+    """The C++ standard's requirement on std::mt19937 ([rand.predef]): the
+    10000th output of a default-seeded engine (seed 5489) is 4123659995."""
+    assert int(oracle.mt19937_words(5489, 10000)[-1]) == 4123659995
+
+
+def test_mt19937_matches_cpp_std_mt19937(oracle, tmp_path):
+    """GSL seeds mt19937 like std::mt19937 (the 2002 initialisation): the
+    restatement equals the C++ library's engine output for output."""
+    import subprocess
+    src = tmp_path / "mt.cc"
+    src.write_text("""
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+int main(int argc, char **argv) {
+  std::mt19937 g(std::strtoul(argv[1], nullptr, 10));
+  for (int i = 0; i < 2000; ++i) std::printf("%u\\n", unsigned(g()));
+}
+""")
+    exe = tmp_path / "mt"
+    subprocess.check_call(["g++", "-O1", "-o", str(exe), str(src)])
+    for seed in (1, 4357, 12345, 2**31 + 5, 4294967295):
+        out = subprocess.run([str(exe), str(seed)], capture_output=True, text=True, check=True).stdout.split()
+        ref = np.array(out, dtype=np.uint64).astype(np.uint32)
+        assert np.array_equal(oracle.mt19937_words(seed, 2000), ref), seed
+
+
+def test_ratio_method_normals_are_standard_normal(oracle):
+    from scipy import stats
+    x = oracle.leva_normals(20261204, 400000)
+    assert abs(x.mean()) < 5e-3 and abs(x.var() - 1.0) < 1e-2
+    assert abs(stats.kurtosis(x)) < 3e-2 and abs(stats.skew(x)) < 1e-2
+    assert stats.kstest(x, "norm").pvalue > 1e-3
+
+
+def test_music_noise_cubes_and_means(oracle):
+    """Each 32^3 cube is the ratio-method stream of seed + cube index (kk
+    fastest), less the two mean subtractions; the field has zero mean."""
+    n, seed, cs = 64, 777, 32
+    f = oracle.music_noise_real(n, seed, cs)
+    assert abs(f.mean()) < 1e-15
+    raw = [oracle.leva_normals(seed + q, cs ** 3).reshape(cs, cs, cs) for q in range(8)]
+    shift = np.mean([r.mean() for r in raw])
+    for q, r in enumerate(raw):
+        ic, jc, kc = q // 4, (q // 2) % 2, q % 2
+        blk = f[ic * cs:(ic + 1) * cs, jc * cs:(jc + 1) * cs, kc * cs:(kc + 1) * cs]
+        d = blk - (r - shift)
+        assert np.ptp(d) < 1e-13  # the remaining zero-mean correction is one constant
+    small = oracle.music_noise_real(16, 3, 32)  # one cube of the whole grid below the cube size
+    r = oracle.leva_normals(3, 16 ** 3).reshape(16, 16, 16)
+    assert np.allclose(small, r - r.mean(), rtol=0, atol=1e-13)

@@ -1,0 +1,141 @@
+"""MUSIC1 white noise on the device against the oracle (oracle/music.c).
+
+The cube normals are the sequential generator's values bit for bit (MT19937
+words and the ratio method's accept/reject decisions reproduced exactly), so
+the FP64 k-space noise matches the oracle's forward transform to FFT rounding;
+the mean subtraction of the reference only moves k = 0, which both sides hold
+at zero.  The whole pipeline then meets the same bars as with NGenIC's noise:
+1e-10 relative for the plain FP64 form, 1e-5 of the interparticle spacing for
+the FP32 form.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_parity import TOL_FP64, Case, check_fields, check_particles, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def music_job(mfxlib, engine, c, seed, cubesize=32, precision=None, **kw):
+    precision = mfxlib.FP64 if precision is None else precision
+    return mfxlib.Job(engine, c.n, c.L, c.order, None, c.amp, c.coef, lattice=c.lattice, precision=precision,
+                      plt_table=c.plt, fixing=c.fixing, inversion=c.inversion, lunit=c.lunit, vunit=c.vunit,
+                      noise_generator=mfxlib.NOISE_MUSIC1, music_seed=seed, music_cubesize=cubesize, **kw)
+
+
+def oracle_noise(oracle, n, seed, cubesize):
+    w = oracle.music_fill(n, seed, cubesize)
+    w[0, 0, 0] = 0.0  # zero mean up to rounding on the reference's side
+    return w
+
+
+@pytest.mark.parametrize("n,cubesize,seed", [(16, 32, 12345), (32, 8, 7), (64, 32, 4242),
+                                             (32, 16, (1 << 32) - 3)])
+def test_music_raw_noise_matches_oracle(mfxlib, engine, oracle, n, cubesize, seed):
+    """One cube below the cube size, 64 small cubes, the default cubes, and cube
+    seeds that cross 2^32 (the low 32 bits of the seed go into the state, and a
+    seed of 2^32 is not GSL's zero seed)."""
+    c = Case(mfxlib, n, 100.0, 49.0, 1, 1)
+    j = music_job(mfxlib, engine, c, seed, cubesize, want_particles=False)
+    j.run_noise(raw=True)
+    got = j.field(mfxlib.FIELD_NOISE)
+    ref = oracle_noise(oracle, n, seed, cubesize)
+    assert got[0, 0, 0] == 0
+    assert np.max(np.abs(got - ref)) < 1e-12
+    # unit variance per mode, Nyquist planes populated (unlike NGenIC)
+    assert abs(np.mean(np.abs(got[1:, 1:, 1:-1]) ** 2) - 1.0) < 0.1
+    assert np.all(got[:, :, n // 2] != 0)
+
+
+@pytest.mark.parametrize("fixing,inversion", [(False, False), (True, True)])
+def test_music_normalised_noise(mfxlib, engine, oracle, fixing, inversion):
+    n, L = 32, 300.0
+    c = Case(mfxlib, n, L, 24.0, 1, 1, fixing=fixing, inversion=inversion)
+    j = music_job(mfxlib, engine, c, 99, 16, want_particles=False)
+    j.run_noise(raw=False)
+    ref = oracle.normalise_noise(oracle_noise(oracle, n, 99, 16), n, L, fixing, inversion)
+    ref[0, 0, 0] = 0.0
+    assert rel_l2(j.field(mfxlib.FIELD_NOISE), ref) < 1e-13
+
+
+@pytest.mark.parametrize("order,lattice,plt", [(2, 0, False), (3, 1, False), (3, 2, True)])
+def test_music_pipeline_fp64(mfxlib, engine, oracle, order, lattice, plt):
+    """With PLT the kz = N/2 plane, which MUSIC1 noise fills, takes the same
+    Hermitian (odd-gradient) treatment as kz = 0."""
+    n, seed = 64, 31337
+    tab = engine.plt_table(lattice) if plt else None
+    c = Case(mfxlib, n, 200.0, 30.0, order, 1, lattice=lattice, plt=tab)
+    j = music_job(mfxlib, engine, c, seed)
+    j.run()
+    grad = None
+    if plt:
+        from oracle import plt as oplt
+        grad = oplt.PLTGradient(n, c.L, tab)
+    res = oracle.run_lpt(n, c.L, None, c.amplitude, order, c.dplus, c.vfac, lattice=lattice, lunit=c.lunit,
+                         vunit=c.vunit, grad=grad, noise=oracle_noise(oracle, n, seed, 32))
+    check_fields(mfxlib, j, res, order, TOL_FP64)
+    check_particles(c, j, res, TOL_FP64)
+
+
+def test_music_pipeline_fp32c_plt(mfxlib, engine, oracle):
+    """FP32 form with PLT on FCC: MUSIC1 noise fills the Nyquist planes, so the
+    job takes the cuFFT route rather than the pruned transforms."""
+    n, seed, lattice = 64, 5, 2
+    tab = engine.plt_table(lattice)
+    c = Case(mfxlib, n, 1000.0 * 64 / 768, 24.0, 3, 1, lattice=lattice, plt=tab)
+    j = music_job(mfxlib, engine, c, seed, precision=mfxlib.FP32C, pos64=True, vel64=False)
+    j.run()
+    from oracle import plt as oplt
+    res = oracle.run_lpt(n, c.L, None, c.amplitude, 3, c.dplus, c.vfac, lattice=lattice, lunit=c.lunit,
+                         vunit=c.vunit, grad=oplt.PLTGradient(n, c.L, tab), noise=oracle_noise(oracle, n, seed, 32))
+    pos, vel, ids = j.particles()
+    delta = c.L / (c.n * 2 ** (lattice / 3.0))
+    err = (pos - res["pos"]) / delta
+    assert np.sqrt(np.mean(err ** 2)) < 1e-5
+    assert np.max(np.abs(err)) < 2e-4
+    assert rel_l2(vel.astype(np.float64), res["vel"]) < 1e-5
+    assert np.array_equal(ids, res["ids"])
+
+
+def test_music_reseed_through_captured_graph(mfxlib, engine, oracle):
+    """The base seed is read from device memory: a captured pipeline replays
+    with the seed uploaded after the capture."""
+    n = 32
+    c = Case(mfxlib, n, 100.0, 49.0, 2, 1)
+    j = music_job(mfxlib, engine, c, 11, 8, want_particles=False)
+    j.capture()
+    for seed in (11, 12):
+        j.upload(music_seed=seed)
+        j.run()
+        w = oracle.normalise_noise(oracle_noise(oracle, n, seed, 8), n, c.L, False, False)
+        phi = oracle.phi1_from_noise(w, n, c.L, c.amplitude)
+        assert rel_l2(j.field(mfxlib.FIELD_PHI1) * c.coef["g1"], phi * c.coef["g1"]) < 1e-12
+
+
+@pytest.mark.parametrize("n,cubesize,why", [(48, 16, "power of two"), (64, 24, "tile"), (64, 1, "tile")])
+def test_music_descriptor_checks(mfxlib, engine, n, cubesize, why):
+    c = Case(mfxlib, n, 100.0, 49.0, 1, 1)
+    with pytest.raises(mfxlib.MfxError, match=why):
+        music_job(mfxlib, engine, c, 5, cubesize, want_particles=False)
+    with pytest.raises(mfxlib.MfxError, match="positive seed"):
+        music_job(mfxlib, engine, Case(mfxlib, 32, 100.0, 49.0, 1, 1), 0, 32, want_particles=False)
+
+
+def test_run_config_music1(mfxlib, engine, tmp_path):
+    """The driver takes [random] generator = MUSIC1 with seed[log2 GridRes]."""
+    f = tmp_path / "ics.bin"
+    engine.run_config(mfxlib.ini_text(32, 50.0, 24.0, 2, 777, "sc", filename=str(f), generator="MUSIC1",
+                                      cubesize=16))
+    raw = f.read_bytes()
+    np_ = int(np.frombuffer(raw[8:16], np.uint64)[0])
+    assert np_ == 32 ** 3
+    c = Case(mfxlib, 32, 50.0, 24.0, 2, 1)
+    j = music_job(mfxlib, engine, c, 777, 16)
+    j.run()
+    pos, vel, ids = j.particles()
+    off = 8 + 8 + 4 + 4 + 24
+    assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
+    bad = mfxlib.ini_text(32, 50.0, 24.0, 2, 777, filename=str(f), generator="MUSIC1").replace(
+        "seed[5] = 777", "seed[4] = 12\nseed[5] = 777")
+    with pytest.raises(mfxlib.MfxError):
+        engine.run_config(bad)
