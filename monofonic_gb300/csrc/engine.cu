@@ -957,6 +957,8 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
 // Particle masses of the job's species (mfx_job_set_species), per sub-lattice:
 // the delta_bc field from phi1 with the sub-lattice phase, its c2r and the
 // read-out (ic_generator.cc:749-780, particle_generator.hh:369-427)
+static NyqSteps nyq_steps(const mfx_job *j);
+
 template <typename R> static int mass_stage(mfx_job *j) {
   const int N = j->N, nsm = num_sm();
   const double N3 = double(N) * N * N;
@@ -972,6 +974,7 @@ template <typename R> static int mass_stage(mfx_job *j) {
   m.c_species = j->c_species;
   m.norm = 1.0 / std::sqrt(N3);
   m.scale = j->mass_factor / (double(j->ns) * N3);
+  m.nyq = nyq_steps(j);
   const size_t total = size_t(N) * N * j->nk;
   for (int s = 0; s < j->ns; ++s) {
     m.shift = s;
@@ -1032,6 +1035,7 @@ template <typename R> static int assemble_stage(mfx_job *j, int mask) {
     a.qvbc32 = j->qvbc32;
     a.qvbc_len = j->sp_len;
   }
+  a.nyq = nyq_steps(j);
   if (j->fused) {
     TRY(assemble_fused(j, a));
     return j->want_masses ? mass_stage<R>(j) : MFX_OK;
@@ -1400,6 +1404,29 @@ static void free_job(mfx_job *j) {
 // get_unit_r_shifted(...)[axis] * lunit (grid_fft.hh:240-250,
 // particle_generator.hh:529-531); s includes the species' secondary-lattice
 // shift (particle_generator.hh:388-395)
+// The per-step angles at the Nyquist wavenumber of the job's sub-lattice
+// shifts (NyqSteps): the secondary species' global shift first, then the
+// steps between consecutive sub-lattices (particle_generator.hh:510-522).
+static NyqSteps nyq_steps(const mfx_job *j) {
+  NyqSteps t{};
+  t.active = j->d.noise_generator != MFX_NOISE_NGENIC;
+  const int N = j->N;
+  const double kny = double(N / 2) * 2.0 * M_PI / j->d.boxlen, dx = j->d.boxlen / N;
+  const bool second = j->lat_off[0] != 0.0 || j->lat_off[1] != 0.0 || j->lat_off[2] != 0.0;
+  for (int s = 0; s < j->ns && s < 4; ++s) {
+    int n = 0;
+    if (second) {
+      for (int ax = 0; ax < 3; ++ax) t.ang[s][n][ax] = j->lat_off[ax] * kny * dx;
+      ++n;
+    }
+    for (int q = 1; q <= s && n < 4; ++q, ++n)
+      for (int ax = 0; ax < 3; ++ax)
+        t.ang[s][n][ax] = (kShifts[j->d.lattice][q][ax] - kShifts[j->d.lattice][q - 1][ax]) * kny * dx;
+    t.nsteps[s] = n;
+  }
+  return t;
+}
+
 static int upload_shift_tables(mfx_job *j) {
   const int N = j->N;
   const mfx_job_desc *d = &j->d;

@@ -411,6 +411,49 @@ template <typename R> __global__ void __launch_bounds__(256) k_trunc_repad(Trunc
 //     with the per-sub-lattice phase shift of Grid_FFT::shift_field
 //     (grid_fft.hh:832-842, particle_generator.hh:510-522) folded in.
 // ---------------------------------------------------------------------------
+// Sub-lattice shifts as the reference applies them: one shift_field per
+// step (grid_fft.hh:832-842, particle_generator.hh:510-522), each an r2c,
+// a phase exp(i s.k dx) and a c2r.  The c2r keeps only the Hermitian part of
+// the kz = 0 and kz = N/2 planes, where a Nyquist index stands for both +k
+// and -k: there a step multiplies the Nyquist axes' phase by its real part,
+// cos(sum of their step angles), so the product over the steps, not the
+// phase of the total shift, is what reaches those modes.  Folding the phase
+// into the assembly keeps that product (nyq_phase).  Active only for noise
+// that fills the Nyquist planes (MUSIC1); NGenIC's potentials vanish there.
+struct NyqSteps {
+  int active;
+  int nsteps[4];         // per sub-lattice
+  double ang[4][4][3];   // [sub-lattice][step][axis]: step shift * Nyquist k * dx
+};
+
+// The phase a sub-lattice's modes on the projected planes receive; false
+// where the plain phase of the total shift applies.  ph: [ns][3][N]
+// exp(i s_a k_a dx) of the total shifts.
+template <typename R>
+__device__ __forceinline__ bool nyq_phase(const NyqSteps &t, const double2 *ph, int s, int i, int j, int k, int N,
+                                          R &er, R &ei) {
+  const int nh = N >> 1;
+  if (!t.active || (k != 0 && k != nh)) return false;
+  const bool nx = i == nh, ny = j == nh, nz = k == nh;
+  if (!(nx || ny || nz)) return false;
+  double c = 1.0;
+  for (int st = 0; st < t.nsteps[s]; ++st)
+    c *= cos((nx ? t.ang[s][st][0] : 0.0) + (ny ? t.ang[s][st][1] : 0.0) + (nz ? t.ang[s][st][2] : 0.0));
+  const double2 *p = ph + size_t(s) * 3 * N;
+  double re = c, im = 0.0;
+  auto mul = [&](double2 e) {
+    const double r = re * e.x - im * e.y;
+    im = re * e.y + im * e.x;
+    re = r;
+  };
+  if (!nx) mul(p[i]);
+  if (!ny) mul(p[N + j]);
+  if (!nz) mul(p[2 * N + k]);
+  er = R(re);
+  ei = R(im);
+  return true;
+}
+
 struct AsmArgs {
   const void *phi[3];   // phi1, phi2, phi3 (N-grid k-space, unscaled)
   const void *A3[3];
@@ -435,6 +478,7 @@ struct AsmArgs {
   const double *qvbc;
   const float *qvbc32;
   size_t qvbc_len;
+  NyqSteps nyq;
 };
 
 // the float coefficients of an AsmArgs from its FP64 ones
@@ -689,6 +733,7 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
 template <typename R>
 __device__ __forceinline__ void lattice_phase(const AsmArgs &a, int s, int i, int j, int k, R &er, R &ei) {
   const int N = a.N;
+  if (nyq_phase<R>(a.nyq, a.phase, s, i, j, k, N, er, ei)) return;
   if constexpr (sizeof(R) == 4) {
     if (a.phase32) {
       const float2 *ph = a.phase32 + size_t(s) * 3 * N;
@@ -761,6 +806,7 @@ struct MassArgs {
   void *mass;            // particle masses (double or float)
   int N, shift, nshift_total;
   double c_species, norm, scale;  // norm = 1/sqrt(N^3), scale = mass_factor / (n_s N^3)
+  NyqSteps nyq;
 };
 
 template <typename R>
@@ -779,9 +825,13 @@ __global__ void __launch_bounds__(256) k_mass_field(MassArgs a) {
     const int si = signed_idx(i, N), sj = signed_idx(j, N);
     const size_t n = size_t(si * si + sj * sj + k * k);
     const double r = (n > 0 && n < a.ratio_len) ? a.ratio[n] : 0.0;
-    const double2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
-    const double exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
-    const double er = exy_re * ez.x - exy_im * ez.y, ei = exy_re * ez.y + exy_im * ez.x;
+    double er, ei;
+    if (!nyq_phase<double>(a.nyq, a.phase, a.shift, i, j, k, N, er, ei)) {
+      const double2 ex = ph[i], ey = ph[N + j], ez = ph[2 * N + k];
+      const double exy_re = ex.x * ey.x - ex.y * ey.y, exy_im = ex.x * ey.y + ex.y * ey.x;
+      er = exy_re * ez.x - exy_im * ez.y;
+      ei = exy_re * ez.y + exy_im * ez.x;
+    }
     const C f = p1[idx];
     const double vr = r * double(f.x), vi = r * double(f.y);
     out[idx] = mkc<R>(R(vr * er - vi * ei), R(vr * ei + vi * er));

@@ -58,10 +58,12 @@ def test_music_normalised_noise(mfxlib, engine, oracle, fixing, inversion):
     assert rel_l2(j.field(mfxlib.FIELD_NOISE), ref) < 1e-13
 
 
-@pytest.mark.parametrize("order,lattice,plt", [(2, 0, False), (3, 1, False), (3, 2, True)])
+@pytest.mark.parametrize("order,lattice,plt", [(2, 0, False), (3, 1, False), (2, 2, False), (3, 2, True)])
 def test_music_pipeline_fp64(mfxlib, engine, oracle, order, lattice, plt):
-    """With PLT the kz = N/2 plane, which MUSIC1 noise fills, takes the same
-    Hermitian (odd-gradient) treatment as kz = 0."""
+    """MUSIC1 noise fills the Nyquist planes: with PLT the kz = N/2 plane takes
+    the same Hermitian (odd-gradient) treatment as kz = 0, and on FCC the
+    sub-lattice phases of the Nyquist modes on both planes follow the
+    reference's step-by-step shifts (three c2r projections, not one)."""
     n, seed = 64, 31337
     tab = engine.plt_table(lattice) if plt else None
     c = Case(mfxlib, n, 200.0, 30.0, order, 1, lattice=lattice, plt=tab)
