@@ -201,6 +201,27 @@ MFX_FAC(1152, 8, 12, 12);
 MFX_FAC(1536, 16, 12, 8);
 #undef MFX_FAC
 
+// The twiddle table of a length in shared memory: W_L^t for t < L, then one
+// table per later Stockham step laid out [r - 1][k] (W_L^(r k S) for the
+// step's r < R, k < NS), so that the lanes of a warp, which hold consecutive
+// butterflies j and so consecutive k = j mod NS, read consecutive words
+// instead of words r k S apart (bank conflicts in the flat table).  The
+// values are copies of the flat table's: the transforms are unchanged.
+template <int L> struct TwTab {
+  using F = Fac<L>;
+  static constexpr int n2 = (F::R2 - 1) * F::R1;                                 // step 2: NS = R1
+  static constexpr int n3 = F::steps == 3 ? (F::R3 - 1) * F::R1 * F::R2 : 0;  // step 3: NS = R1 R2
+  static constexpr int elems = (L + n2 + n3 + 1) & ~1;  // even: what follows stays 16-byte aligned
+  static constexpr int off(int NS) { return NS == F::R1 ? L : L + n2; }
+  // flat-table index of entry e (< n2 + n3) of the per-step tables
+  MFX_HD static int src(int e) {
+    const bool s2 = e < n2;
+    const int NS = s2 ? F::R1 : F::R1 * F::R2, R = s2 ? F::R2 : F::R3, x = s2 ? e : e - n2;
+    const int r = x / NS + 1, k = x - (r - 1) * NS;
+    return r * k * (L / (NS * R));
+  }
+};
+
 // Shared-memory tile of PP pencils of length L.  PF: pencil index fastest
 // (x/y passes, whose pencils are adjacent in global memory); otherwise each
 // pencil is contiguous, padded by one slot per 16 against bank conflicts.
@@ -225,7 +246,8 @@ template <int PP, int J, bool PF> MFX_HD void split(int t, int &q, int &j) {
 // writes y[(j / NS) NS R + (j mod NS) + r NS].  tw[t] = W_L^t.
 template <int L, int R, int NS, bool INV> struct Step {
   static constexpr int J = L / R;
-  template <class Ld> MFX_HD static void gather(int j, const Ld &ld, const float2 *tw, float2 *v) {
+  // TWS: tw holds the per-step tables of TwTab<L> after the flat one
+  template <bool TWS = false, class Ld> MFX_HD static void gather(int j, const Ld &ld, const float2 *tw, float2 *v) {
     static_for<R>([&](auto ri) {
       constexpr int r = decltype(ri)::value;
       v[r] = ld(j + r * J);
@@ -235,7 +257,7 @@ template <int L, int R, int NS, bool INV> struct Step {
       constexpr int S = L / (NS * R);
       static_for<R - 1>([&](auto ri) {
         constexpr int r = decltype(ri)::value + 1;
-        float2 w = tw[r * k * S];
+        float2 w = TWS ? tw[TwTab<L>::off(NS) + (r - 1) * NS + k] : tw[r * k * S];
         if (INV) w.y = -w.y;
         v[r] = cmul(v[r], w);
       });
@@ -281,7 +303,7 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
     int q, j;
     split<PP, S::J, PF>(t, q, j);
     const bool act = t < PP * S::J;
-    if (act) S::gather(j, [&](int n) { return ld(q, n); }, tw, v);
+    if (act) S::template gather<!PF>(j, [&](int n) { return ld(q, n); }, tw, v);
     // ld may read buf; an earlier call's last step may still read it
     if constexpr (B1 && (LDB || F::steps != 3)) __syncthreads();
     if (act) S::scatter(j, [&](int n, float2 x) { buf[T::at(q, n)] = x; }, v);
@@ -294,7 +316,7 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
     int q, j;
     split<PP, S::J, PF>(t, q, j);
     if (t < PP * S::J) {
-      S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw, v);
+      S::template gather<!PF>(j, [&](int n) { return buf[T::at(q, n)]; }, tw, v);
       S::scatter(j, [&](int n, float2 x) { buf2[T::at(q, n)] = x; }, v);
     }
     __syncthreads();
@@ -308,11 +330,11 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
     split<PP, S::J, PF>(t, q, j);
     if constexpr (SL) {
       const bool act = t < PP * S::J;
-      if (act) S::gather(j, [&](int n) { return src[T::at(q, n)]; }, tw, v);
+      if (act) S::template gather<!PF>(j, [&](int n) { return src[T::at(q, n)]; }, tw, v);
       __syncthreads();
       if (act) S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v);
     } else if (t < PP * S::J) {
-      S::gather(j, [&](int n) { return src[T::at(q, n)]; }, tw, v);
+      S::template gather<!PF>(j, [&](int n) { return src[T::at(q, n)]; }, tw, v);
       S::scatter(j, [&](int n, float2 x) { st(q, n, x); }, v);
     }
   }
@@ -497,6 +519,13 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 
 template <int M> __device__ __forceinline__ void load_tw(float2 *tw, const float2 *g) {
   for (int t = threadIdx.x; t < M; t += blockDim.x) tw[t] = g[t];
+  __syncthreads();
+}
+// the flat table and the per-step tables (TwTab<M>) of the non-PF transforms
+template <int M> __device__ __forceinline__ void load_tw_steps(float2 *tw, const float2 *g) {
+  using TT = TwTab<M>;
+  load_tw<M>(tw, g);
+  for (int e = threadIdx.x; e < TT::n2 + TT::n3; e += blockDim.x) tw[M + e] = tw[TT::src(e)];
   __syncthreads();
 }
 
@@ -821,7 +850,7 @@ template <int M, int RW, int G, int NIN, bool WIDE = false> struct ZR {
   static constexpr int threads = G * Fac<M>::maxJ;
   static constexpr int srow = NIN * D::Kh;  // float2 per row in the stage
   static constexpr size_t head = 32;        // two mbarriers and a status word
-  static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(RW * srow) * sizeof(float2) +
+  static constexpr size_t smem = head + size_t(TwTab<M>::elems) * sizeof(float2) + size_t(RW * srow) * sizeof(float2) +
                                  size_t(RW) * nin_pad * M * sizeof(float) +
                                  size_t(2 * Tile<M, G, false>::elems) * sizeof(float2);
   // CTAs per SM: by shared memory (228 KB per SM) and by at least 56
@@ -951,7 +980,7 @@ __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
   uint64_t *bar = reinterpret_cast<uint64_t *>(base);
   volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
   float2 *tw = reinterpret_cast<float2 *>(base + Z::head);
-  float2 *stage = tw + M;  // RW * srow
+  float2 *stage = tw + TwTab<M>::elems;  // RW * srow
   float *h = reinterpret_cast<float *>(stage + RW * Z::srow);
   float2 *buf = reinterpret_cast<float2 *>(h + RW * NP * M);
   float2 *buf2 = buf + Tile<M, G, false>::elems;
@@ -961,7 +990,7 @@ __device__ __forceinline__ void z_rows(const FArgs &a, const Src &sources) {
     *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  load_tw<M>(tw, a.tw);  // includes a barrier
+  load_tw_steps<M>(tw, a.tw);  // includes a barrier
   size_t g = blockIdx.x;
   if (threadIdx.x == 0 && g < ngroups) z_fetch<M, RW, NIN>(a, g, stage, bar);
 #pragma unroll 1
@@ -1061,7 +1090,7 @@ __device__ __forceinline__ void warp_step(const float2 *tw, int lane, const Ld &
 #pragma unroll
   for (int it = 0; it < I; ++it) {
     const int j = lane + 32 * it;
-    if (j < S::J) S::gather(j, ld, tw, v[it]);
+    if (j < S::J) S::template gather<true>(j, ld, tw, v[it]);
   }
   __syncwarp();
 #pragma unroll
@@ -1094,7 +1123,7 @@ template <int M, int NIN> struct ZW {
   static constexpr int threads = 32 * warps;
   static constexpr int padL = WP<M>::padL;
   static constexpr size_t head = 32;
-  static constexpr size_t smem = head + size_t(M) * sizeof(float2) + size_t(NIN * D::Kh) * sizeof(float2) +
+  static constexpr size_t smem = head + size_t(TwTab<M>::elems) * sizeof(float2) + size_t(NIN * D::Kh) * sizeof(float2) +
                                  size_t(NPI * padL) * sizeof(float2);
   // CTAs per SM by shared memory and by about 168 registers a thread (a lane
   // holds up to three butterflies of a step; 128 spilled in the 2LPT pass)
@@ -1113,7 +1142,7 @@ __device__ __forceinline__ void z_rows_w(const FArgs &a, const Src &sources) {
   uint64_t *bar = reinterpret_cast<uint64_t *>(base);
   volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
   float2 *tw = reinterpret_cast<float2 *>(base + Z::head);
-  float2 *stage = tw + M;           // [c][Kh]
+  float2 *stage = tw + TwTab<M>::elems;  // [c][Kh]
   float2 *h = stage + NIN * D::Kh;  // pencil p at h + p * padL (WP layout)
   const size_t ngroups = size_t(M) * M;
   if (threadIdx.x == 0) {
@@ -1121,7 +1150,7 @@ __device__ __forceinline__ void z_rows_w(const FArgs &a, const Src &sources) {
     *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  load_tw<M>(tw, a.tw);  // includes a barrier
+  load_tw_steps<M>(tw, a.tw);  // includes a barrier
   const int warp = int(threadIdx.x) >> 5, lane = int(threadIdx.x) & 31;
   size_t g = blockIdx.x;
   if (threadIdx.x == 0 && g < ngroups) z_fetch<M, 1, NIN>(a, g, stage, bar);

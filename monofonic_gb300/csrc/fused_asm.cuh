@@ -114,7 +114,7 @@ template <int N> struct FA {
   static constexpr size_t head = 32;
   // ASM3: the components land in the tile buffer the transform's last step
   // reads (in place) or has finished with, so no buffer of their own
-  static constexpr size_t s3 = head + size_t(N) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
+  static constexpr size_t s3 = head + size_t(TwTab<N>::elems) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
                                size_t(nbuf * Tile<N, 3 * RW, false>::elems) * sizeof(float2);
   // CTAs per SM the ASM3 registers are sized for (about 104 a thread), no more
   // than shared memory allows
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(FA<N>::t3, FA<N>::minb3) k_fa_z(FAArgs a) {
   uint64_t *bar = reinterpret_cast<uint64_t *>(base);
   volatile int *flag = reinterpret_cast<volatile int *>(base + 16);
   float2 *tw = reinterpret_cast<float2 *>(base + F::head);
-  float2 *stage = tw + N;                        // [w][c][Kh]
+  float2 *stage = tw + TwTab<N>::elems;          // [w][c][Kh]
   float2 *buf = stage + RW * 6 * Kh;
   float2 *buf2 = F::nbuf == 2 ? buf + Tile<N, G, false>::elems : nullptr;
   // [w][pair][z]: written by the transform's last step into buf, which that
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(FA<N>::t3, FA<N>::minb3) k_fa_z(FAArgs a) {
     *flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  load_tw<N>(tw, a.tw);
+  load_tw_steps<N>(tw, a.tw);
   size_t g = blockIdx.x;
   if (threadIdx.x == 0 && g < ngroups) fetch(g);
   const size_t n3 = size_t(N) * N * N, pbase = size_t(a.shift) * n3;

@@ -37,20 +37,20 @@ constexpr size_t kFFSmemMax = 227 * 1024;
 // memory allow (one CTA per SM), the fewest rounds per row and, among those,
 // the fewest idle pencils.  For the long padded lengths, whose narrow shapes
 // leave only a few warps per SM.
-constexpr size_t zw_smem(int M, int NIN, int G) {
+constexpr size_t zw_smem(int M, int NIN, int G, int twe) {
   const size_t kh = size_t(M / 3), np = size_t(NIN + (NIN & 1));
-  return 32 + size_t(M) * 8 + NIN * kh * 8 + np * size_t(M) * 4 + 2 * size_t(G) * size_t(M + (M >> 4)) * 8;
+  return 32 + size_t(twe) * 8 + NIN * kh * 8 + np * size_t(M) * 4 + 2 * size_t(G) * size_t(M + (M >> 4)) * 8;
 }
-constexpr int zw_pick(int M, int NIN, int maxJ) {
+constexpr int zw_pick(int M, int NIN, int maxJ, int twe) {
   const int npi = (NIN + (NIN & 1)) / 2;
   int gmax = 0;
-  for (int g = 1; g <= npi && g * maxJ <= 704 && zw_smem(M, NIN, g) <= kFFSmemMax; ++g) gmax = g;
+  for (int g = 1; g <= npi && g * maxJ <= 704 && zw_smem(M, NIN, g, twe) <= kFFSmemMax; ++g) gmax = g;
   if (gmax == 0) return 0;
   const int rounds = (npi + gmax - 1) / gmax;
   return (npi + rounds - 1) / rounds;
 }
 template <int M, int NIN> struct ZGW {
-  static constexpr int G = zw_pick(M, NIN, Fac<M>::maxJ);
+  static constexpr int G = zw_pick(M, NIN, Fac<M>::maxJ, TwTab<M>::elems);
 };
 
 template <int M, int RW> constexpr bool ff_z_fits() {

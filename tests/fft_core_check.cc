@@ -25,7 +25,7 @@ static void host_pencil_fft(std::vector<float2> &data, const std::vector<float2>
     for (int t = 0; t < PP * S::J; ++t) {
       int q, j;
       split<PP, S::J, PF>(t, q, j);
-      S::gather(j, [&](int n) { return data[size_t(q) * L + n]; }, tw.data(), &regs[size_t(t) * RMAX]);
+      S::template gather<!PF>(j, [&](int n) { return data[size_t(q) * L + n]; }, tw.data(), &regs[size_t(t) * RMAX]);
     }
     for (int t = 0; t < PP * S::J; ++t) {
       int q, j;
@@ -39,7 +39,7 @@ static void host_pencil_fft(std::vector<float2> &data, const std::vector<float2>
     for (int t = 0; t < PP * S::J; ++t) {
       int q, j;
       split<PP, S::J, PF>(t, q, j);
-      S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw.data(), &regs[size_t(t) * RMAX]);
+      S::template gather<!PF>(j, [&](int n) { return buf[T::at(q, n)]; }, tw.data(), &regs[size_t(t) * RMAX]);
     }
     for (int t = 0; t < PP * S::J; ++t) {
       int q, j;
@@ -54,7 +54,7 @@ static void host_pencil_fft(std::vector<float2> &data, const std::vector<float2>
     for (int t = 0; t < PP * S::J; ++t) {
       int q, j;
       split<PP, S::J, PF>(t, q, j);
-      S::gather(j, [&](int n) { return buf[T::at(q, n)]; }, tw.data(), &regs[size_t(t) * RMAX]);
+      S::template gather<!PF>(j, [&](int n) { return buf[T::at(q, n)]; }, tw.data(), &regs[size_t(t) * RMAX]);
     }
     for (int t = 0; t < PP * S::J; ++t) {
       int q, j;
@@ -65,9 +65,11 @@ static void host_pencil_fft(std::vector<float2> &data, const std::vector<float2>
 }
 
 template <int L> static int run(int pp, int inv, int pf, std::vector<float2> &data) {
-  std::vector<float2> tw(L);
+  // the flat table and, after it, the per-step tables the non-PF (z) transforms read
+  std::vector<float2> tw(TwTab<L>::elems);
   for (int t = 0; t < L; ++t)
     tw[t] = make_float2(float(std::cos(-2.0 * M_PI * t / L)), float(std::sin(-2.0 * M_PI * t / L)));
+  for (int e = 0; e < TwTab<L>::n2 + TwTab<L>::n3; ++e) tw[L + e] = tw[TwTab<L>::src(e)];
   if (pp != 3) return 3;
   if (inv && pf) host_pencil_fft<L, 3, true, true>(data, tw);
   if (inv && !pf) host_pencil_fft<L, 3, false, true>(data, tw);
