@@ -622,12 +622,19 @@ def run_serving(args):
         tuned[s["ngrid"]] = list(j.autotune())
         j.close()
     srv = mfx.Server(eng, max_inflight=args.inflight)
-    srv.set_policy(bypass=True, bypass_age_ms=100.0, size_priority=not args.no_priority)
+    srv.set_policy(bypass=True, bypass_age_ms=args.bypass_age_ms, size_priority=not args.no_priority,
+                   largest_first=args.largest_first)
     # warm the plan pool and the memory pool with one pass over the size classes
     warm = {}
     for s in specs:
         warm.setdefault((s["ngrid"], s["order"], s["lattice"]), s)
     drain(srv, {srv.submit(s): 0 for s in warm.values()}, parts)
+    # each size class alone through the server (submit -> done, nothing else
+    # queued or running): the latency floor of the sweep's percentiles
+    alone_ms = {}
+    for key, s in sorted(warm.items()):
+        lat1, _ = drain(srv, {srv.submit(s): 0}, parts)
+        alone_ms["%d/%d/%s" % (key[0], key[1], "sc bcc fcc".split()[key[2]])] = float(lat1[0])
 
     # batched: every request queued at once
     t0 = time.perf_counter()
@@ -653,11 +660,11 @@ def run_serving(args):
                     time.sleep(d)
                 h = srv.submit(s)
                 with lock:
-                    tickets[h] = parts[q]
+                    tickets[h] = q
 
         th = threading.Thread(target=producer)
         th.start()
-        lat, got = [], 0
+        lat, got, by_size = [], 0, {}
         while th.is_alive() or tickets:
             with lock:
                 cur = dict(tickets)
@@ -666,8 +673,10 @@ def run_serving(args):
                     srv.wait(h, 0)
                 except Exception:
                     continue
-                lat.append(srv.times(h)[1])
-                got += cur[h]
+                ms = srv.times(h)[1]
+                lat.append(ms)
+                by_size.setdefault(specs[cur[h]]["ngrid"], []).append(ms)
+                got += parts[cur[h]]
                 srv.release(h)
                 with lock:
                     tickets.pop(h)
@@ -677,7 +686,9 @@ def run_serving(args):
         return {"load": load, "arrival_rate_jobs_per_s": rate, "requests": len(lat), "span_s": span,
                 "throughput": got / span, "throughput_vs_batched": got / span / sat_tput,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "max_ms": float(np.max(lat))}
+                "max_ms": float(np.max(lat)),
+                "p50_ms_by_grid": {str(n): float(np.percentile(v, 50)) for n, v in sorted(by_size.items())},
+                "p99_ms_by_grid": {str(n): float(np.percentile(v, 99)) for n, v in sorted(by_size.items())}}
 
     clocks = Clocks(0, clock_csv("clocks_serving.csv"))
     sweep = [offered(load, 11 + q) for q, load in enumerate(args.loads)]
@@ -711,7 +722,8 @@ def run_serving(args):
         "data": "synthetic (NGenIC white noise, seeds 1..%d; mix from default_rng(7))" % len(specs),
         "config": {"workload": "serve: %d requests per load point, N in {64..384}, order 1-3, SC/BCC/FCC (+PLT), "
                                "FP32-compensated" % len(specs), "max_inflight": args.inflight,
-                   "admission": "oldest job that fits; a head older than 100 ms is not passed",
+                   "admission": ("largest" if args.largest_first else "oldest") + " queued job that fits; a head "
+                                "older than %g ms is not passed" % args.bypass_age_ms,
                    "stream_priority": "by footprint" if not args.no_priority else "default for every job",
                    "particles_per_point": sum(parts), "tiles_per_size": {str(k): v for k, v in tuned.items()}},
         "p99_target_ms": target,
@@ -722,6 +734,7 @@ def run_serving(args):
                     "p50_ms": float(np.percentile(sat_lat, 50)), "p99_ms": float(np.percentile(sat_lat, 99)),
                     "mode": "every request queued at once"},
         "sweep": sweep,
+        "alone_ms": alone_ms,
         "fp64_serial": ({"value": serial_parts / serial_s, "unit": "particles/s", "span_s": serial_s,
                          "requests": len(specs[:args.fp64_sample])} if serial_s else None),
         "clocks": clk,
@@ -898,6 +911,8 @@ def main():
     ap.add_argument("--fp64-sample", type=int, default=48, help="serve: requests run serially in FP64")
     ap.add_argument("--no-priority", action="store_true", help="serve: every job at the default stream priority")
     ap.add_argument("--inflight", type=int, default=4, help="serve: max jobs in flight")
+    ap.add_argument("--largest-first", action="store_true", help="serve: admit the largest queued job that fits")
+    ap.add_argument("--bypass-age-ms", type=float, default=100.0, help="serve: age after which the head is not passed")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")

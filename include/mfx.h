@@ -328,7 +328,9 @@ int mfx_server_destroy(mfx_server *s);
    may pass a head that has waited at most bypass_age_ms.  Jobs run on CUDA
    streams whose priority grows with their footprint (one level per factor of
    four above 64 MB): the largest requests set the latency tail.  bypass bit 1
-   set: every job at the default priority. */
+   set: every job at the default priority.  bypass bit 2 set (with bit 0):
+   while the head may be passed, admit the largest queued job that fits
+   instead of the oldest. */
 int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms);
 
 /* Allocation-free white-noise fill (no counterpart in the reference): writes

@@ -2571,6 +2571,7 @@ struct mfx_server {
   bool bypass = true;
   double bypass_age_ms = 100.0;
   bool size_priority = true;  // stream priority grows with the job's footprint
+  bool largest_first = false; // admit the largest queued job that fits, not the oldest
   std::mutex mu;
   std::condition_variable cv;
   std::deque<Ticket *> queue;     // waiting for admission
@@ -2597,9 +2598,19 @@ static int pick_admission(mfx_server *s, clk::time_point now) {
     in_use = s->eng->in_use;
   }
   const bool head_may_be_passed = s->bypass && ms_between(s->queue.front()->t_submit, now) <= s->bypass_age_ms;
+  const size_t free_bytes = s->eng->budget - std::min(s->eng->budget, in_use + s->reserved);
+  if (s->largest_first && head_may_be_passed) {
+    // the largest jobs set the latency tail: admit the largest that fits
+    // (the oldest among equals) while the head is young enough to be passed
+    int best = -1;
+    for (size_t q = 0; q < s->queue.size(); ++q)
+      if (s->queue[q]->footprint <= free_bytes && (best < 0 || s->queue[q]->footprint > s->queue[size_t(best)]->footprint))
+        best = int(q);
+    return best;
+  }
   for (size_t q = 0; q < s->queue.size(); ++q) {
     if (q > 0 && !head_may_be_passed) break;
-    if (in_use + s->reserved + s->queue[q]->footprint <= s->eng->budget) return int(q);
+    if (s->queue[q]->footprint <= free_bytes) return int(q);
   }
   return -1;
 }
@@ -2710,6 +2721,7 @@ int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms) {
   s->bypass = bypass != 0;
   s->bypass_age_ms = bypass_age_ms;
   s->size_priority = (bypass & 2) == 0;  // bit 1: every job at the default priority
+  s->largest_first = (bypass & 4) != 0;  // bit 2: largest queued job first
   s->cv.notify_all();
   return MFX_OK;
 }

@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(KEEP ? FA<N>::t1k : FA<N>::t1, min_blocks(KEEP
             }
           }
           float er, ei;
-          lattice_phase<float>(a.as, a.shift + s, i, j, kz, er, ei);
+          lattice_phase<float, false>(a.as, a.shift + s, i, j, kz, er, ei);
 #pragma unroll
           for (int c = 0; c < CG; ++c) {
             const float2 v = v6[c];
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
           for (int t = threadIdx.x; t < N * P; t += NT) {
             const int i = t / P, p = t - (t / P) * P;
             float er, ei;
-            lattice_phase<float>(a.as, a.shift + s, i, j, kz0 + p, er, ei);
+            lattice_phase<float, false>(a.as, a.shift + s, i, j, kz0 + p, er, ei);
             const float2 v = pv[c * (N * P) + t];
             buf[T::at(p, i)] = make_float2(v.x * er - v.y * ei, v.x * ei + v.y * er);
           }

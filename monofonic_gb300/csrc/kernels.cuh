@@ -730,10 +730,14 @@ __device__ __forceinline__ void asm_mode(const AsmArgs &a, int i, int j, int k, 
 
 // the phase of sub-lattice s at mode (i, j, k): exp(i s.k dx) (grid_fft.hh:836-839);
 // the FP32 form multiplies the float tables (FP64 arithmetic is slow here)
-template <typename R>
+// NYQ = false: the caller's potentials vanish on every Nyquist index (the
+// FP32 form's fused assembly, which runs with NGenIC noise only)
+template <typename R, bool NYQ = true>
 __device__ __forceinline__ void lattice_phase(const AsmArgs &a, int s, int i, int j, int k, R &er, R &ei) {
   const int N = a.N;
-  if (nyq_phase<R>(a.nyq, a.phase, s, i, j, k, N, er, ei)) return;
+  if constexpr (NYQ) {
+    if (nyq_phase<R>(a.nyq, a.phase, s, i, j, k, N, er, ei)) return;
+  }
   if constexpr (sizeof(R) == 4) {
     if (a.phase32) {
       const float2 *ph = a.phase32 + size_t(s) * 3 * N;

@@ -105,25 +105,49 @@ __device__ __forceinline__ void mt_twist(uint32_t *x, int lane) {
 // order of the sequential C code (no contraction): u = 1 - U1,
 // v = 1.7156 (U2 - 1/2), x = u - s, y = |v| - t, Q = x^2 + y (a y - b x);
 // accepted when Q < r1, or Q <= r2 and v^2 <= -4 u^2 ln u.  A float estimate
-// of Q (error below 1e-6 here) settles the pairs far from both bounds; the
-// rest take the exact double test.
-__device__ __forceinline__ bool leva_accept(uint32_t w1, uint32_t w2, double &u, double &v) {
-  constexpr double s = 0.449871, t = -0.386595, a = 0.19600, b = 0.25472, r1 = 0.27597, r2 = 0.27846;
-  constexpr double two32 = 1.0 / 4294967296.0;
-  u = __dsub_rn(1.0, double(w1) * two32);
-  v = __dmul_rn(double(w2) * two32 - 0.5, 1.7156);
+// of Q (error below 1e-6 here), from u and v formed in float straight from
+// the integers, settles the pairs far from both bounds; the rest take the
+// exact double test.
+constexpr double kS = 0.449871, kT = -0.386595, kA = 0.19600, kB = 0.25472, kR1 = 0.27597, kR2 = 0.27846;
+constexpr double kTwo32 = 1.0 / 4294967296.0;
+
+// u and v in float: 1 - U1 = (2^32 - w1) 2^-32 and U2 - 1/2 = (w2 - 2^31) 2^-32
+// keep their relative precision (a float U1 near 1 would not)
+__device__ __forceinline__ void leva_uv_f(uint32_t w1, uint32_t w2, float &uf, float &vf) {
+  uf = float(0x100000000ull - uint64_t(w1)) * float(kTwo32);
+  vf = float(int32_t(w2 - 0x80000000u)) * float(kTwo32) * 1.7156f;
+}
+__device__ __forceinline__ void leva_uv_d(uint32_t w1, uint32_t w2, double &u, double &v) {
+  u = __dsub_rn(1.0, double(w1) * kTwo32);
+  v = __dmul_rn(double(w2) * kTwo32 - 0.5, 1.7156);
+}
+__device__ __forceinline__ bool leva_accept(uint32_t w1, uint32_t w2, float uf, float vf) {
   {
-    const float uf = float(u), vf = float(v);
-    const float xf = uf - float(s), yf = fabsf(vf) - float(t);
-    const float qf = xf * xf + yf * (float(a) * yf - float(b) * xf);
-    if (qf < float(r1) - 1e-5f) return true;
-    if (qf > float(r2) + 1e-5f) return false;
+    const float xf = uf - float(kS), yf = fabsf(vf) - float(kT);
+    const float qf = xf * xf + yf * (float(kA) * yf - float(kB) * xf);
+    if (qf < float(kR1) - 1e-5f) return true;
+    if (qf > float(kR2) + 1e-5f) return false;
   }
-  const double x = __dsub_rn(u, s), y = __dsub_rn(fabs(v), t);
-  const double q = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, __dsub_rn(__dmul_rn(a, y), __dmul_rn(b, x))));
-  if (q < r1) return true;
-  if (q > r2) return false;
+  double u, v;
+  leva_uv_d(w1, w2, u, v);
+  const double x = __dsub_rn(u, kS), y = __dsub_rn(fabs(v), kT);
+  const double q = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, __dsub_rn(__dmul_rn(kA, y), __dmul_rn(kB, x))));
+  if (q < kR1) return true;
+  if (q > kR2) return false;
   return !(__dmul_rn(v, v) > __dmul_rn(__dmul_rn(__dmul_rn(-4.0, u), u), log(u)));
+}
+
+// The accepted pair's normal v / u: the exact double quotient for the FP64
+// form; for the FP32 form the float quotient of the float u and v (within
+// two units in the last place of the double quotient rounded to float)
+template <typename R> __device__ __forceinline__ R leva_value(uint32_t w1, uint32_t w2, float uf, float vf);
+template <> __device__ __forceinline__ double leva_value<double>(uint32_t w1, uint32_t w2, float, float) {
+  double u, v;
+  leva_uv_d(w1, w2, u, v);
+  return v / u;
+}
+template <> __device__ __forceinline__ float leva_value<float>(uint32_t, uint32_t, float uf, float vf) {
+  return vf / uf;
 }
 
 struct CubeArgs {
@@ -163,13 +187,19 @@ template <typename R> __global__ void __launch_bounds__(32) k_music_cubes(CubeAr
     for (int p0 = 0; p0 < kMtN / 2 && produced < total; p0 += 32) {
       const int p = p0 + lane;
       bool acc = false;
-      double u = 1.0, v = 0.0;
-      if (p < kMtN / 2) acc = leva_accept(mt_temper(x[2 * p]), mt_temper(x[2 * p + 1]), u, v);
+      uint32_t w1 = 0, w2 = 0;
+      float uf = 1.f, vf = 0.f;
+      if (p < kMtN / 2) {
+        w1 = mt_temper(x[2 * p]);
+        w2 = mt_temper(x[2 * p + 1]);
+        leva_uv_f(w1, w2, uf, vf);
+        acc = leva_accept(w1, w2, uf, vf);
+      }
       const unsigned m = __ballot_sync(0xffffffffu, acc);
       const int c = produced + __popc(m & lt);
       if (acc && c < total) {
         const int ii = c / cs2, jj = (c / cs) % cs, kk = c % cs;
-        base[(size_t(ii) * a.N + jj) * size_t(a.row) + kk] = R(v / u);
+        base[(size_t(ii) * a.N + jj) * size_t(a.row) + kk] = leva_value<R>(w1, w2, uf, vf);
       }
       produced += __popc(m);
     }

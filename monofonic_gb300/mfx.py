@@ -641,13 +641,17 @@ class Server:
     def wait(self, ticket: int, timeout_ms: int = -1):
         check(load().mfx_server_wait(self._h, ticket, timeout_ms))
 
-    def set_policy(self, bypass: bool = True, bypass_age_ms: float = 100.0, size_priority: bool = True):
+    def set_policy(self, bypass: bool = True, bypass_age_ms: float = 100.0, size_priority: bool = True,
+                   largest_first: bool = False):
         """Admission order: a later job that fits may pass a head that has
         waited at most bypass_age_ms (bypass), or strict first-in first-out;
-        size_priority: larger jobs on higher-priority streams."""
+        largest_first: while the head may be passed, the largest queued job
+        that fits goes first; size_priority: larger jobs on higher-priority
+        streams."""
         L = load()
         L.mfx_server_set_policy.argtypes = [C.c_void_p, C.c_int, C.c_double]
-        check(L.mfx_server_set_policy(self._h, int(bool(bypass)) | (0 if size_priority else 2), float(bypass_age_ms)))
+        flags = int(bool(bypass)) | (0 if size_priority else 2) | (4 if largest_first else 0)
+        check(L.mfx_server_set_policy(self._h, flags, float(bypass_age_ms)))
 
     def times(self, ticket: int):
         q, l = C.c_double(), C.c_double()

@@ -179,3 +179,34 @@ def test_server_age_limit_stops_bypassing_an_old_head(mfxlib):
     srv.release(ts)
     srv.close()
     eng.close()
+
+
+def test_server_largest_first_admission(mfxlib, engine):
+    """With largest-first admission (and a head young enough to be passed), a
+    large request queued behind small ones is admitted first once a slot
+    frees; first-in first-out admits the small ones first.  Results equal the
+    jobs run alone."""
+    blocker_spec = spec(mfxlib, 128, 300.0, 24.0, 3, 900, precision=mfxlib.FP64)
+    small_specs = [spec(mfxlib, 16, 25.0, 24.0, 1, 910 + q) for q in range(2)]
+    big_spec = spec(mfxlib, 64, 100.0, 24.0, 2, 920)
+    for largest_first in (True, False):
+        srv = mfxlib.Server(engine, max_inflight=1)
+        srv.set_policy(bypass=True, bypass_age_ms=60000.0, largest_first=largest_first)
+        # all three queue behind the blocker (a 128^3 3LPT job in FP64)
+        blocker = srv.submit(blocker_spec)
+        small = [srv.submit(sp) for sp in small_specs]
+        big = srv.submit(big_spec)
+        for t in [blocker] + small + [big]:
+            srv.wait(t, 60000)
+        qb = srv.times(big)[0]
+        qs = [srv.times(t)[0] for t in small]
+        if largest_first:
+            assert all(qb < q for q in qs), (qb, qs)
+        else:
+            assert all(qb > q for q in qs), (qb, qs)
+        got = srv.job(big).particles()
+        for a, b in zip(got, alone(mfxlib, engine, big_spec)):
+            assert np.array_equal(a, b)
+        for t in [blocker] + small + [big]:
+            srv.release(t)
+        srv.close()
