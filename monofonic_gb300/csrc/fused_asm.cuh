@@ -29,6 +29,14 @@ struct FAArgs {
   float2 *q[6];           // component fields [N][N][N/2] of sub-lattice `shift` (ASM2 in place, ASM3 input)
   float2 *qx[24];         // ASM1 output: component c of sub-lattice shift + s at qx[6 s + c], s < nsub
   int nsub;               // sub-lattices ASM1 emits from one assembly of each mode (1 unless FA::keep)
+  // x-only phases: ASM1 applies only the x factor of the sub-lattice phase,
+  // that of sub-lattice xsub[s] for output s, and ASM2 the y and z factors
+  // (yzphase).  The phase factors per axis commute with the other axes'
+  // transforms, so sub-lattices with equal x-shifts share one ASM1 output
+  // (FCC: two instead of four).
+  int xonly, xsub[4];
+  int yzphase;
+  const float2 *qin[6];   // ASM2 input when not in place (null: q)
   int halves;             // ASM1 in halves (tiles of 8 pencils; FA::halves), with nsub > 1
   const float2 *tw;       // W_N^t, t < N
   int *status;            // set when a bounded wait ran out
@@ -191,7 +199,13 @@ __global__ void __launch_bounds__(KEEP ? FA<N>::t1k : FA<N>::t1, min_blocks(KEEP
             }
           }
           float er, ei;
-          lattice_phase<float, false>(a.as, a.shift + s, i, j, kz, er, ei);
+          if (a.xonly) {
+            const float2 e = a.as.phase32[size_t(a.xsub[s]) * 3 * N + i];
+            er = e.x;
+            ei = e.y;
+          } else {
+            lattice_phase<float, false>(a.as, a.shift + s, i, j, kz, er, ei);
+          }
 #pragma unroll
           for (int c = 0; c < CG; ++c) {
             const float2 v = v6[c];
@@ -254,7 +268,13 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
           for (int t = threadIdx.x; t < N * P; t += NT) {
             const int i = t / P, p = t - (t / P) * P;
             float er, ei;
-            lattice_phase<float, false>(a.as, a.shift + s, i, j, kz0 + p, er, ei);
+            if (a.xonly) {
+              const float2 e = a.as.phase32[size_t(a.xsub[s]) * 3 * N + i];
+              er = e.x;
+              ei = e.y;
+            } else {
+              lattice_phase<float, false>(a.as, a.shift + s, i, j, kz0 + p, er, ei);
+            }
             const float2 v = pv[c * (N * P) + t];
             buf[T::at(p, i)] = make_float2(v.x * er - v.y * ei, v.x * ei + v.y * er);
           }
@@ -269,25 +289,42 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
   }
 }
 
-// ASM2: inverse y transforms of the six components, in place
-template <int N>
+// ASM2: inverse y transforms of the six components, in place (or from qin).
+// YZ: the y and z factors of sub-lattice a.shift's phase applied on input
+// (x-only ASM1), the y factors staged in shared memory after the tile areas
+template <int N, bool YZ>
 __global__ void __launch_bounds__(FA<N>::t2, FA<N>::minb2) k_fa_y(FAArgs a) {
   using F = FA<N>;
   constexpr int P = F::P2, KB = F::Kh / P;
   float2 *tw = ff_smem(), *buf = tw + N, *buf2 = buf + (F::nbuf == 2 ? Tile<N, P, true>::elems : 0),
          *stage = buf + F::nbuf * Tile<N, P, true>::elems;
-  load_tw<N>(tw, a.tw);
+  float2 *phy = stage + 2 * N * P;  // YZ: [N] y factors of the sub-lattice phase
+  if constexpr (YZ)
+    for (int t = threadIdx.x; t < N; t += blockDim.x) phy[t] = a.as.phase32[size_t(a.shift) * 3 * N + N + t];
+  load_tw<N>(tw, a.tw);  // includes a barrier
   xy_units(
       unsigned(N * KB * 6), N * P, stage,
       [&](unsigned u, float2 *st) {
         const unsigned c = u % 6, t = u / 6, x = t / KB, kz0 = (t % KB) * P;
-        stage_rows<P, N, 16>(st, a.q[c] + (x * N * F::Kh + kz0), unsigned(F::Kh));
+        const float2 *src = a.qin[c] ? a.qin[c] : a.q[c];
+        stage_rows<P, N, 16>(st, src + (x * N * F::Kh + kz0), unsigned(F::Kh));
       },
       [&](unsigned u, const float2 *st) {
         const unsigned c = u % 6, t = u / 6, x = t / KB, kz0 = (t % KB) * P;
         float2 *out = a.q[c] + (x * N * F::Kh + kz0);
+        const float2 *phz = a.as.phase32 + size_t(a.shift) * 3 * N + 2 * N + kz0;
         pencil_fft<N, P, true, true>(
-            buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
+            buf, buf2, tw,
+            [&](int q, int n) {
+              const float2 v = st[n * P + q];
+              if constexpr (!YZ) {
+                return v;
+              } else {
+                const float2 ey = phy[n], ez = phz[q];
+                const float er = ey.x * ez.x - ey.y * ez.y, ei = ey.x * ez.y + ey.y * ez.x;
+                return make_float2(v.x * er - v.y * ei, v.x * ei + v.y * er);
+              }
+            },
             [&](int q, int y, float2 v) { out[unsigned(y) * F::Kh + q] = v; });
       });
 }

@@ -232,7 +232,10 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
         }
         break;
       case FA_Y:
-        MFX_FF_PERSISTENT((k_fa_y<N>), F::t2, F::s2, size_t(N) * (F::Kh / F::P2) * 6, s, a);
+        if (a.yzphase)
+          MFX_FF_PERSISTENT((k_fa_y<N, true>), F::t2, F::s2 + size_t(N) * 8, size_t(N) * (F::Kh / F::P2) * 6, s, a);
+        else
+          MFX_FF_PERSISTENT((k_fa_y<N, false>), F::t2, F::s2, size_t(N) * (F::Kh / F::P2) * 6, s, a);
         break;
       case FA_Z:
         MFX_FF_PERSISTENT((k_fa_z<N>), F::t3, F::s3, size_t(N) * N / F::RW, s, a);
