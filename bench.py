@@ -623,7 +623,7 @@ def run_serving(args):
         j.close()
     srv = mfx.Server(eng, max_inflight=args.inflight)
     srv.set_policy(bypass=True, bypass_age_ms=args.bypass_age_ms, size_priority=not args.no_priority,
-                   largest_first=args.largest_first)
+                   largest_first=args.largest_first, small_first=not args.large_priority)
     # warm the plan pool and the memory pool with one pass over the size classes
     warm = {}
     for s in specs:
@@ -724,7 +724,8 @@ def run_serving(args):
                                "FP32-compensated" % len(specs), "max_inflight": args.inflight,
                    "admission": ("largest" if args.largest_first else "oldest") + " queued job that fits; a head "
                                 "older than %g ms is not passed" % args.bypass_age_ms,
-                   "stream_priority": "by footprint" if not args.no_priority else "default for every job",
+                   "stream_priority": ("default for every job" if args.no_priority else
+                                       "by footprint, " + ("largest" if args.large_priority else "smallest") + " first"),
                    "particles_per_point": sum(parts), "tiles_per_size": {str(k): v for k, v in tuned.items()}},
         "p99_target_ms": target,
         "throughput_at_target_vs_batched": best["throughput_vs_batched"] if best else None,
@@ -904,14 +905,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fcc768", choices=sorted(WORKLOADS) + ["ensemble64", "serve"])
-    ap.add_argument("--requests", type=int, default=500, help="serve: requests per load point")
+    ap.add_argument("--requests", type=int, default=1000, help="serve: requests per load point")
     ap.add_argument("--loads", type=lambda v: [float(x) for x in v.split(",")],
                     default=[0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1], help="serve: offered loads / batched job rate")
     ap.add_argument("--p99-target-ms", type=float, default=100.0, help="serve: stated p99 job latency target")
     ap.add_argument("--fp64-sample", type=int, default=48, help="serve: requests run serially in FP64")
     ap.add_argument("--no-priority", action="store_true", help="serve: every job at the default stream priority")
-    ap.add_argument("--inflight", type=int, default=4, help="serve: max jobs in flight")
+    ap.add_argument("--inflight", type=int, default=2, help="serve: max jobs in flight")
     ap.add_argument("--largest-first", action="store_true", help="serve: admit the largest queued job that fits")
+    ap.add_argument("--large-priority", action="store_true", help="serve: the largest jobs on the highest priority")
     ap.add_argument("--bypass-age-ms", type=float, default=100.0, help="serve: age after which the head is not passed")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

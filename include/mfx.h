@@ -326,11 +326,13 @@ int mfx_server_release(mfx_server *s, uint64_t ticket);
 int mfx_server_destroy(mfx_server *s);
 /* bypass bit 0 clear: strict first-in first-out admission; set: a later job
    may pass a head that has waited at most bypass_age_ms.  Jobs run on CUDA
-   streams whose priority grows with their footprint (one level per factor of
-   four above 64 MB): the largest requests set the latency tail.  bypass bit 1
-   set: every job at the default priority.  bypass bit 2 set (with bit 0):
-   while the head may be passed, admit the largest queued job that fits
-   instead of the oldest. */
+   streams whose priority follows their footprint (one level per factor of
+   four above 64 MB), the smallest on the highest: jobs on the GPU together
+   run kernel by kernel, and ahead of the large jobs' long kernels the small
+   ones finish in about their own time.  bypass bit 1 set: every job at the
+   default priority; bit 3 set: the largest jobs on the highest priority.
+   bypass bit 2 set (with bit 0): while the head may be passed, admit the
+   largest queued job that fits instead of the oldest. */
 int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms);
 
 /* Allocation-free white-noise fill (no counterpart in the reference): writes

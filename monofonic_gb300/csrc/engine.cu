@@ -938,6 +938,45 @@ static int assemble_fused(mfx_job *j, const AsmArgs &as) {
     return MFX_OK;
   };
   const double in_b = (order == 1 ? 1.0 : (order == 2 ? 2.0 : 6.0)) * nfb;
+  // sub-lattices with equal x-shifts (FCC: 0, 0, 1/2, 1/2) share one x pass
+  // output: the x pass applies only the x factor of the phase and the y pass
+  // the y and z factors; each shared output is read out of place by the other
+  // sub-lattices first and in place by its own last.  MFX_FA_XONLY=0 in the
+  // environment turns this off (for comparisons)
+  int xrep[4] = {0, 0, 0, 0}, xvar[4] = {0, 0, 0, 0}, nxv = 0;
+  for (int s = 0; s < ns; ++s) {
+    int v = 0;
+    while (v < nxv && kShifts[j->d.lattice][xrep[v]][0] != kShifts[j->d.lattice][s][0]) ++v;
+    if (v == nxv) xrep[nxv++] = s;
+    xvar[s] = v;
+  }
+  const char *envx = getenv("MFX_FA_XONLY");
+  if (nsub == ns && nxv < ns && !(envx && envx[0] == '0')) {
+    fa.shift = 0;
+    fa.nsub = nxv;
+    fa.xonly = 1;
+    for (int v = 0; v < nxv; ++v) {
+      fa.xsub[v] = xrep[v];
+      for (int c = 0; c < 6; ++c) fa.qx[6 * v + c] = static_cast<float2 *>(j->asmbuf[6 * xrep[v] + c]);
+    }
+    TRY(pass(ff::FA_X, "fa_x", in_b + 6 * nxv * qf));
+    fa.xonly = 0;
+    fa.yzphase = 1;
+    for (int v = 0; v < nxv; ++v)
+      for (int pass_rep = 0; pass_rep < 2; ++pass_rep)
+        for (int s = 0; s < ns; ++s) {
+          if (xvar[s] != v || (s == xrep[v]) != (pass_rep == 1)) continue;
+          fa.shift = s;
+          for (int c = 0; c < 6; ++c) {
+            fa.q[c] = static_cast<float2 *>(j->asmbuf[6 * s + c]);
+            fa.qin[c] = s == xrep[v] ? nullptr : static_cast<const float2 *>(j->asmbuf[6 * xrep[v] + c]);
+          }
+          fa.qtab = j->qtab + size_t(s) * 3 * N;
+          TRY(pass(ff::FA_Y, "fa_y", 12 * qf));
+          TRY(pass(ff::FA_Z, "fa_z", 6 * qf + pb));
+        }
+    return MFX_OK;
+  }
   for (int s0 = 0; s0 < ns; s0 += nsub) {
     fa.shift = s0;
     fa.nsub = nsub;
@@ -2570,7 +2609,8 @@ struct mfx_server {
   int max_inflight = 8;
   bool bypass = true;
   double bypass_age_ms = 100.0;
-  bool size_priority = true;  // stream priority grows with the job's footprint
+  bool size_priority = true;  // stream priority by the job's footprint
+  bool small_first = true;    // the smallest jobs on the highest priority
   bool largest_first = false; // admit the largest queued job that fits, not the oldest
   std::mutex mu;
   std::condition_variable cv;
@@ -2652,16 +2692,19 @@ static void server_loop(mfx_server *s) {
   }
 }
 
-// Larger jobs run on higher-priority streams: the largest requests set the
-// latency tail, and the kernels of the small ones, which wait for them, are
-// short.  One priority level per factor of four in footprint above 64 MB,
-// up to the device's range.
-static int stream_priority_for(size_t footprint) {
+// Stream priority by footprint, one level per factor of four above 64 MB
+// (up to the device's range).  small_first: the smallest jobs on the highest
+// priority.  The fused kernels are persistent (a grid fills the GPU), so jobs
+// on the GPU together run kernel by kernel rather than side by side, and a
+// small job's forty short kernels would each wait behind a large job's long
+// ones; ahead of them, the small jobs finish in about their own time and
+// delay the large ones by little.  Otherwise the largest jobs go first.
+static int stream_priority_for(size_t footprint, bool small_first) {
   int least = 0, greatest = 0;
   if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return 0;
   int level = 0;
   for (size_t f = footprint >> 26; f >= 4; f >>= 2) ++level;  // 64 MB units, x4 per level
-  return std::max(greatest, least - level);
+  return small_first ? std::min(least, greatest + level) : std::max(greatest, least - level);
 }
 
 static void setup_loop(mfx_server *s) {
@@ -2674,7 +2717,7 @@ static void setup_loop(mfx_server *s) {
     s->setup_q.pop_front();
     lk.unlock();
     mfx_job *j = nullptr;
-    int rc = create_job(s->eng, &t->d, &j, s->size_priority ? stream_priority_for(t->footprint) : 0);
+    int rc = create_job(s->eng, &t->d, &j, s->size_priority ? stream_priority_for(t->footprint, s->small_first) : 0);
     std::string err = rc == MFX_OK ? "" : g_last_error;
     if (rc == MFX_OK) rc = j->fp64 ? run_pipeline<double>(j) : run_pipeline<float>(j);
     if (rc == MFX_OK && cudaEventRecord(t->done, j->stream) != cudaSuccess) rc = MFX_ECUDA;
@@ -2722,6 +2765,7 @@ int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms) {
   s->bypass_age_ms = bypass_age_ms;
   s->size_priority = (bypass & 2) == 0;  // bit 1: every job at the default priority
   s->largest_first = (bypass & 4) != 0;  // bit 2: largest queued job first
+  s->small_first = (bypass & 8) == 0;    // bit 3: the largest jobs on the highest priority
   s->cv.notify_all();
   return MFX_OK;
 }

@@ -642,15 +642,16 @@ class Server:
         check(load().mfx_server_wait(self._h, ticket, timeout_ms))
 
     def set_policy(self, bypass: bool = True, bypass_age_ms: float = 100.0, size_priority: bool = True,
-                   largest_first: bool = False):
+                   largest_first: bool = False, small_first: bool = True):
         """Admission order: a later job that fits may pass a head that has
         waited at most bypass_age_ms (bypass), or strict first-in first-out;
         largest_first: while the head may be passed, the largest queued job
-        that fits goes first; size_priority: larger jobs on higher-priority
-        streams."""
+        that fits goes first; size_priority: stream priority by footprint,
+        the smallest jobs highest (small_first) or the largest."""
         L = load()
         L.mfx_server_set_policy.argtypes = [C.c_void_p, C.c_int, C.c_double]
-        flags = int(bool(bypass)) | (0 if size_priority else 2) | (4 if largest_first else 0)
+        flags = (int(bool(bypass)) | (0 if size_priority else 2) | (4 if largest_first else 0)
+                 | (0 if small_first else 8))
         check(L.mfx_server_set_policy(self._h, flags, float(bypass_age_ms)))
 
     def times(self, ticket: int):
