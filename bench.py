@@ -624,6 +624,8 @@ def run_serving(args):
     srv = mfx.Server(eng, max_inflight=args.inflight)
     srv.set_policy(bypass=True, bypass_age_ms=args.bypass_age_ms, size_priority=not args.no_priority,
                    largest_first=args.largest_first, small_first=not args.large_priority)
+    if args.small_gb > 0:
+        srv.set_small_jobs(int(args.small_gb * 2 ** 30), args.max_small)
     # warm the plan pool and the memory pool with one pass over the size classes
     warm = {}
     for s in specs:
@@ -631,10 +633,12 @@ def run_serving(args):
     drain(srv, {srv.submit(s): 0 for s in warm.values()}, parts)
     # each size class alone through the server (submit -> done, nothing else
     # queued or running): the latency floor of the sweep's percentiles
-    alone_ms = {}
+    alone_ms, footprint_mb = {}, {}
     for key, s in sorted(warm.items()):
         lat1, _ = drain(srv, {srv.submit(s): 0}, parts)
-        alone_ms["%d/%d/%s" % (key[0], key[1], "sc bcc fcc".split()[key[2]])] = float(lat1[0])
+        name = "%d/%d/%s" % (key[0], key[1], "sc bcc fcc".split()[key[2]])
+        alone_ms[name] = float(lat1[0])
+        footprint_mb[name] = mfx.footprint(eng, s) / 2 ** 20
 
     # batched: every request queued at once
     t0 = time.perf_counter()
@@ -664,7 +668,7 @@ def run_serving(args):
 
         th = threading.Thread(target=producer)
         th.start()
-        lat, got, by_size = [], 0, {}
+        lat, qlat, got, by_size = [], [], 0, {}
         while th.is_alive() or tickets:
             with lock:
                 cur = dict(tickets)
@@ -673,8 +677,9 @@ def run_serving(args):
                     srv.wait(h, 0)
                 except Exception:
                     continue
-                ms = srv.times(h)[1]
+                qms, ms = srv.times(h)
                 lat.append(ms)
+                qlat.append(srv.phases(h))
                 by_size.setdefault(specs[cur[h]]["ngrid"], []).append(ms)
                 got += parts[cur[h]]
                 srv.release(h)
@@ -687,6 +692,10 @@ def run_serving(args):
                 "throughput": got / span, "throughput_vs_batched": got / span / sat_tput,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                 "max_ms": float(np.max(lat)),
+                # the slowest 1%: median time queued, in set-up and running
+                "tail_phases_ms": [float(np.median([ph[k] for ph, l in zip(qlat, lat) if l >= np.percentile(lat, 99)]))
+                                   for k in range(3)],
+                "median_phases_ms": [float(np.median([ph[k] for ph in qlat])) for k in range(3)],
                 "p50_ms_by_grid": {str(n): float(np.percentile(v, 50)) for n, v in sorted(by_size.items())},
                 "p99_ms_by_grid": {str(n): float(np.percentile(v, 99)) for n, v in sorted(by_size.items())}}
 
@@ -724,6 +733,8 @@ def run_serving(args):
                                "FP32-compensated" % len(specs), "max_inflight": args.inflight,
                    "admission": ("largest" if args.largest_first else "oldest") + " queued job that fits; a head "
                                 "older than %g ms is not passed" % args.bypass_age_ms,
+                   "small_jobs": ("footprint <= %g GiB beside the slots, at most %d" % (args.small_gb, args.max_small)
+                                  if args.small_gb > 0 else None),
                    "stream_priority": ("default for every job" if args.no_priority else
                                        "by footprint, " + ("largest" if args.large_priority else "smallest") + " first"),
                    "particles_per_point": sum(parts), "tiles_per_size": {str(k): v for k, v in tuned.items()}},
@@ -736,6 +747,7 @@ def run_serving(args):
                     "mode": "every request queued at once"},
         "sweep": sweep,
         "alone_ms": alone_ms,
+        "footprint_mb": footprint_mb,
         "fp64_serial": ({"value": serial_parts / serial_s, "unit": "particles/s", "span_s": serial_s,
                          "requests": len(specs[:args.fp64_sample])} if serial_s else None),
         "clocks": clk,
@@ -914,6 +926,8 @@ def main():
     ap.add_argument("--inflight", type=int, default=2, help="serve: max jobs in flight")
     ap.add_argument("--largest-first", action="store_true", help="serve: admit the largest queued job that fits")
     ap.add_argument("--large-priority", action="store_true", help="serve: the largest jobs on the highest priority")
+    ap.add_argument("--small-gb", type=float, default=0.0, help="serve: jobs up to this footprint take no slot")
+    ap.add_argument("--max-small", type=int, default=16, help="serve: small jobs in flight at most")
     ap.add_argument("--bypass-age-ms", type=float, default=100.0, help="serve: age after which the head is not passed")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -321,6 +321,10 @@ int mfx_server_create(mfx_engine *eng, int max_inflight, mfx_server **out);
 int mfx_server_submit(mfx_server *s, const mfx_job_desc *desc, uint64_t *ticket);
 int mfx_server_wait(mfx_server *s, uint64_t ticket, int timeout_ms);
 int mfx_server_ticket_times(mfx_server *s, uint64_t ticket, double *queued_ms, double *latency_ms);
+/* the latency of a finished ticket in three phases: queued (submit ->
+   admit), set-up (admit -> pipeline enqueued on the job's stream: arena,
+   tables, launches) and run (-> the job's completion seen by the server) */
+int mfx_server_ticket_phases(mfx_server *s, uint64_t ticket, double *queued_ms, double *setup_ms, double *run_ms);
 int mfx_server_job(mfx_server *s, uint64_t ticket, mfx_job **job);
 int mfx_server_release(mfx_server *s, uint64_t ticket);
 int mfx_server_destroy(mfx_server *s);
@@ -334,6 +338,12 @@ int mfx_server_destroy(mfx_server *s);
    bypass bit 2 set (with bit 0): while the head may be passed, admit the
    largest queued job that fits instead of the oldest. */
 int mfx_server_set_policy(mfx_server *s, int bypass, double bypass_age_ms);
+/* Jobs whose footprint is at most footprint_bytes are admitted beside the
+   max_inflight slots, up to max_small of them at once (0: off, the default).
+   Such a job may pass a head that waits only for a slot, at any age: it
+   takes no slot, and its kernels (smallest first by stream priority) finish
+   in about the job's own time. */
+int mfx_server_set_small_jobs(mfx_server *s, size_t footprint_bytes, int max_small);
 
 /* Allocation-free white-noise fill (no counterpart in the reference): writes
    the NGenIC noise of RNG_plugin::Fill_Grid -- raw (raw = 1) or normalised /

@@ -2594,8 +2594,9 @@ struct Ticket {
   std::vector<uint32_t> seeds;
   std::vector<double> amp, plt;
   size_t footprint = 0;
-  clk::time_point t_submit, t_admit, t_done;
+  clk::time_point t_submit, t_admit, t_launch, t_done;  // t_launch: set up, pipeline enqueued
   int state = 0;  // TicketState
+  bool small = false;  // admitted beside the in-flight slots (mfx_server_set_small_jobs)
   int rc = MFX_OK;
   std::string err;
   mfx_job *job = nullptr;
@@ -2623,6 +2624,14 @@ struct mfx_server {
   uint64_t next_id = 1;
   int inflight = 0;     // admitted and not yet finished (setting up or running)
   size_t reserved = 0;  // footprints of admitted jobs whose arenas do not exist yet
+  // small jobs (footprint <= small_bytes) are admitted beside the max_inflight
+  // slots, at most max_small of them at once (mfx_server_set_small_jobs)
+  size_t small_bytes = 0;
+  int max_small = 0, inflight_small = 0;
+  bool is_small(const Ticket *t) const { return small_bytes > 0 && t->footprint <= small_bytes; }
+  bool slot_free(const Ticket *t) const {
+    return is_small(t) ? inflight_small < max_small : inflight < max_inflight;
+  }
 };
 
 static double ms_between(clk::time_point a, clk::time_point b) {
@@ -2644,13 +2653,19 @@ static int pick_admission(mfx_server *s, clk::time_point now) {
     // (the oldest among equals) while the head is young enough to be passed
     int best = -1;
     for (size_t q = 0; q < s->queue.size(); ++q)
-      if (s->queue[q]->footprint <= free_bytes && (best < 0 || s->queue[q]->footprint > s->queue[size_t(best)]->footprint))
+      if (s->queue[q]->footprint <= free_bytes && s->slot_free(s->queue[q]) &&
+          (best < 0 || s->queue[q]->footprint > s->queue[size_t(best)]->footprint))
         best = int(q);
     return best;
   }
+  // a small job takes no in-flight slot: it may pass a head that waits only
+  // for a slot (the head fits the budget) however old the head is
+  const Ticket *head = s->queue.front();
+  const bool head_waits_for_slot_only = !s->is_small(head) && head->footprint <= free_bytes;
   for (size_t q = 0; q < s->queue.size(); ++q) {
-    if (q > 0 && !head_may_be_passed) break;
-    if (s->queue[q]->footprint <= free_bytes) return int(q);
+    const Ticket *t = s->queue[q];
+    if (q > 0 && !head_may_be_passed && !(s->is_small(t) && head_waits_for_slot_only)) continue;
+    if (t->footprint <= free_bytes && s->slot_free(t)) return int(q);
   }
   return -1;
 }
@@ -2671,11 +2686,11 @@ static void server_loop(mfx_server *s) {
         t->rc = MFX_ECUDA;
         t->err = cudaGetErrorString(q);
       }
-      --s->inflight;
+      --(t->small ? s->inflight_small : s->inflight);
       s->cv.notify_all();
     }
     // admit while a slot and the HBM budget allow; the setup threads take it from here
-    while (s->inflight < s->max_inflight) {
+    while (true) {
       const auto now = clk::now();
       const int q = pick_admission(s, now);
       if (q < 0) break;  // wait for running jobs to finish and results to be released
@@ -2683,12 +2698,13 @@ static void server_loop(mfx_server *s) {
       s->queue.erase(s->queue.begin() + q);
       t->t_admit = now;
       t->state = kSetup;
+      t->small = s->is_small(t);
       s->reserved += t->footprint;
-      ++s->inflight;
+      ++(t->small ? s->inflight_small : s->inflight);
       s->setup_q.push_back(t);
       s->cv.notify_all();
     }
-    s->cv.wait_for(lk, std::chrono::microseconds(s->inflight > 0 ? 50 : 2000));
+    s->cv.wait_for(lk, std::chrono::microseconds(s->inflight + s->inflight_small > 0 ? 50 : 2000));
   }
 }
 
@@ -2733,9 +2749,10 @@ static void setup_loop(mfx_server *s) {
       t->rc = rc;
       t->err = err;
       t->t_done = clk::now();
-      --s->inflight;
+      --(t->small ? s->inflight_small : s->inflight);
     } else {
       t->job = j;
+      t->t_launch = clk::now();
       t->state = kRunning;
     }
     s->cv.notify_all();
@@ -2824,6 +2841,28 @@ int mfx_server_ticket_times(mfx_server *s, uint64_t ticket, double *queued_ms, d
   if (t->state < kDone) return set_error(MFX_ESTATE, "ticket not finished");
   if (queued_ms) *queued_ms = ms_between(t->t_submit, t->t_admit);
   if (latency_ms) *latency_ms = ms_between(t->t_submit, t->t_done);
+  return MFX_OK;
+}
+
+int mfx_server_set_small_jobs(mfx_server *s, size_t footprint_bytes, int max_small) {
+  if (!s || max_small < 0) return set_error(MFX_EINVAL, "bad arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->small_bytes = max_small > 0 ? footprint_bytes : 0;
+  s->max_small = max_small;
+  s->cv.notify_all();
+  return MFX_OK;
+}
+
+int mfx_server_ticket_phases(mfx_server *s, uint64_t ticket, double *queued_ms, double *setup_ms, double *run_ms) {
+  if (!s) return set_error(MFX_EINVAL, "null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return set_error(MFX_EINVAL, "unknown ticket");
+  Ticket *t = it->second.get();
+  if (t->state != kDone) return set_error(MFX_ESTATE, "ticket not finished");
+  if (queued_ms) *queued_ms = ms_between(t->t_submit, t->t_admit);
+  if (setup_ms) *setup_ms = ms_between(t->t_admit, t->t_launch);
+  if (run_ms) *run_ms = ms_between(t->t_launch, t->t_done);
   return MFX_OK;
 }
 

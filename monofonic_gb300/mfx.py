@@ -29,7 +29,7 @@ EXPORTS = [
     "mfx_job_algorithmic_bytes", "mfx_job_launch_count", "mfx_job_set_profiling", "mfx_job_kernel_profile",
     "mfx_job_destroy", "mfx_job_autotune", "mfx_job_capture", "mfx_batch_create", "mfx_batch_run", "mfx_batch_wait",
     "mfx_batch_job", "mfx_batch_destroy", "mfx_server_create", "mfx_server_submit", "mfx_server_wait",
-    "mfx_server_ticket_times", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_server_set_policy", "mfx_job_set_species", "mfx_job_fetch_masses", "mfx_job_ppt_fields", "mfx_job_set_host_positions", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
+    "mfx_server_ticket_times", "mfx_server_ticket_phases", "mfx_server_set_small_jobs", "mfx_server_job", "mfx_server_release", "mfx_server_destroy", "mfx_server_set_policy", "mfx_job_set_species", "mfx_job_fetch_masses", "mfx_job_ppt_fields", "mfx_job_set_host_positions", "mfx_noise_fill_noalloc", "mfx_debug_ranlxd1_words",
     "mfx_ngenic_seed_table", "mfx_plt_table_build", "mfx_cosmology_create", "mfx_cosmology_destroy",
     "mfx_cosmology_get", "mfx_cosmology_amplitude", "mfx_cosmology_transfer", "mfx_cosmology_growth",
     "mfx_cosmology_amp_table", "mfx_run_config", "mfx_job_set_output_ring", "mfx_job_fetch_particles_range_async",
@@ -596,6 +596,42 @@ class Batch:
             pass
 
 
+def desc_from_spec(sp):
+    """A job descriptor from a dict of Job() keyword arguments, and the arrays
+    its pointers refer to (keep them alive while the descriptor is used)."""
+    seed = sp.get("seed_table")
+    seed = None if seed is None else np.ascontiguousarray(seed, dtype=np.uint32)
+    amp = np.ascontiguousarray(sp["amp_table"], dtype=np.float64)
+    plt = sp.get("plt_table")
+    plt = None if plt is None else np.ascontiguousarray(plt, dtype=np.float64)
+    d = JobDesc()
+    d.ngrid, d.boxlen, d.lpt_order = sp["ngrid"], sp["boxlen"], sp["order"]
+    d.lattice = sp.get("lattice", SC)
+    d.plt = 1 if plt is not None else 0
+    d.precision = sp.get("precision", FP64)
+    d.fixing, d.inversion = int(sp.get("fixing", False)), int(sp.get("inversion", False))
+    d.seed_table = seed.ctypes.data if seed is not None else None
+    d.amp_table, d.amp_table_len = amp.ctypes.data, amp.size
+    d.plt_table = plt.ctypes.data if plt is not None else None
+    for k in ("g1", "g2", "g3", "g3c", "vfac1", "vfac2", "vfac3"):
+        setattr(d, k, sp["coef"][k])
+    d.lunit, d.vunit = sp.get("lunit", 1.0), sp.get("vunit", 1.0)
+    d.pos64, d.vel64, d.id64 = int(sp.get("pos64", True)), int(sp.get("vel64", True)), int(sp.get("id64", True))
+    d.id_offset = sp.get("id_offset", 0)
+    d.want_particles = int(sp.get("want_particles", True))
+    d.noise_generator = sp.get("noise_generator", NOISE_NGENIC if seed is not None else NOISE_MUSIC1)
+    d.music_seed, d.music_cubesize = sp.get("music_seed", 0), sp.get("music_cubesize", 32)
+    return d, (seed, amp, plt)
+
+
+def footprint(engine, sp) -> int:
+    """The HBM bytes a job of this spec takes (mfx_job_footprint)."""
+    d, _keep = desc_from_spec(sp)
+    fp = C.c_size_t()
+    check(load().mfx_job_footprint(engine.handle, C.byref(d), C.byref(fp)))
+    return fp.value
+
+
 class Server:
     """Request loop with admission by HBM footprint (mfx_server_*)."""
 
@@ -605,6 +641,7 @@ class Server:
         L.mfx_server_submit.argtypes = [C.c_void_p, C.POINTER(JobDesc), C.POINTER(C.c_uint64)]
         L.mfx_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int]
         L.mfx_server_ticket_times.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.mfx_server_ticket_phases.argtypes = [C.c_void_p, C.c_uint64] + [C.POINTER(C.c_double)] * 3
         L.mfx_server_job.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]
         L.mfx_server_release.argtypes = [C.c_void_p, C.c_uint64]
         L.mfx_server_destroy.argtypes = [C.c_void_p]
@@ -615,24 +652,7 @@ class Server:
 
     def submit(self, sp) -> int:
         """sp: dict of Job() keyword arguments (see Batch)."""
-        seed = np.ascontiguousarray(sp["seed_table"], dtype=np.uint32)
-        amp = np.ascontiguousarray(sp["amp_table"], dtype=np.float64)
-        plt = sp.get("plt_table")
-        plt = None if plt is None else np.ascontiguousarray(plt, dtype=np.float64)
-        d = JobDesc()
-        d.ngrid, d.boxlen, d.lpt_order = sp["ngrid"], sp["boxlen"], sp["order"]
-        d.lattice = sp.get("lattice", SC)
-        d.plt = 1 if plt is not None else 0
-        d.precision = sp.get("precision", FP64)
-        d.fixing, d.inversion = int(sp.get("fixing", False)), int(sp.get("inversion", False))
-        d.seed_table, d.amp_table, d.amp_table_len = seed.ctypes.data, amp.ctypes.data, amp.size
-        d.plt_table = plt.ctypes.data if plt is not None else None
-        for k in ("g1", "g2", "g3", "g3c", "vfac1", "vfac2", "vfac3"):
-            setattr(d, k, sp["coef"][k])
-        d.lunit, d.vunit = sp.get("lunit", 1.0), sp.get("vunit", 1.0)
-        d.pos64, d.vel64, d.id64 = int(sp.get("pos64", True)), int(sp.get("vel64", True)), int(sp.get("id64", True))
-        d.id_offset = sp.get("id_offset", 0)
-        d.want_particles = int(sp.get("want_particles", True))
+        d, _keep = desc_from_spec(sp)
         t = C.c_uint64()
         check(load().mfx_server_submit(self._h, C.byref(d), C.byref(t)))
         self._meta[t.value] = ((1 << d.lattice) * d.ngrid ** 3, bool(d.pos64), bool(d.vel64), bool(d.id64), d.ngrid)
@@ -658,6 +678,19 @@ class Server:
         q, l = C.c_double(), C.c_double()
         check(load().mfx_server_ticket_times(self._h, ticket, C.byref(q), C.byref(l)))
         return q.value, l.value
+
+    def set_small_jobs(self, footprint_bytes: int, max_small: int = 16):
+        """Admit jobs with footprint <= footprint_bytes beside the in-flight
+        slots, at most max_small at once (0 turns it off)."""
+        L = load()
+        L.mfx_server_set_small_jobs.argtypes = [C.c_void_p, C.c_size_t, C.c_int]
+        check(L.mfx_server_set_small_jobs(self._h, int(footprint_bytes), int(max_small)))
+
+    def phases(self, ticket: int):
+        """(queued, set-up, run) ms of a finished ticket."""
+        q, su, r = C.c_double(), C.c_double(), C.c_double()
+        check(load().mfx_server_ticket_phases(self._h, ticket, C.byref(q), C.byref(su), C.byref(r)))
+        return q.value, su.value, r.value
 
     def job(self, ticket: int) -> Job:
         h = C.c_void_p()

@@ -210,3 +210,39 @@ def test_server_largest_first_admission(mfxlib, engine):
         for t in [blocker] + small + [big]:
             srv.release(t)
         srv.close()
+
+
+def test_server_small_jobs_beside_the_slots(mfxlib, engine):
+    """A small job takes no in-flight slot: with the one slot held and a large
+    head waiting for it (too old to be passed), the small job is admitted and
+    finishes while the head still waits; without the setting it waits."""
+    import time
+    blocker_spec = spec(mfxlib, 192, 300.0, 24.0, 3, 930, precision=mfxlib.FP64)
+    big_spec = spec(mfxlib, 64, 100.0, 24.0, 3, 931, precision=mfxlib.FP64)
+    small_spec = spec(mfxlib, 16, 25.0, 24.0, 1, 932)
+    fs = mfxlib.footprint(engine, small_spec)
+    assert fs < mfxlib.footprint(engine, big_spec)
+    for beside in (True, False):
+        srv = mfxlib.Server(engine, max_inflight=1)
+        srv.set_policy(bypass=True, bypass_age_ms=0.0)
+        if beside:
+            srv.set_small_jobs(fs, 4)
+        t0 = srv.submit(blocker_spec)
+        t1 = srv.submit(big_spec)
+        time.sleep(0.01)  # the head is now older than the age limit
+        ts = srv.submit(small_spec)
+        if beside:
+            srv.wait(ts, 60000)
+            with pytest.raises(mfxlib.MfxError):
+                srv.wait(t1, 0)  # the head still waits for the slot (or runs)
+        else:
+            with pytest.raises(mfxlib.MfxError):
+                srv.wait(ts, 20)
+        for t in (t0, t1, ts):
+            srv.wait(t, 60000)
+        got = srv.job(ts).particles()
+        for a, b in zip(got, alone(mfxlib, engine, small_spec)):
+            assert np.array_equal(a, b)
+        for t in (t0, t1, ts):
+            srv.release(t)
+        srv.close()
