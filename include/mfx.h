@@ -97,12 +97,19 @@ typedef struct {
   uint64_t id_offset; /* lattice_generator IDoffset (particle_generator.hh:232) */
   int want_particles; /* 0: stop after the LPT potentials (fields only)     */
   /* the [random] generator plugin (random_plugin.cc:62-81): MFX_NOISE_NGENIC
-     reads seed_table; MFX_NOISE_MUSIC1 (random_music.cc, one level: the seed
-     given at the grid's own level, ngrid a power of two) draws the noise on
-     the device from music_seed and music_cubesize and ignores seed_table */
+     reads seed_table; MFX_NOISE_MUSIC1 (random_music.cc; ngrid a power of
+     two) draws the noise on the device from its seeds and music_cubesize and
+     ignores seed_table */
   int noise_generator;
-  int64_t music_seed;       /* [random] seed[log2 ngrid], > 0              */
+  int64_t music_seed;       /* [random] seed[log2 ngrid], > 0 (or 0 with music_seeds) */
   uint32_t music_cubesize;  /* [random] cubesize, 0 = 32 (random_plugin.hh:24) */
+  /* [random] seed[l] for the levels l <= log2 ngrid, 0 where the config has
+     no such key.  The coarsest seeded level is filled and each finer level up
+     to the grid's refines the one below by coarse mode replacement with its
+     own seed, or the level's dummy seed (random_music.cc:160-245,
+     random_music_wnoise_generator.cc:392-547).  Seeds at finer levels than
+     the grid's (restriction) are not supported. */
+  int64_t music_seeds[12];
 } mfx_job_desc;
 
 /* ---- errors -------------------------------------------------------------- */

@@ -198,6 +198,11 @@ struct mfx_job {
   size_t work_bytes = 0;
   Plan m_r2c, m_c2r, n_c2r;
   Plan n_r2c;  // N-grid forward transform of the MUSIC1 cube noise
+  // MUSIC1 from coarser seeded levels: the levels' forward transforms
+  // (level music_l0 + q at music_plans[q]) and two coarse k-space buffers
+  std::vector<Plan> music_plans;
+  int music_l0 = 0, music_lmin = 0;
+  void *music_buf[2] = {nullptr, nullptr};
   // CUDA graph of the whole pipeline (mfx_job_capture)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -268,13 +273,37 @@ int mfx::job_fields(const mfx_job *j, JobFields *o) {
 // ---------------------------------------------------------------------------
 struct Layout {
   size_t seeds, amp, plt, phase, nfields, region, work_est, total;
-  size_t n_field, m_field, asm_bytes, part_bytes, mregion;
+  size_t n_field, m_field, asm_bytes, part_bytes, mregion, music;
   int nslots, group;
   size_t ff_b, ff_d, ff_tw, status;
   int ff_nc;
 };
 
 static size_t n_field_bytes(int N, size_t rs) { return size_t(N) * N * (N / 2 + 1) * 2 * rs; }
+
+// MUSIC1 levels of a descriptor: the grid's level lmin, the coarsest seeded
+// level l0 <= lmin and the effective seed of every level l0..lmin (a given
+// seed[l], music_seed at lmin, else the level's dummy seed)
+struct MusicLevels {
+  int l0 = 0, lmin = 0;
+  int64_t seed[12] = {};
+};
+static MusicLevels music_levels(const mfx_job_desc *d) {
+  MusicLevels m;
+  while ((1u << m.lmin) < d->ngrid && m.lmin < 11) ++m.lmin;
+  m.l0 = m.lmin;
+  for (int l = 0; l <= m.lmin; ++l)
+    if (d->music_seeds[l] > 0) {
+      m.l0 = l;
+      break;
+    }
+  for (int l = m.l0; l <= m.lmin; ++l) {
+    int64_t s = d->music_seeds[l];
+    if (s <= 0 && l == m.lmin && d->music_seed > 0) s = d->music_seed;
+    m.seed[l] = s > 0 ? s : music::dummy_seed(l);
+  }
+  return m;
+}
 
 static int check_desc(const mfx_job_desc *d) {
   if (!d) return set_error(MFX_EINVAL, "null job descriptor");
@@ -291,7 +320,16 @@ static int check_desc(const mfx_job_desc *d) {
     // one level at the grid's own resolution: 2^levelmin cells per axis
     // (random_music.cc:75), cubes that tile it (random_music_wnoise_generator.cc:588-626)
     if (d->ngrid & (d->ngrid - 1)) return set_error(MFX_EINVAL, "MUSIC1 noise needs ngrid a power of two (got %u)", d->ngrid);
-    if (d->music_seed <= 0) return set_error(MFX_EINVAL, "MUSIC1 noise needs a positive seed");
+    int lmin = 0;
+    while ((1u << lmin) < d->ngrid) ++lmin;
+    bool any = d->music_seed > 0;
+    for (int l = 0; l < 12; ++l) {
+      if (d->music_seeds[l] < 0) return set_error(MFX_EINVAL, "MUSIC1 seed[%d] must be positive", l);
+      if (d->music_seeds[l] > 0 && l > lmin)
+        return set_error(MFX_EINVAL, "MUSIC1 seed[%d] finer than the grid's level %d (restriction) is not supported", l, lmin);
+      any = any || d->music_seeds[l] > 0;
+    }
+    if (d->music_seed < 0 || !any) return set_error(MFX_EINVAL, "MUSIC1 noise needs a positive seed");
     const unsigned cs = d->music_cubesize ? d->music_cubesize : 32u;
     if (cs < 2 || (d->ngrid >= cs && d->ngrid % cs != 0))
       return set_error(MFX_EINVAL, "MUSIC1 cubesize %u does not tile ngrid %u", cs, d->ngrid);
@@ -371,7 +409,13 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes, bool group_a
   L.asm_bytes = d->want_particles ? L.part_bytes + size_t(6 * group) * align_up(L.n_field) : 0;
   L.region = std::max(L.mregion, L.asm_bytes);
   L.work_est = align_up(work_bytes);
-  L.total = L.seeds + L.amp + L.plt + L.phase + L.ff_tw + L.status + L.nfields + L.region + L.work_est;
+  // MUSIC1 from coarser seeded levels: two coarse-level k-space fields
+  L.music = 0;
+  if (d->noise_generator == MFX_NOISE_MUSIC1) {
+    const MusicLevels ml = music_levels(d);
+    if (ml.l0 < ml.lmin) L.music = 2 * align_up(n_field_bytes(N / 2, rs));
+  }
+  L.total = L.seeds + L.amp + L.plt + L.phase + L.ff_tw + L.status + L.nfields + L.region + L.work_est + L.music;
   return L;
 }
 
@@ -549,18 +593,42 @@ template <typename R> static int launch_noise(mfx_job *j, int mode, void *out) {
 // transform in place, then the k-space pass (music.cuh)
 template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
   const int N = j->N;
-  music::CubeArgs c;
-  c.seed = reinterpret_cast<const long long *>(j->seeds);
-  c.N = N;
   const int cs = j->d.music_cubesize ? int(j->d.music_cubesize) : 32;
-  c.cs = N < cs ? N : cs;
-  c.nc = N / c.cs;
-  c.row = 2LL * (N / 2 + 1);
+  using C = typename Cplx<R>::T;
+  // one level's cubes into buf (padded real), then its forward transform
+  auto level = [&](int l, void *buf, Plan &plan) -> int {
+    const int n = 1 << l;
+    music::CubeArgs c;
+    c.seed = reinterpret_cast<const long long *>(j->seeds) + l;
+    c.N = n;
+    c.cs = n < cs ? n : cs;
+    c.nc = n / c.cs;
+    c.row = 2LL * (n / 2 + 1);
+    KBEGIN(j);
+    music::k_music_cubes<R><<<unsigned(c.nc) * c.nc * c.nc, 32, 0, j->stream>>>(c, (R *)buf);
+    KEND(j, "music_cubes", double(n) * n * n * sizeof(R));
+    return exec_fft(j, plan, buf, true);
+  };
   const double cells = double(N) * N * N;
-  KBEGIN(j);
-  music::k_music_cubes<R><<<unsigned(c.nc) * c.nc * c.nc, 32, 0, j->stream>>>(c, (R *)out);
-  KEND(j, "music_cubes", cells * sizeof(R));
-  TRY(exec_fft(j, j->n_r2c, out, true));
+  if (j->music_l0 == j->music_lmin) {
+    TRY(level(j->music_lmin, out, j->n_r2c));
+  } else {
+    // the coarsest seeded level, then each finer one with the coarser modes
+    // replaced (its real-space round trip, c2r then r2c, is the identity on
+    // these Hermitian spectra and is left out)
+    void *prev = j->music_buf[0];
+    TRY(level(j->music_l0, prev, j->music_plans[0]));
+    for (int l = j->music_l0 + 1; l <= j->music_lmin; ++l) {
+      void *dst = l == j->music_lmin ? out : j->music_buf[(l - j->music_l0) & 1];
+      TRY(level(l, dst, l == j->music_lmin ? j->n_r2c : j->music_plans[size_t(l - j->music_l0)]));
+      const int nc = 1 << (l - 1);
+      KBEGIN(j);
+      music::k_music_embed<R><<<grid_for(size_t(nc) * nc * (nc / 2 + 1), 256, num_sm()), 256, 0, j->stream>>>(
+          (const C *)prev, (C *)dst, nc, 1 << l);
+      KEND(j, "music_embed", 2.0 * n_field_bytes(nc, j->rsize));
+      prev = dst;
+    }
+  }
   music::KArgs k;
   k.amp = j->amp;
   k.amp_len = j->d.amp_table_len;
@@ -1232,7 +1300,12 @@ static int upload_tables(mfx_job *j, const mfx_job_desc *d) {
   if (d->noise_generator == MFX_NOISE_NGENIC)
     CU(cudaMemcpyAsync(j->seeds, d->seed_table, size_t(N) * N * 4, cudaMemcpyHostToDevice, j->stream));
   else
-    CU(cudaMemcpyAsync(j->seeds, &d->music_seed, sizeof(int64_t), cudaMemcpyHostToDevice, j->stream));
+  {
+    // the effective seed of every level, indexed by level (pageable: staged
+    // before the call returns)
+    const MusicLevels ml = music_levels(d);
+    CU(cudaMemcpyAsync(j->seeds, ml.seed, sizeof(ml.seed), cudaMemcpyHostToDevice, j->stream));
+  }
   CU(cudaMemcpyAsync(j->amp, d->amp_table, d->amp_table_len * 8, cudaMemcpyHostToDevice, j->stream));
   if (d->plt) {
     CU(cudaMemcpyAsync(j->plt, d->plt_table, size_t(MFX_PLT_TABLE_DOUBLES) * 8, cudaMemcpyHostToDevice,
@@ -1388,11 +1461,13 @@ static void free_job(mfx_job *j) {
     release_plan(j->eng, j->m_c2r);
     release_plan(j->eng, j->n_c2r);
     release_plan(j->eng, j->n_r2c);
+    for (auto &p : j->music_plans) release_plan(j->eng, p);
   } else {
     destroy_plan(j->m_r2c);
     destroy_plan(j->m_c2r);
     destroy_plan(j->n_c2r);
     destroy_plan(j->n_r2c);
+    for (auto &p : j->music_plans) destroy_plan(p);
   }
   // stream-ordered free: never synchronises other jobs' streams
   if (j->arena) {
@@ -1556,6 +1631,15 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
   if (d->noise_generator == MFX_NOISE_MUSIC1) {
     if ((rc = acquire_plan(eng, j->n_r2c, j->N, j->fp64, true)) != MFX_OK) return fail(rc);
     work = std::max(work, j->n_r2c.work);
+    const MusicLevels ml = music_levels(d);
+    j->music_l0 = ml.l0;
+    j->music_lmin = ml.lmin;
+    j->music_plans.resize(size_t(ml.lmin - ml.l0));
+    for (int l = ml.l0; l < ml.lmin; ++l) {
+      Plan &p = j->music_plans[size_t(l - ml.l0)];
+      if ((rc = acquire_plan(eng, p, 1 << l, j->fp64, true)) != MFX_OK) return fail(rc);
+      work = std::max(work, p.work);
+    }
   }
   Layout L = plan_layout(d, work);
   {
@@ -1628,6 +1712,11 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
   p += L.region;
   j->work = L.work_est ? p : nullptr;
   j->work_bytes = L.work_est;
+  p += L.work_est;
+  if (L.music) {
+    j->music_buf[0] = p;
+    j->music_buf[1] = p + L.music / 2;
+  }
   for (int q = 0; q < L.nslots; ++q) j->mslot[q] = j->region + size_t(q) * align_up(L.m_field);
   if (j->fused) {
     char *f = j->region;
@@ -1670,9 +1759,15 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
       return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
     if (j->n_r2c.valid && cufftSetWorkArea(j->n_r2c.h, j->work) != CUFFT_SUCCESS)
       return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
+    for (auto &p : j->music_plans)
+      if (p.valid && cufftSetWorkArea(p.h, j->work) != CUFFT_SUCCESS)
+        return fail(set_error(MFX_ECUDA, "cufftSetWorkArea failed"));
   }
   for (Plan *pl : {&j->m_r2c, &j->m_c2r, &j->n_c2r, &j->n_r2c})
     if (pl->valid && cufftSetStream(pl->h, j->stream) != CUFFT_SUCCESS)
+      return fail(set_error(MFX_ECUDA, "cufftSetStream failed"));
+  for (auto &p : j->music_plans)
+    if (p.valid && cufftSetStream(p.h, j->stream) != CUFFT_SUCCESS)
       return fail(set_error(MFX_ECUDA, "cufftSetStream failed"));
   if ((rc = upload_shift_tables(j)) != MFX_OK) return fail(rc);
   if ((rc = upload_tables(j, d)) != MFX_OK) return fail(rc);
@@ -1834,8 +1929,11 @@ int mfx_job_upload(mfx_job *job, const mfx_job_desc *desc) {
   if (desc->ngrid != job->d.ngrid || desc->amp_table_len != job->d.amp_table_len || desc->plt != job->d.plt ||
       desc->noise_generator != job->d.noise_generator || desc->music_cubesize != job->d.music_cubesize)
     return set_error(MFX_EINVAL, "upload descriptor does not match the job's sizes");
+  if (desc->noise_generator == MFX_NOISE_MUSIC1 && music_levels(desc).l0 != job->music_l0)
+    return set_error(MFX_EINVAL, "upload descriptor changes the coarsest seeded MUSIC1 level");
   job->d.seed_table = desc->seed_table;
   job->d.music_seed = desc->music_seed;
+  std::memcpy(job->d.music_seeds, desc->music_seeds, sizeof(desc->music_seeds));
   job->d.amp_table = desc->amp_table;
   job->d.plt_table = desc->plt_table;
   return upload_tables(job, desc);

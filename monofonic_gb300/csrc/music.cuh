@@ -207,6 +207,41 @@ template <typename R> __global__ void __launch_bounds__(32) k_music_cubes(CubeAr
   }
 }
 
+// The dummy seed of a level no seed[level] key names (random_music.cc:176-183):
+// -|(-2 - l) % 123 + (-2 + 7342523521 l) % 123456789|, C's remainder.
+inline long long dummy_seed(int level) {
+  const long long ltemp = -2;
+  const long long v = (ltemp - level) % 123 + (ltemp + 7342523521LL * level) % 123456789;
+  return -(v < 0 ? -v : v);
+}
+
+// Coarse mode replacement (random_music_wnoise_generator.cc:462-505): every
+// coarse k-space mode off the coarse Nyquist indices overwrites the fine
+// mode of the same wave vector, times exp(-i pi/2 (kx + ky + kz)/nc) sqrt(8)
+// (a half coarse cell).  Both fields are unnormalised r2c outputs.
+template <typename R>
+__global__ void __launch_bounds__(256) k_music_embed(const typename Cplx<R>::T *coarse, typename Cplx<R>::T *fine,
+                                                     int nc, int nf) {
+  const int hc = nc >> 1, kc = hc + 1, kf = (nf >> 1) + 1;
+  const size_t total = size_t(nc) * nc * kc;
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int k = int(idx % kc);
+    const size_t t = idx / kc;
+    const int j = int(t % nc), i = int(t / nc);
+    if (i == hc || j == hc || k == hc) continue;
+    const int ii = i > hc ? i + (nf >> 1) : i, jj = j > hc ? j + (nf >> 1) : j;
+    const double kx = i <= hc ? i : i - nc, ky = j <= hc ? j : j - nc;
+    const double ph = (kx / nc + ky / nc + double(k) / nc) * -0.5 * 3.141592653589793;
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    const double s8 = 2.8284271247461903;  // sqrt(8)
+    const auto v = coarse[idx];
+    const double re = double(v.x), im = double(v.y);
+    fine[(size_t(ii) * nf + jj) * kf + k] = mkc<R>(R((re * cs - im * sn) * s8), R((re * sn + im * cs) * s8));
+  }
+}
+
 struct KArgs {
   const double *amp;  // amp[n] = amplitude(kf sqrt n)/(kf^2 n)
   size_t amp_len;

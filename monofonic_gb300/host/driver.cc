@@ -148,22 +148,31 @@ int run_config(mfx_engine *eng, const std::string &text) {
   // 160-215); seeds at other levels need MUSIC1's multi-level refinement
   const std::string gen = cf.get_value<std::string>("random", "generator");
   long seed = 0;
+  int64_t music_seeds[12] = {};
   int noise_gen = MFX_NOISE_NGENIC;
   unsigned cubesize = 0;
   if (gen == "NGENIC") {
     seed = cf.get_value<long>("random", "seed");
   } else if (gen == "MUSIC1") {
+    // seed[l] for every level up to log2(GridRes) (random_music.cc:160-215);
+    // the coarsest seeded level is refined up to the grid's
     int lmin = 0;
     while ((1u << lmin) < ngrid) ++lmin;
     if ((1u << lmin) != ngrid) throw std::runtime_error("MUSIC1 white noise needs GridRes a power of two");
-    for (int l = 0; l < 32; ++l) {
+    bool any = false;
+    for (int l = 0; l <= 100; ++l) {
       const std::string key = "seed[" + std::to_string(l) + "]";
-      if (l != lmin && cf.contains_key("random", key))
-        throw std::runtime_error("MUSIC1 " + key + ": seeds at levels other than log2(GridRes) = " +
-                                 std::to_string(lmin) + " (multi-level refinement) are not supported");
+      if (!cf.contains_key("random", key)) continue;
+      if (l > lmin)
+        throw std::runtime_error("MUSIC1 " + key + ": seeds at levels finer than log2(GridRes) = " +
+                                 std::to_string(lmin) + " (restriction) are not supported");
+      const long v = cf.get_value<long>("random", key);
+      if (v <= 0) throw std::runtime_error("Seed values need to be >0");
+      music_seeds[l] = v;
+      any = true;
     }
-    seed = cf.get_value<long>("random", "seed[" + std::to_string(lmin) + "]");
-    if (seed <= 0) throw std::runtime_error("Seed values need to be >0");
+    if (!any) throw std::runtime_error("No seed specified for MUSIC1 RNG plugin!");
+    seed = music_seeds[lmin];
     cubesize = cf.get_value_safe<unsigned>("random", "cubesize", 32);
     noise_gen = MFX_NOISE_MUSIC1;
   } else {
@@ -207,6 +216,7 @@ int run_config(mfx_engine *eng, const std::string &text) {
   d.noise_generator = noise_gen;
   d.music_seed = noise_gen == MFX_NOISE_MUSIC1 ? seed : 0;
   d.music_cubesize = cubesize;
+  std::memcpy(d.music_seeds, music_seeds, sizeof(music_seeds));
   d.amp_table = amp.data();
   d.amp_table_len = alen;
   d.plt_table = do_plt ? plt.data() : nullptr;

@@ -59,6 +59,7 @@ class JobDesc(C.Structure):
         ("pos64", C.c_int), ("vel64", C.c_int), ("id64", C.c_int), ("id_offset", C.c_uint64),
         ("want_particles", C.c_int),
         ("noise_generator", C.c_int), ("music_seed", C.c_int64), ("music_cubesize", C.c_uint32),
+        ("music_seeds", C.c_int64 * 12),
     ]
 
 
@@ -288,9 +289,11 @@ class Job:
     def __init__(self, engine: Engine, ngrid, boxlen, order, seed_table, amp_table, coef, lattice=SC,
                  precision=FP64, plt_table=None, fixing=False, inversion=False, lunit=1.0, vunit=1.0,
                  pos64=True, vel64=True, id64=True, id_offset=0, want_particles=True,
-                 noise_generator=None, music_seed=0, music_cubesize=32):
+                 noise_generator=None, music_seed=0, music_cubesize=32, music_seeds=None):
         """seed_table: NGenIC's per-column seeds; None with noise_generator=
-        NOISE_MUSIC1, which draws the noise from music_seed and music_cubesize."""
+        NOISE_MUSIC1, which draws the noise from music_seed (the seed at the
+        grid's level) and music_cubesize, or from music_seeds {level: seed}
+        given at coarser levels as well."""
         self.engine = engine
         self.n = ngrid
         self.lattice = lattice
@@ -310,6 +313,8 @@ class Job:
         d.noise_generator = noise_generator
         d.music_seed = music_seed
         d.music_cubesize = music_cubesize
+        for level, sd in (music_seeds or {}).items():
+            d.music_seeds[level] = sd
         d.amp_table = self._amp.ctypes.data
         d.amp_table_len = self._amp.size
         d.plt_table = self._plt.ctypes.data if self._plt is not None else None
@@ -339,11 +344,14 @@ class Job:
     def handle(self):
         return self._h
 
-    def upload(self, seed_table=None, amp_table=None, plt_table=None, music_seed=None):
+    def upload(self, seed_table=None, amp_table=None, plt_table=None, music_seed=None, music_seeds=None):
         if seed_table is not None:
             np.copyto(self._seed, seed_table)
         if music_seed is not None:
             self.desc.music_seed = music_seed
+        if music_seeds is not None:
+            for level in range(12):
+                self.desc.music_seeds[level] = music_seeds.get(level, 0)
         if amp_table is not None:
             np.copyto(self._amp, amp_table)
         if plt_table is not None and self._plt is not None:
@@ -621,6 +629,8 @@ def desc_from_spec(sp):
     d.want_particles = int(sp.get("want_particles", True))
     d.noise_generator = sp.get("noise_generator", NOISE_NGENIC if seed is not None else NOISE_MUSIC1)
     d.music_seed, d.music_cubesize = sp.get("music_seed", 0), sp.get("music_cubesize", 32)
+    for level, sd in (sp.get("music_seeds") or {}).items():
+        d.music_seeds[level] = sd
     return d, (seed, amp, plt)
 
 

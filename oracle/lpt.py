@@ -130,6 +130,7 @@ def lib():
         _lib.mfxo_mt19937_words.argtypes = [ctypes.c_ulong, ctypes.c_size_t, ctypes.c_void_p]
         _lib.mfxo_leva_normals.argtypes = [ctypes.c_ulong, ctypes.c_size_t, ctypes.c_void_p]
         _lib.mfxo_music_noise.argtypes = [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_long, ctypes.c_void_p]
+        _lib.mfxo_music_cubes.argtypes = [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_long, ctypes.c_void_p]
     return _lib
 
 
@@ -150,6 +151,65 @@ def music_noise_real(n: int, seed: int, cubesize: int = 32) -> np.ndarray:
     out = np.zeros((n, n, n))
     lib().mfxo_music_noise(n, cubesize, seed, out.ctypes.data)
     return out
+
+
+def music_cubes_raw(n: int, seed: int, cubesize: int = 32) -> np.ndarray:
+    """One level's cubes without mean subtraction (oracle/music.c)."""
+    out = np.zeros((n, n, n))
+    lib().mfxo_music_cubes(n, cubesize, seed, out.ctypes.data)
+    return out
+
+
+def _cmod(a: int, b: int) -> int:
+    """C's % (truncating toward zero) on integers."""
+    r = abs(a) % abs(b)
+    return r if a >= 0 else -r
+
+
+def music_dummy_seed(level: int) -> int:
+    """The seed of a level no [random] seed[level] names (random_music.cc:176-183):
+    negative, a function of the level only."""
+    ltemp = -2
+    return -abs(_cmod(ltemp - level, 123) + _cmod(ltemp + 7342523521 * level, 123456789))
+
+
+def music_refine(coarse: np.ndarray, fine: np.ndarray) -> np.ndarray:
+    """A finer level from a coarser one by coarse mode replacement
+    (random_music_wnoise_generator.cc:392-547): the fine level's cubes in
+    k-space get the coarse level's modes, phase-shifted by half a coarse cell
+    and scaled by sqrt(8), except on the coarse Nyquist indices; FFTW's
+    unnormalised transforms, the result scaled by 1/n^3 before the c2r."""
+    nc, nf = coarse.shape[0], fine.shape[0]
+    cf = sfft.rfftn(fine, workers=WORKERS)
+    cc = sfft.rfftn(coarse, workers=WORKERS)
+    i = np.arange(nc)
+    k = np.arange(nc // 2 + 1)
+    kx = np.where(i <= nc // 2, i, i - nc).astype(np.float64)
+    kz = k.astype(np.float64)
+    idx = np.where(i > nc // 2, i + nf // 2, i)
+    phase = (kx[:, None, None] / nc + kx[None, :, None] / nc + kz[None, None, :] / nc) * (-0.5) * np.pi
+    val = cc * np.exp(1j * phase) * np.sqrt(8.0)
+    keep = (i != nc // 2)[:, None, None] & (i != nc // 2)[None, :, None] & (k != nc // 2)[None, None, :]
+    sub = cf[np.ix_(idx, idx, k)]
+    cf[np.ix_(idx, idx, k)] = np.where(keep, val, sub)
+    cf *= 1.0 / float(nf) ** 3
+    return sfft.irfftn(cf, s=(nf, nf, nf), workers=WORKERS) * float(nf) ** 3
+
+
+def music_levels(n: int, seeds: dict, cubesize: int = 32) -> np.ndarray:
+    """MUSIC1's real-space noise at level log2(n) when seeds are given at
+    coarser levels (random_music.cc:222-245): the coarsest seeded level is
+    filled (with its mean subtracted), and each finer level up to log2(n)
+    refines the one below with its own seed or the level's dummy seed."""
+    lmin = int(n).bit_length() - 1
+    l0 = min(seeds)
+    if l0 == lmin:
+        return music_noise_real(n, seeds[lmin], cubesize)
+    f = music_noise_real(1 << l0, seeds[l0], cubesize)
+    for level in range(l0 + 1, lmin + 1):
+        seed = seeds.get(level, music_dummy_seed(level))
+        f = music_refine(f, music_cubes_raw(1 << level, seed, cubesize))
+    return f
 
 
 def music_fill(n: int, seed: int, cubesize: int = 32) -> np.ndarray:

@@ -2,10 +2,10 @@
  * ORACLE -- test infrastructure only.  Nothing in the product links this file;
  * only tests/ and bench.py's CPU legs load it, and only as the checker.
  *
- * CPU restatement of monofonIC's MUSIC1 white-noise plugin for a single level
- * (the seed given at the grid's own level): src/plugins/random_music.cc:83-130,
- * 236-283 and src/plugins/random_music_wnoise_generator.cc:27-52, 588-626,
- * 684-797.
+ * CPU restatement of monofonIC's MUSIC1 white-noise plugin: the cube fill of
+ * one level (src/plugins/random_music.cc:83-130, 236-283 and
+ * src/plugins/random_music_wnoise_generator.cc:27-52, 588-626, 684-797); the
+ * refinement from coarser seeded levels is in oracle/lpt.py (music_levels).
  *
  *   - the grid of res^3 cells is cut into cubes of cubesize^3 (32 by default;
  *     one cube of res^3 when res < cubesize), cube (ic, jc, kc) numbered
@@ -102,6 +102,31 @@ void mfxo_leva_normals(unsigned long seed, size_t count, double *out)
     size_t q;
     mt_seed(&m, seed);
     for (q = 0; q < count; ++q) out[q] = leva_normal(&m);
+}
+
+/* The cubes of one level without any mean subtraction (the refinement
+ * levels' fill, random_music_wnoise_generator.cc:392-406: their mean only
+ * moves the k = 0 mode, which the coarse level's replaces). */
+void mfxo_music_cubes(size_t res, size_t cubesize, long seed, double *out)
+{
+    size_t nc, cs, ic, jc, kc, ii, jj, kk;
+    if (res < cubesize) {
+        nc = 1;
+        cs = res;
+    } else {
+        nc = res / cubesize;
+        cs = cubesize;
+    }
+    for (ic = 0; ic < nc; ++ic)
+        for (jc = 0; jc < nc; ++jc)
+            for (kc = 0; kc < nc; ++kc) {
+                oracle_mt m;
+                mt_seed(&m, (unsigned long)(seed + (long)((ic * nc + jc) * nc + kc)));
+                for (ii = 0; ii < cs; ++ii)
+                    for (jj = 0; jj < cs; ++jj)
+                        for (kk = 0; kk < cs; ++kk)
+                            out[((ic * cs + ii) * res + (jc * cs + jj)) * res + (kc * cs + kk)] = leva_normal(&m);
+            }
 }
 
 /* The MUSIC1 single-level white noise in real space, out[(i res + j) res + k]. */

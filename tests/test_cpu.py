@@ -268,3 +268,32 @@ def test_music_noise_cubes_and_means(oracle):
     small = oracle.music_noise_real(16, 3, 32)  # one cube of the whole grid below the cube size
     r = oracle.leva_normals(3, 16 ** 3).reshape(16, 16, 16)
     assert np.allclose(small, r - r.mean(), rtol=0, atol=1e-13)
+
+
+def test_music_dummy_seeds(oracle):
+    """Levels without a seed[level] key get -|(-2 - l) % 123 + (-2 + 7342523521 l) % 123456789|
+    with C's truncating remainder (random_music.cc:176-183)."""
+    assert oracle.music_dummy_seed(0) == -4
+    assert oracle.music_dummy_seed(1) == -(7342523519 % 123456789 - 3)
+    assert oracle.music_dummy_seed(5) == -abs(-7 + (5 * 7342523521 - 2) % 123456789)
+    assert all(oracle.music_dummy_seed(level) < 0 for level in range(12))
+
+
+def test_music_refinement_keeps_the_coarse_modes(oracle):
+    """A refined level carries the coarse level's modes (half-cell phase,
+    sqrt 8) off the coarse Nyquist indices and its own cubes' modes elsewhere."""
+    nc, nf = 8, 16
+    coarse = oracle.music_noise_real(nc, 21, 4)
+    fine_raw = oracle.music_cubes_raw(nf, 22, 4)
+    fine = oracle.music_refine(coarse, fine_raw)
+    cf, cr, cc = (np.fft.rfftn(x) for x in (fine, fine_raw, coarse))
+    for (i, j, k) in [(1, 2, 3), (7, 6, 1), (0, 5, 2), (3, 0, 0)]:
+        ii = i if i <= nc // 2 else i + nf // 2
+        jj = j if j <= nc // 2 else j + nf // 2
+        kx, ky = (i if i <= nc // 2 else i - nc), (j if j <= nc // 2 else j - nc)
+        ph = np.exp(-0.5j * np.pi * (kx + ky + k) / nc)
+        assert abs(cf[ii, jj, k] - cc[i, j, k] * ph * np.sqrt(8.0)) < 1e-10
+    assert abs(cf[5, 9, 6] - cr[5, 9, 6]) < 1e-10  # not a coarse mode: the fine cubes' own
+    assert abs(cf[4, 1, 1] - cr[4, 1, 1]) < 1e-10  # a coarse Nyquist index: kept from the fine level
+    lev = oracle.music_levels(16, {3: 21}, 4)
+    assert np.allclose(lev, oracle.music_refine(coarse, oracle.music_cubes_raw(16, oracle.music_dummy_seed(4), 4)))

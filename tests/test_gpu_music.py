@@ -138,6 +138,40 @@ def test_run_config_music1(mfxlib, engine, tmp_path):
     off = 8 + 8 + 4 + 4 + 24
     assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
     bad = mfxlib.ini_text(32, 50.0, 24.0, 2, 777, filename=str(f), generator="MUSIC1").replace(
-        "seed[5] = 777", "seed[4] = 12\nseed[5] = 777")
+        "seed[5] = 777", "seed[6] = 12\nseed[5] = 777")
     with pytest.raises(mfxlib.MfxError):
-        engine.run_config(bad)
+        engine.run_config(bad)  # a seed finer than the grid's level (restriction)
+
+
+@pytest.mark.parametrize("n,cubesize,seeds", [(32, 8, {3: 4242}), (32, 4, {2: 11, 4: 12}),
+                                              (64, 16, {4: 99, 6: 100}), (32, 8, {3: 5, 4: 6, 5: 7})])
+def test_music_multilevel_noise_matches_oracle(mfxlib, engine, oracle, n, cubesize, seeds):
+    """Seeds at coarser levels: the coarsest seeded level refined up to the
+    grid's by coarse mode replacement, unseeded levels with their dummy seeds
+    (random_music.cc:222-245, random_music_wnoise_generator.cc:392-547)."""
+    c = Case(mfxlib, n, 100.0, 49.0, 1, 1)
+    j = mfxlib.Job(engine, n, c.L, 1, None, c.amp, c.coef, precision=mfxlib.FP64, want_particles=False,
+                   noise_generator=mfxlib.NOISE_MUSIC1, music_cubesize=cubesize, music_seeds=seeds)
+    j.run_noise(raw=True)
+    got = j.field(mfxlib.FIELD_NOISE)
+    ref = oracle.fft_r2c(oracle.music_levels(n, seeds, cubesize))
+    ref[0, 0, 0] = 0.0
+    assert rel_l2(got, ref) < 1e-12
+    # the coarsest level's modes come through to the grid's noise
+    lo = min(seeds)
+    assert np.abs(got[1, 1, 1]) > 0
+
+
+def test_run_config_music1_multilevel(mfxlib, engine, tmp_path):
+    f = tmp_path / "ics.bin"
+    txt = mfxlib.ini_text(32, 50.0, 24.0, 2, 777, "sc", filename=str(f), generator="MUSIC1", cubesize=8)
+    engine.run_config(txt.replace("seed[5] = 777", "seed[3] = 31\nseed[5] = 777"))
+    raw = f.read_bytes()
+    np_ = int(np.frombuffer(raw[8:16], np.uint64)[0])
+    c = Case(mfxlib, 32, 50.0, 24.0, 2, 1)
+    j = mfxlib.Job(engine, 32, c.L, 2, None, c.amp, c.coef, precision=mfxlib.FP64, lunit=c.lunit, vunit=c.vunit,
+                   noise_generator=mfxlib.NOISE_MUSIC1, music_cubesize=8, music_seeds={3: 31, 5: 777})
+    j.run()
+    pos, vel, ids = j.particles()
+    off = 8 + 8 + 4 + 4 + 24
+    assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
