@@ -284,6 +284,8 @@ static size_t n_field_bytes(int N, size_t rs) { return size_t(N) * N * (N / 2 + 
 // MUSIC1 levels of a descriptor: the grid's level lmin, the coarsest seeded
 // level l0 <= lmin and the effective seed of every level l0..lmin (a given
 // seed[l], music_seed at lmin, else the level's dummy seed)
+// (l0 > lmin: seeds only at finer levels; the coarsest of them is filled and
+// restricted down to lmin, random_music.cc:247-272)
 struct MusicLevels {
   int l0 = 0, lmin = 0;
   int64_t seed[12] = {};
@@ -291,12 +293,14 @@ struct MusicLevels {
 static MusicLevels music_levels(const mfx_job_desc *d) {
   MusicLevels m;
   while ((1u << m.lmin) < d->ngrid && m.lmin < 11) ++m.lmin;
-  m.l0 = m.lmin;
-  for (int l = 0; l <= m.lmin; ++l)
-    if (d->music_seeds[l] > 0) {
-      m.l0 = l;
-      break;
-    }
+  m.l0 = -1;
+  for (int l = 0; l < 12 && m.l0 < 0; ++l)
+    if (d->music_seeds[l] > 0 || (l == m.lmin && d->music_seed > 0)) m.l0 = l;
+  if (m.l0 < 0) m.l0 = m.lmin;
+  if (m.l0 > m.lmin) {
+    m.seed[m.l0] = d->music_seeds[m.l0];
+    return m;
+  }
   for (int l = m.l0; l <= m.lmin; ++l) {
     int64_t s = d->music_seeds[l];
     if (s <= 0 && l == m.lmin && d->music_seed > 0) s = d->music_seed;
@@ -325,8 +329,8 @@ static int check_desc(const mfx_job_desc *d) {
     bool any = d->music_seed > 0;
     for (int l = 0; l < 12; ++l) {
       if (d->music_seeds[l] < 0) return set_error(MFX_EINVAL, "MUSIC1 seed[%d] must be positive", l);
-      if (d->music_seeds[l] > 0 && l > lmin)
-        return set_error(MFX_EINVAL, "MUSIC1 seed[%d] finer than the grid's level %d (restriction) is not supported", l, lmin);
+      if (d->music_seeds[l] > 0 && l > lmin + 3)
+        return set_error(MFX_EINVAL, "MUSIC1 seed[%d] more than three levels finer than the grid's (%d)", l, lmin);
       any = any || d->music_seeds[l] > 0;
     }
     if (d->music_seed < 0 || !any) return set_error(MFX_EINVAL, "MUSIC1 noise needs a positive seed");
@@ -414,6 +418,10 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes, bool group_a
   if (d->noise_generator == MFX_NOISE_MUSIC1) {
     const MusicLevels ml = music_levels(d);
     if (ml.l0 < ml.lmin) L.music = 2 * align_up(n_field_bytes(N / 2, rs));
+    // the finer seeded level and, for two steps or more, one level below it
+    if (ml.l0 > ml.lmin)
+      L.music = align_up(n_field_bytes(1 << ml.l0, rs)) +
+                (ml.l0 - ml.lmin >= 2 ? align_up(n_field_bytes(1 << (ml.l0 - 1), rs)) : 0);
   }
   L.total = L.seeds + L.amp + L.plt + L.phase + L.ff_tw + L.status + L.nfields + L.region + L.work_est + L.music;
   return L;
@@ -612,6 +620,26 @@ template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
   const double cells = double(N) * N * N;
   if (j->music_l0 == j->music_lmin) {
     TRY(level(j->music_lmin, out, j->n_r2c));
+  } else if (j->music_l0 > j->music_lmin) {
+    // the finer seeded level, restricted one level at a time in k-space; the
+    // reference's c2r / r2c round trip between levels keeps the Hermitian
+    // part of the kz = 0 and kz = n/2 planes, which the restricted spectrum
+    // need not be on its Nyquist indices
+    TRY(level(j->music_l0, j->music_buf[0], j->music_plans[0]));
+    void *src = j->music_buf[0];
+    for (int l = j->music_l0 - 1, q = 1; l >= j->music_lmin; --l, ++q) {
+      void *dst = l == j->music_lmin ? out : j->music_buf[q & 1];
+      const int nc = 1 << l;
+      KBEGIN(j);
+      music::k_music_restrict<R><<<grid_for(size_t(nc) * nc * (nc / 2 + 1), 256, num_sm()), 256, 0, j->stream>>>(
+          (const C *)src, (C *)dst, nc, 1);
+      KEND(j, "music_restrict", 2.0 * n_field_bytes(nc, j->rsize));
+      KBEGIN(j);
+      music::k_music_hermitian_planes<R><<<grid_for(size_t(nc) * nc * 2, 256, num_sm()), 256, 0, j->stream>>>(
+          (C *)dst, nc);
+      KEND(j, "music_planes", 8.0 * nc * nc * (j->fp64 ? 16 : 8));
+      src = dst;
+    }
   } else {
     // the coarsest seeded level, then each finer one with the coarser modes
     // replaced (its real-space round trip, c2r then r2c, is the identity on
@@ -1634,9 +1662,11 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
     const MusicLevels ml = music_levels(d);
     j->music_l0 = ml.l0;
     j->music_lmin = ml.lmin;
-    j->music_plans.resize(size_t(ml.lmin - ml.l0));
-    for (int l = ml.l0; l < ml.lmin; ++l) {
-      Plan &p = j->music_plans[size_t(l - ml.l0)];
+    // the coarser levels' forward transforms, or the one of the finer seeded level
+    j->music_plans.resize(ml.l0 < ml.lmin ? size_t(ml.lmin - ml.l0) : (ml.l0 > ml.lmin ? 1 : 0));
+    for (size_t q = 0; q < j->music_plans.size(); ++q) {
+      Plan &p = j->music_plans[q];
+      const int l = ml.l0 < ml.lmin ? ml.l0 + int(q) : ml.l0;
       if ((rc = acquire_plan(eng, p, 1 << l, j->fp64, true)) != MFX_OK) return fail(rc);
       work = std::max(work, p.work);
     }
@@ -1715,7 +1745,12 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
   p += L.work_est;
   if (L.music) {
     j->music_buf[0] = p;
-    j->music_buf[1] = p + L.music / 2;
+    // the second coarse buffer of a refinement; of a restriction, the level
+    // below the seeded one
+    j->music_buf[1] = j->music_l0 < j->music_lmin
+                          ? p + L.music / 2
+                          : (j->music_l0 - j->music_lmin >= 2 ? p + align_up(n_field_bytes(1 << j->music_l0, j->rsize))
+                                                             : nullptr);
   }
   for (int q = 0; q < L.nslots; ++q) j->mslot[q] = j->region + size_t(q) * align_up(L.m_field);
   if (j->fused) {

@@ -242,6 +242,57 @@ __global__ void __launch_bounds__(256) k_music_embed(const typename Cplx<R>::T *
   }
 }
 
+// Restriction (random_music_wnoise_generator.cc:288-380), `steps` levels at
+// once: every mode of the coarse grid (nc) takes the mode of the same wave
+// vector of the fine grid (nf = nc 2^steps) times exp(+i pi/2 (kx + ky + kz)
+// / n) / sqrt(8) for each level n = nc, 2 nc, ... passed through.  Both are
+// unnormalised r2c outputs.
+template <typename R>
+__global__ void __launch_bounds__(256) k_music_restrict(const typename Cplx<R>::T *fine, typename Cplx<R>::T *coarse,
+                                                        int nc, int steps) {
+  const int hc = nc >> 1, kc = hc + 1, nf = nc << steps, kf = (nf >> 1) + 1;
+  const size_t total = size_t(nc) * nc * kc;
+  double geo = 0.0;  // sum over the levels passed of 1 / n
+  for (int s = 0; s < steps; ++s) geo += 1.0 / double(nc << s);
+  const double scale = pow(8.0, -0.5 * steps);
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int k = int(idx % kc);
+    const size_t t = idx / kc;
+    const int j = int(t % nc), i = int(t / nc);
+    const int kx = i <= hc ? i : i - nc, ky = j <= hc ? j : j - nc;
+    const int ii = kx >= 0 ? kx : kx + nf, jj = ky >= 0 ? ky : ky + nf;
+    const double ph = double(kx + ky + k) * geo * 0.5 * 3.141592653589793;
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    const auto v = fine[(size_t(ii) * nf + jj) * kf + k];
+    const double re = double(v.x), im = double(v.y);
+    coarse[idx] = mkc<R>(R((re * cs - im * sn) * scale), R((re * sn + im * cs) * scale));
+  }
+}
+
+// The Hermitian part of the kz = 0 and kz = n/2 planes of an r2c spectrum,
+// in place: what a c2r followed by an r2c leaves of them (the reference takes
+// that round trip between levels).  One thread per pair (i, j) <-> (-i, -j).
+template <typename R>
+__global__ void __launch_bounds__(256) k_music_hermitian_planes(typename Cplx<R>::T *f, int n) {
+  const int kn = (n >> 1) + 1;
+  const size_t total = size_t(n) * n * 2;
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const int k = (idx & 1) ? (n >> 1) : 0;
+    const size_t t = idx >> 1;
+    const int j = int(t % n), i = int(t / n);
+    const int pi = i ? n - i : 0, pj = j ? n - j : 0;
+    if (size_t(pi) * n + pj < t) continue;  // the partner's thread writes both
+    auto &a = f[(size_t(i) * n + j) * kn + k];
+    auto &b = f[(size_t(pi) * n + pj) * kn + k];
+    const R re = R(0.5) * (a.x + b.x), im = R(0.5) * (a.y - b.y);
+    a = mkc<R>(re, im);
+    b = mkc<R>(re, -im);
+  }
+}
+
 struct KArgs {
   const double *amp;  // amp[n] = amplitude(kf sqrt n)/(kf^2 n)
   size_t amp_len;

@@ -163,9 +163,9 @@ int run_config(mfx_engine *eng, const std::string &text) {
     for (int l = 0; l <= 100; ++l) {
       const std::string key = "seed[" + std::to_string(l) + "]";
       if (!cf.contains_key("random", key)) continue;
-      if (l > lmin)
-        throw std::runtime_error("MUSIC1 " + key + ": seeds at levels finer than log2(GridRes) = " +
-                                 std::to_string(lmin) + " (restriction) are not supported");
+      if (l > lmin + 3 || l >= 12)
+        throw std::runtime_error("MUSIC1 " + key + ": seeds more than three levels finer than log2(GridRes) = " +
+                                 std::to_string(lmin) + " are not supported");
       const long v = cf.get_value<long>("random", key);
       if (v <= 0) throw std::runtime_error("Seed values need to be >0");
       music_seeds[l] = v;

@@ -196,15 +196,38 @@ def music_refine(coarse: np.ndarray, fine: np.ndarray) -> np.ndarray:
     return sfft.irfftn(cf, s=(nf, nf, nf), workers=WORKERS) * float(nf) ** 3
 
 
+def music_restrict(fine: np.ndarray) -> np.ndarray:
+    """The next coarser level of a field by k-space averaging
+    (random_music_wnoise_generator.cc:288-380): every coarse mode takes the
+    fine mode of the same wave vector times exp(+i pi/2 (kx + ky + kz)/nc) /
+    sqrt(8), FFTW's unnormalised transforms, 1/nc^3 before the c2r."""
+    nf = fine.shape[0]
+    nc = nf // 2
+    cf = sfft.rfftn(fine, workers=WORKERS)
+    i = np.arange(nc)
+    k = np.arange(nc // 2 + 1)
+    kx = np.where(i <= nc // 2, i, i - nc).astype(np.float64)
+    idx = np.where(i > nc // 2, i + nf // 2, i)
+    phase = (kx[:, None, None] / nc + kx[None, :, None] / nc + k[None, None, :].astype(np.float64) / nc) * 0.5 * np.pi
+    cc = cf[np.ix_(idx, idx, k)] * np.exp(1j * phase) * (1.0 / float(nc) ** 3) / np.sqrt(8.0)
+    return sfft.irfftn(cc, s=(nc, nc, nc), workers=WORKERS) * float(nc) ** 3
+
+
 def music_levels(n: int, seeds: dict, cubesize: int = 32) -> np.ndarray:
-    """MUSIC1's real-space noise at level log2(n) when seeds are given at
-    coarser levels (random_music.cc:222-245): the coarsest seeded level is
-    filled (with its mean subtracted), and each finer level up to log2(n)
-    refines the one below with its own seed or the level's dummy seed."""
+    """MUSIC1's real-space noise at level log2(n) (random_music.cc:222-283):
+    with seeds at coarser levels the coarsest seeded level is filled (its mean
+    subtracted) and each finer level up to log2(n) refines the one below with
+    its own seed or the level's dummy seed; with seeds only at finer levels the
+    coarsest of them is filled and restricted down level by level."""
     lmin = int(n).bit_length() - 1
     l0 = min(seeds)
     if l0 == lmin:
         return music_noise_real(n, seeds[lmin], cubesize)
+    if l0 > lmin:
+        f = music_noise_real(1 << l0, seeds[l0], cubesize)
+        for level in range(l0 - 1, lmin - 1, -1):
+            f = music_restrict(f)
+        return f
     f = music_noise_real(1 << l0, seeds[l0], cubesize)
     for level in range(l0 + 1, lmin + 1):
         seed = seeds.get(level, music_dummy_seed(level))

@@ -297,3 +297,17 @@ def test_music_refinement_keeps_the_coarse_modes(oracle):
     assert abs(cf[4, 1, 1] - cr[4, 1, 1]) < 1e-10  # a coarse Nyquist index: kept from the fine level
     lev = oracle.music_levels(16, {3: 21}, 4)
     assert np.allclose(lev, oracle.music_refine(coarse, oracle.music_cubes_raw(16, oracle.music_dummy_seed(4), 4)))
+
+
+def test_music_restriction_is_the_inverse_embedding(oracle):
+    """Restricting a refined level returns the coarse field where the
+    refinement copied its modes: k-space averaging undoes the half-cell phase
+    and the sqrt(8) of the coarse mode replacement (off the Nyquist indices)."""
+    coarse = oracle.music_noise_real(8, 5, 4)
+    fine = oracle.music_refine(coarse, oracle.music_cubes_raw(16, 6, 4))
+    back = np.fft.rfftn(oracle.music_restrict(fine))
+    cc = np.fft.rfftn(coarse)
+    keep = np.ones(cc.shape, bool)
+    keep[4, :, :] = keep[:, 4, :] = False
+    keep[:, :, 4] = False
+    assert np.max(np.abs(back[keep] - cc[keep])) < 1e-10

@@ -138,17 +138,20 @@ def test_run_config_music1(mfxlib, engine, tmp_path):
     off = 8 + 8 + 4 + 4 + 24
     assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
     bad = mfxlib.ini_text(32, 50.0, 24.0, 2, 777, filename=str(f), generator="MUSIC1").replace(
-        "seed[5] = 777", "seed[6] = 12\nseed[5] = 777")
+        "seed[5] = 777", "seed[9] = 12\nseed[5] = 777")
     with pytest.raises(mfxlib.MfxError):
-        engine.run_config(bad)  # a seed finer than the grid's level (restriction)
+        engine.run_config(bad)  # a seed more than three levels finer than the grid's
 
 
 @pytest.mark.parametrize("n,cubesize,seeds", [(32, 8, {3: 4242}), (32, 4, {2: 11, 4: 12}),
-                                              (64, 16, {4: 99, 6: 100}), (32, 8, {3: 5, 4: 6, 5: 7})])
+                                              (64, 16, {4: 99, 6: 100}), (32, 8, {3: 5, 4: 6, 5: 7}),
+                                              (16, 8, {5: 123}), (16, 8, {6: 321, 7: 9})])
 def test_music_multilevel_noise_matches_oracle(mfxlib, engine, oracle, n, cubesize, seeds):
     """Seeds at coarser levels: the coarsest seeded level refined up to the
     grid's by coarse mode replacement, unseeded levels with their dummy seeds
-    (random_music.cc:222-245, random_music_wnoise_generator.cc:392-547)."""
+    (random_music.cc:222-245, random_music_wnoise_generator.cc:392-547).  Seeds
+    only at finer levels: the coarsest of them restricted down by k-space
+    averaging (random_music.cc:247-272, random_music_wnoise_generator.cc:288-380)."""
     c = Case(mfxlib, n, 100.0, 49.0, 1, 1)
     j = mfxlib.Job(engine, n, c.L, 1, None, c.amp, c.coef, precision=mfxlib.FP64, want_particles=False,
                    noise_generator=mfxlib.NOISE_MUSIC1, music_cubesize=cubesize, music_seeds=seeds)
