@@ -291,16 +291,19 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
 
 // ASM2: inverse y transforms of the six components, in place (or from qin).
 // YZ: the y and z factors of sub-lattice a.shift's phase applied on input
-// (x-only ASM1), the y factors staged in shared memory after the tile areas
+// (x-only ASM1), both staged in shared memory after the tile areas (a global
+// load of the z factors at the start of each unit's transform held up its
+// first step: 6.1 instead of 4.4 ms a launch at 768^3)
 template <int N, bool YZ>
 __global__ void __launch_bounds__(FA<N>::t2, FA<N>::minb2) k_fa_y(FAArgs a) {
   using F = FA<N>;
   constexpr int P = F::P2, KB = F::Kh / P;
   float2 *tw = ff_smem(), *buf = tw + N, *buf2 = buf + (F::nbuf == 2 ? Tile<N, P, true>::elems : 0),
          *stage = buf + F::nbuf * Tile<N, P, true>::elems;
-  float2 *phy = stage + 2 * N * P;  // YZ: [N] y factors of the sub-lattice phase
+  float2 *phy = stage + 2 * N * P;  // YZ: [N] y factors, then [Kh] z factors of the sub-lattice phase
+  float2 *phzs = phy + N;
   if constexpr (YZ)
-    for (int t = threadIdx.x; t < N; t += blockDim.x) phy[t] = a.as.phase32[size_t(a.shift) * 3 * N + N + t];
+    for (int t = threadIdx.x; t < N + F::Kh; t += blockDim.x) phy[t] = a.as.phase32[size_t(a.shift) * 3 * N + N + t];
   load_tw<N>(tw, a.tw);  // includes a barrier
   xy_units(
       unsigned(N * KB * 6), N * P, stage,
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(FA<N>::t2, FA<N>::minb2) k_fa_y(FAArgs a) {
       [&](unsigned u, const float2 *st) {
         const unsigned c = u % 6, t = u / 6, x = t / KB, kz0 = (t % KB) * P;
         float2 *out = a.q[c] + (x * N * F::Kh + kz0);
-        const float2 *phz = a.as.phase32 + size_t(a.shift) * 3 * N + 2 * N + kz0;
+        const float2 *phz = phzs + kz0;
         pencil_fft<N, P, true, true>(
             buf, buf2, tw,
             [&](int q, int n) {

@@ -233,7 +233,7 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
         break;
       case FA_Y:
         if (a.yzphase)
-          MFX_FF_PERSISTENT((k_fa_y<N, true>), F::t2, F::s2 + size_t(N) * 8, size_t(N) * (F::Kh / F::P2) * 6, s, a);
+          MFX_FF_PERSISTENT((k_fa_y<N, true>), F::t2, F::s2 + size_t(N + F::Kh) * 8, size_t(N) * (F::Kh / F::P2) * 6, s, a);
         else
           MFX_FF_PERSISTENT((k_fa_y<N, false>), F::t2, F::s2, size_t(N) * (F::Kh / F::P2) * 6, s, a);
         break;
