@@ -115,6 +115,10 @@ template <int N> struct FA {
   static constexpr size_t s1h = size_t(N + N * P8 + 3 * N * P8) * sizeof(float2) +
                                 size_t(PltSlice<N, P8>::elems) * sizeof(float4);
   static constexpr bool halves = Kh % P8 == 0 && s1h <= 227 * 1024;
+  // the x factors of the phases of two shared x pass outputs (x-only), staged
+  // after the PLT slice when they fit
+  static constexpr size_t s1h_x = 2 * size_t(N) * sizeof(float2);
+  static constexpr bool halves_xs = s1h + s1h_x <= 227 * 1024;
   static constexpr size_t s2 = size_t(N + nbuf * Tile<N, P2, true>::elems + 2 * N * P2) * sizeof(float2);
   // CTAs per SM the registers are sized for: no more than shared memory allows
   static constexpr int minb2 = min_blocks(t2) < int(233472 / (s2 + 1024)) ? min_blocks(t2)
@@ -236,7 +240,13 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
   using T = Tile<N, P, true>;
   float2 *tw = ff_smem(), *buf = tw + N, *pv = buf + T::elems;  // pv [3][mode]
   float4 *plts = reinterpret_cast<float4 *>(pv + 3 * N * P);    // PLT slice
-  load_tw<N>(tw, a.tw);
+  // x-only phases from shared memory (two outputs at most), else global
+  float2 *phx = reinterpret_cast<float2 *>(plts + PltSlice<N, P>::elems);
+  const bool xs = F::halves_xs && a.xonly && a.nsub <= 2;
+  if (xs)
+    for (int t = threadIdx.x; t < a.nsub * N; t += NT)
+      phx[t] = a.as.phase32[size_t(a.xsub[t / N]) * 3 * N + (t - (t / N) * N)];
+  load_tw<N>(tw, a.tw);  // includes a barrier
 #pragma unroll 1
   for (unsigned u = blockIdx.x; u < unsigned(N * KB); u += gridDim.x) {
     const int j = int(u / KB), kz0 = int(u % KB) * P;
@@ -268,7 +278,11 @@ __global__ void __launch_bounds__(FA<N>::t1h, 1) k_fa_x_halves(FAArgs a) {
           for (int t = threadIdx.x; t < N * P; t += NT) {
             const int i = t / P, p = t - (t / P) * P;
             float er, ei;
-            if (a.xonly) {
+            if (xs) {
+              const float2 e = phx[s * N + i];
+              er = e.x;
+              ei = e.y;
+            } else if (a.xonly) {
               const float2 e = a.as.phase32[size_t(a.xsub[s]) * 3 * N + i];
               er = e.x;
               ei = e.y;

@@ -214,8 +214,8 @@ template <int M> cudaError_t fa_launch_m(int op, bool plt, const FAArgs &a, cuda
       case FA_X:
         if (a.nsub > 1 && a.halves) {
           if constexpr (F::halves) {
-            if (plt) MFX_FF_PERSISTENT((k_fa_x_halves<N, true>), F::t1h, F::s1h, size_t(N) * (F::Kh / F::P8), s, a);
-            else MFX_FF_PERSISTENT((k_fa_x_halves<N, false>), F::t1h, F::s1h, size_t(N) * (F::Kh / F::P8), s, a);
+            if (plt) MFX_FF_PERSISTENT((k_fa_x_halves<N, true>), F::t1h, F::s1h + (F::halves_xs ? F::s1h_x : 0), size_t(N) * (F::Kh / F::P8), s, a);
+            else MFX_FF_PERSISTENT((k_fa_x_halves<N, false>), F::t1h, F::s1h + (F::halves_xs ? F::s1h_x : 0), size_t(N) * (F::Kh / F::P8), s, a);
           } else {
             return cudaErrorInvalidValue;
           }
