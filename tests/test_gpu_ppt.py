@@ -43,3 +43,24 @@ def test_ppt_needs_potentials(mfxlib, engine):
     with pytest.raises(mfxlib.MfxError):
         j.ppt_fields()
     j.close()
+
+
+def test_ppt_fields_with_music1_noise(mfxlib, engine, oracle):
+    """MUSIC1 noise fills the Nyquist planes the PPT fields' transforms see."""
+    n, order = 32, 2
+    c = Case(mfxlib, n, 200.0, 49.0, order, 1)
+    w = oracle.music_fill(n, 4321, 8)
+    w[0, 0, 0] = 0.0
+    res = oracle.run_lpt(n, c.L, None, c.amplitude, order, c.dplus, c.vfac, lunit=c.lunit, vunit=c.vunit,
+                         want_particles=False, noise=w)
+    ref = oracle.ppt_fields(res["phi"], res["phi2"], res["noise"], order, n, c.L, c.dplus, c.coef["vfac1"], c.vunit)
+    j = mfxlib.Job(engine, n, c.L, order, None, c.amp, c.coef, precision=mfxlib.FP64, want_particles=False,
+                   lunit=c.lunit, vunit=c.vunit, noise_generator=mfxlib.NOISE_MUSIC1, music_seed=4321,
+                   music_cubesize=8)
+    j.run()
+    delta, vel, hbar = j.ppt_fields()
+    j.close()
+    assert abs(hbar - ref[2]) <= 1e-12 * ref[2]
+    assert rel_l2(delta, ref[0]) < TOL_FP64
+    for d in range(3):
+        assert rel_l2(vel[d], ref[1][d]) < TOL_FP64
