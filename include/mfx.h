@@ -44,6 +44,9 @@ extern "C" {
 /* white-noise generators (the [random] generator key) */
 #define MFX_NOISE_NGENIC 0
 #define MFX_NOISE_MUSIC1 1
+/* a white-noise field given in real space (noise_field): MUSIC1's noise read
+   from a file in place of a seed (random_music_wnoise_generator.cc:68-282) */
+#define MFX_NOISE_FIELD 2
 
 /* fields fetchable with mfx_job_fetch_field (k-space, N x N x (N/2+1) complex) */
 #define MFX_FIELD_NOISE 0 /* white noise as RNG_plugin::Fill_Grid leaves it   */
@@ -110,6 +113,11 @@ typedef struct {
      random_music_wnoise_generator.cc:392-547).  Seeds at finer levels than
      the grid's (restriction) are not supported. */
   int64_t music_seeds[12];
+  /* MFX_NOISE_FIELD: ngrid^3 doubles, [x][y][z] with z fastest, the values
+     Fill_Grid copies into the grid; read at every run of the job (host
+     memory: page-locked memory must stay unchanged until the run's noise
+     stage has finished) */
+  const double *noise_field;
 } mfx_job_desc;
 
 /* ---- errors -------------------------------------------------------------- */

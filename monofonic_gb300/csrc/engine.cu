@@ -339,6 +339,8 @@ static int check_desc(const mfx_job_desc *d) {
       return set_error(MFX_EINVAL, "MUSIC1 cubesize %u does not tile ngrid %u", cs, d->ngrid);
     if (std::min(cs, d->ngrid) > 256u)
       return set_error(MFX_EINVAL, "MUSIC1 cubes above 256^3 cells (one sequential stream each) are not supported");
+  } else if (d->noise_generator == MFX_NOISE_FIELD) {
+    if (!d->noise_field) return set_error(MFX_EINVAL, "MFX_NOISE_FIELD needs noise_field");
   } else {
     return set_error(MFX_EINVAL, "unknown noise_generator %d", d->noise_generator);
   }
@@ -415,6 +417,7 @@ static Layout plan_layout(const mfx_job_desc *d, size_t work_bytes, bool group_a
   L.work_est = align_up(work_bytes);
   // MUSIC1 from coarser seeded levels: two coarse-level k-space fields
   L.music = 0;
+  if (d->noise_generator == MFX_NOISE_FIELD) L.music = align_up(size_t(N) * N * N * 8);  // the field's upload
   if (d->noise_generator == MFX_NOISE_MUSIC1) {
     const MusicLevels ml = music_levels(d);
     if (ml.l0 < ml.lmin) L.music = 2 * align_up(n_field_bytes(N / 2, rs));
@@ -618,7 +621,16 @@ template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
     return exec_fft(j, plan, buf, true);
   };
   const double cells = double(N) * N * N;
-  if (j->music_l0 == j->music_lmin) {
+  if (j->d.noise_generator == MFX_NOISE_FIELD) {
+    // the given real-space field: uploaded, rounded into the padded layout,
+    // transformed (pageable memory is staged before the copy call returns)
+    CU(cudaMemcpyAsync(j->music_buf[0], j->d.noise_field, size_t(cells) * 8, cudaMemcpyHostToDevice, j->stream));
+    KBEGIN(j);
+    music::k_field_to_padded<R><<<grid_for(size_t(cells), 256, num_sm()), 256, 0, j->stream>>>(
+        (const double *)j->music_buf[0], (R *)out, N);
+    KEND(j, "field_to_padded", cells * (8.0 + sizeof(R)));
+    TRY(exec_fft(j, j->n_r2c, out, true));
+  } else if (j->music_l0 == j->music_lmin) {
     TRY(level(j->music_lmin, out, j->n_r2c));
   } else if (j->music_l0 > j->music_lmin) {
     // the finer seeded level, restricted one level at a time in k-space; the
@@ -663,6 +675,7 @@ template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
   k.N = N;
   k.mode = mode;
   k.fixing = j->d.fixing;
+  k.keep_dc = j->d.noise_generator == MFX_NOISE_FIELD;
   k.unit = 1.0 / std::sqrt(cells);
   const double volfac = std::pow(j->d.boxlen / N / 2.0 / M_PI, 1.5);
   k.norm = (j->d.inversion ? -1.0 : 1.0) / volfac;
@@ -675,7 +688,7 @@ template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
 }
 
 template <typename R> static int make_noise(mfx_job *j, int mode, void *out) {
-  return j->d.noise_generator == MFX_NOISE_MUSIC1 ? launch_music<R>(j, mode, out) : launch_noise<R>(j, mode, out);
+  return j->d.noise_generator == MFX_NOISE_NGENIC ? launch_noise<R>(j, mode, out) : launch_music<R>(j, mode, out);
 }
 
 static const int8_t kHa[6] = {0, 1, 2, 0, 0, 1};
@@ -1656,6 +1669,10 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
     if ((rc = acquire_plan(eng, j->n_c2r, j->N, j->fp64, false, 6, nfb)) != MFX_OK) return fail(rc);
     work = std::max(work, j->n_c2r.work);
   }
+  if (d->noise_generator == MFX_NOISE_FIELD) {
+    if ((rc = acquire_plan(eng, j->n_r2c, j->N, j->fp64, true)) != MFX_OK) return fail(rc);
+    work = std::max(work, j->n_r2c.work);
+  }
   if (d->noise_generator == MFX_NOISE_MUSIC1) {
     if ((rc = acquire_plan(eng, j->n_r2c, j->N, j->fp64, true)) != MFX_OK) return fail(rc);
     work = std::max(work, j->n_r2c.work);
@@ -1747,7 +1764,8 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
     j->music_buf[0] = p;
     // the second coarse buffer of a refinement; of a restriction, the level
     // below the seeded one
-    j->music_buf[1] = j->music_l0 < j->music_lmin
+    j->music_buf[1] = d->noise_generator != MFX_NOISE_MUSIC1 ? nullptr
+                      : j->music_l0 < j->music_lmin
                           ? p + L.music / 2
                           : (j->music_l0 - j->music_lmin >= 2 ? p + align_up(n_field_bytes(1 << j->music_l0, j->rsize))
                                                              : nullptr);
@@ -1967,6 +1985,7 @@ int mfx_job_upload(mfx_job *job, const mfx_job_desc *desc) {
   if (desc->noise_generator == MFX_NOISE_MUSIC1 && music_levels(desc).l0 != job->music_l0)
     return set_error(MFX_EINVAL, "upload descriptor changes the coarsest seeded MUSIC1 level");
   job->d.seed_table = desc->seed_table;
+  job->d.noise_field = desc->noise_field;
   job->d.music_seed = desc->music_seed;
   std::memcpy(job->d.music_seeds, desc->music_seeds, sizeof(desc->music_seeds));
   job->d.amp_table = desc->amp_table;

@@ -293,12 +293,26 @@ __global__ void __launch_bounds__(256) k_music_hermitian_planes(typename Cplx<R>
   }
 }
 
+// A real-space field (double, [x][y][z]) into the padded real layout of an
+// in-place r2c, rounded to R
+template <typename R>
+__global__ void __launch_bounds__(256) k_field_to_padded(const double *src, R *dst, int n) {
+  const size_t total = size_t(n) * n * n;
+  const size_t row = 2 * size_t(n / 2 + 1);
+  for (size_t idx = size_t(blockIdx.x) * blockDim.x + threadIdx.x; idx < total;
+       idx += size_t(gridDim.x) * blockDim.x) {
+    const size_t k = idx % n, col = idx / n;
+    dst[col * row + k] = R(src[idx]);
+  }
+}
+
 struct KArgs {
   const double *amp;  // amp[n] = amplitude(kf sqrt n)/(kf^2 n)
   size_t amp_len;
   int N;
   int mode;           // 0: raw noise, 1: normalised noise, 2: phi(1)
   int fixing;
+  int keep_dc;        // 1: the k = 0 mode stays (a given field's mean); 0: zero
   double unit;        // 1/sqrt(N^3): the forward transform's norm
   double norm;        // (+-1)/volfac
   double out_scale;   // extra factor on phi(1) (per-field scaling of the FP32 form)
@@ -316,7 +330,7 @@ template <typename R> __global__ void __launch_bounds__(256) k_music_phi1(KArgs 
     const int k = int(idx % nk);
     const size_t col = idx / nk;
     const int j = int(col % N), i = int(col / N);
-    if ((i | j | k) == 0) {
+    if ((i | j | k) == 0 && (a.mode == 2 || !a.keep_dc)) {
       f[idx] = mkc<R>(R(0), R(0));
       continue;
     }

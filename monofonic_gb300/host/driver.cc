@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <new>
@@ -114,6 +115,74 @@ class binary_output_plugin : public output_plugin {
 };
 
 namespace {
+// MUSIC1's white-noise file (grafic records, random_music_wnoise_generator.cc:
+// 68-282): a header record (nx ny nz iseed as 32-bit ints) and nz records of
+// nx*ny floats or doubles, each record framed by its byte count (32- or
+// 64-bit markers); value (x, y) of record z, x fastest, goes to cell
+// [x][y][z], negated unless grafic_sign.  The result is [x][y][z], z fastest.
+std::vector<double> read_grafic_noise(const std::string &path, unsigned res, bool grafic_sign) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("Could not open random number file '" + path + "'!");
+  auto rd = [&](void *p, size_t n) {
+    f.read(reinterpret_cast<char *>(p), std::streamsize(n));
+    if (!f) throw std::runtime_error("corrupt random number file");
+  };
+  uint32_t b32 = 0, nx = 0, ny = 0, nz = 0;
+  int32_t iseed = 0;
+  rd(&b32, 4);
+  rd(&nx, 4);
+  int mw = 4;  // marker width
+  if (b32 != 16 || nx != res) {
+    f.seekg(0);
+    uint64_t b64 = 0;
+    rd(&b64, 8);
+    rd(&nx, 4);
+    if (b64 != 16 || nx != res) throw std::runtime_error("corrupt random number file");
+    mw = 8;
+  }
+  f.seekg(0);
+  auto marker = [&]() -> uint64_t {
+    uint64_t m = 0;
+    if (mw == 4) {
+      uint32_t m32 = 0;
+      rd(&m32, 4);
+      m = m32;
+    } else {
+      rd(&m, 8);
+    }
+    return m;
+  };
+  marker();
+  rd(&nx, 4);
+  rd(&ny, 4);
+  rd(&nz, 4);
+  rd(&iseed, 4);
+  marker();
+  if (nx != res || ny != res || nz != res)
+    throw std::runtime_error("White noise file dimensions do not match level dimensions");
+  const size_t plane = size_t(nx) * ny;
+  std::vector<double> out(plane * nz);
+  std::vector<float> buf4;
+  std::vector<double> buf8;
+  const double sign = grafic_sign ? 1.0 : -1.0;
+  for (uint32_t z = 0; z < nz; ++z) {
+    const uint64_t m = marker();
+    if (m == plane * 4) {
+      buf4.resize(plane);
+      rd(buf4.data(), plane * 4);
+      for (size_t q = 0; q < plane; ++q) out[((q % nx) * ny + q / nx) * nz + z] = sign * double(buf4[q]);
+    } else if (m == plane * 8) {
+      buf8.resize(plane);
+      rd(buf8.data(), plane * 8);
+      for (size_t q = 0; q < plane; ++q) out[((q % nx) * ny + q / nx) * nz + z] = sign * buf8[q];
+    } else {
+      throw std::runtime_error("corrupt random number file");
+    }
+    if (marker() != m) throw std::runtime_error("corrupt random number file");
+  }
+  return out;
+}
+
 std::unique_ptr<output_plugin> make_binary(const config_file &cf, const calculator &cc) {
   return std::make_unique<binary_output_plugin>(cf, cc);
 }
@@ -149,6 +218,7 @@ int run_config(mfx_engine *eng, const std::string &text) {
   const std::string gen = cf.get_value<std::string>("random", "generator");
   long seed = 0;
   int64_t music_seeds[12] = {};
+  std::vector<double> noise_file;  // MUSIC1 noise read from a file
   int noise_gen = MFX_NOISE_NGENIC;
   unsigned cubesize = 0;
   if (gen == "NGENIC") {
@@ -163,6 +233,17 @@ int run_config(mfx_engine *eng, const std::string &text) {
     for (int l = 0; l <= 100; ++l) {
       const std::string key = "seed[" + std::to_string(l) + "]";
       if (!cf.contains_key("random", key)) continue;
+      const std::string val = cf.get_value<std::string>("random", key);
+      const bool number = !val.empty() && val.find_first_not_of("-0123456789") == std::string::npos;
+      if (!number) {
+        // a white-noise file in place of the seed (random_music.cc:186-193)
+        if (l != lmin)
+          throw std::runtime_error("MUSIC1 " + key + ": a noise file is supported at log2(GridRes) = " +
+                                   std::to_string(lmin) + " only");
+        noise_file = read_grafic_noise(val, ngrid, cf.get_value_safe<bool>("random", "grafic_sign", false));
+        any = true;
+        continue;
+      }
       if (l > lmin + 3 || l >= 12)
         throw std::runtime_error("MUSIC1 " + key + ": seeds more than three levels finer than log2(GridRes) = " +
                                  std::to_string(lmin) + " are not supported");
@@ -172,9 +253,14 @@ int run_config(mfx_engine *eng, const std::string &text) {
       any = true;
     }
     if (!any) throw std::runtime_error("No seed specified for MUSIC1 RNG plugin!");
+    if (!noise_file.empty())
+      for (int l = 0; l < 12; ++l)
+        if (music_seeds[l] > 0)
+          throw std::runtime_error("MUSIC1: a noise file together with seed[" + std::to_string(l) +
+                                   "] is not supported");
     seed = music_seeds[lmin];
     cubesize = cf.get_value_safe<unsigned>("random", "cubesize", 32);
-    noise_gen = MFX_NOISE_MUSIC1;
+    noise_gen = noise_file.empty() ? MFX_NOISE_MUSIC1 : MFX_NOISE_FIELD;
   } else {
     throw std::runtime_error("random generator '" + gen + "' is not supported (NGENIC, MUSIC1)");
   }
@@ -217,6 +303,7 @@ int run_config(mfx_engine *eng, const std::string &text) {
   d.music_seed = noise_gen == MFX_NOISE_MUSIC1 ? seed : 0;
   d.music_cubesize = cubesize;
   std::memcpy(d.music_seeds, music_seeds, sizeof(music_seeds));
+  d.noise_field = noise_file.empty() ? nullptr : noise_file.data();
   d.amp_table = amp.data();
   d.amp_table_len = alen;
   d.plt_table = do_plt ? plt.data() : nullptr;

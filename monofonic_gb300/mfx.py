@@ -14,7 +14,7 @@ from . import build as _build
 
 MFX_OK, MFX_EINVAL, MFX_ENOMEM, MFX_ECUDA, MFX_ETIMEOUT, MFX_ECANCEL, MFX_ESTATE, MFX_EADMIT = 0, -1, -2, -3, -4, -5, -6, -7
 SC, BCC, FCC = 0, 1, 2
-NOISE_NGENIC, NOISE_MUSIC1 = 0, 1
+NOISE_NGENIC, NOISE_MUSIC1, NOISE_FIELD = 0, 1, 2
 FP64, FP32C = 0, 1
 FIELD_NOISE, FIELD_PHI1, FIELD_PHI2, FIELD_PHI3, FIELD_A3X, FIELD_A3Y, FIELD_A3Z = range(7)
 PLT_NGRID = 64
@@ -60,6 +60,7 @@ class JobDesc(C.Structure):
         ("want_particles", C.c_int),
         ("noise_generator", C.c_int), ("music_seed", C.c_int64), ("music_cubesize", C.c_uint32),
         ("music_seeds", C.c_int64 * 12),
+        ("noise_field", C.c_void_p),
     ]
 
 
@@ -289,18 +290,21 @@ class Job:
     def __init__(self, engine: Engine, ngrid, boxlen, order, seed_table, amp_table, coef, lattice=SC,
                  precision=FP64, plt_table=None, fixing=False, inversion=False, lunit=1.0, vunit=1.0,
                  pos64=True, vel64=True, id64=True, id_offset=0, want_particles=True,
-                 noise_generator=None, music_seed=0, music_cubesize=32, music_seeds=None):
+                 noise_generator=None, music_seed=0, music_cubesize=32, music_seeds=None, noise_field=None):
         """seed_table: NGenIC's per-column seeds; None with noise_generator=
         NOISE_MUSIC1, which draws the noise from music_seed (the seed at the
         grid's level) and music_cubesize, or from music_seeds {level: seed}
-        given at coarser levels as well."""
+        given at coarser levels as well; noise_field: a real-space white-noise
+        field [x][y][z] (NOISE_FIELD), e.g. MUSIC1's noise read from a file."""
         self.engine = engine
         self.n = ngrid
         self.lattice = lattice
         self.precision = precision
         self.pos64, self.vel64, self.id64 = pos64, vel64, id64
+        self._field = None if noise_field is None else np.ascontiguousarray(noise_field, dtype=np.float64)
         if noise_generator is None:
-            noise_generator = NOISE_NGENIC if seed_table is not None else NOISE_MUSIC1
+            noise_generator = (NOISE_FIELD if self._field is not None else
+                               NOISE_NGENIC if seed_table is not None else NOISE_MUSIC1)
         self._seed = None if seed_table is None else np.ascontiguousarray(seed_table, dtype=np.uint32)
         self._amp = np.ascontiguousarray(amp_table, dtype=np.float64)
         self._plt = None if plt_table is None else np.ascontiguousarray(plt_table, dtype=np.float64)
@@ -315,6 +319,7 @@ class Job:
         d.music_cubesize = music_cubesize
         for level, sd in (music_seeds or {}).items():
             d.music_seeds[level] = sd
+        d.noise_field = self._field.ctypes.data if self._field is not None else None
         d.amp_table = self._amp.ctypes.data
         d.amp_table_len = self._amp.size
         d.plt_table = self._plt.ctypes.data if self._plt is not None else None
@@ -627,11 +632,15 @@ def desc_from_spec(sp):
     d.pos64, d.vel64, d.id64 = int(sp.get("pos64", True)), int(sp.get("vel64", True)), int(sp.get("id64", True))
     d.id_offset = sp.get("id_offset", 0)
     d.want_particles = int(sp.get("want_particles", True))
-    d.noise_generator = sp.get("noise_generator", NOISE_NGENIC if seed is not None else NOISE_MUSIC1)
+    field = sp.get("noise_field")
+    field = None if field is None else np.ascontiguousarray(field, dtype=np.float64)
+    d.noise_generator = sp.get("noise_generator", NOISE_FIELD if field is not None else
+                               NOISE_NGENIC if seed is not None else NOISE_MUSIC1)
+    d.noise_field = field.ctypes.data if field is not None else None
     d.music_seed, d.music_cubesize = sp.get("music_seed", 0), sp.get("music_cubesize", 32)
     for level, sd in (sp.get("music_seeds") or {}).items():
         d.music_seeds[level] = sd
-    return d, (seed, amp, plt)
+    return d, (seed, amp, plt, field)
 
 
 def footprint(engine, sp) -> int:

@@ -235,6 +235,32 @@ def music_levels(n: int, seeds: dict, cubesize: int = 32) -> np.ndarray:
     return f
 
 
+def read_grafic_noise(path: str, res: int, grafic_sign: bool = False) -> np.ndarray:
+    """MUSIC1's white-noise file (random_music_wnoise_generator.cc:68-282):
+    a header record (nx ny nz iseed, int32) and nz records of nx*ny float32 or
+    float64, framed by 32- or 64-bit byte counts; record z, x fastest, fills
+    [x][y][z], negated unless grafic_sign."""
+    raw = open(path, "rb").read()
+    mw = 4
+    if not (int.from_bytes(raw[0:4], "little") == 16 and int.from_bytes(raw[4:8], "little") == res):
+        mw = 8
+        if not (int.from_bytes(raw[0:8], "little") == 16 and int.from_bytes(raw[8:12], "little") == res):
+            raise ValueError("corrupt random number file")
+    pos = mw
+    nx, ny, nz, _ = np.frombuffer(raw[pos:pos + 16], np.int32)
+    pos += 16 + mw
+    assert nx == ny == nz == res
+    out = np.zeros((res, res, res))
+    for z in range(res):
+        m = int.from_bytes(raw[pos:pos + mw], "little")
+        pos += mw
+        dt = np.float32 if m == res * res * 4 else np.float64
+        rec = np.frombuffer(raw[pos:pos + m], dt).astype(np.float64).reshape(res, res)  # [y][x]
+        pos += m + mw
+        out[:, :, z] = rec.T
+    return out if grafic_sign else -out
+
+
 def music_fill(n: int, seed: int, cubesize: int = 32) -> np.ndarray:
     """RNG_music::Fill_Grid followed by the IC generator's forward transform:
     the k-space white noise (random_music.cc:92-116, ic_generator.cc:305-383)."""

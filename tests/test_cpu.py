@@ -311,3 +311,28 @@ def test_music_restriction_is_the_inverse_embedding(oracle):
     keep[4, :, :] = keep[:, 4, :] = False
     keep[:, :, 4] = False
     assert np.max(np.abs(back[keep] - cc[keep])) < 1e-10
+
+
+def write_grafic(path, field_xyz, marker=4, dtype=np.float32, sign=-1.0):
+    """A MUSIC1 white-noise file holding field_xyz ([x][y][z]) as the reader
+    of random_music_wnoise_generator.cc:68-282 expects it (values stored
+    negated for the default grafic_sign = false)."""
+    n = field_xyz.shape[0]
+    mk = (lambda v: np.array([v], np.uint32 if marker == 4 else np.uint64).tobytes())
+    with open(path, "wb") as f:
+        f.write(mk(16) + np.array([n, n, n, 7], np.int32).tobytes() + mk(16))
+        for z in range(n):
+            rec = (sign * field_xyz[:, :, z].T).astype(dtype).tobytes()  # [y][x], x fastest
+            f.write(mk(len(rec)) + rec + mk(len(rec)))
+
+
+@pytest.mark.parametrize("marker,dtype", [(4, np.float32), (8, np.float64)])
+def test_grafic_noise_reader(oracle, tmp_path, marker, dtype):
+    rng = np.random.default_rng(3)
+    field = rng.standard_normal((8, 8, 8))
+    p = tmp_path / "wn.bin"
+    write_grafic(p, field, marker, dtype)
+    got = oracle.read_grafic_noise(str(p), 8)
+    tol = 1e-6 if dtype == np.float32 else 0.0
+    assert np.max(np.abs(got - field)) <= tol
+    assert np.allclose(oracle.read_grafic_noise(str(p), 8, grafic_sign=True), -got)

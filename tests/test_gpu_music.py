@@ -178,3 +178,45 @@ def test_run_config_music1_multilevel(mfxlib, engine, tmp_path):
     pos, vel, ids = j.particles()
     off = 8 + 8 + 4 + 4 + 24
     assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
+
+
+def test_noise_field_matches_oracle(mfxlib, engine, oracle):
+    """A white-noise field given in real space (MFX_NOISE_FIELD): its unitary
+    forward transform, the mean kept in the raw noise (zeroed in phi(1))."""
+    n = 32
+    rng = np.random.default_rng(17)
+    field = rng.standard_normal((n, n, n)) + 0.01
+    c = Case(mfxlib, n, 100.0, 49.0, 2, 1)
+    j = mfxlib.Job(engine, n, c.L, 2, None, c.amp, c.coef, precision=mfxlib.FP64, lunit=c.lunit, vunit=c.vunit,
+                   noise_field=field)
+    j.run_noise(raw=True)
+    ref = oracle.fft_r2c(field)
+    assert rel_l2(j.field(mfxlib.FIELD_NOISE), ref) < 1e-13
+    j.run()
+    res = oracle.run_lpt(n, c.L, None, c.amplitude, 2, c.dplus, c.vfac, lunit=c.lunit, vunit=c.vunit, noise=ref)
+    check_fields(mfxlib, j, res, 2, TOL_FP64)
+    check_particles(c, j, res, TOL_FP64)
+
+
+def test_run_config_music1_noise_file(mfxlib, engine, tmp_path):
+    """[random] seed[log2 GridRes] = <file>: the grafic white noise read by the
+    driver (negated unless grafic_sign), the same particles as a job given the
+    field."""
+    from test_cpu import write_grafic
+    n = 32
+    rng = np.random.default_rng(5)
+    field = rng.standard_normal((n, n, n))
+    wn = tmp_path / "wn.bin"
+    write_grafic(wn, field)
+    f = tmp_path / "ics.bin"
+    txt = mfxlib.ini_text(n, 50.0, 24.0, 2, 777, "sc", filename=str(f), generator="MUSIC1")
+    engine.run_config(txt.replace("seed[5] = 777", "seed[5] = %s" % wn))
+    raw = f.read_bytes()
+    np_ = int(np.frombuffer(raw[8:16], np.uint64)[0])
+    c = Case(mfxlib, n, 50.0, 24.0, 2, 1)
+    j = mfxlib.Job(engine, n, c.L, 2, None, c.amp, c.coef, precision=mfxlib.FP64, lunit=c.lunit, vunit=c.vunit,
+                   noise_field=field.astype(np.float32).astype(np.float64))
+    j.run()
+    pos, vel, ids = j.particles()
+    off = 8 + 8 + 4 + 4 + 24
+    assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
