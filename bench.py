@@ -340,34 +340,73 @@ def run_ours(args):
         except RuntimeError:
             continue
     progress("end to end, pipelined with %d device set(s)" % ring)
+    modes = {}
     if ring:
         nh = host_sets
         host = [(pinned(npart * 3 * 8), pinned(npart * 3 * (8 if vel64 else 4)), pinned(npart * 8)) for _ in range(nh)]
-        sets = [tuple(x[1] for x in st) for st in host]  # numpy views; `host` keeps the tensors alive
+        hsets = [tuple(x[1] for x in st) for st in host]  # numpy views; `host` keeps the tensors alive
 
         def step(k):
             job.upload(hs, ha, hp)
             job.run(wait=False)
-            p, v, i = sets[k % nh]
+            p, v, i = hsets[k % nh]
             job.fetch_particles_range_async(0, npart, p.ctypes.data, v.ctypes.data, i.ctypes.data)
 
-        for k in range(2):
-            step(k)
-        job.wait()
-        job.wait_fetch()
-        barrier()
-        t1 = time.perf_counter()
-        for k in range(args.steps):
-            step(k)
-        job.wait()
-        job.wait_fetch()
-        barrier()
-        e2e_ms, e2e_val = replica_throughput((time.perf_counter() - t1) * 1e3 / args.steps, npart, device="cuda")
-        e2e = {"value": e2e_val, "unit": "particles/s", "ms_per_step": e2e_ms,
-               "mode": ("pipelined: step k+1 computes while step k's particles download (output ring of two sets)"
-                        if ring == 2 else
-                        "pipelined: step k+1's noise and potentials run while step k's particles download "
-                        "(output ring of one set; its assembly waits for the download)")}
+        def pipelined():
+            for k in range(2):
+                step(k)
+            job.wait()
+            job.wait_fetch()
+            barrier()
+            t1 = time.perf_counter()
+            for k in range(args.steps):
+                step(k)
+            job.wait()
+            job.wait_fetch()
+            barrier()
+            return replica_throughput((time.perf_counter() - t1) * 1e3 / args.steps, npart, device="cuda")
+
+        mode = ("pipelined: step k+1 computes while step k's particles download (output ring of two sets)"
+                if ring == 2 else
+                "pipelined: step k+1's noise and potentials run while step k's particles download "
+                "(output ring of one set; its assembly waits for the download)")
+        e2e_ms, e2e_val = pipelined()
+        modes["device_positions"] = {"value": e2e_val, "ms_per_step": e2e_ms, "d2h_bytes_per_step": int(d2h),
+                                     "device_sets": ring}
+        e2e = {"value": e2e_val, "unit": "particles/s", "ms_per_step": e2e_ms, "mode": mode}
+        # the other output form of the same public API: float displacements
+        # cross the host link and the fetch's host threads form q + Psi in FP64
+        # (the same doubles).  Which is faster depends on the machine's host link
+        # against its host memory bandwidth; the line reports the faster.
+        if prec == mfx.FP32C and not host_pos:
+            try:
+                job.set_output_ring(0)
+                job.set_host_positions(True)
+                # float displacements make a device set smaller: two may fit
+                # where only one did
+                ring2 = 0
+                for nsets in (2, 1):
+                    try:
+                        job.set_output_ring(nsets)
+                        ring2 = nsets
+                        break
+                    except RuntimeError:
+                        continue
+                if ring2:
+                    progress("end to end, pipelined with %d device set(s), positions formed on the host" % ring2)
+                    ms2, val2 = pipelined()
+                    d2h2 = npart * (3 * 4 + 3 * (8 if vel64 else 4))
+                    modes["host_positions"] = {"value": val2, "ms_per_step": ms2, "d2h_bytes_per_step": int(d2h2),
+                                               "device_sets": ring2}
+                    if val2 > e2e_val:
+                        mode2 = ("pipelined: step k+1 computes while step k's particles download "
+                                 "(output ring of two sets)" if ring2 == 2 else mode)
+                        e2e = {"value": val2, "unit": "particles/s", "ms_per_step": ms2, "mode": mode2}
+                        host_pos, d2h = True, d2h2
+                job.set_output_ring(0)
+                job.set_host_positions(False)
+            except RuntimeError:
+                pass
         job.set_output_ring(0)
     e2e.update({"h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ids": "written into the host buffers by the fetch (host threads, beside the copies)",
@@ -375,6 +414,8 @@ def run_ours(args):
                               if host_pos else "FP64 positions copied")})
     if ring:
         e2e["serial"] = e2e_serial
+    if modes:
+        e2e["output_forms"] = modes
 
     out = None
     if rank == 0:
