@@ -342,11 +342,17 @@ __device__ __forceinline__ void pencil_fft(float2 *buf, float2 *buf2, const floa
 #endif
 
 #if defined(__CUDACC__)
+// a step hook that does nothing
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
 // One step of the in-place, multi-item form: NT threads each hold up to
-// ceil(PP J / NT) butterflies, read all of them (ld), meet at a barrier and
-// write them (st); task order as split<PP, J, PF>.
-template <int L, int R, int NS, bool INV, int PP, bool PF, int NT, class Ld, class St>
-__device__ __forceinline__ void mi_step(const float2 *tw, const Ld &ld, const St &st) {
+// ceil(PP J / NT) butterflies, read all of them (ld), meet at a barrier, call
+// hk (every thread: the step's source is no longer read) and write them (st);
+// task order as split<PP, J, PF>.
+template <int L, int R, int NS, bool INV, int PP, bool PF, int NT, class Ld, class St, class Hk = NoHook>
+__device__ __forceinline__ void mi_step(const float2 *tw, const Ld &ld, const St &st, const Hk &hk = Hk()) {
   using S = Step<L, R, NS, INV>;
   constexpr int NI = PP * S::J, I = (NI + NT - 1) / NT;
   float2 v[I][R];
@@ -360,6 +366,7 @@ __device__ __forceinline__ void mi_step(const float2 *tw, const Ld &ld, const St
     }
   }
   __syncthreads();
+  hk();
 #pragma unroll
   for (int it = 0; it < I; ++it) {
     const int t = int(threadIdx.x) + it * NT;
@@ -375,21 +382,26 @@ __device__ __forceinline__ void mi_step(const float2 *tw, const Ld &ld, const St
 // the x/y tiles fewer than PP * maxJ: the tiles too wide for one butterfly
 // per thread).  ld(q, n) may read buf and st(q, k, v) may write it; the
 // caller synchronises before reading what st wrote.  One barrier per step and
-// one between steps.
-template <int L, int PP, bool PF, bool INV, int NT, class Ld, class St>
-__device__ __forceinline__ void pencil_fft_mi(float2 *buf, const float2 *tw, const Ld &ld, const St &st) {
+// one between steps.  h1 runs (every thread) once the first step has read its
+// input, h2 once the last step has read buf.
+// LD (PF only): the row stride of buf, for PP pencils within a wider tile
+template <int L, int PP, bool PF, bool INV, int NT, int LD = PP, class Ld, class St, class H1 = NoHook,
+          class H2 = NoHook>
+__device__ __forceinline__ void pencil_fft_mi(float2 *buf, const float2 *tw, const Ld &ld, const St &st,
+                                              const H1 &h1 = H1(), const H2 &h2 = H2()) {
   using F = Fac<L>;
   using T = Tile<L, PP, PF>;
-  auto lb = [&](int q, int n) { return buf[T::at(q, n)]; };
-  auto sb = [&](int q, int n, float2 x) { buf[T::at(q, n)] = x; };
-  mi_step<L, F::R1, 1, INV, PP, PF, NT>(tw, ld, sb);
+  auto at = [](int q, int n) { return PF ? n * LD + q : T::at(q, n); };
+  auto lb = [&](int q, int n) { return buf[at(q, n)]; };
+  auto sb = [&](int q, int n, float2 x) { buf[at(q, n)] = x; };
+  mi_step<L, F::R1, 1, INV, PP, PF, NT>(tw, ld, sb, h1);
   __syncthreads();
   if constexpr (F::steps == 3) {
     mi_step<L, F::R2, F::R1, INV, PP, PF, NT>(tw, lb, sb);
     __syncthreads();
   }
   constexpr int RL = F::steps == 3 ? F::R3 : F::R2;
-  mi_step<L, RL, L / RL, INV, PP, PF, NT>(tw, lb, st);
+  mi_step<L, RL, L / RL, INV, PP, PF, NT>(tw, lb, st, h2);
 }
 #endif
 
@@ -566,12 +578,34 @@ __device__ __forceinline__ void stage_rows(float2 *stage, const float2 *src, uns
 // butterflies of a step (registers for them: the register file is shared out
 // in whole warps per scheduler), and one tile buffer (in-place transforms)
 // beside the staging.
+//
+// In-place form, for lean tiles whose two stages do not fit beside the tile
+// (P = 16 at M = 1152: 128-byte row pieces, where 64-byte ones halve the HBM
+// rate of these strided rows): one stage only, the tile itself, which holds
+// the unit's input rows from `side` up (at their stage positions r * P + q)
+// while rows below `side` sit in a side buffer.  The side buffer of the next
+// unit is fetched once the first transform step has read this unit's input,
+// the tile's rows once the last step has read the tile; a unit makes one
+// output (the transform overwrites its input).
+constexpr size_t kXYSmemMax = 227 * 1024;
 template <int M, int P, int ROWS> struct XY {
   static constexpr bool lean = P * Fac<M>::maxJ > 1024;
-  static constexpr int threads = lean ? (P * Fac<M>::maxJ / 3) / 32 * 32 : P * Fac<M>::maxJ;
-  static constexpr int minb = lean ? 1 : min_blocks(threads);
   static constexpr int nbuf = lean ? 1 : 2;
-  static constexpr size_t smem = size_t(M + nbuf * Tile<M, P, true>::elems + 2 * ROWS * P) * sizeof(float2);
+  static constexpr int tile = Tile<M, P, true>::elems;
+  static constexpr size_t staged(int rows) { return size_t(M + nbuf * tile + 2 * rows * P) * sizeof(float2); }
+  // decided on M rows, so that both row counts of a length take one form
+  static constexpr bool inplace = lean && staged(M) > kXYSmemMax;
+  // the in-place form transforms the tile in two halves of P / 2 pencils (the
+  // registers of a P / 2 tile: all of a step's data is held across its barrier)
+  static constexpr int HP = inplace ? P / 2 : P;
+  static constexpr bool hlean = HP * Fac<M>::maxJ > 1024;
+  static constexpr int threads = hlean ? (HP * Fac<M>::maxJ / 3) / 32 * 32 : HP * Fac<M>::maxJ;
+  static constexpr int minb = (lean || inplace) ? 1 : min_blocks(threads);
+  static constexpr size_t side_room = kXYSmemMax - size_t(M + tile) * sizeof(float2);
+  static constexpr int side = !inplace ? 0
+                              : (side_room / (P * sizeof(float2)) < size_t(ROWS) ? int(side_room / (P * sizeof(float2)))
+                                                                                   : ROWS);
+  static constexpr size_t smem = inplace ? size_t(M + tile + side * P) * sizeof(float2) : staged(ROWS);
 };
 
 // the transform of an x/y tile: pencil_fft, or pencil_fft_mi in the lean form
@@ -584,8 +618,60 @@ __device__ __forceinline__ void xy_fft(float2 *buf, float2 *buf2, const float2 *
   else
     pencil_fft<M, P, true, INV, LDB>(buf, buf2, tw, ld, st);
 }
+// The in-place form's transform: the P-pencil tile buf in two halves of P / 2
+// pencils, each in place in its columns (ld(q, n) and st(q, k, v) take the
+// tile's pencil index q < P).  The first steps of both halves run first (the
+// reads of the staged input), then h1 (the side buffer is free: the next
+// unit's side rows load during the remaining steps), then the other steps of
+// one half and of the other.  One copy of each step's code serves both halves
+// (two inlined copies spill); the halves touch disjoint columns.  The caller
+// synchronises before reading what st wrote.
+template <int M, int P, bool INV, class Ld, class St, class H1 = NoHook>
+__device__ __forceinline__ void xy_fft_halves(float2 *buf, const float2 *tw, const Ld &ld, const St &st,
+                                              const H1 &h1 = H1()) {
+  using F = Fac<M>;
+  constexpr int H = P / 2, NT = XY<M, P, M>::threads;
+#pragma unroll 1
+  for (int h = 0; h < 2; ++h) {
+    const int q0 = h * H;
+    mi_step<M, F::R1, 1, INV, H, true, NT>(
+        tw, [&](int q, int n) { return ld(q + q0, n); }, [&](int q, int n, float2 x) { buf[n * P + q0 + q] = x; });
+  }
+  h1();
+  __syncthreads();
+#pragma unroll 1
+  for (int h = 0; h < 2; ++h) {
+    const int q0 = h * H;
+    auto lb = [&](int q, int n) { return buf[n * P + q0 + q]; };
+    if constexpr (F::steps == 3) {
+      mi_step<M, F::R2, F::R1, INV, H, true, NT>(tw, lb, [&](int q, int n, float2 x) { buf[n * P + q0 + q] = x; });
+      __syncthreads();
+    }
+    constexpr int RL = F::steps == 3 ? F::R3 : F::R2;
+    mi_step<M, RL, M / RL, INV, H, true, NT>(tw, lb, [&](int q, int k, float2 v) { st(q + q0, k, v); });
+  }
+}
+// the same into the tile, then out2(q, k, v0, v1) for each pair of pencils
+// (q even) of each row k: a row's P pencils leave in one piece (128 bytes for
+// 16); h2 runs once the tile has been read
+template <int M, int P, bool INV, class Ld, class Out2, class H1 = NoHook, class H2 = NoHook>
+__device__ __forceinline__ void xy_fft_halves_out(float2 *buf, const float2 *tw, const Ld &ld, const Out2 &out2,
+                                                  const H1 &h1 = H1(), const H2 &h2 = H2()) {
+  xy_fft_halves<M, P, INV>(buf, tw, ld, [&](int q, int k, float2 v) { buf[k * P + q] = v; }, h1);
+  __syncthreads();
+  constexpr int PR = P / 2;  // pencil pairs per row
+  for (int t = threadIdx.x; t < M * PR; t += blockDim.x) {
+    const int k = t / PR, q = (t - k * PR) * 2;
+    const float4 v = *reinterpret_cast<const float4 *>(buf + k * P + q);
+    out2(q, k, make_float2(v.x, v.y), make_float2(v.z, v.w));
+  }
+  __syncthreads();
+  h2();
+}
+
 // the tile buffers and the staging area of an x/y kernel's shared memory
-template <int M, int P> struct XYMem {
+// (in the in-place form `stage` is the side buffer)
+template <int M, int P, int ROWS = M> struct XYMem {
   float2 *tw, *buf, *buf2, *stage;
   __device__ __forceinline__ XYMem(float2 *base) {
     tw = base;
@@ -594,6 +680,24 @@ template <int M, int P> struct XYMem {
     stage = buf + XY<M, P, M>::nbuf * Tile<M, P, true>::elems;
   }
 };
+
+// the in-place form's input rows: stage row r at side[r * P + q] below the
+// side buffer's rows, at tile[r * P + q] from there on
+struct SplitStage {
+  const float2 *side, *tile;
+  int lim;  // side rows * P
+  __device__ __forceinline__ float2 operator[](int i) const { return i < lim ? side[i] : tile[i]; }
+};
+
+// stages rows [r0, r1) of P complex (row r at src + r * stride) as dst[r * P + q]
+template <int P, int CHUNK>
+__device__ __forceinline__ void stage_row_range(float2 *dst, const float2 *src, unsigned stride, int r0, int r1) {
+  constexpr int per_row = P * 8 / CHUNK, E = CHUNK / 8;
+  for (int t = threadIdx.x + r0 * per_row; t < r1 * per_row; t += blockDim.x) {
+    const int r = t / per_row, c = t - r * per_row;
+    cp_async<CHUNK>(dst + r * P + c * E, src + r * stride + c * E);
+  }
+}
 
 // The persistent unit loop: fetch(u, stage) issues unit u's copies,
 // work(u, stage) transforms it.  One barrier per unit: after it every
@@ -619,118 +723,222 @@ __device__ __forceinline__ void xy_units(unsigned units, unsigned stage_elems, f
   }
 }
 
+// The in-place form's unit loop: src(u) is unit u's first input row (ROWS
+// rows, `stride` apart); work(u, stage, h1, h2) transforms unit u from the
+// SplitStage and calls h1 and h2 through its transforms (xy_fft), which fetch
+// the next unit's side rows and tile rows.  One barrier per unit: after it
+// every thread's copies of unit u have landed.
+template <int M, int P, int ROWS, int CHUNK = 16, class Src, class Work>
+__device__ __forceinline__ void xy_units_inplace(unsigned units, float2 *side, float2 *tile, unsigned stride,
+                                                 const Src &src, const Work &work) {
+  constexpr int S = XY<M, P, ROWS>::side;
+  const SplitStage st{side, tile, S * P};
+  unsigned u = blockIdx.x;
+  if (u < units) {
+    stage_row_range<P, CHUNK>(side, src(u), stride, 0, S);
+    stage_row_range<P, CHUNK>(tile, src(u), stride, S, ROWS);
+  }
+  cp_async_commit();
+#pragma unroll 1
+  for (; u < units; u += gridDim.x) {
+    const unsigned un = u + gridDim.x;
+    cp_async_wait_all();
+    __syncthreads();
+    work(
+        u, st,
+        [&] {
+          if (un < units) stage_row_range<P, CHUNK>(side, src(un), stride, 0, S);
+          cp_async_commit();
+        },
+        [&] {
+          if (un < units) stage_row_range<P, CHUNK>(tile, src(un), stride, S, ROWS);
+          cp_async_commit();
+        });
+  }
+}
+
 // Y3: B_o = inverse-y of fac (ky)^o phi, o < 3, padded in y.
-// units: (i < N) x (Kh/P kz blocks); input rows j < N of phi (8-byte aligned)
+// units: (i < N) x (Kh/P kz blocks), times the three outputs in the in-place
+// form; input rows j < N of phi (8-byte aligned)
 template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::threads, XY<M, P, 2 * M / 3>::minb)
     k_ff_y3(FArgs a) {
   using D = Dims<M>;
+  using X = XY<M, P, D::N>;
   constexpr int ROWS = D::N, KB = D::Kh / P;
   const XYMem<M, P> sm(ff_smem());
   float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
-  xy_units(
-      unsigned(D::N * KB), ROWS * P, stage,
-      [&](unsigned u, float2 *st) {
-        const unsigned i = u / KB, kz0 = (u % KB) * P;
-        stage_rows<P, ROWS, 8>(st, a.src[0] + (i * D::N * D::nk + kz0), D::nk);
-      },
-      [&](unsigned u, const float2 *st) {
-        const unsigned i = u / KB, kz0 = (u % KB) * P;
+  // output o of unit (i, kz block) from its staged rows
+  auto one = [&](unsigned i, unsigned kz0, int o, const auto &st, const auto &h1, const auto &h2) {
+    float2 *out = a.dst[o] + (i * M * D::Kh + kz0);
+    auto ld = [&](int q, int n) -> float2 {
+      const int j = unpad_index(n, D::N);
+      if (j < 0) return make_float2(0.f, 0.f);
+      const float2 v = st[j * P + q];
+      float f = a.fac;
+      if (o > 0) {
+        const float gy = (j != D::nh) ? float(sidx(j, D::N)) * a.kfac : 0.f;
+        f *= (o == 1) ? gy : gy * gy;
+      }
+      return make_float2(v.x * f, v.y * f);
+    };
+    if constexpr (X::inplace)
+      xy_fft_halves_out<M, P, true>(
+          buf, tw, ld,
+          [&](int q, int n, float2 v0, float2 v1) {
+            *reinterpret_cast<float4 *>(out + unsigned(n) * D::Kh + q) = make_float4(v0.x, v0.y, v1.x, v1.y);
+          },
+          h1, h2);
+    else
+      xy_fft<M, P, true, false>(buf, buf2, tw, ld, [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+  };
+  if constexpr (X::inplace) {
+    xy_units_inplace<M, P, ROWS, 8>(
+        unsigned(D::N * KB) * 3u, stage, buf, D::nk,
+        [&](unsigned u) {
+          const unsigned t = u / 3, i = t / KB, kz0 = (t % KB) * P;
+          return a.src[0] + (i * D::N * D::nk + kz0);
+        },
+        [&](unsigned u, const SplitStage &st, const auto &h1, const auto &h2) {
+          const unsigned t = u / 3, i = t / KB, kz0 = (t % KB) * P;
+          one(i, kz0, int(u % 3), st, h1, h2);
+        });
+  } else {
+    xy_units(
+        unsigned(D::N * KB), ROWS * P, stage,
+        [&](unsigned u, float2 *st) {
+          const unsigned i = u / KB, kz0 = (u % KB) * P;
+          stage_rows<P, ROWS, 8>(st, a.src[0] + (i * D::N * D::nk + kz0), D::nk);
+        },
+        [&](unsigned u, const float2 *st) {
+          const unsigned i = u / KB, kz0 = (u % KB) * P;
 #pragma unroll 1
-        for (int o = 0; o < 3; ++o) {
-          float2 *out = a.dst[o] + (i * M * D::Kh + kz0);
-          xy_fft<M, P, true, false>(
-              buf, buf2, tw,
-              [&](int q, int n) -> float2 {
-                const int j = unpad_index(n, D::N);
-                if (j < 0) return make_float2(0.f, 0.f);
-                const float2 v = st[j * P + q];
-                float f = a.fac;
-                if (o > 0) {
-                  const float gy = (j != D::nh) ? float(sidx(j, D::N)) * a.kfac : 0.f;
-                  f *= (o == 1) ? gy : gy * gy;
-                }
-                return make_float2(v.x * f, v.y * f);
-              },
-              [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
-        }
-      });
+          for (int o = 0; o < 3; ++o) one(i, kz0, o, st, NoHook(), NoHook());
+        });
+  }
 }
 
 // X inverse into C-space.  mode 0: the six Hessians from B0 = Y(phi),
 // B1 = Y(ky phi), B2 = Y(ky^2 phi) (slot order xx yy zz xy xz yz; the factor
 // -k_a k_b splits into its x and z parts): a unit stages one B tile and makes
-// every Hessian that derives from it (B0: xx zz xz, B1: xy yz, B2: yy).
+// every Hessian that derives from it (B0: xx zz xz, B1: xy yz, B2: yy), or in
+// the in-place form one Hessian (units over the six slots).
 // mode 1: component c of src[c] (units also run over c < ncomp).
-// units: (y < M) x (Kh/P kz blocks) x (3 sources | ncomp); input rows i < N
+// units: (y < M) x (Kh/P kz blocks) x (3 sources | 6 slots | ncomp); input rows i < N
 template <int M, int P> __global__ void __launch_bounds__(XY<M, P, 2 * M / 3>::threads, XY<M, P, 2 * M / 3>::minb)
     k_ff_x_inv(FArgs a) {
   using D = Dims<M>;
+  using X = XY<M, P, D::N>;
   constexpr int ROWS = D::N, KB = D::Kh / P;
   const XYMem<M, P> sm(ff_smem());
   float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
-  const unsigned nsrc = a.mode ? unsigned(a.ncomp) : 3u;
-  xy_units(
-      unsigned(M * KB) * nsrc, ROWS * P, stage,
-      [&](unsigned u, float2 *st) {
-        const unsigned s = u % nsrc, t = u / nsrc, yy = t / KB, kz0 = (t % KB) * P;
-        stage_rows<P, ROWS, 16>(st, a.src[s] + (yy * D::Kh + kz0), unsigned(M * D::Kh));
-      },
-      [&](unsigned u, const float2 *st) {
-        const unsigned s = u % nsrc, t = u / nsrc, yy = t / KB, kz0 = (t % KB) * P;
-        const unsigned off = yy * D::Kh + kz0;
-        // components made from source s: mode 0: B0 -> xx zz xz, B1 -> xy yz, B2 -> yy
-        const int ncs = a.mode ? 1 : (s == 0 ? 3 : (s == 1 ? 2 : 1));
+  // output slot c of the unit at offset off (kz block kz0) from its staged rows
+  auto one = [&](unsigned off, unsigned kz0, int c, const auto &st, const auto &h1, const auto &h2) {
+    float2 *out = a.dst[c] + off;
+    auto ld = [&](int q, int n) -> float2 {
+      const int i = unpad_index(n, D::N);
+      if (i < 0) return make_float2(0.f, 0.f);
+      float2 v = st[i * P + q];
+      if (a.mode == 0) {
+        const float gx = (i != D::nh) ? float(sidx(i, D::N)) * a.kfac : 0.f;
+        const float gz = float(kz0 + q) * a.kfac;
+        const float f = c == 0 ? -gx * gx : c == 1 ? -1.f : c == 2 ? -gz * gz : c == 3 ? -gx : c == 4 ? -gx * gz : -gz;
+        v.x *= f;
+        v.y *= f;
+      }
+      return v;
+    };
+    if constexpr (X::inplace)
+      xy_fft_halves_out<M, P, true>(
+          buf, tw, ld,
+          [&](int q, int n, float2 v0, float2 v1) {
+            *reinterpret_cast<float4 *>(out + unsigned(n) * M * D::Kh + q) = make_float4(v0.x, v0.y, v1.x, v1.y);
+          },
+          h1, h2);
+    else
+      xy_fft<M, P, true, false>(buf, buf2, tw, ld,
+                                [&](int q, int n, float2 v) { out[unsigned(n) * M * D::Kh + q] = v; });
+  };
+  if constexpr (X::inplace) {
+    // mode 0: slot c from source B0 (xx zz xz), B1 (xy yz) or B2 (yy)
+    const unsigned nout = a.mode ? unsigned(a.ncomp) : 6u;
+    auto source = [&](unsigned c) -> unsigned {
+      return a.mode ? c : (c == 1 ? 2u : (c == 3 || c == 5) ? 1u : 0u);
+    };
+    xy_units_inplace<M, P, ROWS>(
+        unsigned(M * KB) * nout, stage, buf, unsigned(M * D::Kh),
+        [&](unsigned u) {
+          const unsigned c = u % nout, t = u / nout, yy = t / KB, kz0 = (t % KB) * P;
+          return a.src[source(c)] + (yy * D::Kh + kz0);
+        },
+        [&](unsigned u, const SplitStage &st, const auto &h1, const auto &h2) {
+          const unsigned c = u % nout, t = u / nout, yy = t / KB, kz0 = (t % KB) * P;
+          one(yy * D::Kh + kz0, kz0, int(c), st, h1, h2);
+        });
+  } else {
+    const unsigned nsrc = a.mode ? unsigned(a.ncomp) : 3u;
+    xy_units(
+        unsigned(M * KB) * nsrc, ROWS * P, stage,
+        [&](unsigned u, float2 *st) {
+          const unsigned s = u % nsrc, t = u / nsrc, yy = t / KB, kz0 = (t % KB) * P;
+          stage_rows<P, ROWS, 16>(st, a.src[s] + (yy * D::Kh + kz0), unsigned(M * D::Kh));
+        },
+        [&](unsigned u, const float2 *st) {
+          const unsigned s = u % nsrc, t = u / nsrc, yy = t / KB, kz0 = (t % KB) * P;
+          const unsigned off = yy * D::Kh + kz0;
+          // components made from source s: mode 0: B0 -> xx zz xz, B1 -> xy yz, B2 -> yy
+          const int ncs = a.mode ? 1 : (s == 0 ? 3 : (s == 1 ? 2 : 1));
 #pragma unroll 1
-        for (int k = 0; k < ncs; ++k) {
-          const int c = a.mode ? int(s) : (s == 0 ? 2 * k : (s == 1 ? (k == 0 ? 3 : 5) : 1));
-          float2 *out = a.dst[c] + off;
-          xy_fft<M, P, true, false>(
-              buf, buf2, tw,
-              [&](int q, int n) -> float2 {
-                const int i = unpad_index(n, D::N);
-                if (i < 0) return make_float2(0.f, 0.f);
-                float2 v = st[i * P + q];
-                if (a.mode == 0) {
-                  const float gx = (i != D::nh) ? float(sidx(i, D::N)) * a.kfac : 0.f;
-                  const float gz = float(kz0 + q) * a.kfac;
-                  const float f = c == 0 ? -gx * gx : c == 1 ? -1.f : c == 2 ? -gz * gz : c == 3 ? -gx : c == 4 ? -gx * gz : -gz;
-                  v.x *= f;
-                  v.y *= f;
-                }
-                return v;
-              },
-              [&](int q, int n, float2 v) { out[unsigned(n) * M * D::Kh + q] = v; });
-        }
-      });
+          for (int k = 0; k < ncs; ++k) {
+            const int c = a.mode ? int(s) : (s == 0 ? 2 * k : (s == 1 ? (k == 0 ? 3 : 5) : 1));
+            one(off, kz0, c, st, NoHook(), NoHook());
+          }
+        });
+  }
 }
 
 // X forward: C-space layout -> B-space layout, keeping the N-grid kx.
 // units: (y < M) x (Kh/P kz blocks) x (c < ncomp); input rows n < M
 template <int M, int P> __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_x_fwd(FArgs a) {
   using D = Dims<M>;
+  using X = XY<M, P, M>;
   constexpr int ROWS = M, KB = D::Kh / P;
   const XYMem<M, P> sm(ff_smem());
   float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
   const unsigned nc = unsigned(a.ncomp);
-  xy_units(
-      unsigned(M * KB) * nc, ROWS * P, stage,
-      [&](unsigned u, float2 *st) {
-        const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
-        stage_rows<P, ROWS, 16>(st, a.src[c] + (yy * D::Kh + kz0), unsigned(M * D::Kh));
-      },
-      [&](unsigned u, const float2 *st) {
-        const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
-        float2 *dst = a.dst[c] + (yy * D::Kh + kz0);
-        xy_fft<M, P, false, false>(
-            buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
-            [&](int q, int k, float2 v) {
-              const int i = unpad_index(k, D::N);
-              if (i >= 0) dst[unsigned(i) * M * D::Kh + q] = v;
-            });
+  auto src = [&](unsigned u) {
+    const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
+    return a.src[c] + (yy * D::Kh + kz0);
+  };
+  auto one = [&](unsigned u, const auto &st, const auto &h1, const auto &h2) {
+    const unsigned c = u % nc, t = u / nc, yy = t / KB, kz0 = (t % KB) * P;
+    float2 *dst = a.dst[c] + (yy * D::Kh + kz0);
+    auto ld = [&](int q, int n) { return st[n * P + q]; };
+    if constexpr (X::inplace)
+      xy_fft_halves_out<M, P, false>(
+          buf, tw, ld,
+          [&](int q, int k, float2 v0, float2 v1) {
+            const int i = unpad_index(k, D::N);
+            if (i >= 0)
+              *reinterpret_cast<float4 *>(dst + unsigned(i) * M * D::Kh + q) = make_float4(v0.x, v0.y, v1.x, v1.y);
+          },
+          h1, h2);
+    else
+      xy_fft<M, P, false, false>(buf, buf2, tw, ld, [&](int q, int k, float2 v) {
+        const int i = unpad_index(k, D::N);
+        if (i >= 0) dst[unsigned(i) * M * D::Kh + q] = v;
       });
+  };
+  if constexpr (X::inplace) {
+    xy_units_inplace<M, P, ROWS>(unsigned(M * KB) * nc, stage, buf, unsigned(M * D::Kh), src, one);
+  } else {
+    xy_units(
+        unsigned(M * KB) * nc, ROWS * P, stage,
+        [&](unsigned u, float2 *st) { stage_rows<P, ROWS, 16>(st, src(u), unsigned(M * D::Kh)); },
+        [&](unsigned u, const float2 *st) { one(u, st, NoHook(), NoHook()); });
+  }
 }
 
 // Y forward.  MODE 0: keep the N-grid ky, zero every Nyquist index and the
@@ -744,57 +952,83 @@ template <int M, int P, int MODE>
 __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_y_fwd(FArgs a) {
   using D = Dims<M>;
   using T = Tile<M, P, true>;
+  using X = XY<M, P, M>;
   constexpr int ROWS = M, KB = D::Kh / P;
   const XYMem<M, P> sm(ff_smem());
   float2 *tw = sm.tw, *buf = sm.buf, *buf2 = sm.buf2, *stage = sm.stage;
   load_tw<M>(tw, a.tw);
   const unsigned nc = unsigned(a.ncomp);
-  xy_units(
-      unsigned(D::N * KB) * nc, ROWS * P, stage,
-      [&](unsigned u, float2 *st) {
-        const unsigned c = u % nc, t = u / nc, i = t / KB, kz0 = (t % KB) * P;
-        stage_rows<P, ROWS, 16>(st, a.src[c] + (i * M * D::Kh + kz0), unsigned(D::Kh));
-      },
-      [&](unsigned u, const float2 *st) {
-        const unsigned c = u % nc, t = u / nc, i = t / KB, kz0 = (t % KB) * P;
-        float2 *dst = a.dst[c];
-        if constexpr (MODE == 0) {
-          const float kx = float(sidx(int(i), D::N)) * a.kfac;
-          float2 *out = dst + i * D::N * D::nk + kz0;
-          xy_fft<M, P, false, false>(
-              buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
-              [&](int q, int k, float2 v) {
-                const int j = unpad_index(k, D::N);
-                if (j < 0) return;
-                const int kz = int(kz0) + q;
-                float2 r = make_float2(0.f, 0.f);
-                if (int(i) != D::nh && j != D::nh && (int(i) | j | kz) != 0) {
-                  const float ky = float(sidx(j, D::N)) * a.kfac, kk = float(kz) * a.kfac;
-                  const float f = -a.fac * __frcp_rn(kx * kx + ky * ky + kk * kk);
-                  r = make_float2(v.x * f, v.y * f);
-                }
-                out[unsigned(j) * D::nk + q] = r;
-              });
-          if (kz0 == 0)
-            for (int j = threadIdx.x; j < D::N; j += blockDim.x)
-              dst[(i * D::N + j) * D::nk + D::nh] = make_float2(0.f, 0.f);
-        } else {
-          float2 *out = dst + (i * M * D::Kh + kz0);
-          const bool row_kept = int(i) != D::nh;
-          float2 *mid = obuf<M>(buf, buf2);
-          xy_fft<M, P, false, false>(
-              buf, buf2, tw, [&](int q, int n) { return st[n * P + q]; },
-              [&](int q, int k, float2 v) {
-                const int j = unpad_index(k, D::N);
-                const bool keep = row_kept && j >= 0 && j != D::nh;
-                mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
-              });
-          __syncthreads();
-          xy_fft<M, P, true>(
-              buf, buf2, tw, [&](int q, int n) { return mid[T::at(q, n)]; },
-              [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+  auto src = [&](unsigned u) {
+    const unsigned c = u % nc, t = u / nc, i = t / KB, kz0 = (t % KB) * P;
+    return a.src[c] + (i * M * D::Kh + kz0);
+  };
+  auto one = [&](unsigned u, const auto &st, const auto &h1, const auto &h2) {
+    const unsigned c = u % nc, t = u / nc, i = t / KB, kz0 = (t % KB) * P;
+    float2 *dst = a.dst[c];
+    auto ld = [&](int q, int n) { return st[n * P + q]; };
+    if constexpr (MODE == 0) {
+      const float kx = float(sidx(int(i), D::N)) * a.kfac;
+      float2 *out = dst + i * D::N * D::nk + kz0;
+      // the N-grid spectrum's rows (nk apart: 8-byte aligned only)
+      auto put = [&](int q, int k, float2 v) {
+        const int j = unpad_index(k, D::N);
+        if (j < 0) return;
+        const int kz = int(kz0) + q;
+        float2 r = make_float2(0.f, 0.f);
+        if (int(i) != D::nh && j != D::nh && (int(i) | j | kz) != 0) {
+          const float ky = float(sidx(j, D::N)) * a.kfac, kk = float(kz) * a.kfac;
+          const float f = -a.fac * __frcp_rn(kx * kx + ky * ky + kk * kk);
+          r = make_float2(v.x * f, v.y * f);
         }
-      });
+        out[unsigned(j) * D::nk + q] = r;
+      };
+      if constexpr (X::inplace)
+        xy_fft_halves_out<M, P, false>(
+            buf, tw, ld,
+            [&](int q, int k, float2 v0, float2 v1) {
+              put(q, k, v0);
+              put(q + 1, k, v1);
+            },
+            h1, h2);
+      else
+        xy_fft<M, P, false, false>(buf, buf2, tw, ld, put);
+      if (kz0 == 0)
+        for (int j = threadIdx.x; j < D::N; j += blockDim.x)
+          dst[(i * D::N + j) * D::nk + D::nh] = make_float2(0.f, 0.f);
+    } else {
+      float2 *out = dst + (i * M * D::Kh + kz0);
+      const bool row_kept = int(i) != D::nh;
+      float2 *mid = obuf<M>(buf, buf2);
+      auto trunc = [&](int q, int k, float2 v) {
+        const int j = unpad_index(k, D::N);
+        const bool keep = row_kept && j >= 0 && j != D::nh;
+        mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
+      };
+      auto lm = [&](int q, int n) { return mid[T::at(q, n)]; };
+      if constexpr (X::inplace) {
+        xy_fft_halves<M, P, false>(buf, tw, ld, trunc, h1);
+        __syncthreads();
+        xy_fft_halves_out<M, P, true>(
+            buf, tw, lm,
+            [&](int q, int n, float2 v0, float2 v1) {
+              *reinterpret_cast<float4 *>(out + unsigned(n) * D::Kh + q) = make_float4(v0.x, v0.y, v1.x, v1.y);
+            },
+            NoHook(), h2);
+      } else {
+        xy_fft<M, P, false, false>(buf, buf2, tw, ld, trunc);
+        __syncthreads();
+        xy_fft<M, P, true>(buf, buf2, tw, lm, [&](int q, int n, float2 v) { out[unsigned(n) * D::Kh + q] = v; });
+      }
+    }
+  };
+  if constexpr (X::inplace) {
+    xy_units_inplace<M, P, ROWS>(unsigned(D::N * KB) * nc, stage, buf, unsigned(D::Kh), src, one);
+  } else {
+    xy_units(
+        unsigned(D::N * KB) * nc, ROWS * P, stage,
+        [&](unsigned u, float2 *st) { stage_rows<P, ROWS, 16>(st, src(u), unsigned(D::Kh)); },
+        [&](unsigned u, const float2 *st) { one(u, st, NoHook(), NoHook()); });
+  }
 }
 
 // ---------------------------------------------------------------------------

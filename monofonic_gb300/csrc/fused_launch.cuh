@@ -63,9 +63,12 @@ template <int M, int RW> constexpr bool ff_z_fits() {
   }
 }
 
-// an x/y tile of P pencils fits one CTA (threads, shared memory) and the kz range
+// an x/y tile of P pencils fits one CTA (threads, shared memory) and the kz
+// range; the in-place form needs a side buffer of at least one row
 template <int M, int P> constexpr bool xy_ok() {
-  return (M / 3) % P == 0 && XY<M, P, M>::threads <= 1024 && XY<M, P, M>::smem <= kFFSmemMax;
+  return (M / 3) % P == 0 && XY<M, P, M>::threads <= 1024 && XY<M, P, M>::smem <= kFFSmemMax &&
+         XY<M, P, 2 * M / 3>::smem <= kFFSmemMax && (!XY<M, P, M>::inplace || XY<M, P, M>::side > 0) &&
+         (!XY<M, P, 2 * M / 3>::inplace || XY<M, P, 2 * M / 3>::side > 0);
 }
 
 template <int M> bool ff_valid_m(int op, int p) {
@@ -120,11 +123,13 @@ template <int M, int P> cudaError_t ff_launch_xy(int op, const FArgs &a, cudaStr
     using XM = XY<M, P, M>;
     const size_t nc = size_t(a.ncomp > 0 ? a.ncomp : 1);
     switch (op) {
+      // the in-place form makes one output a unit: Y3's three, mode 0's six Hessians
       case FF_Y3:
-        MFX_FF_PERSISTENT((k_ff_y3<M, P>), XN::threads, XN::smem, size_t(N) * KB, s, a);
+        MFX_FF_PERSISTENT((k_ff_y3<M, P>), XN::threads, XN::smem, size_t(N) * KB * (XN::inplace ? 3 : 1), s, a);
         break;
       case FF_XINV:
-        MFX_FF_PERSISTENT((k_ff_x_inv<M, P>), XN::threads, XN::smem, size_t(M) * KB * (a.mode ? nc : 3), s, a);
+        MFX_FF_PERSISTENT((k_ff_x_inv<M, P>), XN::threads, XN::smem,
+                          size_t(M) * KB * (a.mode ? nc : (XN::inplace ? 6 : 3)), s, a);
         break;
       case FF_XFWD:
         MFX_FF_PERSISTENT((k_ff_x_fwd<M, P>), XM::threads, XM::smem, size_t(M) * KB * nc, s, a);

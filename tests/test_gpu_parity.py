@@ -314,11 +314,13 @@ def test_fused_transforms_match_cufft_path(mfxlib, engine, n, lattice, order, mo
     assert np.array_equal(pf[2], pr[2])
 
 
-@pytest.mark.parametrize("n,lean,plain", [(192, 32, 8), (384, 16, 8)])
+@pytest.mark.parametrize("n,lean,plain", [(192, 32, 8), (384, 16, 8), (384, 32, 8)])
 def test_lean_xy_tiles_match_plain_tiles(mfxlib, engine, n, lean, plain, monkeypatch):
     """x/y tiles too wide for one butterfly per thread (lean form: a third as
     many threads, in-place transforms) give the fields and particles of the
-    plain tiles to rounding."""
+    plain tiles to rounding; so do tiles whose two stages do not fit (384^3,
+    32 pencils: the in-place form, input rows split between a side buffer and
+    the tile, transformed in halves of 16 pencils)."""
     monkeypatch.setenv("MFX_FUSED", "1")
     c = Case(mfxlib, n, 300.0, 24.0, 3, 5, lattice=1, plt=engine.plt_table(1))
     fids = [mfxlib.FIELD_PHI2, mfxlib.FIELD_PHI3, mfxlib.FIELD_A3X, mfxlib.FIELD_A3Z]
