@@ -654,10 +654,8 @@ __device__ __forceinline__ void xy_fft_halves(float2 *buf, const float2 *tw, con
 // the same into the tile, then out2(q, k, v0, v1) for each pair of pencils
 // (q even) of each row k: a row's P pencils leave in one piece (128 bytes for
 // 16); h2 runs once the tile has been read
-template <int M, int P, bool INV, class Ld, class Out2, class H1 = NoHook, class H2 = NoHook>
-__device__ __forceinline__ void xy_fft_halves_out(float2 *buf, const float2 *tw, const Ld &ld, const Out2 &out2,
-                                                  const H1 &h1 = H1(), const H2 &h2 = H2()) {
-  xy_fft_halves<M, P, INV>(buf, tw, ld, [&](int q, int k, float2 v) { buf[k * P + q] = v; }, h1);
+template <int M, int P, class Out2, class H2 = NoHook>
+__device__ __forceinline__ void xy_store_rows(const float2 *buf, const Out2 &out2, const H2 &h2 = H2()) {
   __syncthreads();
   constexpr int PR = P / 2;  // pencil pairs per row
   for (int t = threadIdx.x; t < M * PR; t += blockDim.x) {
@@ -667,6 +665,12 @@ __device__ __forceinline__ void xy_fft_halves_out(float2 *buf, const float2 *tw,
   }
   __syncthreads();
   h2();
+}
+template <int M, int P, bool INV, class Ld, class Out2, class H1 = NoHook, class H2 = NoHook>
+__device__ __forceinline__ void xy_fft_halves_out(float2 *buf, const float2 *tw, const Ld &ld, const Out2 &out2,
+                                                  const H1 &h1 = H1(), const H2 &h2 = H2()) {
+  xy_fft_halves<M, P, INV>(buf, tw, ld, [&](int q, int k, float2 v) { buf[k * P + q] = v; }, h1);
+  xy_store_rows<M, P>(buf, out2, h2);
 }
 
 // the tile buffers and the staging area of an x/y kernel's shared memory
@@ -1005,15 +1009,55 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
         mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
       };
       auto lm = [&](int q, int n) { return mid[T::at(q, n)]; };
+      // lean forms: one copy of the transform's code for both transforms,
+      // the inverse as the conjugate of the forward transform of the
+      // conjugate (negations are exact: the same roundings); two inlined
+      // transforms spill
       if constexpr (X::inplace) {
-        xy_fft_halves<M, P, false>(buf, tw, ld, trunc, h1);
-        __syncthreads();
-        xy_fft_halves_out<M, P, true>(
-            buf, tw, lm,
+#pragma unroll 1
+        for (int ph = 0; ph < 2; ++ph) {
+          xy_fft_halves<M, P, false>(
+              buf, tw,
+              [&](int q, int n) -> float2 {
+                if (ph == 0) return st[n * P + q];
+                const float2 v = mid[T::at(q, n)];
+                return make_float2(v.x, -v.y);
+              },
+              [&](int q, int k, float2 v) {
+                if (ph == 0)
+                  trunc(q, k, v);
+                else
+                  buf[k * P + q] = make_float2(v.x, -v.y);
+              },
+              [&] {
+                if (ph == 0) h1();
+              });
+          __syncthreads();
+        }
+        xy_store_rows<M, P>(
+            buf,
             [&](int q, int n, float2 v0, float2 v1) {
               *reinterpret_cast<float4 *>(out + unsigned(n) * D::Kh + q) = make_float4(v0.x, v0.y, v1.x, v1.y);
             },
-            NoHook(), h2);
+            h2);
+      } else if constexpr (X::lean) {
+#pragma unroll 1
+        for (int ph = 0; ph < 2; ++ph) {
+          xy_fft<M, P, false, false>(
+              buf, buf2, tw,
+              [&](int q, int n) -> float2 {
+                if (ph == 0) return st[n * P + q];
+                const float2 v = mid[T::at(q, n)];
+                return make_float2(v.x, -v.y);
+              },
+              [&](int q, int k, float2 v) {
+                if (ph == 0)
+                  trunc(q, k, v);
+                else
+                  out[unsigned(k) * D::Kh + q] = make_float2(v.x, -v.y);
+              });
+          __syncthreads();
+        }
       } else {
         xy_fft<M, P, false, false>(buf, buf2, tw, ld, trunc);
         __syncthreads();
