@@ -193,7 +193,7 @@ struct mfx_job {
   // mfx_job_particles_device from this array, filled on request
   void *ids_dev = nullptr;
   std::vector<double> qhost;
-  cudaEvent_t psi_ev[16] = {};
+  std::vector<cudaEvent_t> psi_ev;  // one per staging chunk of a fetch
   void *work = nullptr;
   size_t work_bytes = 0;
   Plan m_r2c, m_c2r, n_c2r;
@@ -1444,26 +1444,39 @@ static void write_positions(const mfx_job *j, size_t p0, size_t p1, double *dst)
 }
 
 // The float displacements of particles [first, first + count) to the staging
-// buffer on stream x, in chunks each followed by an event, and host threads
-// that wait for their chunk and write q + Psi into dst (joined by join_id_fill).
+// buffer on stream x, in chunks of 4M particles (48 MB) each followed by an
+// event, and host threads that take the chunks in turn (thread t: chunks t,
+// t + nt, ...), each waiting for its chunk and writing q + Psi into dst
+// (joined by join_id_fill): every thread starts with the first chunks, and
+// one chunk's work is left after the last copy.  At 768^3 the fetch is then
+// bound by the host's memory (about 120 GB a step through DRAM: the staging
+// written and read, positions, velocities and ids written).
 static int start_pos_fill(mfx_job *j, size_t first, size_t count, void *dst, cudaStream_t x) {
   if (!j->psi_host) {
     CU(cudaHostAlloc(reinterpret_cast<void **>(&j->psi_host), j->npart * 3 * sizeof(float), cudaHostAllocDefault));
   }
-  const size_t hw = std::max(2u, std::thread::hardware_concurrency());
-  const size_t nt = std::max<size_t>(1, std::min<size_t>({size_t(16), hw, (count >> 18) + 1}));
-  const size_t per = (count + nt - 1) / nt;
+  constexpr size_t kChunk = size_t(1) << 22;
+  const size_t nch = (count + kChunk - 1) / kChunk;
+  while (j->psi_ev.size() < nch) {
+    cudaEvent_t e = nullptr;
+    CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    j->psi_ev.push_back(e);
+  }
   const float *src = static_cast<const float *>(j->pos);
-  for (size_t t = 0; t < nt; ++t) {
-    const size_t a = first + t * per, b = std::min(first + count, a + per);
-    if (a >= b) break;
-    if (!j->psi_ev[t]) CU(cudaEventCreateWithFlags(&j->psi_ev[t], cudaEventDisableTiming));
+  for (size_t c = 0; c < nch; ++c) {
+    const size_t a = first + c * kChunk, b = std::min(first + count, a + kChunk);
     CU(cudaMemcpyAsync(j->psi_host + 3 * a, src + 3 * a, (b - a) * 3 * sizeof(float), cudaMemcpyDeviceToHost, x));
-    CU(cudaEventRecord(j->psi_ev[t], x));
-    cudaEvent_t ev = j->psi_ev[t];
-    double *o = static_cast<double *>(dst) + 3 * (a - first);
-    auto work = [j, ev, a, b, o] {
-      if (cudaEventSynchronize(ev) == cudaSuccess) write_positions(j, a, b, o);
+    CU(cudaEventRecord(j->psi_ev[c], x));
+  }
+  const size_t hw = std::max(2u, std::thread::hardware_concurrency());
+  const size_t nt = std::max<size_t>(1, std::min<size_t>({size_t(16), hw, nch}));
+  for (size_t t = 0; t < nt; ++t) {
+    auto work = [j, t, nt, nch, first, count, dst] {
+      for (size_t c = t; c < nch; c += nt) {
+        const size_t a = first + c * kChunk, b = std::min(first + count, a + kChunk);
+        if (cudaEventSynchronize(j->psi_ev[c]) != cudaSuccess) return;
+        write_positions(j, a, b, static_cast<double *>(dst) + 3 * (a - first));
+      }
     };
     try {
       j->id_fill.emplace_back(work);

@@ -18,9 +18,12 @@ def _job(mfx, engine, sp, **kw):
                    lunit=sp["lunit"], vunit=sp["vunit"], pos64=True, vel64=False, id64=True, **kw)
 
 
-@pytest.mark.parametrize("lattice,plt", [(1, True), (2, False)])
-def test_host_positions_equal_device_positions(mfxlib, engine, lattice, plt):
-    sp = spec(mfxlib, 64, 200.0, 24.0, 3, 21, lattice=lattice, precision=mfxlib.FP32C)
+@pytest.mark.parametrize("n,lattice,plt", [(64, 1, True), (64, 2, False), (128, 2, True)])
+def test_host_positions_equal_device_positions(mfxlib, engine, n, lattice, plt):
+    """128^3 FCC: 8.4M particles, three staging chunks of 4M taken by
+    different host threads; the range crosses a chunk and a sub-lattice
+    boundary."""
+    sp = spec(mfxlib, n, 200.0 * n / 64, 24.0, 3, 21, lattice=lattice, precision=mfxlib.FP32C)
     if plt:
         sp["plt_table"] = engine.plt_table(lattice)
     j = _job(mfxlib, engine, sp)
@@ -30,8 +33,10 @@ def test_host_positions_equal_device_positions(mfxlib, engine, lattice, plt):
     got = j.particles()
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
-    n3 = 64 ** 3
+    n3 = n ** 3
     first, count = n3 - 777, min(n3 + 1555, j.num_particles - (n3 - 777))
+    if n == 128:
+        count = j.num_particles - first - 5  # across both chunk boundaries
     rng = j.particles_range(first, count)
     for a, b in zip(rng, ref):
         assert np.array_equal(a, b[first:first + count])
