@@ -128,9 +128,11 @@ template <int N> struct FA {
   // reads (in place) or has finished with, so no buffer of their own
   static constexpr size_t s3 = head + size_t(TwTab<N>::elems) * sizeof(float2) + size_t(RW * 6 * Kh) * sizeof(float2) +
                                size_t(nbuf * Tile<N, 3 * RW, false>::elems) * sizeof(float2);
-  // CTAs per SM the ASM3 registers are sized for (about 104 a thread), no more
-  // than shared memory allows
-  static constexpr int minb3_r = 65536 / (t3 * 104) < 1 ? 1 : 65536 / (t3 * 104);
+  // CTAs per SM the ASM3 registers are sized for (about 104 a thread; 72 for
+  // the one-row groups of the long lengths, which fit them without spills),
+  // no more than shared memory allows
+  static constexpr int regs3 = RW == 1 ? 72 : 104;
+  static constexpr int minb3_r = 65536 / (t3 * regs3) < 1 ? 1 : 65536 / (t3 * regs3);
   static constexpr int minb3_s = int(233472 / (s3 + 1024)) < 1 ? 1 : int(233472 / (s3 + 1024));
   static constexpr int minb3 = minb3_r < minb3_s ? minb3_r : minb3_s;
 };
