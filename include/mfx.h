@@ -279,7 +279,9 @@ int mfx_job_destroy(mfx_job *job);
 /* Sets the pencil-tile shape of the fused transforms by hand (the choice
    mfx_job_autotune makes by timing): pencils per CTA of the x/y passes
    (4, 8, 16 or 32; tiles wider than 1024 butterflies run in the lean form:
-   a third as many threads, in-place transforms) and the z passes' shape:
+   a third as many threads, in-place transforms; lean tiles whose two input
+   stages do not fit beside the transform run in an in-place form, the tile
+   its own stage) and the z passes' shape:
    1 or 2 rows per CTA, 3 for one row per CTA and as many pencils per
    transform as one CTA per SM holds (the wide shape of the long padded
    lengths), or 4 for one row per CTA of three warps, each pencil transformed
