@@ -1009,10 +1009,13 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
         mid[T::at(q, k)] = keep ? make_float2(v.x * a.fac, v.y * a.fac) : make_float2(0.f, 0.f);
       };
       auto lm = [&](int q, int n) { return mid[T::at(q, n)]; };
-      // lean forms: one copy of the transform's code for both transforms,
+      // in-place form: one copy of the transform's code for both transforms,
       // the inverse as the conjugate of the forward transform of the
       // conjugate (negations are exact: the same roundings); two inlined
-      // transforms spill
+      // transforms spill there (456 bytes a thread; 40 this way).  The
+      // 8-pencil lean form keeps two transforms: its single copy, with the
+      // phase tests in the loads and stores, measured slower (768^3 YF-trunc
+      // 12.2 -> 17.2 ms)
       if constexpr (X::inplace) {
 #pragma unroll 1
         for (int ph = 0; ph < 2; ++ph) {
@@ -1040,24 +1043,6 @@ __global__ void __launch_bounds__(XY<M, P, M>::threads, XY<M, P, M>::minb) k_ff_
               *reinterpret_cast<float4 *>(out + unsigned(n) * D::Kh + q) = make_float4(v0.x, v0.y, v1.x, v1.y);
             },
             h2);
-      } else if constexpr (X::lean) {
-#pragma unroll 1
-        for (int ph = 0; ph < 2; ++ph) {
-          xy_fft<M, P, false, false>(
-              buf, buf2, tw,
-              [&](int q, int n) -> float2 {
-                if (ph == 0) return st[n * P + q];
-                const float2 v = mid[T::at(q, n)];
-                return make_float2(v.x, -v.y);
-              },
-              [&](int q, int k, float2 v) {
-                if (ph == 0)
-                  trunc(q, k, v);
-                else
-                  out[unsigned(k) * D::Kh + q] = make_float2(v.x, -v.y);
-              });
-          __syncthreads();
-        }
       } else {
         xy_fft<M, P, false, false>(buf, buf2, tw, ld, trunc);
         __syncthreads();
