@@ -502,6 +502,47 @@ MFX_HD void unpack_pair(float2 z, float2 zm, float2 &a, float2 &b) {
   b = make_float2(0.5f * (z.y + zm.y), -0.5f * (z.x - zm.x));
 }
 
+// CTAs per SM the register allocation is sized for: as many as leave each
+// thread at least 64 registers, at most four
+MFX_CX int min_blocks(int threads) {
+  return 65536 / (threads * 64) < 1 ? 1 : (65536 / (threads * 64) > 4 ? 4 : 65536 / (threads * 64));
+}
+
+// x/y tile of P pencils.  Lean form, for tiles whose P * maxJ butterflies
+// exceed 1024 threads: a third as many threads, each holding up to three
+// butterflies of a step (registers for them: the register file is shared out
+// in whole warps per scheduler), and one tile buffer (in-place transforms)
+// beside the staging.
+//
+// In-place form, for lean tiles whose two stages do not fit beside the tile
+// (P = 16 at M = 1152: 128-byte row pieces, where 64-byte ones halve the HBM
+// rate of these strided rows): one stage only, the tile itself, which holds
+// the unit's input rows from `side` up (at their stage positions r * P + q)
+// while rows below `side` sit in a side buffer.  The side buffer of the next
+// unit is fetched once the first transform step has read this unit's input,
+// the tile's rows once the last step has read the tile; a unit makes one
+// output (the transform overwrites its input).
+constexpr size_t kXYSmemMax = 227 * 1024;
+template <int M, int P, int ROWS> struct XY {
+  static constexpr bool lean = P * Fac<M>::maxJ > 1024;
+  static constexpr int nbuf = lean ? 1 : 2;
+  static constexpr int tile = Tile<M, P, true>::elems;
+  static constexpr size_t staged(int rows) { return size_t(M + nbuf * tile + 2 * rows * P) * sizeof(float2); }
+  // decided on M rows, so that both row counts of a length take one form
+  static constexpr bool inplace = lean && staged(M) > kXYSmemMax;
+  // the in-place form transforms the tile in two halves of P / 2 pencils (the
+  // registers of a P / 2 tile: all of a step's data is held across its barrier)
+  static constexpr int HP = inplace ? P / 2 : P;
+  static constexpr bool hlean = HP * Fac<M>::maxJ > 1024;
+  static constexpr int threads = hlean ? (HP * Fac<M>::maxJ / 3) / 32 * 32 : HP * Fac<M>::maxJ;
+  static constexpr int minb = (lean || inplace) ? 1 : min_blocks(threads);
+  static constexpr size_t side_room = kXYSmemMax - size_t(M + tile) * sizeof(float2);
+  static constexpr int side = !inplace ? 0
+                              : (side_room / (P * sizeof(float2)) < size_t(ROWS) ? int(side_room / (P * sizeof(float2)))
+                                                                                   : ROWS);
+  static constexpr size_t smem = inplace ? size_t(M + tile + side * P) * sizeof(float2) : staged(ROWS);
+};
+
 #if defined(__CUDACC__)
 // ---------------------------------------------------------------------------
 // kernels
@@ -541,12 +582,6 @@ template <int M> __device__ __forceinline__ void load_tw_steps(float2 *tw, const
   __syncthreads();
 }
 
-// CTAs per SM the register allocation is sized for: as many as leave each
-// thread at least 64 registers, at most four
-MFX_CX int min_blocks(int threads) {
-  return 65536 / (threads * 64) < 1 ? 1 : (65536 / (threads * 64) > 4 ? 4 : 65536 / (threads * 64));
-}
-
 // ---------------------------------------------------------------------------
 // x/y passes (persistent): each CTA walks units blockIdx.x, + gridDim.x, ...
 // A unit is one tile of P adjacent kz pencils (one outer index, one kz block,
@@ -572,41 +607,6 @@ __device__ __forceinline__ void stage_rows(float2 *stage, const float2 *src, uns
     cp_async<CHUNK>(stage + r * P + c * E, src + r * stride + c * E);
   }
 }
-
-// x/y tile of P pencils.  Lean form, for tiles whose P * maxJ butterflies
-// exceed 1024 threads: a third as many threads, each holding up to three
-// butterflies of a step (registers for them: the register file is shared out
-// in whole warps per scheduler), and one tile buffer (in-place transforms)
-// beside the staging.
-//
-// In-place form, for lean tiles whose two stages do not fit beside the tile
-// (P = 16 at M = 1152: 128-byte row pieces, where 64-byte ones halve the HBM
-// rate of these strided rows): one stage only, the tile itself, which holds
-// the unit's input rows from `side` up (at their stage positions r * P + q)
-// while rows below `side` sit in a side buffer.  The side buffer of the next
-// unit is fetched once the first transform step has read this unit's input,
-// the tile's rows once the last step has read the tile; a unit makes one
-// output (the transform overwrites its input).
-constexpr size_t kXYSmemMax = 227 * 1024;
-template <int M, int P, int ROWS> struct XY {
-  static constexpr bool lean = P * Fac<M>::maxJ > 1024;
-  static constexpr int nbuf = lean ? 1 : 2;
-  static constexpr int tile = Tile<M, P, true>::elems;
-  static constexpr size_t staged(int rows) { return size_t(M + nbuf * tile + 2 * rows * P) * sizeof(float2); }
-  // decided on M rows, so that both row counts of a length take one form
-  static constexpr bool inplace = lean && staged(M) > kXYSmemMax;
-  // the in-place form transforms the tile in two halves of P / 2 pencils (the
-  // registers of a P / 2 tile: all of a step's data is held across its barrier)
-  static constexpr int HP = inplace ? P / 2 : P;
-  static constexpr bool hlean = HP * Fac<M>::maxJ > 1024;
-  static constexpr int threads = hlean ? (HP * Fac<M>::maxJ / 3) / 32 * 32 : HP * Fac<M>::maxJ;
-  static constexpr int minb = (lean || inplace) ? 1 : min_blocks(threads);
-  static constexpr size_t side_room = kXYSmemMax - size_t(M + tile) * sizeof(float2);
-  static constexpr int side = !inplace ? 0
-                              : (side_room / (P * sizeof(float2)) < size_t(ROWS) ? int(side_room / (P * sizeof(float2)))
-                                                                                   : ROWS);
-  static constexpr size_t smem = inplace ? size_t(M + tile + side * P) * sizeof(float2) : staged(ROWS);
-};
 
 // the transform of an x/y tile: pencil_fft, or pencil_fft_mi in the lean form
 // (buf2 == buf there).  LDB as for pencil_fft: false where ld reads the stage
