@@ -519,9 +519,9 @@ MFX_CX int min_blocks(int threads) {
 // rate of these strided rows): one stage only, the tile itself, which holds
 // the unit's input rows from `side` up (at their stage positions r * P + q)
 // while rows below `side` sit in a side buffer.  The side buffer of the next
-// unit is fetched once the first transform step has read this unit's input,
-// the tile's rows once the last step has read the tile; a unit makes one
-// output (the transform overwrites its input).
+// unit is fetched once the first steps of the transform's two halves have
+// read this unit's input, the tile's rows once the result has left the tile;
+// a unit makes one output (the transform overwrites its input).
 constexpr size_t kXYSmemMax = 227 * 1024;
 template <int M, int P, int ROWS> struct XY {
   static constexpr bool lean = P * Fac<M>::maxJ > 1024;
@@ -729,9 +729,10 @@ __device__ __forceinline__ void xy_units(unsigned units, unsigned stage_elems, f
 
 // The in-place form's unit loop: src(u) is unit u's first input row (ROWS
 // rows, `stride` apart); work(u, stage, h1, h2) transforms unit u from the
-// SplitStage and calls h1 and h2 through its transforms (xy_fft), which fetch
-// the next unit's side rows and tile rows.  One barrier per unit: after it
-// every thread's copies of unit u have landed.
+// SplitStage and calls h1 and h2 through its transforms (xy_fft_halves,
+// xy_fft_halves_out, xy_store_rows), which fetch the next unit's side rows and
+// tile rows.  One barrier per unit: after it every thread's copies of unit u
+// have landed.
 template <int M, int P, int ROWS, int CHUNK = 16, class Src, class Work>
 __device__ __forceinline__ void xy_units_inplace(unsigned units, float2 *side, float2 *tile, unsigned stride,
                                                  const Src &src, const Work &work) {
