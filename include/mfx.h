@@ -106,18 +106,28 @@ typedef struct {
   int noise_generator;
   int64_t music_seed;       /* [random] seed[log2 ngrid], > 0 (or 0 with music_seeds) */
   uint32_t music_cubesize;  /* [random] cubesize, 0 = 32 (random_plugin.hh:24) */
-  /* [random] seed[l] for the levels l <= log2 ngrid, 0 where the config has
-     no such key.  The coarsest seeded level is filled and each finer level up
-     to the grid's refines the one below by coarse mode replacement with its
-     own seed, or the level's dummy seed (random_music.cc:160-245,
-     random_music_wnoise_generator.cc:392-547).  Seeds at finer levels than
-     the grid's (restriction) are not supported. */
+  /* [random] seed[l] for the levels l <= log2 ngrid + 3, 0 where the config
+     has no such key.  The coarsest seeded level is filled; if it is coarser
+     than the grid's, each finer level up to the grid's refines the one below
+     by coarse mode replacement with its own seed, or the level's dummy seed
+     (random_music.cc:160-245, random_music_wnoise_generator.cc:392-547); if
+     it is finer, it is restricted down to the grid's level by k-space
+     averaging (random_music.cc:238-265, random_music_wnoise_generator.cc:
+     288-380). */
   int64_t music_seeds[12];
   /* MFX_NOISE_FIELD: ngrid^3 doubles, [x][y][z] with z fastest, the values
-     Fill_Grid copies into the grid; read at every run of the job (host
-     memory: page-locked memory must stay unchanged until the run's noise
-     stage has finished) */
+     Fill_Grid copies into the grid.  MFX_NOISE_MUSIC1: NULL, or the noise of
+     a level coarser than the grid's read from a file (random_music.cc:216-236,
+     a noise file at the coarsest level given): noise_field_res^3 doubles, the
+     start of the refinement chain, whose finer levels come from music_seeds
+     (or their dummy seeds).  Read at every run of the job (host memory:
+     page-locked memory must stay unchanged until the run's noise stage has
+     finished) */
   const double *noise_field;
+  /* cells per axis of noise_field: 0 = ngrid.  With MFX_NOISE_MUSIC1 a power
+     of two, at least 2 and below ngrid, with no music_seeds at or below its
+     level */
+  uint32_t noise_field_res;
 } mfx_job_desc;
 
 /* ---- errors -------------------------------------------------------------- */

@@ -201,7 +201,7 @@ struct mfx_job {
   // MUSIC1 from coarser seeded levels: the levels' forward transforms
   // (level music_l0 + q at music_plans[q]) and two coarse k-space buffers
   std::vector<Plan> music_plans;
-  int music_l0 = 0, music_lmin = 0;
+  int music_l0 = 0, music_lmin = 0, music_lfile = -1;
   void *music_buf[2] = {nullptr, nullptr};
   // CUDA graph of the whole pipeline (mfx_job_capture)
   cudaGraph_t graph = nullptr;
@@ -288,12 +288,18 @@ static size_t n_field_bytes(int N, size_t rs) { return size_t(N) * N * (N / 2 + 
 // restricted down to lmin, random_music.cc:247-272)
 struct MusicLevels {
   int l0 = 0, lmin = 0;
+  int lfile = -1;  // the level a noise field gives (the chain's coarsest), else -1
   int64_t seed[12] = {};
 };
 static MusicLevels music_levels(const mfx_job_desc *d) {
   MusicLevels m;
   while ((1u << m.lmin) < d->ngrid && m.lmin < 11) ++m.lmin;
   m.l0 = -1;
+  if (d->noise_generator == MFX_NOISE_MUSIC1 && d->noise_field && d->noise_field_res > 1) {
+    m.lfile = 0;
+    while ((1u << m.lfile) < d->noise_field_res && m.lfile < 11) ++m.lfile;
+    m.l0 = m.lfile;
+  }
   for (int l = 0; l < 12 && m.l0 < 0; ++l)
     if (d->music_seeds[l] > 0 || (l == m.lmin && d->music_seed > 0)) m.l0 = l;
   if (m.l0 < 0) m.l0 = m.lmin;
@@ -333,6 +339,18 @@ static int check_desc(const mfx_job_desc *d) {
         return set_error(MFX_EINVAL, "MUSIC1 seed[%d] more than three levels finer than the grid's (%d)", l, lmin);
       any = any || d->music_seeds[l] > 0;
     }
+    if (d->noise_field) {
+      // a noise file at the chain's coarsest level (random_music.cc:216-236)
+      const uint32_t r = d->noise_field_res;
+      if (r < 2 || (r & (r - 1)) || r >= d->ngrid)
+        return set_error(MFX_EINVAL, "MUSIC1 noise_field_res must be a power of two from 2 below ngrid (got %u)", r);
+      int lf = 0;
+      while ((1u << lf) < r) ++lf;
+      for (int l = 0; l <= lf; ++l)
+        if (d->music_seeds[l] > 0)
+          return set_error(MFX_EINVAL, "MUSIC1 seed[%d] at or below the noise field's level %d", l, lf);
+      any = true;
+    }
     if (d->music_seed < 0 || !any) return set_error(MFX_EINVAL, "MUSIC1 noise needs a positive seed");
     const unsigned cs = d->music_cubesize ? d->music_cubesize : 32u;
     if (cs < 2 || (d->ngrid >= cs && d->ngrid % cs != 0))
@@ -341,6 +359,8 @@ static int check_desc(const mfx_job_desc *d) {
       return set_error(MFX_EINVAL, "MUSIC1 cubes above 256^3 cells (one sequential stream each) are not supported");
   } else if (d->noise_generator == MFX_NOISE_FIELD) {
     if (!d->noise_field) return set_error(MFX_EINVAL, "MFX_NOISE_FIELD needs noise_field");
+    if (d->noise_field_res && d->noise_field_res != d->ngrid)
+      return set_error(MFX_EINVAL, "MFX_NOISE_FIELD gives the grid's level: noise_field_res must be 0 or ngrid");
   } else {
     return set_error(MFX_EINVAL, "unknown noise_generator %d", d->noise_generator);
   }
@@ -657,7 +677,21 @@ template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
     // replaced (its real-space round trip, c2r then r2c, is the identity on
     // these Hermitian spectra and is left out)
     void *prev = j->music_buf[0];
-    TRY(level(j->music_l0, prev, j->music_plans[0]));
+    if (j->music_lfile >= 0) {
+      // the level a noise file gives: uploaded (staged in the grid-level
+      // buffer, which the chain writes last), into the padded layout,
+      // transformed
+      const int n0 = 1 << j->music_l0;
+      const size_t c0 = size_t(n0) * n0 * n0;
+      CU(cudaMemcpyAsync(out, j->d.noise_field, c0 * 8, cudaMemcpyHostToDevice, j->stream));
+      KBEGIN(j);
+      music::k_field_to_padded<R><<<grid_for(c0, 256, num_sm()), 256, 0, j->stream>>>((const double *)out, (R *)prev,
+                                                                                     n0);
+      KEND(j, "field_to_padded", double(c0) * (8.0 + sizeof(R)));
+      TRY(exec_fft(j, j->music_plans[0], prev, true));
+    } else {
+      TRY(level(j->music_l0, prev, j->music_plans[0]));
+    }
     for (int l = j->music_l0 + 1; l <= j->music_lmin; ++l) {
       void *dst = l == j->music_lmin ? out : j->music_buf[(l - j->music_l0) & 1];
       TRY(level(l, dst, l == j->music_lmin ? j->n_r2c : j->music_plans[size_t(l - j->music_l0)]));
@@ -675,7 +709,7 @@ template <typename R> static int launch_music(mfx_job *j, int mode, void *out) {
   k.N = N;
   k.mode = mode;
   k.fixing = j->d.fixing;
-  k.keep_dc = j->d.noise_generator == MFX_NOISE_FIELD;
+  k.keep_dc = j->d.noise_generator == MFX_NOISE_FIELD || j->music_lfile >= 0;  // a file's mean is kept
   k.unit = 1.0 / std::sqrt(cells);
   const double volfac = std::pow(j->d.boxlen / N / 2.0 / M_PI, 1.5);
   k.norm = (j->d.inversion ? -1.0 : 1.0) / volfac;
@@ -1692,6 +1726,7 @@ static int create_job(mfx_engine *eng, const mfx_job_desc *d, mfx_job **out, int
     const MusicLevels ml = music_levels(d);
     j->music_l0 = ml.l0;
     j->music_lmin = ml.lmin;
+    j->music_lfile = ml.lfile;
     // the coarser levels' forward transforms, or the one of the finer seeded level
     j->music_plans.resize(ml.l0 < ml.lmin ? size_t(ml.lmin - ml.l0) : (ml.l0 > ml.lmin ? 1 : 0));
     for (size_t q = 0; q < j->music_plans.size(); ++q) {
@@ -1995,8 +2030,9 @@ int mfx_job_upload(mfx_job *job, const mfx_job_desc *desc) {
   if (desc->ngrid != job->d.ngrid || desc->amp_table_len != job->d.amp_table_len || desc->plt != job->d.plt ||
       desc->noise_generator != job->d.noise_generator || desc->music_cubesize != job->d.music_cubesize)
     return set_error(MFX_EINVAL, "upload descriptor does not match the job's sizes");
-  if (desc->noise_generator == MFX_NOISE_MUSIC1 && music_levels(desc).l0 != job->music_l0)
-    return set_error(MFX_EINVAL, "upload descriptor changes the coarsest seeded MUSIC1 level");
+  if (desc->noise_generator == MFX_NOISE_MUSIC1 &&
+      (music_levels(desc).l0 != job->music_l0 || music_levels(desc).lfile != job->music_lfile))
+    return set_error(MFX_EINVAL, "upload descriptor changes the coarsest seeded MUSIC1 level or its noise file");
   job->d.seed_table = desc->seed_table;
   job->d.noise_field = desc->noise_field;
   job->d.music_seed = desc->music_seed;

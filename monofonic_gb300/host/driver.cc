@@ -213,12 +213,12 @@ int run_config(mfx_engine *eng, const std::string &text) {
   else if (load == "fcc") lattice = MFX_LATTICE_FCC;
   else throw std::runtime_error("ParticleLoad '" + load + "' is not supported by this engine (sc, bcc, fcc)");
   // [random] generator (random_plugin.cc:62-81): NGENIC with its seed, or
-  // MUSIC1 with one seed[level] at the grid's own level (random_music.cc:75,
-  // 160-215); seeds at other levels need MUSIC1's multi-level refinement
+  // MUSIC1 with seed[level] keys (random_music.cc:75, 160-283)
   const std::string gen = cf.get_value<std::string>("random", "generator");
   long seed = 0;
   int64_t music_seeds[12] = {};
   std::vector<double> noise_file;  // MUSIC1 noise read from a file
+  unsigned noise_file_res = 0;     // its cells per axis below GridRes: the refinement chain's start
   int noise_gen = MFX_NOISE_NGENIC;
   unsigned cubesize = 0;
   if (gen == "NGENIC") {
@@ -236,11 +236,20 @@ int run_config(mfx_engine *eng, const std::string &text) {
       const std::string val = cf.get_value<std::string>("random", key);
       const bool number = !val.empty() && val.find_first_not_of("-0123456789") == std::string::npos;
       if (!number) {
-        // a white-noise file in place of the seed (random_music.cc:186-193)
-        if (l != lmin)
-          throw std::runtime_error("MUSIC1 " + key + ": a noise file is supported at log2(GridRes) = " +
-                                   std::to_string(lmin) + " only");
-        noise_file = read_grafic_noise(val, ngrid, cf.get_value_safe<bool>("random", "grafic_sign", false));
+        // a white-noise file in place of the seed (random_music.cc:186-193).
+        // Used at the coarsest level given (levelmin_seed): at the grid's
+        // level as the noise itself, below it as the start of the refinement
+        // chain; a file above a coarser seed or file is ignored, as the
+        // reference does (random_music.cc:231-234)
+        if (any) {
+          std::fprintf(stderr, "MUSIC1 %s: a noise file above the coarsest level given is ignored\n", key.c_str());
+          continue;
+        }
+        if (l > lmin)
+          throw std::runtime_error("MUSIC1 " + key + ": a noise file finer than log2(GridRes) = " +
+                                   std::to_string(lmin) + " is not supported");
+        noise_file = read_grafic_noise(val, 1u << l, cf.get_value_safe<bool>("random", "grafic_sign", false));
+        noise_file_res = l < lmin ? (1u << l) : 0;
         any = true;
         continue;
       }
@@ -253,14 +262,14 @@ int run_config(mfx_engine *eng, const std::string &text) {
       any = true;
     }
     if (!any) throw std::runtime_error("No seed specified for MUSIC1 RNG plugin!");
-    if (!noise_file.empty())
+    if (!noise_file.empty() && noise_file_res == 0)
       for (int l = 0; l < 12; ++l)
         if (music_seeds[l] > 0)
-          throw std::runtime_error("MUSIC1: a noise file together with seed[" + std::to_string(l) +
+          throw std::runtime_error("MUSIC1: a noise file at log2(GridRes) together with seed[" + std::to_string(l) +
                                    "] is not supported");
     seed = music_seeds[lmin];
     cubesize = cf.get_value_safe<unsigned>("random", "cubesize", 32);
-    noise_gen = noise_file.empty() ? MFX_NOISE_MUSIC1 : MFX_NOISE_FIELD;
+    noise_gen = (noise_file.empty() || noise_file_res) ? MFX_NOISE_MUSIC1 : MFX_NOISE_FIELD;
   } else {
     throw std::runtime_error("random generator '" + gen + "' is not supported (NGENIC, MUSIC1)");
   }
@@ -304,6 +313,7 @@ int run_config(mfx_engine *eng, const std::string &text) {
   d.music_cubesize = cubesize;
   std::memcpy(d.music_seeds, music_seeds, sizeof(music_seeds));
   d.noise_field = noise_file.empty() ? nullptr : noise_file.data();
+  d.noise_field_res = noise_file_res;
   d.amp_table = amp.data();
   d.amp_table_len = alen;
   d.plt_table = do_plt ? plt.data() : nullptr;

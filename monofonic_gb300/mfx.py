@@ -61,6 +61,7 @@ class JobDesc(C.Structure):
         ("noise_generator", C.c_int), ("music_seed", C.c_int64), ("music_cubesize", C.c_uint32),
         ("music_seeds", C.c_int64 * 12),
         ("noise_field", C.c_void_p),
+        ("noise_field_res", C.c_uint32),
     ]
 
 
@@ -284,6 +285,16 @@ def lpt_coefficients(dplus: float, vfac: float, order: int) -> dict:
                 vfac1=vfac, vfac2=2 * vfac, vfac3=3 * vfac)
 
 
+def _field_res(field) -> int:
+    """Cells per axis of a cubic real-space noise field (0 for none)."""
+    if field is None:
+        return 0
+    n = field.shape[0] if field.ndim == 3 else int(round(field.size ** (1.0 / 3.0)))
+    if n ** 3 != field.size:
+        raise ValueError("noise field of %d values is not a cube" % field.size)
+    return n
+
+
 class Job:
     """One IC job on the device (mfx_job_*)."""
 
@@ -295,15 +306,18 @@ class Job:
         NOISE_MUSIC1, which draws the noise from music_seed (the seed at the
         grid's level) and music_cubesize, or from music_seeds {level: seed}
         given at coarser levels as well; noise_field: a real-space white-noise
-        field [x][y][z] (NOISE_FIELD), e.g. MUSIC1's noise read from a file."""
+        field [x][y][z] (NOISE_FIELD), e.g. MUSIC1's noise read from a file;
+        a field coarser than the grid starts MUSIC1's refinement chain at its
+        level, the finer levels from music_seeds."""
         self.engine = engine
         self.n = ngrid
         self.lattice = lattice
         self.precision = precision
         self.pos64, self.vel64, self.id64 = pos64, vel64, id64
         self._field = None if noise_field is None else np.ascontiguousarray(noise_field, dtype=np.float64)
+        field_res = _field_res(self._field)
         if noise_generator is None:
-            noise_generator = (NOISE_FIELD if self._field is not None else
+            noise_generator = ((NOISE_FIELD if field_res == ngrid else NOISE_MUSIC1) if self._field is not None else
                                NOISE_NGENIC if seed_table is not None else NOISE_MUSIC1)
         self._seed = None if seed_table is None else np.ascontiguousarray(seed_table, dtype=np.uint32)
         self._amp = np.ascontiguousarray(amp_table, dtype=np.float64)
@@ -320,6 +334,7 @@ class Job:
         for level, sd in (music_seeds or {}).items():
             d.music_seeds[level] = sd
         d.noise_field = self._field.ctypes.data if self._field is not None else None
+        d.noise_field_res = field_res if noise_generator == NOISE_MUSIC1 else 0
         d.amp_table = self._amp.ctypes.data
         d.amp_table_len = self._amp.size
         d.plt_table = self._plt.ctypes.data if self._plt is not None else None
@@ -634,9 +649,11 @@ def desc_from_spec(sp):
     d.want_particles = int(sp.get("want_particles", True))
     field = sp.get("noise_field")
     field = None if field is None else np.ascontiguousarray(field, dtype=np.float64)
-    d.noise_generator = sp.get("noise_generator", NOISE_FIELD if field is not None else
-                               NOISE_NGENIC if seed is not None else NOISE_MUSIC1)
+    res = _field_res(field)
+    d.noise_generator = sp.get("noise_generator", (NOISE_FIELD if res == sp["ngrid"] else NOISE_MUSIC1)
+                               if field is not None else NOISE_NGENIC if seed is not None else NOISE_MUSIC1)
     d.noise_field = field.ctypes.data if field is not None else None
+    d.noise_field_res = res if d.noise_generator == NOISE_MUSIC1 else 0
     d.music_seed, d.music_cubesize = sp.get("music_seed", 0), sp.get("music_cubesize", 32)
     for level, sd in (sp.get("music_seeds") or {}).items():
         d.music_seeds[level] = sd

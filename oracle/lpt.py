@@ -213,13 +213,21 @@ def music_restrict(fine: np.ndarray) -> np.ndarray:
     return sfft.irfftn(cc, s=(nc, nc, nc), workers=WORKERS) * float(nc) ** 3
 
 
-def music_levels(n: int, seeds: dict, cubesize: int = 32) -> np.ndarray:
+def music_levels(n: int, seeds: dict, cubesize: int = 32, field=None) -> np.ndarray:
     """MUSIC1's real-space noise at level log2(n) (random_music.cc:222-283):
     with seeds at coarser levels the coarsest seeded level is filled (its mean
     subtracted) and each finer level up to log2(n) refines the one below with
     its own seed or the level's dummy seed; with seeds only at finer levels the
-    coarsest of them is filled and restricted down level by level."""
+    coarsest of them is filled and restricted down level by level.  field: the
+    noise of a coarser level read from a file (random_music.cc:216-236, values
+    as read, no mean subtracted), the start of the refinement chain."""
     lmin = int(n).bit_length() - 1
+    if field is not None:
+        f = np.asarray(field, dtype=np.float64)
+        l0 = int(f.shape[0]).bit_length() - 1
+        for level in range(l0 + 1, lmin + 1):
+            f = music_refine(f, music_cubes_raw(1 << level, seeds.get(level, music_dummy_seed(level)), cubesize))
+        return f
     l0 = min(seeds)
     if l0 == lmin:
         return music_noise_real(n, seeds[lmin], cubesize)

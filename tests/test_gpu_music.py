@@ -220,3 +220,61 @@ def test_run_config_music1_noise_file(mfxlib, engine, tmp_path):
     pos, vel, ids = j.particles()
     off = 8 + 8 + 4 + 4 + 24
     assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
+
+
+@pytest.mark.parametrize("n,cubesize,res,seeds", [(32, 8, 8, {4: 77}), (32, 8, 16, {}), (16, 4, 2, {3: 5, 4: 6})])
+def test_music_noise_file_at_coarser_level(mfxlib, engine, oracle, n, cubesize, res, seeds):
+    """A noise file at a level coarser than the grid's starts the refinement
+    chain (random_music.cc:216-236): its values as read (mean kept), each
+    finer level refining it with its seed or the level's dummy seed."""
+    rng = np.random.default_rng(n + res)
+    field = rng.standard_normal((res, res, res)) + 0.05
+    c = Case(mfxlib, n, 100.0, 49.0, 1, 1)
+    j = mfxlib.Job(engine, n, c.L, 1, None, c.amp, c.coef, precision=mfxlib.FP64, want_particles=False,
+                   noise_generator=mfxlib.NOISE_MUSIC1, music_cubesize=cubesize, music_seeds=seeds,
+                   noise_field=field)
+    j.run_noise(raw=True)
+    got = j.field(mfxlib.FIELD_NOISE)
+    ref = oracle.fft_r2c(oracle.music_levels(n, seeds, cubesize, field=field))
+    assert rel_l2(got, ref) < 1e-12
+    assert abs(got[0, 0, 0]) > 0  # the file's mean comes through
+    j.run_noise(raw=True)  # a second run reads the field again
+    assert np.array_equal(j.field(mfxlib.FIELD_NOISE), got)
+    j.close()
+    with pytest.raises(mfxlib.MfxError, match="noise field"):
+        mfxlib.Job(engine, n, c.L, 1, None, c.amp, c.coef, precision=mfxlib.FP64, want_particles=False,
+                   noise_generator=mfxlib.NOISE_MUSIC1, music_cubesize=cubesize,
+                   music_seeds={**seeds, int(res).bit_length() - 1: 9}, noise_field=field)
+
+
+def test_run_config_music1_noise_file_at_coarser_level(mfxlib, engine, tmp_path):
+    """[random] seed[3] = <file> with seed[5] on a 32^3 grid: the file's noise
+    refined up to the grid's level, the same particles as a job given the
+    field and the seed."""
+    from test_cpu import write_grafic
+    rng = np.random.default_rng(9)
+    field = rng.standard_normal((8, 8, 8))
+    wn = tmp_path / "wn8.bin"
+    write_grafic(wn, field)
+    f = tmp_path / "ics.bin"
+    txt = mfxlib.ini_text(32, 50.0, 24.0, 2, 777, "sc", filename=str(f), generator="MUSIC1", cubesize=8)
+    engine.run_config(txt.replace("seed[5] = 777", "seed[3] = %s\nseed[5] = 777" % wn))
+    raw = f.read_bytes()
+    np_ = int(np.frombuffer(raw[8:16], np.uint64)[0])
+    c = Case(mfxlib, 32, 50.0, 24.0, 2, 1)
+    j = mfxlib.Job(engine, 32, c.L, 2, None, c.amp, c.coef, precision=mfxlib.FP64, lunit=c.lunit, vunit=c.vunit,
+                   noise_generator=mfxlib.NOISE_MUSIC1, music_cubesize=8, music_seeds={5: 777},
+                   noise_field=field.astype(np.float32).astype(np.float64))
+    j.run()
+    pos, vel, ids = j.particles()
+    off = 8 + 8 + 4 + 4 + 24
+    assert np.array_equal(np.frombuffer(raw[off:off + 24 * np_], np.float64).reshape(-1, 3), pos)
+    j.close()
+    # a file above a coarser seed is ignored (the reference warns and goes on)
+    g = tmp_path / "ics2.bin"
+    txt2 = mfxlib.ini_text(32, 50.0, 24.0, 2, 777, "sc", filename=str(g), generator="MUSIC1", cubesize=8)
+    engine.run_config(txt2.replace("seed[5] = 777", "seed[3] = 31\nseed[4] = %s\nseed[5] = 777" % wn))
+    h = tmp_path / "ics3.bin"
+    txt3 = mfxlib.ini_text(32, 50.0, 24.0, 2, 777, "sc", filename=str(h), generator="MUSIC1", cubesize=8)
+    engine.run_config(txt3.replace("seed[5] = 777", "seed[3] = 31\nseed[5] = 777"))
+    assert g.read_bytes() == h.read_bytes()
